@@ -1,0 +1,321 @@
+"""Benchmark: particle-steps/s of the GPU direct-sum KDK step on one GB300.
+
+Workload (the direct-sum precision study at its largest size): Plummer sphere
+N = 2^20 (reference sampler, seed 1), eps = 0.04 / N^(1/3), leapfrog KDK with
+dt = 1e-4, pair forces in mixed precision (f32 pairs on f64 tile centres,
+compensated sums), f64 kick/drift.  One step = one KDK step (half-kick, drift,
+Morton sort + tile packing, all-pairs force, half-kick).  Inputs are larger
+than L2 only in the f64 state, so L2 is also flushed between timed steps.
+
+Arms:
+  default          the engine (libgvs.so) on cuda:LOCAL_RANK
+  --impl reference the reference's CPU algorithm (the C restatement in oracle/,
+                   since the Rust reference cannot be built here) on all host
+                   cores, timed on a bounded sample of the same workload.
+
+Prints ONE JSON line on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s on 1 GB300: mixed vs FP64 at force rel err <=1e-6; adjoint/fwd"
+UNIT = "particle-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gvs", choices=["gvs", "reference"])
+    ap.add_argument("--n", type=int, default=1 << 20)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--dt", type=float, default=1e-4)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "fp64", "fp64_exact"])
+    ap.add_argument("--fp64-n", type=int, default=1 << 16, help="N of the bounded FP64 comparison run")
+    ap.add_argument("--cpu-targets", type=int, default=1024, help="targets in the bounded CPU sample")
+    ap.add_argument("--no-extras", action="store_true", help="skip FP64 / accuracy / CPU side measurements")
+    return ap.parse_args()
+
+
+# ---- distributed plumbing (replicas only: no data-path collective) -------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---- clocks sampler -------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows = []
+        self.stop = threading.Event()
+        self.t = threading.Thread(target=self.run, daemon=True)
+
+    def run(self):
+        while not self.stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.rows.append([s.strip() for s in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self.stop.wait(0.2)
+
+    def __enter__(self):
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if len(r) > 5 + k and r[5 + k] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def workload(n, seed):
+    return {"workload": f"direct-sum KDK, Plummer N={n} (seed {seed}), eps=0.04/N^(1/3), dt=1e-4",
+            "n": n, "seed": seed, "eps": 0.04 / n ** (1.0 / 3.0), "dt": 1e-4, "l2": "flushed between steps",
+            "parallelism": "replicas (one independent system per GPU)"}
+
+
+PREC = {"mixed": 3, "fp32": 2, "fp64": 1, "fp64_exact": 0}
+
+
+# ---- the CPU reference arm ------------------------------------------------------------
+def cpu_sample(n, seed, eps, targets, rng_seed=0):
+    """Times the oracle's direct sum on `targets` targets against all n sources
+    on all host cores; returns (particle-steps/s, cores, seconds, sample text)."""
+    import oracle as O
+    p = O.plummer(n, seed)
+    idx = np.sort(np.random.default_rng(rng_seed).choice(n, size=min(targets, n), replace=False))
+    cores = O.lib().orc_max_threads()
+    O.bf_subset(p, eps, idx[: min(32, len(idx))])  # warm the threads
+    t0 = time.perf_counter()
+    O.bf_subset(p, eps, idx)
+    dt = time.perf_counter() - t0
+    step_s = dt * n / len(idx)  # one full force evaluation, extrapolated by target count
+    return n / step_s, cores, dt, f"{len(idx)} of {n} targets x {n} sources (one force evaluation), extrapolated"
+
+
+def run_reference(a, d: Dist):
+    if d.rank != 0:
+        return
+    w = workload(a.n, a.seed)
+    vals = []
+    for _ in range(max(1, a.warmup)):
+        cpu_sample(a.n, a.seed, w["eps"], max(64, a.cpu_targets // 8))
+    last = None
+    for s in range(a.steps):
+        v, cores, secs, sample = cpu_sample(a.n, a.seed, w["eps"], a.cpu_targets, rng_seed=s)
+        vals.append(v)
+        last = (cores, sample)
+    v = float(np.median(vals))
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": a.n / v * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (reference Plummer sampler)", "impl": "reference",
+            "config": w,
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": last[0], "kind": "port", "sample": last[1]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---- the engine arm ---------------------------------------------------------------------
+def read_traffic():
+    path = os.path.join(ROOT, "profiles", "direct_mixed_traffic.json")
+    try:
+        with open(path) as fh:
+            return json.load(fh)
+    except Exception:
+        return None
+
+
+def run_engine(a, d: Dist):
+    import gravis_gb300 as G
+    from gravis_gb300 import _lib as L
+    w = workload(a.n, a.seed)
+    prec = PREC[a.precision]
+    ctx = G.Context(d.local)
+    p = G.PlummerSphere(a.n, seed=a.seed).generate()
+    eps, dt = w["eps"], a.dt
+    ctx.set_state(p)
+    tune = ctx.autotune(prec, eps) if prec in (2, 3) else None
+    ctx.set_state(p)
+    ctx.compute_forces(G.ALGO_DIRECT, prec, eps)
+    for _ in range(a.warmup):
+        ctx.kdk_steps(G.ALGO_DIRECT, prec, eps, 0.0, dt, 1)
+    ctx.sync()
+
+    # -- device-resident timed region: K steps, per-step events, L2 flushed between
+    ctx.profile(True)
+    d.barrier()
+    ctx.sync()
+    step_ms = []
+    wall0 = time.perf_counter()
+    with Clocks(d.local) as clk:
+        for _ in range(a.steps):
+            ctx.l2_flush()
+            ctx.event(0)
+            ctx.kdk_steps(G.ALGO_DIRECT, prec, eps, 0.0, dt, 1)
+            ctx.event(1)
+            step_ms.append(ctx.elapsed(0, 1))
+    ctx.sync()
+    wall = time.perf_counter() - wall0
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    d.barrier()
+    t_ms = d.max(sum(step_ms))
+    value = a.n * a.steps * d.world / (t_ms * 1e-3)
+
+    # -- e2e through the Integrator drop-in with pinned host buffers
+    import torch
+    names = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "mass")
+    host = {k: torch.empty(a.n, dtype=torch.float64, pin_memory=True).numpy() for k in names}
+    q = G.Particles(a.n)
+    ctx.get_state(q)
+    for k in names:
+        host[k][:] = getattr(q, k)
+    lib = L.load()
+    ptr = {k: host[k].ctypes.data for k in names}
+    e2e_s = []
+    d.barrier()
+    for _ in range(max(1, min(a.steps, 5))):
+        t0 = time.perf_counter()
+        st = lib.gvs_kdk_step_host(ctx.h, a.n, ptr["x"], ptr["y"], ptr["z"], ptr["vx"], ptr["vy"], ptr["vz"],
+                                   ptr["ax"], ptr["ay"], ptr["az"], ptr["mass"], G.ALGO_DIRECT, prec, eps, 0.0, dt)
+        L.check(st, ctx.h)
+        e2e_s.append(time.perf_counter() - t0)
+    e2e_t = d.max(sum(e2e_s))
+    e2e_value = a.n * len(e2e_s) * d.world / e2e_t
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": t_ms / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": {"mixed": "f32 pairs / f64 state", "fp32": "f32", "fp64": "f64",
+                                           "fp64_exact": "f64"}[a.precision],
+            "data": "synthetic (reference Plummer sampler, seed 1)", "config": w,
+            "wall_s_timed_region": wall, "autotune": tune,
+            "gpu_launches": int(prof["launches"]),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 10 * 8 * a.n,
+                    "d2h_bytes_per_step": 9 * 8 * a.n, "steps": len(e2e_s)},
+            "clocks": clk.summary()}
+
+    # -- roofline of the dominant kernel (the tiled f32 pair kernel)
+    kernel_ms = prof["force_ms"] / max(1, prof["force_launches"])
+    flops = prof["force_flops"] / max(1, prof["force_launches"])
+    peak = ctx.fp32_peak_tflops() if d.rank == 0 else None
+    achieved = flops / (kernel_ms * 1e-3) / 1e12
+    tr = read_traffic()
+    line["roofline"] = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                        "frac": achieved / peak if peak else None,
+                        "traffic": (tr or {}).get("bytes_per_launch_scaled"),
+                        "kernel": "k_direct32 (mixed, f32x2 pairs)", "kernel_ms": kernel_ms,
+                        "flops_per_launch": flops, "peak_source": "measured FP32 FMA probe (gvs_measure_fp32_peak)",
+                        "interactions_per_s": flops / 20.0 / (kernel_ms * 1e-3)}
+
+    if d.rank == 0 and not a.no_extras:
+        extras = {}
+        # FP64 form of the same kernel, bounded N
+        n64 = min(a.fp64_n, a.n)
+        p64 = G.PlummerSphere(n64, seed=a.seed).generate()
+        e64 = 0.04 / n64 ** (1.0 / 3.0)
+        rates = {}
+        for name, pr in (("fp64", 1), ("mixed", 3)):
+            ctx.set_state(p64)
+            ctx.compute_forces(G.ALGO_DIRECT, pr, e64)
+            ctx.profile(True)
+            for _ in range(3):
+                ctx.compute_forces(G.ALGO_DIRECT, pr, e64)
+            pf = ctx.profile_read()
+            ctx.profile(False)
+            rates[name] = pf["force_flops"] / 20.0 / (pf["force_ms"] * 1e-3)
+        extras["fp64_interactions_per_s"] = rates["fp64"]
+        extras["mixed_interactions_per_s_same_n"] = rates["mixed"]
+        extras["mixed_vs_fp64"] = rates["mixed"] / rates["fp64"]
+        extras["fp64_n"] = n64
+        # force error of mixed at the bench N against exact f64 on a target subset
+        ctx.set_state(p)
+        ctx.compute_forces(G.ALGO_DIRECT, 3, eps)
+        full = G.Particles(a.n)
+        ctx.get_state(full)
+        idx = np.sort(np.random.default_rng(123).choice(a.n, size=1024, replace=False))
+        ref = ctx.direct_subset(idx, eps, G.PREC_FP64_EXACT)
+        got = full.acc()[idx]
+        extras["force_rel_rms_mixed_vs_fp64"] = float(np.sqrt(((got - ref) ** 2).sum() / (ref ** 2).sum()))
+        extras["force_rel_err_subset"] = "1024 random targets, exact f64 reference on the GPU"
+        line["extras"] = extras
+        try:
+            v, cores, secs, sample = cpu_sample(a.n, a.seed, eps, a.cpu_targets)
+            line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+                                    "seconds": secs}
+        except Exception as ex:  # the oracle must be built (build() does it)
+            line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": None, "kind": "port",
+                                    "sample": f"unavailable: {ex}"}
+    ctx.close()
+    if d.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    d = Dist()
+    try:
+        if a.impl == "reference":
+            run_reference(a, d)
+        else:
+            run_engine(a, d)
+    finally:
+        d.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,791 @@
+// direct.cu -- all-pairs softened gravity (BruteForce, crates/sim-core/src/gravity.rs:47-80).
+//
+// Four forms, one per GVS_PREC_* mode:
+//
+//  FP64_EXACT  one thread per target i, j ascending over the caller's order,
+//              IEEE f64 with no FMA contraction (__dadd_rn/__dmul_rn/__dsqrt_rn/
+//              __ddiv_rn).  For every target this performs exactly the
+//              operations of the reference loop in the same order (the j<i
+//              terms of the symmetric loop equal the gather terms with dx
+//              negated, and negation is exact), so results are bit-identical.
+//
+//  FP64        the tiled kernel below in f64 (double4 j-tiles, FMA, rsqrt
+//              refined in f64): the FP64 form of the mixed kernel, used for
+//              the "mixed vs FP64" throughput ratio.
+//
+//  FP32        f32 absolute positions, plain f32 accumulation.
+//
+//  MIXED       particles are put in Morton order and cut into tiles of TJ=256;
+//              each tile stores its centre in f64 (as an f32 hi+lo pair) and its
+//              members as f32 offsets from that centre.  For target i and source
+//              tile J the kernel forms x_i - c_J = (c_I - c_J) + off_i from the
+//              hi/lo pairs, so pair separations are computed from small numbers
+//              and keep ~f32 relative precision even in the dense core.  The
+//              per-tile partial force is accumulated in f32 and folded into a
+//              (hi, lo) two-sum accumulator, so summation error does not grow
+//              with N.  Pair arithmetic uses packed f32x2 FMA/ADD/MUL (two
+//              targets per instruction) and one MUFU rsqrt per pair.
+//
+// Tiled kernels: a block owns NT*IPT consecutive targets (sorted order) and a
+// contiguous range of source tiles (grid.y = j-split).  Source tiles stream
+// into shared memory through a ring of cp.async.bulk copies completed on
+// mbarriers; one elected thread issues them.  Each block writes per-split
+// partial sums; a deterministic reduce kernel adds the splits in fixed order
+// and scatters the f64 result to the caller's order.
+#include "gvs_internal.cuh"
+
+namespace gvs {
+
+namespace {
+
+constexpr int TJ64 = 64;              // particles per f64 tile
+
+// ---------------------------------------------------------------------------
+// bounding box (f64 min/max), two passes
+// ---------------------------------------------------------------------------
+__global__ void k_bbox_part(const double *__restrict__ x, const double *__restrict__ y,
+                            const double *__restrict__ z, size_t n, double *__restrict__ part) {
+    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        double v[3] = {x[i], y[i], z[i]};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            mn[d] = fmin(mn[d], v[d]);
+            mx[d] = fmax(mx[d], v[d]);
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        for (int o = 16; o > 0; o >>= 1) {
+            mn[d] = fmin(mn[d], __shfl_xor_sync(0xFFFFFFFFu, mn[d], o));
+            mx[d] = fmax(mx[d], __shfl_xor_sync(0xFFFFFFFFu, mx[d], o));
+        }
+    }
+    __shared__ double s[32][6];
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0)
+        for (int d = 0; d < 3; ++d) { s[w][d] = mn[d]; s[w][3 + d] = mx[d]; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int ww = 1; ww < (int)(blockDim.x >> 5); ++ww)
+            for (int d = 0; d < 3; ++d) {
+                s[0][d] = fmin(s[0][d], s[ww][d]);
+                s[0][3 + d] = fmax(s[0][3 + d], s[ww][3 + d]);
+            }
+        for (int k = 0; k < 6; ++k) part[blockIdx.x * 6 + k] = s[0][k];
+    }
+}
+
+__global__ void k_bbox_final(double *part, int nparts) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int b = 1; b < nparts; ++b)
+        for (int d = 0; d < 3; ++d) {
+            part[d] = fmin(part[d], part[b * 6 + d]);
+            part[3 + d] = fmax(part[3 + d], part[b * 6 + 3 + d]);
+        }
+}
+
+// 21 bits per axis -> 63-bit Morton key.  The bounding box of a Plummer sphere
+// is set by a few outliers (r ~ 1e3 at N = 2^20), so coarse keys would leave
+// the whole core inside one cell; 21 bits keep core tiles compact.
+__device__ __forceinline__ uint64_t spread21(uint64_t v) {
+    v &= 0x1FFFFFull;
+    v = (v | (v << 32)) & 0x1F00000000FFFFull;
+    v = (v | (v << 16)) & 0x1F0000FF0000FFull;
+    v = (v | (v << 8)) & 0x100F00F00F00F00Full;
+    v = (v | (v << 4)) & 0x10C30C30C30C30C3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+__global__ void k_morton(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
+                         size_t n, const double *__restrict__ bb, uint64_t *__restrict__ keys,
+                         uint32_t *__restrict__ idx) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double ext = fmax(fmax(bb[3] - bb[0], bb[4] - bb[1]), bb[5] - bb[2]);
+    double inv = ext > 0.0 ? 2097151.99 / ext : 0.0;
+    uint64_t q[3];
+    double v[3] = {x[i], y[i], z[i]};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        double t = (v[d] - bb[d]) * inv;
+        t = fmin(fmax(t, 0.0), 2097151.0);
+        q[d] = (uint64_t)t;
+    }
+    keys[i] = spread21(q[0]) | (spread21(q[1]) << 1) | (spread21(q[2]) << 2);
+    idx[i] = (uint32_t)i;
+}
+
+// ---------------------------------------------------------------------------
+// packing of source tiles
+// ---------------------------------------------------------------------------
+// Tile t holds sorted slots [t*TJ, (t+1)*TJ) in tile_f4(TJ) = 2 + 2*TJ float4:
+// [0] centre hi (x,y,z,0), [1] centre lo, then per member (x,x,y,y)(z,z,m,m).
+// MIXED: centre = midpoint of the members' bounding box in f64, stored as an
+// f32 hi + lo pair whose exact f64 sum is the canonical centre; members are
+// f32 offsets from it.  FP32: centre 0, members as rounded absolute positions.
+// Members are stored twice per component so the pair kernel reads ready-made
+// f32x2 broadcast pairs.  Padding slots sit at the centre with zero mass.
+__host__ __device__ constexpr int tile_f4(int tj) { return 2 + 2 * tj; }
+
+template <int TJ, bool MIXED>
+__global__ void __launch_bounds__(TJ) k_pack32(const double *__restrict__ X, const double *__restrict__ Y,
+                                               const double *__restrict__ Z, const double *__restrict__ M,
+                                               const uint32_t *__restrict__ perm, size_t n,
+                                               float4 *__restrict__ pack) {
+    constexpr int TF4 = tile_f4(TJ);
+    const int t = blockIdx.x, tid = threadIdx.x;
+    const size_t s = (size_t)t * TJ + tid;
+    const bool valid = s < n;
+    const uint32_t o = perm[valid ? s : (size_t)t * TJ];
+    double p[3] = {X[o], Y[o], Z[o]};
+    const double mass = valid ? M[o] : 0.0;
+    double c[3] = {0.0, 0.0, 0.0};
+    float chi[3] = {0.f, 0.f, 0.f}, clo[3] = {0.f, 0.f, 0.f};
+    if (MIXED) {
+        __shared__ double red[TJ / 32][6];
+        double mn[3] = {p[0], p[1], p[2]}, mx[3] = {p[0], p[1], p[2]};
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+            for (int off = 16; off > 0; off >>= 1) {
+                mn[d] = fmin(mn[d], __shfl_xor_sync(0xFFFFFFFFu, mn[d], off));
+                mx[d] = fmax(mx[d], __shfl_xor_sync(0xFFFFFFFFu, mx[d], off));
+            }
+        if ((tid & 31) == 0)
+            for (int d = 0; d < 3; ++d) { red[tid >> 5][d] = mn[d]; red[tid >> 5][3 + d] = mx[d]; }
+        __syncthreads();
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            double lo = red[0][d], hi = red[0][3 + d];
+            for (int w = 1; w < TJ / 32; ++w) { lo = fmin(lo, red[w][d]); hi = fmax(hi, red[w][3 + d]); }
+            const double mid = 0.5 * (lo + hi);
+            chi[d] = __double2float_rn(mid);
+            clo[d] = __double2float_rn(mid - (double)chi[d]);
+            c[d] = (double)chi[d] + (double)clo[d];  // exact: the canonical centre
+        }
+    }
+    float off[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) off[d] = valid ? __double2float_rn(p[d] - c[d]) : 0.f;
+    float4 *tile = pack + (size_t)t * TF4;
+    if (tid == 0) {
+        tile[0] = make_float4(chi[0], chi[1], chi[2], 0.f);
+        tile[1] = make_float4(clo[0], clo[1], clo[2], 0.f);
+    }
+    const float mf = (float)mass;
+    tile[2 + 2 * tid] = make_float4(off[0], off[0], off[1], off[1]);
+    tile[3 + 2 * tid] = make_float4(off[2], off[2], mf, mf);
+}
+
+__global__ void k_pack64(const double *__restrict__ X, const double *__restrict__ Y, const double *__restrict__ Z,
+                         const double *__restrict__ M, const uint32_t *__restrict__ perm, size_t n, size_t npad,
+                         double4 *__restrict__ pack) {
+    size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= npad) return;
+    bool valid = s < n;
+    uint32_t o = perm[valid ? s : (s / TJ64) * TJ64 < n ? (s / TJ64) * TJ64 : 0];
+    pack[s] = make_double4(X[o], Y[o], Z[o], valid ? M[o] : 0.0);
+}
+
+// ---------------------------------------------------------------------------
+// f32x2 helpers (packed two-lane f32 arithmetic, sm_100+)
+// ---------------------------------------------------------------------------
+typedef unsigned long long f2;  // two f32 lanes in one 64-bit register pair
+
+__device__ __forceinline__ f2 pk(float a, float b) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void upk(f2 v, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+// (hi, lo) += v, lane-wise, with Knuth's two-sum (error-free for hi + v).
+__device__ __forceinline__ void two_sum2(f2 &hi, f2 &lo, f2 v) {
+    const f2 s = add2(hi, v);
+    const f2 bp = sub2(s, hi);
+    const f2 e = add2(sub2(hi, sub2(s, bp)), sub2(v, bp));
+    lo = add2(lo, e);
+    hi = s;
+}
+
+// ---------------------------------------------------------------------------
+// tiled f32 kernel (FP32 and MIXED)
+// ---------------------------------------------------------------------------
+// Block size NT equals the tile size, so target k (k = 0..IPT-1) of every
+// thread lies in tile blockIdx.x*IPT + k: the target-side centres are uniform
+// over the block and live in shared memory.  Thread t owns targets
+// i = blockIdx.x*NT*IPT + k*NT + t; NP = IPT/2 packed pairs (k = 2p, 2p+1).
+// Per source tile J and pair p: d = (c_I - c_J) from the hi/lo pairs, then
+// -(x_i - c_J) = -(d + off_i) as one f32x2 vector; per source particle j:
+// 3 ADD2 + 3 FMA2 (r^2) + 2 MUFU.RSQ + 3 MUL2 + 3 FMA2 (accumulate).
+template <int NT, int NP, int NSTAGE, bool MIXED, bool GUARD>
+__global__ void __launch_bounds__(NT) k_direct32(const float4 *__restrict__ pack, int ntiles, int tiles_per_split,
+                                                 float eps2, double *__restrict__ partial, size_t npad,
+                                                 unsigned *__restrict__ err) {
+    constexpr int TJ = NT;
+    constexpr int IPT = 2 * NP;
+    constexpr int TF4 = tile_f4(TJ);
+    constexpr unsigned TILE_BYTES = TF4 * 16;
+    extern __shared__ __align__(128) float4 smem[];
+    __shared__ __align__(8) uint64_t bar[NSTAGE];
+    __shared__ float4 ci[IPT][2];  // target-tile centres (hi, lo)
+
+    const int tid = threadIdx.x;
+    const size_t ibase = (size_t)blockIdx.x * NT * IPT;
+    const int t0 = blockIdx.y * tiles_per_split;
+    const int t1 = min(ntiles, t0 + tiles_per_split);
+    const int nt = max(0, t1 - t0);
+
+    if (tid == 0) {
+        for (int s = 0; s < NSTAGE; ++s) mbar_init(&bar[s], 1);
+        fence_mbar_init();
+    }
+    if (tid < IPT) {
+        const float4 *tp = pack + ((size_t)blockIdx.x * IPT + tid) * TF4;
+        ci[tid][0] = __ldg(tp);
+        ci[tid][1] = __ldg(tp + 1);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (int s = 0; s < NSTAGE && s < nt; ++s) {
+            mbar_arrive_expect_tx(&bar[s], TILE_BYTES);
+            bulk_g2s(smem + s * TF4, pack + (size_t)(t0 + s) * TF4, TILE_BYTES, &bar[s]);
+        }
+    }
+
+    // target offsets from their own tile centre, packed by pair
+    f2 ox[NP], oy[NP], oz[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        float v[2][3];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const float4 *tp = pack + ((size_t)blockIdx.x * IPT + 2 * p + q) * TF4;
+            const float4 a = __ldg(tp + 2 + 2 * tid), b = __ldg(tp + 3 + 2 * tid);
+            v[q][0] = a.x; v[q][1] = a.z; v[q][2] = b.x;
+        }
+        ox[p] = pk(v[0][0], v[1][0]);
+        oy[p] = pk(v[0][1], v[1][1]);
+        oz[p] = pk(v[0][2], v[1][2]);
+    }
+
+    f2 accx[NP], accy[NP], accz[NP], hx[NP], hy[NP], hz[NP], lx[NP], ly[NP], lz[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) accx[p] = accy[p] = accz[p] = hx[p] = hy[p] = hz[p] = lx[p] = ly[p] = lz[p] = 0ull;
+    const f2 e2 = pk(eps2, eps2);
+
+    int it = 0;
+    bool bail = false;
+    for (; it < nt; ++it) {
+        const int s = it % NSTAGE;
+        const unsigned parity = (unsigned)(it / NSTAGE) & 1u;
+        const bool ok = mbar_wait_bounded(&bar[s], parity, err);
+        if (__syncthreads_or(!ok)) { bail = true; break; }
+        const float4 *tile = smem + s * TF4;
+        f2 nx[NP], ny[NP], nz[NP];
+        if (MIXED) {
+            const float4 jh = tile[0], jl = tile[1];
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                const float4 h0 = ci[2 * p][0], l0 = ci[2 * p][1], h1 = ci[2 * p + 1][0], l1 = ci[2 * p + 1][1];
+                // -(c_I - c_J) per lane, then minus the target offset
+                const f2 dx = pk(-((h0.x - jh.x) + (l0.x - jl.x)), -((h1.x - jh.x) + (l1.x - jl.x)));
+                const f2 dy = pk(-((h0.y - jh.y) + (l0.y - jl.y)), -((h1.y - jh.y) + (l1.y - jl.y)));
+                const f2 dz = pk(-((h0.z - jh.z) + (l0.z - jl.z)), -((h1.z - jh.z) + (l1.z - jl.z)));
+                nx[p] = sub2(dx, ox[p]);
+                ny[p] = sub2(dy, oy[p]);
+                nz[p] = sub2(dz, oz[p]);
+            }
+        } else {
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                nx[p] = sub2(0ull, ox[p]);
+                ny[p] = sub2(0ull, oy[p]);
+                nz[p] = sub2(0ull, oz[p]);
+            }
+        }
+        const f2 *jd = reinterpret_cast<const f2 *>(tile + 2);
+#pragma unroll 4
+        for (int j = 0; j < TJ; ++j) {
+            const f2 xj = jd[4 * j + 0], yj = jd[4 * j + 1], zj = jd[4 * j + 2], mj = jd[4 * j + 3];
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                const f2 dx = add2(xj, nx[p]);
+                const f2 dy = add2(yj, ny[p]);
+                const f2 dz = add2(zj, nz[p]);
+                f2 r2 = fma2(dx, dx, e2);
+                r2 = fma2(dy, dy, r2);
+                r2 = fma2(dz, dz, r2);
+                float ra, rb;
+                upk(r2, ra, rb);
+                if (GUARD) { ra = fmaxf(ra, 1e-24f); rb = fmaxf(rb, 1e-24f); }
+                const f2 ri = pk(rsqrt_approx(ra), rsqrt_approx(rb));
+                f2 sm = mul2(mj, ri);
+                const f2 ri2 = mul2(ri, ri);
+                sm = mul2(sm, ri2);
+                accx[p] = fma2(sm, dx, accx[p]);
+                accy[p] = fma2(sm, dy, accy[p]);
+                accz[p] = fma2(sm, dz, accz[p]);
+            }
+        }
+        if (MIXED) {
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                two_sum2(hx[p], lx[p], accx[p]);
+                two_sum2(hy[p], ly[p], accy[p]);
+                two_sum2(hz[p], lz[p], accz[p]);
+                accx[p] = accy[p] = accz[p] = 0ull;
+            }
+        }
+        __syncthreads();  // every thread is done with stage s
+        if (tid == 0 && it + NSTAGE < nt) {
+            mbar_arrive_expect_tx(&bar[s], TILE_BYTES);
+            bulk_g2s(smem + s * TF4, pack + (size_t)(t0 + it + NSTAGE) * TF4, TILE_BYTES, &bar[s]);
+        }
+    }
+    if (bail) {
+        // drain copies still in flight before the CTA exits (bounded)
+        if (tid == 0)
+            for (int j = it; j < nt && j < it + NSTAGE; ++j)
+                mbar_wait_bounded(&bar[j % NSTAGE], (unsigned)(j / NSTAGE) & 1u, err);
+        return;
+    }
+    double *dst = partial + (size_t)blockIdx.y * 3 * npad;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        float v[3][2][2];  // component, lane, (hi, lo)
+        if (MIXED) {
+            upk(hx[p], v[0][0][0], v[0][1][0]); upk(lx[p], v[0][0][1], v[0][1][1]);
+            upk(hy[p], v[1][0][0], v[1][1][0]); upk(ly[p], v[1][0][1], v[1][1][1]);
+            upk(hz[p], v[2][0][0], v[2][1][0]); upk(lz[p], v[2][0][1], v[2][1][1]);
+        } else {
+            upk(accx[p], v[0][0][0], v[0][1][0]);
+            upk(accy[p], v[1][0][0], v[1][1][0]);
+            upk(accz[p], v[2][0][0], v[2][1][0]);
+            for (int c = 0; c < 3; ++c) v[c][0][1] = v[c][1][1] = 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const size_t i = ibase + (size_t)(2 * p + q) * NT + tid;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) dst[(size_t)c * npad + i] = (double)v[c][q][0] + (double)v[c][q][1];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// tiled f64 kernel (FP64): same tiling, double4 tiles, f64 rsqrt
+// ---------------------------------------------------------------------------
+template <int NT, int IPT, int NSTAGE, bool GUARD>
+__global__ void __launch_bounds__(NT) k_direct64(const double4 *__restrict__ pack, int ntiles, int tiles_per_split,
+                                                 double eps2, double *__restrict__ partial, size_t npad,
+                                                 unsigned *__restrict__ err) {
+    constexpr unsigned TILE_BYTES = TJ64 * 32;
+    extern __shared__ __align__(128) double4 smem64[];
+    __shared__ __align__(8) uint64_t bar[NSTAGE];
+    const int tid = threadIdx.x;
+    const size_t ibase = (size_t)blockIdx.x * NT * IPT;
+    const int t0 = blockIdx.y * tiles_per_split;
+    const int t1 = min(ntiles, t0 + tiles_per_split);
+    const int nt = max(0, t1 - t0);
+    double xi[IPT], yi[IPT], zi[IPT], ax[IPT], ay[IPT], az[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        double4 v = pack[ibase + (size_t)k * NT + tid];
+        xi[k] = v.x; yi[k] = v.y; zi[k] = v.z;
+        ax[k] = ay[k] = az[k] = 0.0;
+    }
+    if (tid == 0) {
+        for (int s = 0; s < NSTAGE; ++s) mbar_init(&bar[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0)
+        for (int s = 0; s < NSTAGE && s < nt; ++s) {
+            mbar_arrive_expect_tx(&bar[s], TILE_BYTES);
+            bulk_g2s(smem64 + s * TJ64, pack + (size_t)(t0 + s) * TJ64, TILE_BYTES, &bar[s]);
+        }
+    int it = 0;
+    bool bail = false;
+    for (; it < nt; ++it) {
+        const int s = it % NSTAGE;
+        bool ok = mbar_wait_bounded(&bar[s], (unsigned)(it / NSTAGE) & 1u, err);
+        if (__syncthreads_or(!ok)) { bail = true; break; }
+        const double4 *tile = smem64 + s * TJ64;
+#pragma unroll 2
+        for (int j = 0; j < TJ64; ++j) {
+            const double4 q = tile[j];
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                double dx = q.x - xi[k], dy = q.y - yi[k], dz = q.z - zi[k];
+                double r2 = fma(dz, dz, fma(dy, dy, fma(dx, dx, eps2)));
+                if (GUARD) r2 = fmax(r2, 1e-200);
+                double ri = rsqrt(r2);
+                double sm = q.w * ri * ri * ri;
+                ax[k] = fma(sm, dx, ax[k]);
+                ay[k] = fma(sm, dy, ay[k]);
+                az[k] = fma(sm, dz, az[k]);
+            }
+        }
+        __syncthreads();
+        if (tid == 0 && it + NSTAGE < nt) {
+            mbar_arrive_expect_tx(&bar[s], TILE_BYTES);
+            bulk_g2s(smem64 + s * TJ64, pack + (size_t)(t0 + it + NSTAGE) * TJ64, TILE_BYTES, &bar[s]);
+        }
+    }
+    if (bail) {
+        if (tid == 0)
+            for (int j = it; j < nt && j < it + NSTAGE; ++j)
+                mbar_wait_bounded(&bar[j % NSTAGE], (unsigned)(j / NSTAGE) & 1u, err);
+        return;
+    }
+    double *dst = partial + (size_t)blockIdx.y * 3 * npad;
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        size_t i = ibase + (size_t)k * NT + tid;
+        dst[i] = ax[k];
+        dst[npad + i] = ay[k];
+        dst[2 * npad + i] = az[k];
+    }
+}
+
+// Adds the nsplit partials in fixed order and scatters to caller order.
+__global__ void k_reduce(const double *__restrict__ partial, int nsplit, size_t npad, size_t n,
+                         const uint32_t *__restrict__ perm, double *__restrict__ AX, double *__restrict__ AY,
+                         double *__restrict__ AZ, int accumulate) {
+    size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    double r[3] = {0.0, 0.0, 0.0};
+    for (int js = 0; js < nsplit; ++js)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) r[c] += partial[((size_t)js * 3 + c) * npad + s];
+    uint32_t o = perm[s];
+    if (accumulate) {
+        AX[o] += r[0]; AY[o] += r[1]; AZ[o] += r[2];
+    } else {
+        AX[o] = r[0]; AY[o] = r[1]; AZ[o] = r[2];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FP64_EXACT: the reference's arithmetic, one target per thread
+// ---------------------------------------------------------------------------
+constexpr int EX_NT = 128;
+
+__global__ void __launch_bounds__(EX_NT) k_direct_exact(const double *__restrict__ X, const double *__restrict__ Y,
+                                                        const double *__restrict__ Z, const double *__restrict__ M,
+                                                        size_t n, double eps2, double *__restrict__ AX,
+                                                        double *__restrict__ AY, double *__restrict__ AZ,
+                                                        int accumulate, const int64_t *__restrict__ targets,
+                                                        size_t ntargets) {
+    __shared__ double4 tile[EX_NT];
+    const size_t k = (size_t)blockIdx.x * EX_NT + threadIdx.x;
+    const size_t nt = targets ? ntargets : n;
+    const bool active = k < nt;
+    const size_t i = active ? (targets ? (size_t)targets[k] : k) : 0;
+    const double xi = X[i], yi = Y[i], zi = Z[i];
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (size_t j0 = 0; j0 < n; j0 += EX_NT) {
+        const size_t jl = j0 + threadIdx.x;
+        __syncthreads();
+        if (jl < n) tile[threadIdx.x] = make_double4(X[jl], Y[jl], Z[jl], M[jl]);
+        __syncthreads();
+        const int jn = (int)min((size_t)EX_NT, n - j0);
+        for (int jj = 0; jj < jn; ++jj) {
+            const size_t j = j0 + jj;
+            if (j == i) continue;
+            const double4 q = tile[jj];
+            const double dx = __dsub_rn(q.x, xi), dy = __dsub_rn(q.y, yi), dz = __dsub_rn(q.z, zi);
+            const double r2 = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)),
+                                        eps2);
+            const double inv_r3 = __ddiv_rn(1.0, __dmul_rn(r2, __dsqrt_rn(r2)));
+            const double f = __dmul_rn(q.w, inv_r3);
+            sx = __dadd_rn(sx, __dmul_rn(f, dx));
+            sy = __dadd_rn(sy, __dmul_rn(f, dy));
+            sz = __dadd_rn(sz, __dmul_rn(f, dz));
+        }
+    }
+    if (!active) return;
+    const size_t o = targets ? k : i;
+    if (accumulate) {
+        AX[o] = __dadd_rn(AX[o], sx); AY[o] = __dadd_rn(AY[o], sy); AZ[o] = __dadd_rn(AZ[o], sz);
+    } else {
+        AX[o] = sx; AY[o] = sy; AZ[o] = sz;
+    }
+}
+
+template <class T>
+void set_smem(T kernel, int bytes) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+// Morton order of the resident positions: c->perm[s] = caller index of sorted slot s.
+gvs_status spatial_order(Ctx *c) {
+    const size_t n = c->n;
+    const int nb = std::min(c->num_sms * 4, std::max(1, ceil_div((long long)n, 256)));
+    GVS_CUDA(c, ensure(c, c->bbox_part, (size_t)nb * 6 * sizeof(double)));
+    GVS_CUDA(c, ensure(c, c->keys, n * 8));
+    GVS_CUDA(c, ensure(c, c->keys_alt, n * 8));
+    GVS_CUDA(c, ensure(c, c->perm, n * 4));
+    GVS_CUDA(c, ensure(c, c->perm_alt, n * 4));
+    double *bb = as<double>(c->bbox_part);
+    k_bbox_part<<<nb, 256, 0, c->stream>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z), n, bb);
+    k_bbox_final<<<1, 32, 0, c->stream>>>(bb, nb);
+    k_morton<<<ceil_div((long long)n, 256), 256, 0, c->stream>>>(as<double>(c->x), as<double>(c->y),
+                                                                  as<double>(c->z), n, bb, as<uint64_t>(c->keys),
+                                                                  as<uint32_t>(c->perm));
+    c->prof.launches += 3;
+    GVS_TRY(check_launch(c, "morton keys"));
+    uint64_t *ko;
+    uint32_t *vo;
+    GVS_TRY(radix_sort_u64(c, as<uint64_t>(c->keys), as<uint32_t>(c->perm), as<uint64_t>(c->keys_alt),
+                           as<uint32_t>(c->perm_alt), n, 0, 64, &ko, &vo));
+    if (vo != as<uint32_t>(c->perm)) {
+        std::swap(c->perm, c->perm_alt);
+        std::swap(c->keys, c->keys_alt);
+    }
+    return GVS_OK;
+}
+
+namespace {
+
+struct Launch32 {
+    int nt, np, nsplit;
+};
+
+// Chooses the j-split so that the grid covers every SM several times.
+int auto_split(Ctx *c, int iblocks, int ntiles, int blocks_per_sm) {
+    int want = c->num_sms * blocks_per_sm * 4;
+    int ns = std::max(1, (want + iblocks - 1) / iblocks);
+    ns = std::min(ns, std::max(1, ntiles / 2));
+    return std::min(ns, 64);
+}
+
+template <int NT, int NP, bool MIXED, bool GUARD>
+gvs_status launch32_t(Ctx *c, float eps2, int nsplit_req, double **partial_out, int *nsplit_out, size_t *npad_out) {
+    constexpr int NSTAGE = 4;
+    constexpr int TJ = NT;
+    constexpr int IPT = 2 * NP;
+    constexpr int TF4 = tile_f4(TJ);
+    const size_t n = c->n;
+    const int ntiles = ceil_div((long long)n, TJ);
+    const size_t per_block = (size_t)NT * IPT;
+    const int iblocks = ceil_div((long long)n, (long long)per_block);
+    const size_t npad = (size_t)iblocks * per_block;
+    const int ntiles_pad = (int)(npad / TJ);  // >= ntiles
+    GVS_CUDA(c, ensure(c, c->jpack32, (size_t)ntiles_pad * TF4 * sizeof(float4)));
+    k_pack32<TJ, MIXED><<<ntiles, TJ, 0, c->stream>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z),
+                                                       as<double>(c->m), as<uint32_t>(c->perm), n,
+                                                       as<float4>(c->jpack32));
+    c->prof.launches += 1;
+    if (ntiles_pad > ntiles)  // target-side padding tiles: zero mass at the origin, never reduced
+        GVS_CUDA(c, cudaMemsetAsync(as<float4>(c->jpack32) + (size_t)ntiles * TF4, 0,
+                                    (size_t)(ntiles_pad - ntiles) * TF4 * sizeof(float4), c->stream));
+    const int smem = NSTAGE * TF4 * (int)sizeof(float4);
+    auto kern = k_direct32<NT, NP, NSTAGE, MIXED, GUARD>;
+    set_smem(kern, smem);
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
+    const int nsplit = nsplit_req > 0 ? std::min(nsplit_req, ntiles) : auto_split(c, iblocks, ntiles, std::max(1, per_sm));
+    const int tps = ceil_div(ntiles, nsplit);
+    const int nsplit_eff = ceil_div(ntiles, tps);
+    GVS_CUDA(c, ensure(c, c->partial, (size_t)nsplit_eff * 3 * npad * sizeof(double)));
+    dim3 grid(iblocks, nsplit_eff);
+    if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], c->stream));
+    kern<<<grid, NT, smem, c->stream>>>(as<float4>(c->jpack32), ntiles, tps, eps2, as<double>(c->partial), npad,
+                                        err_ptr(c));
+    c->prof.launches += 1;
+    GVS_TRY(check_launch(c, "direct f32 kernel"));
+    if (c->prof.on) {
+        GVS_CUDA(c, cudaEventRecord(c->prof.ev[1], c->stream));
+        GVS_CUDA(c, cudaEventSynchronize(c->prof.ev[1]));
+        float ms = 0.f;
+        GVS_CUDA(c, cudaEventElapsedTime(&ms, c->prof.ev[0], c->prof.ev[1]));
+        c->prof.force_ms += ms;
+        c->prof.force_launches += 1;
+        c->prof.force_flops += 20.0 * (double)n * (double)n;
+        c->prof.force_bytes += (double)nsplit_eff * (double)npad * 24.0 + (double)iblocks * nsplit_eff * tps *
+                                                                              (double)TF4 * 16.0;
+    }
+    *partial_out = as<double>(c->partial);
+    *nsplit_out = nsplit_eff;
+    *npad_out = npad;
+    return GVS_OK;
+}
+
+template <bool MIXED, bool GUARD>
+gvs_status launch32(Ctx *c, float eps2, double **partial, int *nsplit, size_t *npad) {
+    const long long bucket = 63 - __builtin_clzll((unsigned long long)std::max<size_t>(c->n, 1));
+    for (const auto &e : c->tune_cache)
+        if (e.first == bucket) c->tune = e.second;
+    const Tune &t = c->tune;
+    if (t.nthreads == 128 && t.ipt == 4) return launch32_t<128, 2, MIXED, GUARD>(c, eps2, t.nsplit, partial, nsplit, npad);
+    if (t.nthreads == 128 && t.ipt == 8) return launch32_t<128, 4, MIXED, GUARD>(c, eps2, t.nsplit, partial, nsplit, npad);
+    if (t.nthreads == 256 && t.ipt == 8) return launch32_t<256, 4, MIXED, GUARD>(c, eps2, t.nsplit, partial, nsplit, npad);
+    if (t.nthreads == 256 && t.ipt == 2) return launch32_t<256, 1, MIXED, GUARD>(c, eps2, t.nsplit, partial, nsplit, npad);
+    return launch32_t<256, 2, MIXED, GUARD>(c, eps2, t.nsplit, partial, nsplit, npad);
+}
+
+gvs_status launch64(Ctx *c, double eps2, double **partial_out, int *nsplit_out, size_t *npad_out) {
+    constexpr int NT = 128, IPT = 2, NSTAGE = 4;
+    const size_t n = c->n;
+    const size_t per_block = (size_t)NT * IPT;
+    const int iblocks = ceil_div((long long)n, (long long)per_block);
+    const size_t npad = (size_t)iblocks * per_block;
+    const int ntiles = ceil_div((long long)n, TJ64);
+    const size_t nslots = std::max(npad, (size_t)ntiles * TJ64);
+    GVS_CUDA(c, ensure(c, c->jpack64, nslots * sizeof(double4)));
+    k_pack64<<<ceil_div((long long)nslots, 256), 256, 0, c->stream>>>(as<double>(c->x), as<double>(c->y),
+                                                                      as<double>(c->z), as<double>(c->m),
+                                                                      as<uint32_t>(c->perm), n, nslots,
+                                                                      as<double4>(c->jpack64));
+    c->prof.launches += 1;
+    const int nsplit = auto_split(c, iblocks, ntiles, 4);
+    const int tps = ceil_div(ntiles, nsplit);
+    const int nsplit_eff = ceil_div(ntiles, tps);
+    GVS_CUDA(c, ensure(c, c->partial, (size_t)nsplit_eff * 3 * npad * sizeof(double)));
+    const int smem = NSTAGE * TJ64 * (int)sizeof(double4);
+    auto kern = eps2 > 0.0 ? k_direct64<NT, IPT, NSTAGE, false> : k_direct64<NT, IPT, NSTAGE, true>;
+    set_smem(kern, smem);
+    if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], c->stream));
+    kern<<<dim3(iblocks, nsplit_eff), NT, smem, c->stream>>>(as<double4>(c->jpack64), ntiles, tps, eps2,
+                                                              as<double>(c->partial), npad, err_ptr(c));
+    c->prof.launches += 1;
+    GVS_TRY(check_launch(c, "direct f64 kernel"));
+    if (c->prof.on) {
+        GVS_CUDA(c, cudaEventRecord(c->prof.ev[1], c->stream));
+        GVS_CUDA(c, cudaEventSynchronize(c->prof.ev[1]));
+        float ms = 0.f;
+        GVS_CUDA(c, cudaEventElapsedTime(&ms, c->prof.ev[0], c->prof.ev[1]));
+        c->prof.force_ms += ms;
+        c->prof.force_launches += 1;
+        c->prof.force_flops += 20.0 * (double)n * (double)n;
+    }
+    *partial_out = as<double>(c->partial);
+    *nsplit_out = nsplit_eff;
+    *npad_out = npad;
+    return GVS_OK;
+}
+
+}  // namespace
+
+gvs_status direct_forces(Ctx *c, int precision, double eps, bool accumulate) {
+    const size_t n = c->n;
+    if (n == 0) return GVS_OK;
+    const double eps2 = eps * eps;
+    if (precision == GVS_PREC_FP64_EXACT) {
+        if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], c->stream));
+        k_direct_exact<<<ceil_div((long long)n, EX_NT), EX_NT, 0, c->stream>>>(
+            as<double>(c->x), as<double>(c->y), as<double>(c->z), as<double>(c->m), n, eps2, as<double>(c->ax),
+            as<double>(c->ay), as<double>(c->az), accumulate ? 1 : 0, nullptr, 0);
+        c->prof.launches += 1;
+        GVS_TRY(check_launch(c, "direct exact kernel"));
+        if (c->prof.on) {
+            GVS_CUDA(c, cudaEventRecord(c->prof.ev[1], c->stream));
+            GVS_CUDA(c, cudaEventSynchronize(c->prof.ev[1]));
+            float ms = 0.f;
+            GVS_CUDA(c, cudaEventElapsedTime(&ms, c->prof.ev[0], c->prof.ev[1]));
+            c->prof.force_ms += ms;
+            c->prof.force_launches += 1;
+            c->prof.force_flops += 20.0 * (double)n * (double)(n - 1);
+        }
+        return GVS_OK;
+    }
+    GVS_TRY(spatial_order(c));
+    double *partial = nullptr;
+    int nsplit = 0;
+    size_t npad = 0;
+    if (precision == GVS_PREC_FP64) {
+        GVS_TRY(launch64(c, eps2, &partial, &nsplit, &npad));
+    } else {
+        const float e2 = (float)eps2;
+        const bool guard = !(e2 > 0.f);
+        const bool mixed = precision == GVS_PREC_MIXED;
+        if (mixed && !guard) GVS_TRY((launch32<true, false>(c, e2, &partial, &nsplit, &npad)));
+        else if (mixed) GVS_TRY((launch32<true, true>(c, e2, &partial, &nsplit, &npad)));
+        else if (!guard) GVS_TRY((launch32<false, false>(c, e2, &partial, &nsplit, &npad)));
+        else GVS_TRY((launch32<false, true>(c, e2, &partial, &nsplit, &npad)));
+    }
+    k_reduce<<<ceil_div((long long)n, 256), 256, 0, c->stream>>>(partial, nsplit, npad, n, as<uint32_t>(c->perm),
+                                                                  as<double>(c->ax), as<double>(c->ay),
+                                                                  as<double>(c->az), accumulate ? 1 : 0);
+    c->prof.launches += 1;
+    return check_launch(c, "direct reduce");
+}
+
+// Times every compiled (block size, targets per thread) variant of the f32
+// pair kernel on the resident state and keeps the fastest for this N bucket.
+gvs_status autotune_direct(Ctx *c, int precision, double eps, int *best_nt, int *best_ipt, double *best_ms) {
+    static const int cand[][2] = {{256, 4}, {256, 2}, {256, 8}, {128, 4}, {128, 8}};
+    const bool was_on = c->prof.on;
+    Tune best = c->tune;
+    double best_t = 1e300;
+    for (const auto &cd : cand) {
+        c->tune.nthreads = cd[0];
+        c->tune.ipt = cd[1];
+        c->tune.nsplit = 0;
+        GVS_TRY(direct_forces(c, precision, eps, false));  // warm (also builds the order)
+        c->prof.on = true;
+        const double ms0 = c->prof.force_ms;
+        for (int r = 0; r < 2; ++r) GVS_TRY(direct_forces(c, precision, eps, false));
+        const double t = (c->prof.force_ms - ms0) / 2.0;
+        c->prof.on = was_on;
+        if (t < best_t) {
+            best_t = t;
+            best = c->tune;
+        }
+    }
+    c->tune = best;
+    long long bucket = 63 - __builtin_clzll((unsigned long long)std::max<size_t>(c->n, 1));
+    bool found = false;
+    for (auto &e : c->tune_cache)
+        if (e.first == bucket) { e.second = best; found = true; }
+    if (!found) c->tune_cache.push_back({bucket, best});
+    if (best_nt) *best_nt = best.nthreads;
+    if (best_ipt) *best_ipt = best.ipt;
+    if (best_ms) *best_ms = best_t;
+    return GVS_OK;
+}
+
+// FP64_EXACT accelerations of selected targets (accuracy probes at large N).
+gvs_status direct_forces_subset(Ctx *c, int precision, double eps, const int64_t *idx_dev, size_t nidx,
+                                double *out_dev) {
+    (void)precision;
+    if (nidx == 0) return GVS_OK;
+    k_direct_exact<<<ceil_div((long long)nidx, EX_NT), EX_NT, 0, c->stream>>>(
+        as<double>(c->x), as<double>(c->y), as<double>(c->z), as<double>(c->m), c->n, eps * eps, out_dev,
+        out_dev + nidx, out_dev + 2 * nidx, 0, idx_dev, nidx);
+    c->prof.launches += 1;
+    return check_launch(c, "direct subset kernel");
+}
+
+}  // namespace gvs

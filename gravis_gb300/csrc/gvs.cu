@@ -1,0 +1,552 @@
+// gvs.cu -- context management and the C ABI entry points of libgvs.so.
+//
+// The entry points mirror sim-core's hot-path interfaces:
+//   GravitySolver::compute_accelerations  (crates/sim-core/src/gravity.rs:6-10)
+//   LeapfrogKDK::step                      (crates/sim-core/src/integrator.rs:42-76)
+//   diagnostics::compute                   (crates/sim-core/src/diagnostics.rs:37-48)
+// Every call validates its arguments before touching the device, runs on the
+// context's stream, and reports failures as a gvs_status plus a message.
+#include <stdarg.h>
+#include <stdlib.h>
+
+#include <algorithm>
+
+#include "gvs_internal.cuh"
+
+namespace gvs {
+
+static char g_last_error[512] = "";
+
+cudaError_t ensure(Ctx *c, DevBuf &b, size_t bytes) {
+    if (bytes <= b.bytes && b.ptr) return cudaSuccess;
+    if (c->fault_kind == 1) return cudaErrorMemoryAllocation;  // injected
+    if (b.ptr) {
+        cudaError_t e = cudaFree(b.ptr);  // synchronises: no kernel still uses it
+        if (e != cudaSuccess) return e;
+        b.ptr = nullptr;
+        b.bytes = 0;
+    }
+    size_t want = std::max<size_t>(bytes, 256);
+    cudaError_t e = cudaMalloc(&b.ptr, want);
+    if (e != cudaSuccess) {
+        b.ptr = nullptr;
+        return e;
+    }
+    b.bytes = want;
+    return cudaSuccess;
+}
+
+gvs_status fail(Ctx *c, gvs_status s, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->last_error = buf;
+    snprintf(g_last_error, sizeof g_last_error, "%s", buf);
+    return s;
+}
+
+gvs_status cuda_fail(Ctx *c, cudaError_t e, const char *what) {
+    gvs_status s = (e == cudaErrorMemoryAllocation) ? GVS_ERR_OOM : GVS_ERR_LAUNCH;
+    if (c && c->fault_kind == 1 && e == cudaErrorMemoryAllocation) s = GVS_ERR_INJECTED;
+    return fail(c, s, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+gvs_status check_launch(Ctx *c, const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, what);
+    return GVS_OK;
+}
+
+gvs_status read_device_errors(Ctx *c) {
+    unsigned flags = 0;
+    GVS_CUDA(c, cudaMemcpyAsync(&flags, c->err_word.ptr, sizeof flags, cudaMemcpyDeviceToHost, c->stream));
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (flags) {
+        GVS_CUDA(c, cudaMemsetAsync(c->err_word.ptr, 0, sizeof(unsigned), c->stream));
+        gvs_status s = (flags & (DERR_MBAR_TIMEOUT | DERR_SPIN_TIMEOUT)) ? GVS_ERR_TIMEOUT : GVS_ERR_DEVICE;
+        return fail(c, s, "device error word 0x%x (1 mbarrier timeout, 2 stack overflow, 4 neighbour overflow, "
+                          "8 non-finite, 16 tree, 32 bounds, 64 queue timeout)", flags);
+    }
+    return GVS_OK;
+}
+
+gvs_status gravity(Ctx *c, int algo, int precision, double eps, double theta, bool accumulate) {
+    if (c->fault_kind == 2) return fail(c, GVS_ERR_INJECTED, "injected launch fault");
+    switch (algo) {
+    case GVS_ALGO_NONE:
+        return accumulate ? GVS_OK : clear_acc(c);
+    case GVS_ALGO_DIRECT:
+        return direct_forces(c, precision, eps, accumulate);
+    case GVS_ALGO_BH:
+        return bh_forces(c, eps, theta, precision, accumulate);
+    default:
+        return fail(c, GVS_ERR_INVALID_ARG, "unknown gravity algorithm %d", algo);
+    }
+}
+
+static gvs_status upload(Ctx *c, DevBuf &b, const void *src, size_t bytes) {
+    GVS_CUDA(c, ensure(c, b, bytes));
+    if (src) GVS_CUDA(c, cudaMemcpyAsync(b.ptr, src, bytes, cudaMemcpyHostToDevice, c->stream));
+    return GVS_OK;
+}
+
+static gvs_status download(Ctx *c, void *dst, DevBuf &b, size_t bytes) {
+    if (!dst || bytes == 0) return GVS_OK;
+    GVS_CUDA(c, cudaMemcpyAsync(dst, b.ptr, bytes, cudaMemcpyDeviceToHost, c->stream));
+    return GVS_OK;
+}
+
+static gvs_status alloc_state(Ctx *c, size_t n) {
+    const size_t b = std::max<size_t>(n, 1) * sizeof(double);
+    DevBuf *f64s[] = {&c->x, &c->y, &c->z, &c->vx, &c->vy, &c->vz, &c->ax, &c->ay, &c->az, &c->m,
+                      &c->u, &c->h, &c->alpha, &c->rho, &c->pres, &c->cs, &c->du_dt, &c->omega,
+                      &c->div_v, &c->max_mu, &c->dalpha_dt};
+    for (DevBuf *d : f64s) GVS_CUDA(c, ensure(c, *d, b));
+    GVS_CUDA(c, ensure(c, c->ptype, std::max<size_t>(n, 1)));
+    c->n = n;
+    return GVS_OK;
+}
+
+static bool nan_fault_due(Ctx *c) {
+    return c->fault_kind == 3 && c->fault_step >= 0 && c->step_counter == c->fault_step;
+}
+
+// One KDK step on the resident state (integrator.rs:42-76).
+static gvs_status kdk_one(Ctx *c, int algo, int precision, double eps, double theta, double dt) {
+    const double half = 0.5 * dt;
+    GVS_TRY(kick_drift(c, half, dt));  // half-kick, drift, clear_accelerations
+    GVS_TRY(gravity(c, algo, precision, eps, theta, /*accumulate=*/false));
+    GVS_TRY(kick(c, half));
+    c->step_counter++;
+    return GVS_OK;
+}
+
+}  // namespace gvs
+
+using namespace gvs;
+
+struct gvs_ctx : public Ctx {};
+
+static gvs_status check_ctx(const gvs_ctx *ctx) {
+    if (!ctx) {
+        snprintf(g_last_error, sizeof g_last_error, "null context");
+        return GVS_ERR_INVALID_ARG;
+    }
+    return GVS_OK;
+}
+
+extern "C" {
+
+const char *gvs_version(void) { return "gravis-gb300 0.1.0 (sm_103a)"; }
+
+gvs_status gvs_create(gvs_ctx **out, int device) {
+    if (!out) return fail(nullptr, GVS_ERR_INVALID_ARG, "gvs_create: out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(nullptr, GVS_ERR_NO_DEVICE, "no CUDA device (%s)", cudaGetErrorString(e));
+    if (device < 0 || device >= ndev) return fail(nullptr, GVS_ERR_INVALID_ARG, "device %d out of range", device);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess)
+        return fail(nullptr, GVS_ERR_NO_DEVICE, "cannot query device %d", device);
+    if (prop.major < 10)
+        return fail(nullptr, GVS_ERR_NO_DEVICE, "device %d is sm_%d%d; this build targets sm_103a", device,
+                    prop.major, prop.minor);
+    if (cudaSetDevice(device) != cudaSuccess) return fail(nullptr, GVS_ERR_NO_DEVICE, "cudaSetDevice failed");
+    gvs_ctx *c = new gvs_ctx();
+    c->device = device;
+    c->num_sms = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&c->prof.ev[0]) != cudaSuccess || cudaEventCreate(&c->prof.ev[1]) != cudaSuccess) {
+        delete c;
+        return fail(nullptr, GVS_ERR_LAUNCH, "stream/event creation failed");
+    }
+    if (ensure(c, c->err_word, 256) != cudaSuccess ||
+        cudaMemsetAsync(c->err_word.ptr, 0, 256, c->stream) != cudaSuccess) {
+        gvs_destroy(c);
+        return fail(nullptr, GVS_ERR_OOM, "cannot allocate the device error word");
+    }
+    if (const char *f = getenv("GVS_FAULT")) gvs_set_fault(c, f);
+    *out = c;
+    return GVS_OK;
+}
+
+gvs_status gvs_destroy(gvs_ctx *c) {
+    if (!c) return GVS_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    tree_free(c);
+    sph_free(c);
+    DevBuf *all[] = {&c->x, &c->y, &c->z, &c->vx, &c->vy, &c->vz, &c->ax, &c->ay, &c->az, &c->m,
+                     &c->ptype, &c->u, &c->h, &c->alpha, &c->rho, &c->pres, &c->cs, &c->du_dt, &c->omega,
+                     &c->div_v, &c->max_mu, &c->dalpha_dt, &c->keys, &c->keys_alt, &c->perm, &c->perm_alt,
+                     &c->sort_hist, &c->bbox_part, &c->jpack32, &c->jpack64, &c->partial, &c->scratch_a,
+                     &c->scratch_b, &c->err_word, &c->red_part, &c->l2_flush};
+    for (DevBuf *b : all)
+        if (b->ptr) cudaFree(b->ptr);
+    if (c->pinned) cudaFreeHost(c->pinned);
+    for (int k = 0; k < 2; ++k)
+        if (c->prof.ev[k]) cudaEventDestroy(c->prof.ev[k]);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return GVS_OK;
+}
+
+gvs_status gvs_last_error(const gvs_ctx *c, char *buf, size_t len) {
+    if (!buf || len == 0) return GVS_ERR_INVALID_ARG;
+    const char *msg = c ? c->last_error.c_str() : g_last_error;
+    snprintf(buf, len, "%s", msg);
+    return GVS_OK;
+}
+
+gvs_status gvs_set_fault(gvs_ctx *c, const char *spec) {
+    GVS_TRY(check_ctx(c));
+    if (!spec) return fail(c, GVS_ERR_INVALID_ARG, "fault spec is NULL");
+    if (!strcmp(spec, "none") || !*spec) {
+        c->fault_kind = 0;
+    } else if (!strcmp(spec, "alloc")) {
+        c->fault_kind = 1;
+    } else if (!strcmp(spec, "launch")) {
+        c->fault_kind = 2;
+    } else if (!strncmp(spec, "nan@", 4)) {
+        char *end = nullptr;
+        long long k = strtoll(spec + 4, &end, 10);
+        if (!end || *end || k < 0) return fail(c, GVS_ERR_INVALID_ARG, "bad fault spec '%s'", spec);
+        c->fault_kind = 3;
+        c->fault_step = k;
+        c->step_counter = 0;
+    } else {
+        return fail(c, GVS_ERR_INVALID_ARG, "unknown fault spec '%s' (none|alloc|launch|nan@K)", spec);
+    }
+    return GVS_OK;
+}
+
+gvs_status gvs_sync(gvs_ctx *c) {
+    GVS_TRY(check_ctx(c));
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return read_device_errors(c);
+}
+
+gvs_status gvs_device_errors(gvs_ctx *c, unsigned *flags) {
+    GVS_TRY(check_ctx(c));
+    if (!flags) return fail(c, GVS_ERR_INVALID_ARG, "flags is NULL");
+    GVS_CUDA(c, cudaMemcpyAsync(flags, c->err_word.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    GVS_CUDA(c, cudaMemsetAsync(c->err_word.ptr, 0, sizeof(unsigned), c->stream));
+    return GVS_OK;
+}
+
+size_t gvs_count(const gvs_ctx *c) { return c ? c->n : 0; }
+
+gvs_status gvs_set_state(gvs_ctx *c, size_t n, const double *x, const double *y, const double *z, const double *vx,
+                         const double *vy, const double *vz, const double *mass, const uint8_t *ptype,
+                         const double *u, const double *h, const double *alpha) {
+    GVS_TRY(check_ctx(c));
+    if (!x || !y || !z || !vx || !vy || !vz || !mass) return fail(c, GVS_ERR_INVALID_ARG, "null state array");
+    if (n > 0xFFFFFFF0ull) return fail(c, GVS_ERR_INVALID_ARG, "n = %zu exceeds 32-bit indexing", n);
+    if (c->fault_kind == 1) return fail(c, GVS_ERR_INJECTED, "injected allocation fault");
+    cudaSetDevice(c->device);
+    GVS_TRY(alloc_state(c, n));
+    const size_t b = n * sizeof(double);
+    GVS_TRY(upload(c, c->x, x, b)); GVS_TRY(upload(c, c->y, y, b)); GVS_TRY(upload(c, c->z, z, b));
+    GVS_TRY(upload(c, c->vx, vx, b)); GVS_TRY(upload(c, c->vy, vy, b)); GVS_TRY(upload(c, c->vz, vz, b));
+    GVS_TRY(upload(c, c->m, mass, b));
+    GVS_TRY(clear_acc(c));
+    c->has_gas = ptype != nullptr;
+    if (ptype) GVS_CUDA(c, cudaMemcpyAsync(c->ptype.ptr, ptype, n, cudaMemcpyHostToDevice, c->stream));
+    else GVS_CUDA(c, cudaMemsetAsync(c->ptype.ptr, 0, std::max<size_t>(n, 1), c->stream));
+    DevBuf *zero[] = {&c->rho, &c->pres, &c->cs, &c->du_dt, &c->div_v, &c->max_mu, &c->dalpha_dt};
+    for (DevBuf *d : zero) GVS_CUDA(c, cudaMemsetAsync(d->ptr, 0, std::max<size_t>(b, 8), c->stream));
+    if (u) GVS_TRY(upload(c, c->u, u, b)); else GVS_CUDA(c, cudaMemsetAsync(c->u.ptr, 0, std::max<size_t>(b, 8), c->stream));
+    if (h) GVS_TRY(upload(c, c->h, h, b)); else GVS_CUDA(c, cudaMemsetAsync(c->h.ptr, 0, std::max<size_t>(b, 8), c->stream));
+    if (alpha) GVS_TRY(upload(c, c->alpha, alpha, b));
+    else GVS_CUDA(c, cudaMemsetAsync(c->alpha.ptr, 0, std::max<size_t>(b, 8), c->stream));
+    c->step_counter = 0;
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return GVS_OK;
+}
+
+gvs_status gvs_get_state(gvs_ctx *c, double *x, double *y, double *z, double *vx, double *vy, double *vz, double *ax,
+                         double *ay, double *az) {
+    GVS_TRY(check_ctx(c));
+    const size_t b = c->n * sizeof(double);
+    GVS_TRY(download(c, x, c->x, b)); GVS_TRY(download(c, y, c->y, b)); GVS_TRY(download(c, z, c->z, b));
+    GVS_TRY(download(c, vx, c->vx, b)); GVS_TRY(download(c, vy, c->vy, b)); GVS_TRY(download(c, vz, c->vz, b));
+    GVS_TRY(download(c, ax, c->ax, b)); GVS_TRY(download(c, ay, c->ay, b)); GVS_TRY(download(c, az, c->az, b));
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return read_device_errors(c);
+}
+
+gvs_status gvs_set_accelerations(gvs_ctx *c, const double *ax, const double *ay, const double *az) {
+    GVS_TRY(check_ctx(c));
+    if (!ax || !ay || !az) return fail(c, GVS_ERR_INVALID_ARG, "null acceleration array");
+    const size_t b = c->n * sizeof(double);
+    GVS_TRY(upload(c, c->ax, ax, b)); GVS_TRY(upload(c, c->ay, ay, b)); GVS_TRY(upload(c, c->az, az, b));
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return GVS_OK;
+}
+
+gvs_status gvs_get_gas(gvs_ctx *c, double *density, double *pressure, double *u, double *du_dt, double *h,
+                       double *sound_speed, double *alpha) {
+    GVS_TRY(check_ctx(c));
+    const size_t b = c->n * sizeof(double);
+    GVS_TRY(download(c, density, c->rho, b)); GVS_TRY(download(c, pressure, c->pres, b));
+    GVS_TRY(download(c, u, c->u, b)); GVS_TRY(download(c, du_dt, c->du_dt, b));
+    GVS_TRY(download(c, h, c->h, b)); GVS_TRY(download(c, sound_speed, c->cs, b));
+    GVS_TRY(download(c, alpha, c->alpha, b));
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return read_device_errors(c);
+}
+
+static gvs_status check_prec_algo(gvs_ctx *c, int algo, int precision, double eps, double theta) {
+    if (algo < GVS_ALGO_NONE || algo > GVS_ALGO_BH) return fail(c, GVS_ERR_INVALID_ARG, "bad algo %d", algo);
+    if (precision < GVS_PREC_FP64_EXACT || precision > GVS_PREC_MIXED)
+        return fail(c, GVS_ERR_INVALID_ARG, "bad precision %d", precision);
+    if (!(eps >= 0.0)) return fail(c, GVS_ERR_INVALID_ARG, "softening must be >= 0 (got %g)", eps);
+    if (algo == GVS_ALGO_BH && !(theta >= 0.0)) return fail(c, GVS_ERR_INVALID_ARG, "theta must be >= 0");
+    return GVS_OK;
+}
+
+gvs_status gvs_gravity_direct(gvs_ctx *c, size_t n, const double *x, const double *y, const double *z,
+                              const double *mass, double eps, int precision, double *ax, double *ay, double *az) {
+    GVS_TRY(check_ctx(c));
+    if (!x || !y || !z || !mass || !ax || !ay || !az) return fail(c, GVS_ERR_INVALID_ARG, "null array");
+    GVS_TRY(check_prec_algo(c, GVS_ALGO_DIRECT, precision, eps, 0.0));
+    if (n > 0xFFFFFFF0ull) return fail(c, GVS_ERR_INVALID_ARG, "n too large");
+    if (n == 0) return GVS_OK;
+    cudaSetDevice(c->device);
+    if (c->n != n) GVS_TRY(alloc_state(c, n));
+    const size_t b = n * sizeof(double);
+    GVS_TRY(upload(c, c->x, x, b)); GVS_TRY(upload(c, c->y, y, b)); GVS_TRY(upload(c, c->z, z, b));
+    GVS_TRY(upload(c, c->m, mass, b));
+    // accumulate semantics: upload the caller's a, add forces, download
+    GVS_TRY(upload(c, c->ax, ax, b)); GVS_TRY(upload(c, c->ay, ay, b)); GVS_TRY(upload(c, c->az, az, b));
+    GVS_TRY(gravity(c, GVS_ALGO_DIRECT, precision, eps, 0.0, true));
+    GVS_TRY(download(c, ax, c->ax, b)); GVS_TRY(download(c, ay, c->ay, b)); GVS_TRY(download(c, az, c->az, b));
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return read_device_errors(c);
+}
+
+gvs_status gvs_compute_forces(gvs_ctx *c, int algo, int precision, double eps, double theta) {
+    GVS_TRY(check_ctx(c));
+    GVS_TRY(check_prec_algo(c, algo, precision, eps, theta));
+    cudaSetDevice(c->device);
+    GVS_TRY(gravity(c, algo, precision, eps, theta, false));
+    return GVS_OK;
+}
+
+gvs_status gvs_kdk_steps(gvs_ctx *c, int algo, int precision, double eps, double theta, double dt,
+                         long long nsteps) {
+    GVS_TRY(check_ctx(c));
+    GVS_TRY(check_prec_algo(c, algo, precision, eps, theta));
+    if (!(dt > 0.0) || nsteps < 0) return fail(c, GVS_ERR_INVALID_ARG, "dt must be > 0 and nsteps >= 0");
+    cudaSetDevice(c->device);
+    for (long long s = 0; s < nsteps; ++s) {
+        if (nan_fault_due(c)) return fail(c, GVS_ERR_INJECTED, "injected non-finite fault at step %lld", s);
+        GVS_TRY(kdk_one(c, algo, precision, eps, theta, dt));
+    }
+    return GVS_OK;
+}
+
+gvs_status gvs_kdk_step_host(gvs_ctx *c, size_t n, double *x, double *y, double *z, double *vx, double *vy,
+                             double *vz, double *ax, double *ay, double *az, const double *mass, int algo,
+                             int precision, double eps, double theta, double dt) {
+    GVS_TRY(check_ctx(c));
+    if (!x || !y || !z || !vx || !vy || !vz || !ax || !ay || !az || !mass)
+        return fail(c, GVS_ERR_INVALID_ARG, "null array");
+    GVS_TRY(check_prec_algo(c, algo, precision, eps, theta));
+    if (!(dt > 0.0)) return fail(c, GVS_ERR_INVALID_ARG, "dt must be > 0");
+    if (n > 0xFFFFFFF0ull) return fail(c, GVS_ERR_INVALID_ARG, "n too large");
+    if (n == 0) return GVS_OK;
+    cudaSetDevice(c->device);
+    if (c->n != n) GVS_TRY(alloc_state(c, n));
+    const size_t b = n * sizeof(double);
+    GVS_TRY(upload(c, c->x, x, b)); GVS_TRY(upload(c, c->y, y, b)); GVS_TRY(upload(c, c->z, z, b));
+    GVS_TRY(upload(c, c->vx, vx, b)); GVS_TRY(upload(c, c->vy, vy, b)); GVS_TRY(upload(c, c->vz, vz, b));
+    GVS_TRY(upload(c, c->ax, ax, b)); GVS_TRY(upload(c, c->ay, ay, b)); GVS_TRY(upload(c, c->az, az, b));
+    GVS_TRY(upload(c, c->m, mass, b));
+    if (nan_fault_due(c)) return fail(c, GVS_ERR_INJECTED, "injected non-finite fault");
+    GVS_TRY(kdk_one(c, algo, precision, eps, theta, dt));
+    GVS_TRY(download(c, x, c->x, b)); GVS_TRY(download(c, y, c->y, b)); GVS_TRY(download(c, z, c->z, b));
+    GVS_TRY(download(c, vx, c->vx, b)); GVS_TRY(download(c, vy, c->vy, b)); GVS_TRY(download(c, vz, c->vz, b));
+    GVS_TRY(download(c, ax, c->ax, b)); GVS_TRY(download(c, ay, c->ay, b)); GVS_TRY(download(c, az, c->az, b));
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return read_device_errors(c);
+}
+
+gvs_status gvs_diagnostics(gvs_ctx *c, double eps, int with_potential, gvs_diag *out) {
+    GVS_TRY(check_ctx(c));
+    if (!out) return fail(c, GVS_ERR_INVALID_ARG, "out is NULL");
+    if (!(eps >= 0.0)) return fail(c, GVS_ERR_INVALID_ARG, "softening must be >= 0");
+    cudaSetDevice(c->device);
+    GVS_TRY(diagnostics(c, eps, with_potential, out));
+    return read_device_errors(c);
+}
+
+gvs_status gvs_direct_subset(gvs_ctx *c, int precision, double eps, const int64_t *idx, size_t nidx, double *oax,
+                             double *oay, double *oaz) {
+    GVS_TRY(check_ctx(c));
+    if (!idx || !oax || !oay || !oaz) return fail(c, GVS_ERR_INVALID_ARG, "null array");
+    for (size_t k = 0; k < nidx; ++k)
+        if (idx[k] < 0 || (size_t)idx[k] >= c->n) return fail(c, GVS_ERR_INVALID_ARG, "target index out of range");
+    if (nidx == 0) return GVS_OK;
+    cudaSetDevice(c->device);
+    GVS_CUDA(c, ensure(c, c->scratch_a, nidx * sizeof(int64_t)));
+    GVS_CUDA(c, ensure(c, c->scratch_b, 3 * nidx * sizeof(double)));
+    GVS_CUDA(c, cudaMemcpyAsync(c->scratch_a.ptr, idx, nidx * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
+    GVS_TRY(direct_forces_subset(c, precision, eps, as<int64_t>(c->scratch_a), nidx, as<double>(c->scratch_b)));
+    double *d = as<double>(c->scratch_b);
+    GVS_CUDA(c, cudaMemcpyAsync(oax, d, nidx * 8, cudaMemcpyDeviceToHost, c->stream));
+    GVS_CUDA(c, cudaMemcpyAsync(oay, d + nidx, nidx * 8, cudaMemcpyDeviceToHost, c->stream));
+    GVS_CUDA(c, cudaMemcpyAsync(oaz, d + 2 * nidx, nidx * 8, cudaMemcpyDeviceToHost, c->stream));
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return read_device_errors(c);
+}
+
+gvs_status gvs_autotune_direct(gvs_ctx *c, int precision, double eps, int *nthreads, int *ipt, double *ms) {
+    GVS_TRY(check_ctx(c));
+    if (precision != GVS_PREC_MIXED && precision != GVS_PREC_FP32)
+        return fail(c, GVS_ERR_INVALID_ARG, "autotune covers the f32 pair kernel (FP32 / MIXED)");
+    if (!(eps >= 0.0)) return fail(c, GVS_ERR_INVALID_ARG, "softening must be >= 0");
+    if (c->n == 0) return fail(c, GVS_ERR_STATE, "no particles");
+    cudaSetDevice(c->device);
+    GVS_TRY(autotune_direct(c, precision, eps, nthreads, ipt, ms));
+    return read_device_errors(c);
+}
+
+// ---- profiling -----------------------------------------------------------------
+
+struct EventSlots {
+    cudaEvent_t ev[16] = {};
+};
+
+gvs_status gvs_profile_enable(gvs_ctx *c, int on) {
+    GVS_TRY(check_ctx(c));
+    c->prof.on = on != 0;
+    c->prof.force_ms = 0.0;
+    c->prof.force_launches = 0;
+    c->prof.launches = 0;
+    c->prof.force_flops = 0.0;
+    c->prof.force_bytes = 0.0;
+    return GVS_OK;
+}
+
+gvs_status gvs_profile_read(gvs_ctx *c, gvs_profile *out) {
+    GVS_TRY(check_ctx(c));
+    if (!out) return fail(c, GVS_ERR_INVALID_ARG, "out is NULL");
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    out->force_ms = c->prof.force_ms;
+    out->force_launches = c->prof.force_launches;
+    out->launches = c->prof.launches;
+    out->force_flops = c->prof.force_flops;
+    out->force_bytes = c->prof.force_bytes;
+    return GVS_OK;
+}
+
+static std::vector<std::pair<const gvs_ctx *, EventSlots>> g_slots;
+
+static cudaEvent_t *slots_for(gvs_ctx *c) {
+    for (auto &p : g_slots)
+        if (p.first == c) return p.second.ev;
+    g_slots.push_back({c, EventSlots()});
+    return g_slots.back().second.ev;
+}
+
+gvs_status gvs_event_record(gvs_ctx *c, int slot) {
+    GVS_TRY(check_ctx(c));
+    if (slot < 0 || slot >= 16) return fail(c, GVS_ERR_INVALID_ARG, "event slot out of range");
+    cudaEvent_t *ev = slots_for(c);
+    if (!ev[slot]) GVS_CUDA(c, cudaEventCreate(&ev[slot]));
+    GVS_CUDA(c, cudaEventRecord(ev[slot], c->stream));
+    return GVS_OK;
+}
+
+gvs_status gvs_event_elapsed(gvs_ctx *c, int a, int b, float *ms) {
+    GVS_TRY(check_ctx(c));
+    if (a < 0 || a >= 16 || b < 0 || b >= 16 || !ms) return fail(c, GVS_ERR_INVALID_ARG, "bad event slots");
+    cudaEvent_t *ev = slots_for(c);
+    if (!ev[a] || !ev[b]) return fail(c, GVS_ERR_STATE, "event slot not recorded");
+    GVS_CUDA(c, cudaEventSynchronize(ev[b]));
+    GVS_CUDA(c, cudaEventElapsedTime(ms, ev[a], ev[b]));
+    return GVS_OK;
+}
+
+gvs_status gvs_l2_flush(gvs_ctx *c) {
+    GVS_TRY(check_ctx(c));
+    const size_t bytes = 512ull << 20;  // 4x the 129 MB L2
+    GVS_CUDA(c, ensure(c, c->l2_flush, bytes));
+    GVS_CUDA(c, cudaMemsetAsync(c->l2_flush.ptr, (int)(c->step_counter & 0xFF), bytes, c->stream));
+    return GVS_OK;
+}
+
+}  // extern "C"
+
+// ---- FP32 throughput probe ----------------------------------------------------------
+namespace {
+constexpr int PEAK_ITERS = 4096;
+
+__global__ void k_fp32_peak_scalar(float *out, float a, float b) {
+    float r[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) r[k] = (float)(threadIdx.x + k);
+    for (int it = 0; it < PEAK_ITERS; ++it)
+#pragma unroll
+        for (int k = 0; k < 16; ++k) r[k] = fmaf(r[k], a, b);
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) s += r[k];
+    if (s == 12345.678f) out[0] = s;
+}
+
+__global__ void k_fp32_peak_packed(float *out, float a, float b) {
+    unsigned long long r[8], av, bv;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(av) : "f"(a));
+    asm("mov.b64 %0, {%1, %1};" : "=l"(bv) : "f"(b));
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        float x = (float)(threadIdx.x + k), y = x + 0.5f;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(r[k]) : "f"(x), "f"(y));
+    }
+    for (int it = 0; it < PEAK_ITERS; ++it)
+#pragma unroll
+        for (int k = 0; k < 8; ++k) asm volatile("fma.rn.f32x2 %0, %0, %1, %2;" : "+l"(r[k]) : "l"(av), "l"(bv));
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        float x, y;
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(r[k]));
+        s += x + y;
+    }
+    if (s == 12345.678f) out[0] = s;
+}
+}  // namespace
+
+extern "C" gvs_status gvs_measure_fp32_peak(gvs_ctx *c, double *tflops) {
+    GVS_TRY(check_ctx(c));
+    if (!tflops) return fail(c, GVS_ERR_INVALID_ARG, "tflops is NULL");
+    cudaSetDevice(c->device);
+    GVS_CUDA(c, ensure(c, c->scratch_b, 64));
+    const int blocks = c->num_sms * 8, threads = 256;
+    double best = 0.0;
+    for (int variant = 0; variant < 2; ++variant) {
+        for (int rep = 0; rep < 3; ++rep) {
+            GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], c->stream));
+            if (variant == 0)
+                k_fp32_peak_scalar<<<blocks, threads, 0, c->stream>>>(as<float>(c->scratch_b), 0.999f, 0.001f);
+            else
+                k_fp32_peak_packed<<<blocks, threads, 0, c->stream>>>(as<float>(c->scratch_b), 0.999f, 0.001f);
+            GVS_CUDA(c, cudaEventRecord(c->prof.ev[1], c->stream));
+            GVS_TRY(check_launch(c, "fp32 peak probe"));
+            GVS_CUDA(c, cudaEventSynchronize(c->prof.ev[1]));
+            float ms = 0.f;
+            GVS_CUDA(c, cudaEventElapsedTime(&ms, c->prof.ev[0], c->prof.ev[1]));
+            const double flops = 2.0 * 16.0 * PEAK_ITERS * (double)blocks * threads;
+            if (ms > 0.f) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+        }
+    }
+    *tflops = best;
+    return GVS_OK;
+}

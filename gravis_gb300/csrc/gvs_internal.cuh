@@ -1,0 +1,222 @@
+// gvs_internal.cuh -- shared definitions for the gravis GB300 engine (sm_103a).
+//
+// The engine keeps one context per (caller, device): a CUDA stream, the
+// particle state resident in HBM as f64 structure-of-arrays in the caller's
+// order (the same 18 arrays as sim-core's Particles), and the scratch that the
+// force paths need (spatial sort, packed j-tiles, per-split partial sums,
+// octree arrays, SPH neighbour lists).  Every C-ABI call validates its
+// arguments, runs on the context's stream and returns a gvs_status.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gvs.h"
+
+namespace gvs {
+
+// ---------------------------------------------------------------------------
+// device error word (bit flags written by kernels, read by the host)
+// ---------------------------------------------------------------------------
+enum DeviceError : unsigned {
+    DERR_MBAR_TIMEOUT = 1u << 0,   // an mbarrier wait hit its iteration cap
+    DERR_STACK_OVERFLOW = 1u << 1, // tree walk stack exhausted
+    DERR_NEIGH_OVERFLOW = 1u << 2, // SPH neighbour buffer too small
+    DERR_NAN = 1u << 3,            // non-finite value detected
+    DERR_TREE = 1u << 4,           // tree build invariant violated
+    DERR_BOUNDS = 1u << 5,         // checked build: index out of range
+    DERR_SPIN_TIMEOUT = 1u << 6,   // persistent-kernel queue wait hit its cap
+};
+
+// ---------------------------------------------------------------------------
+// a growable device buffer owned by the context
+// ---------------------------------------------------------------------------
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+struct Ctx;
+cudaError_t ensure(Ctx *c, DevBuf &b, size_t bytes);  // grows, never shrinks
+template <class T> T *as(DevBuf &b) { return reinterpret_cast<T *>(b.ptr); }
+
+// Profiling counters of one context (kernel time of the dominant kernels).
+struct Prof {
+    bool on = false;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    double force_ms = 0.0;   // summed device time of force kernels
+    long long force_launches = 0;
+    long long launches = 0;  // every kernel this context launched
+    double force_bytes = 0;  // algorithmic bytes moved by timed force kernels
+    double force_flops = 0;  // algorithmic flops (20 per pair interaction)
+};
+
+struct Tune {
+    int ipt = 4;       // i-particles per thread
+    int nthreads = 256;
+    int nsplit = 0;    // 0 = automatic
+};
+
+struct Ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+
+    // resident state, caller order, capacity >= n
+    size_t n = 0, cap = 0;
+    DevBuf x, y, z, vx, vy, vz, ax, ay, az, m;
+    DevBuf ptype, u, h, alpha, rho, pres, cs, du_dt, omega, div_v, max_mu, dalpha_dt;
+    bool has_gas = false;
+
+    // direct-sum scratch
+    DevBuf keys, keys_alt, perm, perm_alt, sort_hist, bbox_part;
+    DevBuf jpack32, jpack64, partial;
+    // generic scratch
+    DevBuf scratch_a, scratch_b, err_word, red_part, l2_flush;
+
+    // host staging (pinned)
+    void *pinned = nullptr;
+    size_t pinned_bytes = 0;
+
+    // tree / BH / SPH state lives in its own struct (bh.cu / sph.cu)
+    void *tree = nullptr;
+    void *sph = nullptr;
+    void *ens = nullptr;
+    void *adj = nullptr;
+
+    Prof prof;
+    Tune tune;
+    std::vector<std::pair<long long, Tune>> tune_cache;  // (n bucket, choice)
+
+    // fault injection: GVS_FAULT / gvs_set_fault ("alloc", "launch", "nan@K")
+    int fault_kind = 0;  // 0 none, 1 alloc, 2 launch, 3 nan
+    long long fault_step = -1;
+    long long step_counter = 0;
+};
+
+// Records an error message on the context and returns the status.
+gvs_status fail(Ctx *c, gvs_status s, const char *fmt, ...);
+gvs_status cuda_fail(Ctx *c, cudaError_t e, const char *what);
+gvs_status check_launch(Ctx *c, const char *what);
+gvs_status read_device_errors(Ctx *c);  // syncs the stream; DEVICE_ERROR if any flag
+
+#define GVS_CUDA(c, expr)                                                  \
+    do {                                                                   \
+        cudaError_t _e = (expr);                                           \
+        if (_e != cudaSuccess) return ::gvs::cuda_fail((c), _e, #expr);    \
+    } while (0)
+
+#define GVS_TRY(expr)                          \
+    do {                                       \
+        gvs_status _s = (expr);                \
+        if (_s != GVS_OK) return _s;           \
+    } while (0)
+
+inline unsigned *err_ptr(Ctx *c) { return as<unsigned>(c->err_word); }
+
+// ---------------------------------------------------------------------------
+// PTX helpers: mbarrier + untiled bulk copy (cp.async.bulk), sm_90+ / sm_103a
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: returns false (and sets the error flag) after `cap` polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity, unsigned *err,
+                                                  unsigned cap = 1u << 22) {
+    for (unsigned it = 0; it < cap; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    if (err) atomicOr(err, (unsigned)DERR_MBAR_TIMEOUT);
+    return false;
+}
+
+// 1-D bulk copy global -> this CTA's shared memory, completing on `bar`.
+// Both addresses 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst_smem, const void *src_gmem, unsigned bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst_smem)),
+        "l"(src_gmem), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Error-free transformation (Knuth two-sum): s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    float bp = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// ---------------------------------------------------------------------------
+// subsystem entry points (defined in the .cu files)
+// ---------------------------------------------------------------------------
+// sort.cu
+gvs_status radix_sort_u32(Ctx *c, uint32_t *keys, uint32_t *vals, uint32_t *keys_alt, uint32_t *vals_alt, size_t n,
+                          int begin_bit, int end_bit, uint32_t **keys_out, uint32_t **vals_out);
+gvs_status radix_sort_u64(Ctx *c, uint64_t *keys, uint32_t *vals, uint64_t *keys_alt, uint32_t *vals_alt, size_t n,
+                          int begin_bit, int end_bit, uint64_t **keys_out, uint32_t **vals_out);
+// direct.cu
+gvs_status direct_forces(Ctx *c, int precision, double eps, bool accumulate);
+gvs_status direct_forces_subset(Ctx *c, int precision, double eps, const int64_t *idx_dev, size_t nidx,
+                                double *out_dev);
+gvs_status spatial_order(Ctx *c);
+gvs_status autotune_direct(Ctx *c, int precision, double eps, int *best_nt, int *best_ipt, double *best_ms);
+// kdk.cu
+gvs_status kick(Ctx *c, double half_dt);
+gvs_status drift(Ctx *c, double dt);
+gvs_status kick_drift(Ctx *c, double half_dt, double dt);
+gvs_status clear_acc(Ctx *c);
+// diag.cu
+gvs_status diagnostics(Ctx *c, double eps, int with_potential, gvs_diag *out);
+// bh.cu
+gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accumulate);
+gvs_status tree_build(Ctx *c);
+void tree_free(Ctx *c);
+// sph.cu
+gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm);
+gvs_status sph_timestep(Ctx *c, const gvs_sph_params *prm, double *dt_out);
+void sph_free(Ctx *c);
+
+// forces on resident state according to the algorithm selector
+gvs_status gravity(Ctx *c, int algo, int precision, double eps, double theta, bool accumulate);
+
+}  // namespace gvs

@@ -1,0 +1,141 @@
+// sort.cu -- stable LSD radix sort of (key, u32 value) pairs on the device.
+//
+// Used to put particles in space-filling-curve order: the direct sum sorts
+// 30-bit Morton keys so that consecutive particles form compact tiles (the
+// tile-centre split of the mixed-precision kernel needs that), and the
+// Barnes-Hut build sorts 126-bit octant-path keys (two u64 words, sorted as
+// low word then high word) so that the sorted order is the depth-first order
+// of the reference octree (crates/sim-core/src/octree.rs:156-239).
+//
+// One pass per 8-bit digit: (1) per-block digit histograms, (2) one exclusive
+// scan over the [digit][block] table, (3) a stable scatter in which each block
+// ranks its keys in index order with warp match/ballot and per-warp counters.
+#include "gvs_internal.cuh"
+
+namespace gvs {
+
+namespace {
+constexpr int NT = 256;              // threads per block
+constexpr int IPT = 16;              // keys per thread per pass
+constexpr int TILE = NT * IPT;       // keys per block
+constexpr int RADIX = 256;
+constexpr int NWARP = NT / 32;
+
+template <class K>
+__global__ void __launch_bounds__(NT) k_hist(const K *__restrict__ keys, size_t n, int shift,
+                                             uint32_t *__restrict__ hist, int nblocks) {
+    __shared__ uint32_t h[RADIX];
+    for (int i = threadIdx.x; i < RADIX; i += NT) h[i] = 0;
+    __syncthreads();
+    size_t base = (size_t)blockIdx.x * TILE;
+#pragma unroll 4
+    for (int k = 0; k < IPT; ++k) {
+        size_t idx = base + (size_t)k * NT + threadIdx.x;
+        if (idx < n) atomicAdd(&h[(unsigned)(keys[idx] >> shift) & 0xFFu], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < RADIX; i += NT) hist[(size_t)i * nblocks + blockIdx.x] = h[i];
+}
+
+// Exclusive scan of m entries by one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_scan1(uint32_t *a, int m) {
+    __shared__ uint32_t part[1024];
+    int t = threadIdx.x;
+    int per = (m + 1023) / 1024;
+    int s = t * per, e = min(m, s + per);
+    uint32_t sum = 0;
+    for (int i = s; i < e; ++i) sum += a[i];
+    part[t] = sum;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        uint32_t v = (t >= off) ? part[t - off] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    uint32_t run = (t == 0) ? 0u : part[t - 1];
+    for (int i = s; i < e; ++i) {
+        uint32_t v = a[i];
+        a[i] = run;
+        run += v;
+    }
+}
+
+template <class K>
+__global__ void __launch_bounds__(NT) k_scatter(const K *__restrict__ keys, const uint32_t *__restrict__ vals,
+                                                K *__restrict__ kout, uint32_t *__restrict__ vout, size_t n,
+                                                int shift, const uint32_t *__restrict__ hist, int nblocks) {
+    __shared__ uint32_t base[RADIX];
+    __shared__ uint32_t wcnt[NWARP][RADIX];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < RADIX; i += NT) base[i] = hist[(size_t)i * nblocks + blockIdx.x];
+    const size_t tbase = (size_t)blockIdx.x * TILE;
+    for (int k = 0; k < IPT; ++k) {
+        for (int i = tid; i < NWARP * RADIX; i += NT) (&wcnt[0][0])[i] = 0u;
+        __syncthreads();
+        const size_t idx = tbase + (size_t)k * NT + tid;
+        const bool valid = idx < n;
+        K key = 0;
+        unsigned d = 256u;  // out-of-range lanes form their own group
+        if (valid) {
+            key = keys[idx];
+            d = (unsigned)(key >> shift) & 0xFFu;
+        }
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+        const unsigned rank = __popc(peers & ((1u << lane) - 1u));
+        if (valid && lane == __ffs(peers) - 1) wcnt[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            uint32_t off = base[d];
+            for (int w = 0; w < warp; ++w) off += wcnt[w][d];
+            const size_t dst = (size_t)off + rank;
+            kout[dst] = key;
+            vout[dst] = vals[idx];
+        }
+        __syncthreads();
+        for (int dd = tid; dd < RADIX; dd += NT) {
+            uint32_t s = 0;
+#pragma unroll
+            for (int w = 0; w < NWARP; ++w) s += wcnt[w][dd];
+            base[dd] += s;
+        }
+        __syncthreads();
+    }
+}
+
+template <class K>
+gvs_status radix_sort_impl(Ctx *c, K *keys, uint32_t *vals, K *keys_alt, uint32_t *vals_alt, size_t n,
+                           int begin_bit, int end_bit, K **keys_out, uint32_t **vals_out) {
+    K *kin = keys, *kout = keys_alt;
+    uint32_t *vin = vals, *vout = vals_alt;
+    if (n > 1) {
+        const int nblocks = ceil_div((long long)n, TILE);
+        GVS_CUDA(c, ensure(c, c->sort_hist, (size_t)RADIX * nblocks * sizeof(uint32_t)));
+        uint32_t *hist = as<uint32_t>(c->sort_hist);
+        for (int bit = begin_bit; bit < end_bit; bit += 8) {
+            k_hist<K><<<nblocks, NT, 0, c->stream>>>(kin, n, bit, hist, nblocks);
+            k_scan1<<<1, 1024, 0, c->stream>>>(hist, RADIX * nblocks);
+            k_scatter<K><<<nblocks, NT, 0, c->stream>>>(kin, vin, kout, vout, n, bit, hist, nblocks);
+            c->prof.launches += 3;
+            GVS_TRY(check_launch(c, "radix sort pass"));
+            K *tk = kin; kin = kout; kout = tk;
+            uint32_t *tv = vin; vin = vout; vout = tv;
+        }
+    }
+    *keys_out = kin;
+    *vals_out = vin;
+    return GVS_OK;
+}
+}  // namespace
+
+gvs_status radix_sort_u32(Ctx *c, uint32_t *keys, uint32_t *vals, uint32_t *keys_alt, uint32_t *vals_alt, size_t n,
+                          int begin_bit, int end_bit, uint32_t **keys_out, uint32_t **vals_out) {
+    return radix_sort_impl<uint32_t>(c, keys, vals, keys_alt, vals_alt, n, begin_bit, end_bit, keys_out, vals_out);
+}
+
+gvs_status radix_sort_u64(Ctx *c, uint64_t *keys, uint32_t *vals, uint64_t *keys_alt, uint32_t *vals_alt, size_t n,
+                          int begin_bit, int end_bit, uint64_t **keys_out, uint32_t **vals_out) {
+    return radix_sort_impl<uint64_t>(c, keys, vals, keys_alt, vals_alt, n, begin_bit, end_bit, keys_out, vals_out);
+}
+
+}  // namespace gvs

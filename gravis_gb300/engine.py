@@ -1,0 +1,458 @@
+"""Host-side mirror of gravis sim-core's hot-path interfaces, backed by libgvs.so.
+
+Names, argument meanings and accumulate semantics follow sim-core:
+
+  Particles                   crates/sim-core/src/particle.rs:22-227
+  GravitySolver / NoGravity   crates/sim-core/src/gravity.rs:6-19
+  BruteForce                  crates/sim-core/src/gravity.rs:47-80
+  BarnesHut                   crates/sim-core/src/barnes_hut.rs:21-192
+  LeapfrogKDK                 crates/sim-core/src/integrator.rs:5-76
+  SphSolver / step_with_sph   crates/sim-core/src/sph/solver.rs:20-212
+  diagnostics.compute         crates/sim-core/src/diagnostics.rs:37-148
+  PlummerSphere, TwoBody,     crates/sim-core/src/scenarios/{plummer_sphere,two_body,
+  EvrardCollapse                evrard_collapse}.rs
+
+Every numeric operation runs on the GPU through the C ABI (include/gvs.h);
+this module only moves numpy arrays across it.  There is no CPU fallback: if
+libgvs.so is missing or no GB300 is visible, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import check
+
+GAS = 4
+_F64 = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "mass", "density", "pressure", "internal_energy",
+        "du_dt", "smoothing_length", "sound_speed", "alpha_visc")
+
+
+def _ptr(a: np.ndarray):
+    assert a.flags.c_contiguous
+    return a.ctypes.data
+
+
+class Particles:
+    """Structure-of-arrays particle store (particle.rs:22-64), f64 numpy arrays."""
+
+    def __init__(self, n: int = 0):
+        self.count = int(n)
+        for f in _F64:
+            setattr(self, f, np.zeros(self.count, dtype=np.float64))
+        self.particle_type = np.zeros(self.count, dtype=np.uint8)
+
+    @classmethod
+    def from_arrays(cls, x, y, z, vx, vy, vz, mass, **gas) -> "Particles":
+        p = cls(len(x))
+        p.x[:], p.y[:], p.z[:] = x, y, z
+        p.vx[:], p.vy[:], p.vz[:] = vx, vy, vz
+        p.mass[:] = mass
+        for k, v in gas.items():
+            getattr(p, k)[:] = v
+        return p
+
+    def add(self, x, y, z, vx, vy, vz, mass, ptype: int = 0) -> int:
+        """Particles::add / add_typed (particle.rs:94-132)."""
+        i = self.count
+        self.count += 1
+        for f in _F64:
+            setattr(self, f, np.append(getattr(self, f), 0.0))
+        self.particle_type = np.append(self.particle_type, np.uint8(ptype))
+        self.x[i], self.y[i], self.z[i], self.vx[i], self.vy[i], self.vz[i], self.mass[i] = x, y, z, vx, vy, vz, mass
+        return i
+
+    def add_gas(self, x, y, z, vx, vy, vz, mass, internal_energy, smoothing_length) -> int:
+        """Particles::add_gas (particle.rs:136-154): alpha starts at 1."""
+        i = self.add(x, y, z, vx, vy, vz, mass, GAS)
+        self.internal_energy[i] = internal_energy
+        self.smoothing_length[i] = smoothing_length
+        self.alpha_visc[i] = 1.0
+        return i
+
+    def is_gas(self, i: int) -> bool:
+        return self.particle_type[i] == GAS
+
+    def has_gas(self) -> bool:
+        return bool(np.any(self.particle_type == GAS))
+
+    def total_mass(self) -> float:
+        return float(np.sum(self.mass))
+
+    def clear_accelerations(self):
+        self.ax[:] = 0.0
+        self.ay[:] = 0.0
+        self.az[:] = 0.0
+
+    def clear_sph_rates(self):
+        self.du_dt[:] = 0.0
+
+    def shift_to_com_frame(self):
+        """particle.rs:189-226 (sequential sums, as the reference)."""
+        mt = 0.0
+        for m in self.mass:
+            mt += m
+        if mt == 0.0:
+            return
+        c = [0.0] * 6
+        for i in range(self.count):
+            m = self.mass[i]
+            c[0] += m * self.x[i]; c[1] += m * self.y[i]; c[2] += m * self.z[i]
+            c[3] += m * self.vx[i]; c[4] += m * self.vy[i]; c[5] += m * self.vz[i]
+        c = [v / mt for v in c]
+        self.x -= c[0]; self.y -= c[1]; self.z -= c[2]
+        self.vx -= c[3]; self.vy -= c[4]; self.vz -= c[5]
+
+    def copy(self) -> "Particles":
+        q = Particles(self.count)
+        for f in _F64 + ("particle_type",):
+            getattr(q, f)[:] = getattr(self, f)
+        return q
+
+    def acc(self) -> np.ndarray:
+        return np.stack([self.ax, self.ay, self.az], axis=1)
+
+
+class Context:
+    """One engine context: a CUDA stream on `device` plus device-resident state."""
+
+    def __init__(self, device: int = 0):
+        self._lib = L.load()
+        h = C.c_void_p()
+        st = self._lib.gvs_create(C.byref(h), device)
+        if st != L.OK:
+            raise L.GvsError(st, L.last_error(None))
+        self.h = h.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.gvs_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, st):
+        check(st, self.h)
+
+    # ---- state ---------------------------------------------------------------
+    def set_state(self, p: Particles):
+        gas = p.has_gas()
+        self._ck(self._lib.gvs_set_state(
+            self.h, p.count, _ptr(p.x), _ptr(p.y), _ptr(p.z), _ptr(p.vx), _ptr(p.vy), _ptr(p.vz), _ptr(p.mass),
+            _ptr(p.particle_type) if gas else None, _ptr(p.internal_energy) if gas else None,
+            _ptr(p.smoothing_length) if gas else None, _ptr(p.alpha_visc) if gas else None))
+
+    def set_accelerations(self, p: Particles):
+        self._ck(self._lib.gvs_set_accelerations(self.h, _ptr(p.ax), _ptr(p.ay), _ptr(p.az)))
+
+    def get_state(self, p: Particles):
+        self._ck(self._lib.gvs_get_state(self.h, _ptr(p.x), _ptr(p.y), _ptr(p.z), _ptr(p.vx), _ptr(p.vy),
+                                         _ptr(p.vz), _ptr(p.ax), _ptr(p.ay), _ptr(p.az)))
+
+    def get_gas(self, p: Particles):
+        self._ck(self._lib.gvs_get_gas(self.h, _ptr(p.density), _ptr(p.pressure), _ptr(p.internal_energy),
+                                       _ptr(p.du_dt), _ptr(p.smoothing_length), _ptr(p.sound_speed),
+                                       _ptr(p.alpha_visc)))
+
+    # ---- device-resident operations -------------------------------------------
+    def compute_forces(self, algo: int, precision: int, softening: float, theta: float = 0.5):
+        self._ck(self._lib.gvs_compute_forces(self.h, algo, precision, softening, theta))
+
+    def kdk_steps(self, algo: int, precision: int, softening: float, theta: float, dt: float, nsteps: int):
+        self._ck(self._lib.gvs_kdk_steps(self.h, algo, precision, softening, theta, dt, nsteps))
+
+    def diagnostics(self, softening: float, with_potential: bool = True) -> "Diagnostics":
+        d = L.Diag()
+        self._ck(self._lib.gvs_diagnostics(self.h, softening, 1 if with_potential else 0, C.byref(d)))
+        return Diagnostics.from_c(d)
+
+    def direct_subset(self, idx, softening: float, precision: int = L.PREC_FP64_EXACT) -> np.ndarray:
+        idx = np.ascontiguousarray(idx, dtype=np.int64)
+        out = np.zeros((3, len(idx)))
+        self._ck(self._lib.gvs_direct_subset(self.h, precision, softening, _ptr(idx), len(idx), _ptr(out[0]),
+                                             _ptr(out[1]), _ptr(out[2])))
+        return out.T.copy()
+
+    def autotune(self, precision: int, softening: float) -> dict:
+        nt, ipt, ms = C.c_int(), C.c_int(), C.c_double()
+        self._ck(self._lib.gvs_autotune_direct(self.h, precision, softening, C.byref(nt), C.byref(ipt),
+                                               C.byref(ms)))
+        return {"nthreads": nt.value, "ipt": ipt.value, "ms": ms.value}
+
+    def sync(self):
+        self._ck(self._lib.gvs_sync(self.h))
+
+    def set_fault(self, spec: str):
+        self._ck(self._lib.gvs_set_fault(self.h, spec.encode()))
+
+    def device_errors(self) -> int:
+        f = C.c_uint()
+        self._ck(self._lib.gvs_device_errors(self.h, C.byref(f)))
+        return f.value
+
+    # ---- timing -------------------------------------------------------------------
+    def profile(self, on: bool):
+        self._ck(self._lib.gvs_profile_enable(self.h, 1 if on else 0))
+
+    def profile_read(self) -> dict:
+        pr = L.Profile()
+        self._ck(self._lib.gvs_profile_read(self.h, C.byref(pr)))
+        return {"force_ms": pr.force_ms, "force_launches": pr.force_launches, "launches": pr.launches,
+                "force_flops": pr.force_flops, "force_bytes": pr.force_bytes}
+
+    def event(self, slot: int):
+        self._ck(self._lib.gvs_event_record(self.h, slot))
+
+    def elapsed(self, a: int, b: int) -> float:
+        ms = C.c_float()
+        self._ck(self._lib.gvs_event_elapsed(self.h, a, b, C.byref(ms)))
+        return ms.value
+
+    def l2_flush(self):
+        self._ck(self._lib.gvs_l2_flush(self.h))
+
+    def fp32_peak_tflops(self) -> float:
+        v = C.c_double()
+        self._ck(self._lib.gvs_measure_fp32_peak(self.h, C.byref(v)))
+        return v.value
+
+
+_default_ctx: Context | None = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+# ---- gravity solvers ------------------------------------------------------------
+class GravitySolver:
+    """gravity.rs:6-10: compute_accelerations ACCUMULATES into ax/ay/az."""
+    algo = L.ALGO_NONE
+    softening = 0.0
+    theta = 0.5
+    precision = L.PREC_FP64_EXACT
+
+    def compute_accelerations(self, p: Particles):
+        raise NotImplementedError
+
+    def context(self) -> Context:
+        return getattr(self, "ctx", None) or default_context()
+
+
+class NoGravity(GravitySolver):
+    """gravity.rs:13-19."""
+
+    def compute_accelerations(self, p: Particles):
+        return None
+
+
+class BruteForce(GravitySolver):
+    """gravity.rs:47-80 on the GPU.  precision=PREC_FP64_EXACT reproduces the
+    reference bit for bit; PREC_MIXED is the fast f32-pair path."""
+    algo = L.ALGO_DIRECT
+
+    def __init__(self, softening: float, precision: int = L.PREC_FP64_EXACT, ctx: Context | None = None):
+        self.softening = float(softening)
+        self.precision = precision
+        self.ctx = ctx
+
+    def compute_accelerations(self, p: Particles):
+        c = self.context()
+        c._ck(c._lib.gvs_gravity_direct(c.h, p.count, _ptr(p.x), _ptr(p.y), _ptr(p.z), _ptr(p.mass),
+                                        self.softening, self.precision, _ptr(p.ax), _ptr(p.ay), _ptr(p.az)))
+
+
+class BarnesHut(GravitySolver):
+    """barnes_hut.rs:21-192 on the GPU (octree from sorted octant-path keys)."""
+    algo = L.ALGO_BH
+
+    def __init__(self, softening: float, theta: float = 0.5, precision: int = L.PREC_FP64,
+                 ctx: Context | None = None):
+        self.softening = float(softening)
+        self.theta = float(theta)
+        self.precision = precision
+        self.ctx = ctx
+
+    def compute_accelerations(self, p: Particles):
+        c = self.context()
+        c.set_state(p)
+        c.compute_forces(L.ALGO_BH, self.precision, self.softening, self.theta)
+        a = np.zeros((3, p.count))
+        c._ck(c._lib.gvs_get_state(c.h, None, None, None, None, None, None, _ptr(a[0]), _ptr(a[1]), _ptr(a[2])))
+        p.ax += a[0]
+        p.ay += a[1]
+        p.az += a[2]
+
+
+class LeapfrogKDK:
+    """integrator.rs:42-76: one KDK step on the GPU (x, v, a round-trip through the ABI)."""
+
+    def step(self, p: Particles, gravity: GravitySolver, dt: float):
+        c = gravity.context()
+        c._ck(c._lib.gvs_kdk_step_host(c.h, p.count, _ptr(p.x), _ptr(p.y), _ptr(p.z), _ptr(p.vx), _ptr(p.vy),
+                                       _ptr(p.vz), _ptr(p.ax), _ptr(p.ay), _ptr(p.az), _ptr(p.mass), gravity.algo,
+                                       gravity.precision, gravity.softening, gravity.theta, dt))
+
+
+# ---- diagnostics ------------------------------------------------------------------
+@dataclass
+class Diagnostics:
+    kinetic_energy: float = 0.0
+    potential_energy: float = 0.0
+    thermal_energy: float = 0.0
+    total_energy: float = 0.0
+    momentum: np.ndarray = field(default_factory=lambda: np.zeros(3))
+    angular_momentum: np.ndarray = field(default_factory=lambda: np.zeros(3))
+    center_of_mass: np.ndarray = field(default_factory=lambda: np.zeros(3))
+    center_of_mass_velocity: np.ndarray = field(default_factory=lambda: np.zeros(3))
+    virial_ratio: float = 0.0
+    time: float = 0.0
+    step: int = 0
+
+    @classmethod
+    def from_c(cls, d: L.Diag) -> "Diagnostics":
+        return cls(d.kinetic_energy, d.potential_energy, d.thermal_energy, d.total_energy,
+                   np.array(d.momentum[:]), np.array(d.angular_momentum[:]), np.array(d.center_of_mass[:]),
+                   np.array(d.center_of_mass_velocity[:]), d.virial_ratio)
+
+    def momentum_magnitude(self) -> float:
+        return float(np.sqrt(self.momentum @ self.momentum))
+
+    def angular_momentum_magnitude(self) -> float:
+        return float(np.sqrt(self.angular_momentum @ self.angular_momentum))
+
+    def com_drift(self) -> float:
+        return float(np.sqrt(self.center_of_mass @ self.center_of_mass))
+
+    @staticmethod
+    def csv_header() -> str:
+        """diagnostics.rs:170-172."""
+        return ("step,time,kinetic_energy,potential_energy,thermal_energy,total_energy,momentum_mag,"
+                "angular_momentum_mag,com_drift,virial_ratio")
+
+    def to_csv_row(self) -> str:
+        """diagnostics.rs:175-189 ({:.6e} / {:.10e} in Rust's exponent style)."""
+        def e(v, prec):
+            s = f"{v:.{prec}e}"
+            mant, ex = s.split("e")
+            return f"{mant}e{int(ex)}"
+        vals = [e(self.kinetic_energy, 10), e(self.potential_energy, 10), e(self.thermal_energy, 10),
+                e(self.total_energy, 10), e(self.momentum_magnitude(), 10), e(self.angular_momentum_magnitude(), 10),
+                e(self.com_drift(), 10)]
+        return f"{self.step},{e(self.time, 6)}," + ",".join(vals) + f",{self.virial_ratio:.6f}"
+
+
+def compute_diagnostics(p: Particles, softening: float, time: float = 0.0, step: int = 0,
+                        ctx: Context | None = None, with_potential: bool = True) -> Diagnostics:
+    """diagnostics::compute (diagnostics.rs:37-39) on the GPU for a host Particles."""
+    c = ctx or default_context()
+    c.set_state(p)
+    d = c.diagnostics(softening, with_potential)
+    d.time, d.step = time, step
+    return d
+
+
+# ---- scenarios ----------------------------------------------------------------------
+class PlummerSphere:
+    """scenarios/plummer_sphere.rs:79-153."""
+
+    def __init__(self, n: int = 1000, scale_radius: float = 1.0, total_mass: float = 1.0, seed: int = 42):
+        self.n, self.scale_radius, self.total_mass, self.seed = n, scale_radius, total_mass, seed
+
+    def name(self) -> str:
+        return "Plummer Sphere"
+
+    def generate(self) -> Particles:
+        p = Particles(self.n)
+        check(L.load().gvs_ic_plummer(self.n, self.seed, self.scale_radius, self.total_mass, _ptr(p.x), _ptr(p.y),
+                                      _ptr(p.z), _ptr(p.vx), _ptr(p.vy), _ptr(p.vz), _ptr(p.mass)))
+        return p
+
+    def suggested_dt(self) -> float:
+        return math.sqrt(self.scale_radius ** 3 / (1.0 * self.total_mass)) / 100.0
+
+    def suggested_softening(self) -> float:
+        r_h = 1.305 * self.scale_radius
+        return (4.0 / 3.0 * math.pi * (r_h * r_h * r_h) / self.n) ** (1.0 / 3.0) * 0.5
+
+
+class TwoBody:
+    """scenarios/two_body.rs:17-106."""
+
+    def __init__(self, mass_ratio: float = 0.5, eccentricity: float = 0.5, semi_major_axis: float = 1.0):
+        self.mass_ratio, self.eccentricity, self.semi_major_axis = mass_ratio, eccentricity, semi_major_axis
+
+    def period(self) -> float:
+        return 2.0 * math.pi * math.sqrt(self.semi_major_axis ** 3 / 1.0)
+
+    def generate(self) -> Particles:
+        p = Particles(2)
+        check(L.load().gvs_ic_two_body(self.mass_ratio, self.eccentricity, self.semi_major_axis, _ptr(p.x),
+                                       _ptr(p.y), _ptr(p.z), _ptr(p.vx), _ptr(p.vy), _ptr(p.vz), _ptr(p.mass)))
+        return p
+
+    def suggested_dt(self) -> float:
+        return self.period() / 10000.0
+
+    def suggested_softening(self) -> float:
+        return self.semi_major_axis * (1.0 - self.eccentricity) * 0.001
+
+
+class EvrardCollapse:
+    """scenarios/evrard_collapse.rs:15-71 (uniform gas sphere)."""
+
+    def __init__(self, n_particles: int = 5000, total_mass: float = 1.0, radius: float = 1.0, u_0: float = 0.05,
+                 seed: int = 42):
+        self.n, self.total_mass, self.radius, self.u_0, self.seed = n_particles, total_mass, radius, u_0, seed
+
+    def generate(self) -> Particles:
+        p = Particles(self.n)
+        check(L.load().gvs_ic_evrard(self.n, self.seed, self.total_mass, self.radius, self.u_0, _ptr(p.x),
+                                     _ptr(p.y), _ptr(p.z), _ptr(p.mass), _ptr(p.internal_energy),
+                                     _ptr(p.smoothing_length)))
+        p.particle_type[:] = GAS
+        p.alpha_visc[:] = 1.0
+        return p
+
+    def suggested_softening(self) -> float:
+        vol = 4.0 / 3.0 * math.pi * self.radius ** 3
+        return 0.3 * (vol / self.n) ** (1.0 / 3.0)
+
+    def suggested_dt(self) -> float:
+        return math.pi / 2 * math.sqrt(self.radius ** 3 / (2.0 * self.total_mass)) / 500.0
+
+
+def collision(n: int, seed: int = 7, separation: float = 20.0) -> Particles:
+    """Two Plummer spheres on a parabolic head-on orbit (see gvs_ic_collision)."""
+    p = Particles(n)
+    check(L.load().gvs_ic_collision(n, seed, separation, _ptr(p.x), _ptr(p.y), _ptr(p.z), _ptr(p.vx), _ptr(p.vy),
+                                    _ptr(p.vz), _ptr(p.mass)))
+    return p
+
+
+def gas_sphere_1r(n: int, total_mass: float = 1.0, radius: float = 1.0, u0: float = 0.05,
+                  eta: float = 1.2) -> Particles:
+    """Seedless rho ~ 1/r gas sphere (see gvs_ic_gas_sphere_1r)."""
+    p = Particles(n)
+    check(L.load().gvs_ic_gas_sphere_1r(n, total_mass, radius, u0, eta, _ptr(p.x), _ptr(p.y), _ptr(p.z),
+                                        _ptr(p.mass), _ptr(p.internal_energy), _ptr(p.smoothing_length)))
+    p.particle_type[:] = GAS
+    p.alpha_visc[:] = 1.0
+    return p
+
+
+def ensemble_sizes(count: int, seed: int, lo: float = 256, hi: float = 16384) -> np.ndarray:
+    out = np.zeros(count, dtype=np.int64)
+    check(L.load().gvs_ic_ensemble_sizes(count, seed, lo, hi, _ptr(out)))
+    return out

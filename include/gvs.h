@@ -1,0 +1,187 @@
+/*
+ * gvs.h -- C ABI of the gravis GB300 engine (libgvs.so, CUDA sm_103a).
+ *
+ * The engine replaces the hot path of gravis sim-core: force calculation and
+ * time integration.  Each entry point names the sim-core interface it stands
+ * in for (paths inside the gravis repository, file:line).  Plain pointers and
+ * sizes only; no C++ or torch types cross this boundary.
+ *
+ * Conventions
+ *   - Every function returns a gvs_status; nothing throws or aborts across
+ *     the ABI.  gvs_last_error() gives the message of the last failure.
+ *   - Host arrays are f64 structure-of-arrays of length n, in the caller's
+ *     particle order, exactly the Vec<f64> fields of sim-core's Particles
+ *     (crates/sim-core/src/particle.rs:22-64).  They are borrowed for the
+ *     duration of one call only.
+ *   - A context owns one CUDA stream, the device-resident copy of the state
+ *     and all scratch.  One context is used by one host thread at a time.
+ *   - "accumulate" means: results are ADDED to the caller's arrays, which the
+ *     caller zeroed before, as GravitySolver::compute_accelerations requires
+ *     (crates/sim-core/src/gravity.rs:6-10).
+ */
+#ifndef GVS_H
+#define GVS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gvs_status {
+    GVS_OK = 0,
+    GVS_ERR_INVALID_ARG = 1,  /* bad pointer / size / parameter */
+    GVS_ERR_OOM = 2,          /* device or pinned allocation failed */
+    GVS_ERR_LAUNCH = 3,       /* kernel launch or CUDA runtime error */
+    GVS_ERR_DEVICE = 4,       /* a kernel raised a flag in the device error word */
+    GVS_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up */
+    GVS_ERR_INJECTED = 6,     /* fault injected on the host (GVS_FAULT / gvs_set_fault) */
+    GVS_ERR_NO_DEVICE = 7,    /* no CUDA device / wrong architecture */
+    GVS_ERR_STATE = 8         /* call made in the wrong state (e.g. no particles) */
+} gvs_status;
+
+/* Force precision of the direct-sum (and tree-walk) paths. */
+enum {
+    GVS_PREC_FP64_EXACT = 0, /* f64, j ascending, no FMA: bit-identical to BruteForce (gravity.rs:55-78) */
+    GVS_PREC_FP64 = 1,       /* f64 tiled kernel with FMA and rsqrt: the FP64 form of the mixed kernel */
+    GVS_PREC_FP32 = 2,       /* f32 absolute positions, plain f32 accumulation */
+    GVS_PREC_MIXED = 3       /* f32 pairs on f64 tile centre + f32 offsets, two-sum compensated sums */
+};
+
+/* Gravity algorithm selector (headless --algorithm, crates/headless/src/main.rs:114-121). */
+enum {
+    GVS_ALGO_NONE = 0,   /* NoGravity (gravity.rs:13-19) */
+    GVS_ALGO_DIRECT = 1, /* BruteForce (gravity.rs:47-80) */
+    GVS_ALGO_BH = 2      /* BarnesHut (barnes_hut.rs:21-192) */
+};
+
+typedef struct gvs_ctx gvs_ctx;
+
+/* Diagnostics::compute / compute_fast (crates/sim-core/src/diagnostics.rs:37-148). */
+typedef struct gvs_diag {
+    double kinetic_energy, potential_energy, thermal_energy, total_energy;
+    double momentum[3], angular_momentum[3], center_of_mass[3], center_of_mass_velocity[3];
+    double virial_ratio;
+} gvs_diag;
+
+/* SphSolver::new + ForceParams::default (crates/sim-core/src/sph/solver.rs:40-49,
+ * crates/sim-core/src/sph/forces.rs:30-41). */
+typedef struct gvs_sph_params {
+    double gamma, eta, cfl_factor, force_factor, h_max;
+    double beta_visc, alpha_min, alpha_max, alpha_cond, sigma_visc;
+} gvs_sph_params;
+
+/* Kernel-time counters of one context (CUDA events on the context stream). */
+typedef struct gvs_profile {
+    double force_ms;          /* device time of the force kernels since reset */
+    long long force_launches; /* force-kernel launches since reset */
+    long long launches;       /* all kernel launches since reset */
+    double force_flops;       /* algorithmic flops of those launches (20 per pair) */
+    double force_bytes;       /* algorithmic bytes of those launches */
+} gvs_profile;
+
+/* ---- library / context ---------------------------------------------------- */
+const char *gvs_version(void);
+/* Creates a context on `device` (one stream, no particles yet). */
+gvs_status gvs_create(gvs_ctx **out, int device);
+gvs_status gvs_destroy(gvs_ctx *ctx);
+/* Copies the last error message of ctx (or of the library if ctx is NULL). */
+gvs_status gvs_last_error(const gvs_ctx *ctx, char *buf, size_t len);
+/* Host-side fault injection: "none", "alloc", "launch", "nan@K" (K = step). */
+gvs_status gvs_set_fault(gvs_ctx *ctx, const char *spec);
+/* Waits for the context stream; returns GVS_ERR_DEVICE if a kernel flagged an error. */
+gvs_status gvs_sync(gvs_ctx *ctx);
+/* Reads and clears the device error word (bit flags). */
+gvs_status gvs_device_errors(gvs_ctx *ctx, unsigned *flags);
+
+/* ---- state transfer (Particles <-> device) ------------------------------------ */
+/* Uploads the particle state (Particles fields, particle.rs:22-64).  ptype, u,
+ * h and alpha may be NULL (non-gas system).  Accelerations are zeroed. */
+gvs_status gvs_set_state(gvs_ctx *ctx, size_t n, const double *x, const double *y, const double *z,
+                         const double *vx, const double *vy, const double *vz, const double *mass,
+                         const uint8_t *ptype, const double *u, const double *h, const double *alpha);
+/* Downloads any subset of the state; NULL pointers are skipped. */
+gvs_status gvs_get_state(gvs_ctx *ctx, double *x, double *y, double *z, double *vx, double *vy, double *vz,
+                         double *ax, double *ay, double *az);
+/* Sets / reads the resident accelerations (e.g. after a snapshot restore). */
+gvs_status gvs_set_accelerations(gvs_ctx *ctx, const double *ax, const double *ay, const double *az);
+gvs_status gvs_get_gas(gvs_ctx *ctx, double *density, double *pressure, double *u, double *du_dt, double *h,
+                       double *sound_speed, double *alpha);
+size_t gvs_count(const gvs_ctx *ctx);
+
+/* ---- GravitySolver drop-ins (host arrays in, accelerations accumulated) -------- */
+/* BruteForce::compute_accelerations (crates/sim-core/src/gravity.rs:47-80).
+ * Uploads x,y,z,mass (replacing the resident positions), adds a_i to ax..az. */
+gvs_status gvs_gravity_direct(gvs_ctx *ctx, size_t n, const double *x, const double *y, const double *z,
+                              const double *mass, double softening, int precision, double *ax, double *ay,
+                              double *az);
+
+/* ---- device-resident force / integration --------------------------------------- */
+/* clear_accelerations + compute_accelerations on the resident state
+ * (integrator.rs:67-68): a = forces (overwrites the resident a). */
+gvs_status gvs_compute_forces(gvs_ctx *ctx, int algo, int precision, double softening, double theta);
+/* LeapfrogKDK::step x nsteps on the resident state (crates/sim-core/src/integrator.rs:42-76).
+ * Requires valid resident accelerations (as after gvs_compute_forces). */
+gvs_status gvs_kdk_steps(gvs_ctx *ctx, int algo, int precision, double softening, double theta, double dt,
+                         long long nsteps);
+/* Integrator::step drop-in with host arrays (integrator.rs:5-8,42-76): uploads
+ * x,v,a,m, runs one KDK step on the GPU and writes x,v,a back. */
+gvs_status gvs_kdk_step_host(gvs_ctx *ctx, size_t n, double *x, double *y, double *z, double *vx, double *vy,
+                             double *vz, double *ax, double *ay, double *az, const double *mass, int algo,
+                             int precision, double softening, double theta, double dt);
+
+/* ---- diagnostics (crates/sim-core/src/diagnostics.rs:37-148) ------------------- */
+gvs_status gvs_diagnostics(gvs_ctx *ctx, double softening, int with_potential, gvs_diag *out);
+
+/* ---- direct-sum accuracy probe ---------------------------------------------------- */
+/* Accelerations of the targets idx[0..nidx) against all resident particles,
+ * written (not accumulated) to out_ax..out_az (host arrays of length nidx). */
+gvs_status gvs_direct_subset(gvs_ctx *ctx, int precision, double softening, const int64_t *idx, size_t nidx,
+                             double *out_ax, double *out_ay, double *out_az);
+
+/* Autotuner (no reference counterpart): times the compiled (block size, targets per
+ * thread) variants of the f32 pair kernel on the resident state, keeps the fastest
+ * for this N (power-of-two bucket) and reports it. */
+gvs_status gvs_autotune_direct(gvs_ctx *ctx, int precision, double softening, int *nthreads, int *ipt, double *ms);
+
+/* ---- initial conditions (crates/sim-core/src/scenarios/) --------------------------- */
+/* PlummerSphere::generate (plummer_sphere.rs:106-133): ChaCha20Rng::seed_from_u64(seed),
+ * sample_plummer_particle x n, shift_to_com_frame.  Outputs have length n. */
+gvs_status gvs_ic_plummer(size_t n, uint64_t seed, double scale_radius, double total_mass, double *x, double *y,
+                          double *z, double *vx, double *vy, double *vz, double *mass);
+
+/* TwoBody::generate (scenarios/two_body.rs:49-94): 2 particles at periapsis, COM frame. */
+gvs_status gvs_ic_two_body(double mass_ratio, double e, double a, double *x, double *y, double *z, double *vx,
+                           double *vy, double *vz, double *mass);
+/* EvrardCollapse::generate (scenarios/evrard_collapse.rs:45-57, mod.rs:33-52): uniform gas
+ * sphere by cube rejection; outputs positions, mass, u and h (velocities are zero). */
+gvs_status gvs_ic_evrard(size_t n, uint64_t seed, double total_mass, double radius, double u0, double *x, double *y,
+                         double *z, double *mass, double *u, double *h);
+/* Two Plummer spheres (n/2 each, total mass 1, scale radius 1) from one ChaCha20 stream,
+ * `separation` apart on x, parabolic head-on approach, COM frame (composed from
+ * sample_plummer_particle, plummer_sphere.rs:13-58, as galaxy_collision.rs:94-155 does). */
+gvs_status gvs_ic_collision(size_t n, uint64_t seed, double separation, double *x, double *y, double *z,
+                            double *vx, double *vy, double *vz, double *mass);
+/* Seedless gas sphere with rho ~ 1/r (stretched, jittered cubic lattice); no reference
+ * counterpart (the reference's Evrard sphere is uniform). */
+gvs_status gvs_ic_gas_sphere_1r(size_t n, double total_mass, double radius, double u0, double eta, double *x,
+                                double *y, double *z, double *mass, double *u, double *h);
+/* N_i = round(exp(U[ln lo, ln hi])) for batched ensembles, engine RNG (no reference counterpart). */
+gvs_status gvs_ic_ensemble_sizes(size_t count, uint64_t seed, double lo, double hi, int64_t *sizes);
+
+/* ---- timing / profiling ------------------------------------------------------------- */
+gvs_status gvs_profile_enable(gvs_ctx *ctx, int on);  /* resets counters */
+gvs_status gvs_profile_read(gvs_ctx *ctx, gvs_profile *out);
+/* Records event `slot` (0..15) on the context stream; elapsed ms between two slots. */
+gvs_status gvs_event_record(gvs_ctx *ctx, int slot);
+gvs_status gvs_event_elapsed(gvs_ctx *ctx, int slot_a, int slot_b, float *ms);
+/* Writes a buffer larger than L2 on the context stream (cold-cache timing). */
+gvs_status gvs_l2_flush(gvs_ctx *ctx);
+/* Measured FP32 FMA throughput of this GPU (TFLOP/s, 2 flop per FMA). */
+gvs_status gvs_measure_fp32_peak(gvs_ctx *ctx, double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
