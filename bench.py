@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--fp64-n", type=int, default=1 << 16, help="N of the bounded FP64 comparison run")
     ap.add_argument("--cpu-targets", type=int, default=1024, help="targets in the bounded CPU sample")
     ap.add_argument("--no-extras", action="store_true", help="skip FP64 / accuracy / CPU side measurements")
+    ap.add_argument("--no-autotune", action="store_true", help="use the default kernel shape (profiling runs)")
     return ap.parse_args()
 
 
@@ -189,7 +190,7 @@ def run_engine(a, d: Dist):
     p = G.PlummerSphere(a.n, seed=a.seed).generate()
     eps, dt = w["eps"], a.dt
     ctx.set_state(p)
-    tune = ctx.autotune(prec, eps) if prec in (2, 3) else None
+    tune = ctx.autotune(prec, eps) if prec in (2, 3) and not a.no_autotune else None
     ctx.set_state(p)
     ctx.compute_forces(G.ALGO_DIRECT, prec, eps)
     for _ in range(a.warmup):

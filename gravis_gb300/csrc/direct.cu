@@ -120,14 +120,19 @@ __global__ void k_morton(const double *__restrict__ x, const double *__restrict_
 // ---------------------------------------------------------------------------
 // packing of source tiles
 // ---------------------------------------------------------------------------
-// Tile t holds sorted slots [t*TJ, (t+1)*TJ) in tile_f4(TJ) = 2 + 2*TJ float4:
-// [0] centre hi (x,y,z,0), [1] centre lo, then per member (x,x,y,y)(z,z,m,m).
-// MIXED: centre = midpoint of the members' bounding box in f64, stored as an
-// f32 hi + lo pair whose exact f64 sum is the canonical centre; members are
-// f32 offsets from it.  FP32: centre 0, members as rounded absolute positions.
-// Members are stored twice per component so the pair kernel reads ready-made
-// f32x2 broadcast pairs.  Padding slots sit at the centre with zero mass.
-__host__ __device__ constexpr int tile_f4(int tj) { return 2 + 2 * tj; }
+// Tile t holds sorted slots [t*TJ, (t+1)*TJ) in tile_f4(TJ) = 2 + 4*TJ float4:
+//   [0]            centre hi (x, y, z, r)   r = max |offset| over members (f32, rounded up)
+//   [1]            centre lo (x, y, z, 0)
+//   [2+2k, 3+2k]   member k offset hi: (x,x,y,y) (z,z,m,m)
+//   [2+2TJ+2k, ..] member k offset lo: (x,x,y,y) (z,z,0,0)
+// MIXED: the centre is the midpoint of the members' bounding box in f64, kept
+// as an f32 hi + lo pair whose exact f64 sum is the canonical centre c; each
+// member stores off = x - c as f32 hi + f32 lo (hi + lo = x - c to ~2^-48).
+// The fast path reads only hi; tiles close to the targets also use lo.
+// FP32: centre 0, members as rounded absolute positions, lo = 0.
+// Components are stored twice so the pair kernel reads ready-made f32x2
+// broadcast pairs.  Padding slots sit at the centre with zero mass.
+__host__ __device__ constexpr int tile_f4(int tj) { return 2 + 4 * tj; }
 
 template <int TJ, bool MIXED>
 __global__ void __launch_bounds__(TJ) k_pack32(const double *__restrict__ X, const double *__restrict__ Y,
@@ -135,6 +140,8 @@ __global__ void __launch_bounds__(TJ) k_pack32(const double *__restrict__ X, con
                                                const uint32_t *__restrict__ perm, size_t n,
                                                float4 *__restrict__ pack) {
     constexpr int TF4 = tile_f4(TJ);
+    __shared__ double red[TJ / 32][6];
+    __shared__ float rred[TJ / 32];
     const int t = blockIdx.x, tid = threadIdx.x;
     const size_t s = (size_t)t * TJ + tid;
     const bool valid = s < n;
@@ -144,7 +151,6 @@ __global__ void __launch_bounds__(TJ) k_pack32(const double *__restrict__ X, con
     double c[3] = {0.0, 0.0, 0.0};
     float chi[3] = {0.f, 0.f, 0.f}, clo[3] = {0.f, 0.f, 0.f};
     if (MIXED) {
-        __shared__ double red[TJ / 32][6];
         double mn[3] = {p[0], p[1], p[2]}, mx[3] = {p[0], p[1], p[2]};
 #pragma unroll
         for (int d = 0; d < 3; ++d)
@@ -165,17 +171,30 @@ __global__ void __launch_bounds__(TJ) k_pack32(const double *__restrict__ X, con
             c[d] = (double)chi[d] + (double)clo[d];  // exact: the canonical centre
         }
     }
-    float off[3];
+    float oh[3], ol[3];
+    float rad = 0.f;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) off[d] = valid ? __double2float_rn(p[d] - c[d]) : 0.f;
+    for (int d = 0; d < 3; ++d) {
+        const double e = p[d] - c[d];
+        oh[d] = valid ? __double2float_rn(e) : 0.f;
+        ol[d] = (valid && MIXED) ? __double2float_rn(e - (double)oh[d]) : 0.f;
+        rad = fmaxf(rad, fabsf(oh[d]));
+    }
+    for (int off = 16; off > 0; off >>= 1) rad = fmaxf(rad, __shfl_xor_sync(0xFFFFFFFFu, rad, off));
+    if ((tid & 31) == 0) rred[tid >> 5] = rad;
+    __syncthreads();
     float4 *tile = pack + (size_t)t * TF4;
     if (tid == 0) {
-        tile[0] = make_float4(chi[0], chi[1], chi[2], 0.f);
+        float r = rred[0];
+        for (int w = 1; w < TJ / 32; ++w) r = fmaxf(r, rred[w]);
+        tile[0] = make_float4(chi[0], chi[1], chi[2], r * 1.0001f);
         tile[1] = make_float4(clo[0], clo[1], clo[2], 0.f);
     }
     const float mf = (float)mass;
-    tile[2 + 2 * tid] = make_float4(off[0], off[0], off[1], off[1]);
-    tile[3 + 2 * tid] = make_float4(off[2], off[2], mf, mf);
+    tile[2 + 2 * tid] = make_float4(oh[0], oh[0], oh[1], oh[1]);
+    tile[3 + 2 * tid] = make_float4(oh[2], oh[2], mf, mf);
+    tile[2 + 2 * TJ + 2 * tid] = make_float4(ol[0], ol[0], ol[1], ol[1]);
+    tile[3 + 2 * TJ + 2 * tid] = make_float4(ol[2], ol[2], 0.f, 0.f);
 }
 
 __global__ void k_pack64(const double *__restrict__ X, const double *__restrict__ Y, const double *__restrict__ Z,
@@ -231,6 +250,62 @@ __device__ __forceinline__ void two_sum2(f2 &hi, f2 &lo, f2 v) {
     hi = s;
 }
 
+// One source tile against NP target pairs.  nx.. hold -(x_i - c_J) per pair.
+// PRECISE adds the f32 lo parts of both sides (float-float separations) for
+// tiles close to the targets, where f32 offsets alone lose relative accuracy.
+template <int TJ, int NP, bool PRECISE, bool GUARD>
+__device__ __forceinline__ void tile_pairs(const float4 *__restrict__ tile, const f2 *nx, const f2 *ny, const f2 *nz,
+                                           const f2 *nxl, const f2 *nyl, const f2 *nzl, f2 e2, f2 *accx,
+                                           f2 *accy, f2 *accz) {
+    const f2 *jd = reinterpret_cast<const f2 *>(tile + 2);
+    const f2 *jl = reinterpret_cast<const f2 *>(tile + 2 + 2 * TJ);
+#pragma unroll 4
+    for (int j = 0; j < TJ; ++j) {
+        const f2 xj = jd[4 * j + 0], yj = jd[4 * j + 1], zj = jd[4 * j + 2], mj = jd[4 * j + 3];
+        f2 xl = 0ull, yl = 0ull, zl = 0ull;
+        if (PRECISE) { xl = jl[4 * j + 0]; yl = jl[4 * j + 1]; zl = jl[4 * j + 2]; }
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            f2 dx = add2(xj, nx[p]);
+            f2 dy = add2(yj, ny[p]);
+            f2 dz = add2(zj, nz[p]);
+            if (PRECISE) {
+                dx = add2(dx, add2(xl, nxl[p]));
+                dy = add2(dy, add2(yl, nyl[p]));
+                dz = add2(dz, add2(zl, nzl[p]));
+            }
+            f2 r2 = fma2(dx, dx, e2);
+            r2 = fma2(dy, dy, r2);
+            r2 = fma2(dz, dz, r2);
+            float ra, rb;
+            upk(r2, ra, rb);
+            if (GUARD) { ra = fmaxf(ra, 1e-24f); rb = fmaxf(rb, 1e-24f); }
+            const f2 ri = pk(rsqrt_approx(ra), rsqrt_approx(rb));
+            f2 sm = mul2(mj, ri);
+            const f2 ri2 = mul2(ri, ri);
+            sm = mul2(sm, ri2);
+            accx[p] = fma2(sm, dx, accx[p]);
+            accy[p] = fma2(sm, dy, accy[p]);
+            accz[p] = fma2(sm, dz, accz[p]);
+        }
+    }
+}
+
+// -(c_I + off_i - c_J) as an f32 hi + lo pair, from the f32 hi/lo parts of the
+// two centres and of the offset (two-sum at each step, error ~2^-48 relative).
+__device__ __forceinline__ void ff_rel(float cih, float cil, float cjh, float cjl, float oh, float ol, float &nh,
+                                       float &nl) {
+    const float th = __fsub_rn(cih, cjh);
+    const float b1 = __fsub_rn(th, cih);
+    const float te = __fadd_rn(__fsub_rn(cih, __fsub_rn(th, b1)), __fsub_rn(-cjh, b1));
+    const float dl = __fadd_rn(te, __fsub_rn(cil, cjl));
+    const float sh = __fadd_rn(th, oh);
+    const float b2 = __fsub_rn(sh, th);
+    const float se = __fadd_rn(__fsub_rn(th, __fsub_rn(sh, b2)), __fsub_rn(oh, b2));
+    nh = -sh;
+    nl = -__fadd_rn(__fadd_rn(se, dl), ol);
+}
+
 // ---------------------------------------------------------------------------
 // tiled f32 kernel (FP32 and MIXED)
 // ---------------------------------------------------------------------------
@@ -276,20 +351,29 @@ __global__ void __launch_bounds__(NT) k_direct32(const float4 *__restrict__ pack
         }
     }
 
-    // target offsets from their own tile centre, packed by pair
-    f2 ox[NP], oy[NP], oz[NP];
+    // target offsets from their own tile centre (hi and lo), packed by pair
+    f2 ox[NP], oy[NP], oz[NP], oxl[NP], oyl[NP], ozl[NP];
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
-        float v[2][3];
+        float v[2][6];
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
             const float4 *tp = pack + ((size_t)blockIdx.x * IPT + 2 * p + q) * TF4;
             const float4 a = __ldg(tp + 2 + 2 * tid), b = __ldg(tp + 3 + 2 * tid);
             v[q][0] = a.x; v[q][1] = a.z; v[q][2] = b.x;
+            if (MIXED) {
+                const float4 al = __ldg(tp + 2 + 2 * TJ + 2 * tid), bl = __ldg(tp + 3 + 2 * TJ + 2 * tid);
+                v[q][3] = al.x; v[q][4] = al.z; v[q][5] = bl.x;
+            } else {
+                v[q][3] = v[q][4] = v[q][5] = 0.f;
+            }
         }
         ox[p] = pk(v[0][0], v[1][0]);
         oy[p] = pk(v[0][1], v[1][1]);
         oz[p] = pk(v[0][2], v[1][2]);
+        oxl[p] = pk(v[0][3], v[1][3]);
+        oyl[p] = pk(v[0][4], v[1][4]);
+        ozl[p] = pk(v[0][5], v[1][5]);
     }
 
     f2 accx[NP], accy[NP], accz[NP], hx[NP], hy[NP], hz[NP], lx[NP], ly[NP], lz[NP];
@@ -305,19 +389,47 @@ __global__ void __launch_bounds__(NT) k_direct32(const float4 *__restrict__ pack
         const bool ok = mbar_wait_bounded(&bar[s], parity, err);
         if (__syncthreads_or(!ok)) { bail = true; break; }
         const float4 *tile = smem + s * TF4;
-        f2 nx[NP], ny[NP], nz[NP];
+        f2 nx[NP], ny[NP], nz[NP], nxl[NP], nyl[NP], nzl[NP];
+        bool near = false;
         if (MIXED) {
-            const float4 jh = tile[0], jl = tile[1];
+            const float4 jh = tile[0], jo = tile[1];
+            // near-field test (block-uniform): Chebyshev distance of the tile
+            // centres against twice the sum of the tile radii
 #pragma unroll
-            for (int p = 0; p < NP; ++p) {
-                const float4 h0 = ci[2 * p][0], l0 = ci[2 * p][1], h1 = ci[2 * p + 1][0], l1 = ci[2 * p + 1][1];
-                // -(c_I - c_J) per lane, then minus the target offset
-                const f2 dx = pk(-((h0.x - jh.x) + (l0.x - jl.x)), -((h1.x - jh.x) + (l1.x - jl.x)));
-                const f2 dy = pk(-((h0.y - jh.y) + (l0.y - jl.y)), -((h1.y - jh.y) + (l1.y - jl.y)));
-                const f2 dz = pk(-((h0.z - jh.z) + (l0.z - jl.z)), -((h1.z - jh.z) + (l1.z - jl.z)));
-                nx[p] = sub2(dx, ox[p]);
-                ny[p] = sub2(dy, oy[p]);
-                nz[p] = sub2(dz, oz[p]);
+            for (int k = 0; k < IPT; ++k) {
+                const float4 h = ci[k][0];
+                const float dist = fmaxf(fabsf(h.x - jh.x), fmaxf(fabsf(h.y - jh.y), fabsf(h.z - jh.z)));
+                near |= dist < 2.0f * (h.w + jh.w) + 1e-30f;
+            }
+            if (near) {
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    float o[2][6], hh[2][3], ll[2][3];
+                    upk(ox[p], o[0][0], o[1][0]); upk(oy[p], o[0][1], o[1][1]); upk(oz[p], o[0][2], o[1][2]);
+                    upk(oxl[p], o[0][3], o[1][3]); upk(oyl[p], o[0][4], o[1][4]); upk(ozl[p], o[0][5], o[1][5]);
+#pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        const float4 h = ci[2 * p + q][0], l = ci[2 * p + q][1];
+                        ff_rel(h.x, l.x, jh.x, jo.x, o[q][0], o[q][3], hh[q][0], ll[q][0]);
+                        ff_rel(h.y, l.y, jh.y, jo.y, o[q][1], o[q][4], hh[q][1], ll[q][1]);
+                        ff_rel(h.z, l.z, jh.z, jo.z, o[q][2], o[q][5], hh[q][2], ll[q][2]);
+                    }
+                    nx[p] = pk(hh[0][0], hh[1][0]); nxl[p] = pk(ll[0][0], ll[1][0]);
+                    ny[p] = pk(hh[0][1], hh[1][1]); nyl[p] = pk(ll[0][1], ll[1][1]);
+                    nz[p] = pk(hh[0][2], hh[1][2]); nzl[p] = pk(ll[0][2], ll[1][2]);
+                }
+            } else {
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    const float4 h0 = ci[2 * p][0], l0 = ci[2 * p][1], h1 = ci[2 * p + 1][0], l1 = ci[2 * p + 1][1];
+                    // -(c_I - c_J) per lane, then minus the target offset
+                    const f2 dx = pk(-((h0.x - jh.x) + (l0.x - jo.x)), -((h1.x - jh.x) + (l1.x - jo.x)));
+                    const f2 dy = pk(-((h0.y - jh.y) + (l0.y - jo.y)), -((h1.y - jh.y) + (l1.y - jo.y)));
+                    const f2 dz = pk(-((h0.z - jh.z) + (l0.z - jo.z)), -((h1.z - jh.z) + (l1.z - jo.z)));
+                    nx[p] = sub2(dx, ox[p]);
+                    ny[p] = sub2(dy, oy[p]);
+                    nz[p] = sub2(dz, oz[p]);
+                }
             }
         } else {
 #pragma unroll
@@ -327,30 +439,10 @@ __global__ void __launch_bounds__(NT) k_direct32(const float4 *__restrict__ pack
                 nz[p] = sub2(0ull, oz[p]);
             }
         }
-        const f2 *jd = reinterpret_cast<const f2 *>(tile + 2);
-#pragma unroll 4
-        for (int j = 0; j < TJ; ++j) {
-            const f2 xj = jd[4 * j + 0], yj = jd[4 * j + 1], zj = jd[4 * j + 2], mj = jd[4 * j + 3];
-#pragma unroll
-            for (int p = 0; p < NP; ++p) {
-                const f2 dx = add2(xj, nx[p]);
-                const f2 dy = add2(yj, ny[p]);
-                const f2 dz = add2(zj, nz[p]);
-                f2 r2 = fma2(dx, dx, e2);
-                r2 = fma2(dy, dy, r2);
-                r2 = fma2(dz, dz, r2);
-                float ra, rb;
-                upk(r2, ra, rb);
-                if (GUARD) { ra = fmaxf(ra, 1e-24f); rb = fmaxf(rb, 1e-24f); }
-                const f2 ri = pk(rsqrt_approx(ra), rsqrt_approx(rb));
-                f2 sm = mul2(mj, ri);
-                const f2 ri2 = mul2(ri, ri);
-                sm = mul2(sm, ri2);
-                accx[p] = fma2(sm, dx, accx[p]);
-                accy[p] = fma2(sm, dy, accy[p]);
-                accz[p] = fma2(sm, dz, accz[p]);
-            }
-        }
+        if (MIXED && near)
+            tile_pairs<TJ, NP, true, GUARD>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
+        else
+            tile_pairs<TJ, NP, false, GUARD>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
         if (MIXED) {
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
@@ -592,7 +684,7 @@ int auto_split(Ctx *c, int iblocks, int ntiles, int blocks_per_sm) {
 
 template <int NT, int NP, bool MIXED, bool GUARD>
 gvs_status launch32_t(Ctx *c, float eps2, int nsplit_req, double **partial_out, int *nsplit_out, size_t *npad_out) {
-    constexpr int NSTAGE = 4;
+    constexpr int NSTAGE = 3;
     constexpr int TJ = NT;
     constexpr int IPT = 2 * NP;
     constexpr int TF4 = tile_f4(TJ);
