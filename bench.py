@@ -261,7 +261,8 @@ def run_engine(a, d: Dist):
                         "traffic": (tr or {}).get("bytes_per_launch_scaled"),
                         "kernel": "k_direct32 (mixed, f32x2 pairs)", "kernel_ms": kernel_ms,
                         "flops_per_launch": flops, "peak_source": "measured FP32 FMA probe (gvs_measure_fp32_peak)",
-                        "interactions_per_s": flops / 20.0 / (kernel_ms * 1e-3)}
+                        "interactions_per_s": flops / 20.0 / (kernel_ms * 1e-3),
+                        "near_field_tile_fraction": prof["near_tile_visits"] / max(1.0, prof["tile_visits"])}
 
     if d.rank == 0 and not a.no_extras:
         extras = {}

@@ -41,7 +41,8 @@ class SphParams(C.Structure):
 
 class Profile(C.Structure):
     _fields_ = [("force_ms", C.c_double), ("force_launches", C.c_longlong), ("launches", C.c_longlong),
-                ("force_flops", C.c_double), ("force_bytes", C.c_double)]
+                ("force_flops", C.c_double), ("force_bytes", C.c_double), ("tile_visits", C.c_double),
+                ("near_tile_visits", C.c_double)]
 
 
 _P = C.c_void_p  # every array argument is passed as a raw address

@@ -15,12 +15,16 @@
 //
 //  FP32        f32 absolute positions, plain f32 accumulation.
 //
-//  MIXED       particles are put in Morton order and cut into tiles of TJ=256;
-//              each tile stores its centre in f64 (as an f32 hi+lo pair) and its
-//              members as f32 offsets from that centre.  For target i and source
+//  MIXED       particles are put in Hilbert order and cut into tiles of TJ
+//              (= the block size, 128 by default); each tile stores its centre
+//              in f64 (as an f32 hi+lo pair) and its members as f32 offsets
+//              from that centre (plus the f32 residual of each offset).  For target i and source
 //              tile J the kernel forms x_i - c_J = (c_I - c_J) + off_i from the
 //              hi/lo pairs, so pair separations are computed from small numbers
-//              and keep ~f32 relative precision even in the dense core.  The
+//              and keep ~f32 relative precision even in the dense core.  Tiles
+//              whose bounding boxes nearly touch the target tile (Chebyshev
+//              centre distance < half the sum of the radii) add the residuals
+//              (float-float separations), which keeps close pairs accurate.  The
 //              per-tile partial force is accumulated in f32 and folded into a
 //              (hi, lo) two-sum accumulator, so summation error does not grow
 //              with N.  Pair arithmetic uses packed f32x2 FMA/ADD/MUL (two
@@ -85,35 +89,57 @@ __global__ void k_bbox_final(double *part, int nparts) {
         }
 }
 
-// 21 bits per axis -> 63-bit Morton key.  The bounding box of a Plummer sphere
-// is set by a few outliers (r ~ 1e3 at N = 2^20), so coarse keys would leave
-// the whole core inside one cell; 21 bits keep core tiles compact.
-__device__ __forceinline__ uint64_t spread21(uint64_t v) {
-    v &= 0x1FFFFFull;
-    v = (v | (v << 32)) & 0x1F00000000FFFFull;
-    v = (v | (v << 16)) & 0x1F0000FF0000FFull;
-    v = (v | (v << 8)) & 0x100F00F00F00F00Full;
-    v = (v | (v << 4)) & 0x10C30C30C30C30C3ull;
-    v = (v | (v << 2)) & 0x1249249249249249ull;
-    return v;
+// 63-bit Hilbert key of a point quantised to 21 bits per axis (Skilling's
+// transpose method, "Programming the Hilbert curve", AIP Conf. Proc. 707, 2004).
+// The bounding box of a Plummer sphere is set by a few outliers (r ~ 1e3 at
+// N = 2^20), so 21 bits are needed to resolve the core; Hilbert rather than
+// Morton order because consecutive runs of a Hilbert curve stay contiguous,
+// which keeps the 128-particle tiles (and their f32 offsets) small.
+__device__ __forceinline__ uint64_t hilbert_key(uint32_t x0, uint32_t x1, uint32_t x2) {
+    uint32_t X[3] = {x0, x1, x2};
+    const uint32_t M = 1u << 20;
+    for (uint32_t Q = M; Q > 1; Q >>= 1) {
+        const uint32_t P = Q - 1;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            if (X[i] & Q) {
+                X[0] ^= P;
+            } else {
+                const uint32_t t = (X[0] ^ X[i]) & P;
+                X[0] ^= t;
+                X[i] ^= t;
+            }
+        }
+    }
+    X[1] ^= X[0];
+    X[2] ^= X[1];
+    uint32_t t = 0;
+    for (uint32_t Q = M; Q > 1; Q >>= 1)
+        if (X[2] & Q) t ^= Q - 1;
+    X[0] ^= t; X[1] ^= t; X[2] ^= t;
+    uint64_t key = 0;
+    for (int b = 20; b >= 0; --b)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) key = (key << 1) | ((X[i] >> b) & 1u);
+    return key;
 }
 
-__global__ void k_morton(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
-                         size_t n, const double *__restrict__ bb, uint64_t *__restrict__ keys,
-                         uint32_t *__restrict__ idx) {
+__global__ void k_hilbert(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
+                          size_t n, const double *__restrict__ bb, uint64_t *__restrict__ keys,
+                          uint32_t *__restrict__ idx) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double ext = fmax(fmax(bb[3] - bb[0], bb[4] - bb[1]), bb[5] - bb[2]);
     double inv = ext > 0.0 ? 2097151.99 / ext : 0.0;
-    uint64_t q[3];
+    uint32_t q[3];
     double v[3] = {x[i], y[i], z[i]};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         double t = (v[d] - bb[d]) * inv;
         t = fmin(fmax(t, 0.0), 2097151.0);
-        q[d] = (uint64_t)t;
+        q[d] = (uint32_t)t;
     }
-    keys[i] = spread21(q[0]) | (spread21(q[1]) << 1) | (spread21(q[2]) << 2);
+    keys[i] = hilbert_key(q[0], q[1], q[2]);
     idx[i] = (uint32_t)i;
 }
 
@@ -251,9 +277,10 @@ __device__ __forceinline__ void two_sum2(f2 &hi, f2 &lo, f2 v) {
 }
 
 // One source tile against NP target pairs.  nx.. hold -(x_i - c_J) per pair.
-// PRECISE adds the f32 lo parts of both sides (float-float separations) for
-// tiles close to the targets, where f32 offsets alone lose relative accuracy.
-template <int TJ, int NP, bool PRECISE, bool GUARD>
+// Pairs whose bit is set in MASK also add the f32 lo parts of both sides
+// (float-float separations): tiles close to the targets, where f32 offsets
+// alone would lose relative accuracy.
+template <int TJ, int NP, int MASK, bool GUARD>
 __device__ __forceinline__ void tile_pairs(const float4 *__restrict__ tile, const f2 *nx, const f2 *ny, const f2 *nz,
                                            const f2 *nxl, const f2 *nyl, const f2 *nzl, f2 e2, f2 *accx,
                                            f2 *accy, f2 *accz) {
@@ -263,13 +290,13 @@ __device__ __forceinline__ void tile_pairs(const float4 *__restrict__ tile, cons
     for (int j = 0; j < TJ; ++j) {
         const f2 xj = jd[4 * j + 0], yj = jd[4 * j + 1], zj = jd[4 * j + 2], mj = jd[4 * j + 3];
         f2 xl = 0ull, yl = 0ull, zl = 0ull;
-        if (PRECISE) { xl = jl[4 * j + 0]; yl = jl[4 * j + 1]; zl = jl[4 * j + 2]; }
+        if (MASK) { xl = jl[4 * j + 0]; yl = jl[4 * j + 1]; zl = jl[4 * j + 2]; }
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
             f2 dx = add2(xj, nx[p]);
             f2 dy = add2(yj, ny[p]);
             f2 dz = add2(zj, nz[p]);
-            if (PRECISE) {
+            if ((MASK >> p) & 1) {
                 dx = add2(dx, add2(xl, nxl[p]));
                 dy = add2(dy, add2(yl, nyl[p]));
                 dz = add2(dz, add2(zl, nzl[p]));
@@ -319,7 +346,8 @@ __device__ __forceinline__ void ff_rel(float cih, float cil, float cjh, float cj
 template <int NT, int NP, int NSTAGE, bool MIXED, bool GUARD>
 __global__ void __launch_bounds__(NT) k_direct32(const float4 *__restrict__ pack, int ntiles, int tiles_per_split,
                                                  float eps2, double *__restrict__ partial, size_t npad,
-                                                 unsigned *__restrict__ err) {
+                                                 unsigned *__restrict__ err,
+                                                 unsigned long long *__restrict__ near_count) {
     constexpr int TJ = NT;
     constexpr int IPT = 2 * NP;
     constexpr int TF4 = tile_f4(TJ);
@@ -382,6 +410,7 @@ __global__ void __launch_bounds__(NT) k_direct32(const float4 *__restrict__ pack
     const f2 e2 = pk(eps2, eps2);
 
     int it = 0;
+    unsigned near_tiles = 0;
     bool bail = false;
     for (; it < nt; ++it) {
         const int s = it % NSTAGE;
@@ -390,20 +419,23 @@ __global__ void __launch_bounds__(NT) k_direct32(const float4 *__restrict__ pack
         if (__syncthreads_or(!ok)) { bail = true; break; }
         const float4 *tile = smem + s * TF4;
         f2 nx[NP], ny[NP], nz[NP], nxl[NP], nyl[NP], nzl[NP];
-        bool near = false;
+        int mask = 0;
         if (MIXED) {
             const float4 jh = tile[0], jo = tile[1];
-            // near-field test (block-uniform): Chebyshev distance of the tile
-            // centres against twice the sum of the tile radii
+            // near-field test per pair (block-uniform): Chebyshev distance of the
+            // tile centres below half the sum of the two tile radii
 #pragma unroll
-            for (int k = 0; k < IPT; ++k) {
-                const float4 h = ci[k][0];
-                const float dist = fmaxf(fabsf(h.x - jh.x), fmaxf(fabsf(h.y - jh.y), fabsf(h.z - jh.z)));
-                near |= dist < 2.0f * (h.w + jh.w) + 1e-30f;
+            for (int p = 0; p < NP; ++p) {
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const float4 h = ci[2 * p + q][0];
+                    const float dist = fmaxf(fabsf(h.x - jh.x), fmaxf(fabsf(h.y - jh.y), fabsf(h.z - jh.z)));
+                    if (dist < 0.5f * (h.w + jh.w)) mask |= 1 << p;
+                }
             }
-            if (near) {
 #pragma unroll
-                for (int p = 0; p < NP; ++p) {
+            for (int p = 0; p < NP; ++p) {
+                if ((mask >> p) & 1) {
                     float o[2][6], hh[2][3], ll[2][3];
                     upk(ox[p], o[0][0], o[1][0]); upk(oy[p], o[0][1], o[1][1]); upk(oz[p], o[0][2], o[1][2]);
                     upk(oxl[p], o[0][3], o[1][3]); upk(oyl[p], o[0][4], o[1][4]); upk(ozl[p], o[0][5], o[1][5]);
@@ -417,10 +449,7 @@ __global__ void __launch_bounds__(NT) k_direct32(const float4 *__restrict__ pack
                     nx[p] = pk(hh[0][0], hh[1][0]); nxl[p] = pk(ll[0][0], ll[1][0]);
                     ny[p] = pk(hh[0][1], hh[1][1]); nyl[p] = pk(ll[0][1], ll[1][1]);
                     nz[p] = pk(hh[0][2], hh[1][2]); nzl[p] = pk(ll[0][2], ll[1][2]);
-                }
-            } else {
-#pragma unroll
-                for (int p = 0; p < NP; ++p) {
+                } else {
                     const float4 h0 = ci[2 * p][0], l0 = ci[2 * p][1], h1 = ci[2 * p + 1][0], l1 = ci[2 * p + 1][1];
                     // -(c_I - c_J) per lane, then minus the target offset
                     const f2 dx = pk(-((h0.x - jh.x) + (l0.x - jo.x)), -((h1.x - jh.x) + (l1.x - jo.x)));
@@ -429,6 +458,7 @@ __global__ void __launch_bounds__(NT) k_direct32(const float4 *__restrict__ pack
                     nx[p] = sub2(dx, ox[p]);
                     ny[p] = sub2(dy, oy[p]);
                     nz[p] = sub2(dz, oz[p]);
+                    nxl[p] = nyl[p] = nzl[p] = 0ull;
                 }
             }
         } else {
@@ -437,12 +467,19 @@ __global__ void __launch_bounds__(NT) k_direct32(const float4 *__restrict__ pack
                 nx[p] = sub2(0ull, ox[p]);
                 ny[p] = sub2(0ull, oy[p]);
                 nz[p] = sub2(0ull, oz[p]);
+                nxl[p] = nyl[p] = nzl[p] = 0ull;
             }
         }
-        if (MIXED && near)
-            tile_pairs<TJ, NP, true, GUARD>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
-        else
-            tile_pairs<TJ, NP, false, GUARD>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
+        near_tiles += (unsigned)__popc(mask);
+        if (!MIXED || mask == 0) {
+            tile_pairs<TJ, NP, 0, GUARD>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
+        } else if (NP == 1 || mask == 3) {
+            tile_pairs<TJ, NP, (NP == 1 ? 1 : 3), GUARD>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
+        } else if (mask == 1) {
+            tile_pairs<TJ, NP, 1, GUARD>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
+        } else {
+            tile_pairs<TJ, NP, 2, GUARD>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
+        }
         if (MIXED) {
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
@@ -465,6 +502,7 @@ __global__ void __launch_bounds__(NT) k_direct32(const float4 *__restrict__ pack
                 mbar_wait_bounded(&bar[j % NSTAGE], (unsigned)(j / NSTAGE) & 1u, err);
         return;
     }
+    if (tid == 0 && near_count) atomicAdd(near_count, (unsigned long long)near_tiles);
     double *dst = partial + (size_t)blockIdx.y * 3 * npad;
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
@@ -640,7 +678,7 @@ void set_smem(T kernel, int bytes) {
 // host side
 // ---------------------------------------------------------------------------
 
-// Morton order of the resident positions: c->perm[s] = caller index of sorted slot s.
+// Hilbert order of the resident positions: c->perm[s] = caller index of sorted slot s.
 gvs_status spatial_order(Ctx *c) {
     const size_t n = c->n;
     const int nb = std::min(c->num_sms * 4, std::max(1, ceil_div((long long)n, 256)));
@@ -652,11 +690,11 @@ gvs_status spatial_order(Ctx *c) {
     double *bb = as<double>(c->bbox_part);
     k_bbox_part<<<nb, 256, 0, c->stream>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z), n, bb);
     k_bbox_final<<<1, 32, 0, c->stream>>>(bb, nb);
-    k_morton<<<ceil_div((long long)n, 256), 256, 0, c->stream>>>(as<double>(c->x), as<double>(c->y),
+    k_hilbert<<<ceil_div((long long)n, 256), 256, 0, c->stream>>>(as<double>(c->x), as<double>(c->y),
                                                                   as<double>(c->z), n, bb, as<uint64_t>(c->keys),
                                                                   as<uint32_t>(c->perm));
     c->prof.launches += 3;
-    GVS_TRY(check_launch(c, "morton keys"));
+    GVS_TRY(check_launch(c, "hilbert keys"));
     uint64_t *ko;
     uint32_t *vo;
     GVS_TRY(radix_sort_u64(c, as<uint64_t>(c->keys), as<uint32_t>(c->perm), as<uint64_t>(c->keys_alt),
@@ -713,8 +751,9 @@ gvs_status launch32_t(Ctx *c, float eps2, int nsplit_req, double **partial_out, 
     GVS_CUDA(c, ensure(c, c->partial, (size_t)nsplit_eff * 3 * npad * sizeof(double)));
     dim3 grid(iblocks, nsplit_eff);
     if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], c->stream));
+    unsigned long long *nearc = reinterpret_cast<unsigned long long *>(err_ptr(c) + 8);
     kern<<<grid, NT, smem, c->stream>>>(as<float4>(c->jpack32), ntiles, tps, eps2, as<double>(c->partial), npad,
-                                        err_ptr(c));
+                                        err_ptr(c), nearc);
     c->prof.launches += 1;
     GVS_TRY(check_launch(c, "direct f32 kernel"));
     if (c->prof.on) {
@@ -727,6 +766,7 @@ gvs_status launch32_t(Ctx *c, float eps2, int nsplit_req, double **partial_out, 
         c->prof.force_flops += 20.0 * (double)n * (double)n;
         c->prof.force_bytes += (double)nsplit_eff * (double)npad * 24.0 + (double)iblocks * nsplit_eff * tps *
                                                                               (double)TF4 * 16.0;
+        c->prof.tile_visits += (double)iblocks * (double)ntiles;
     }
     *partial_out = as<double>(c->partial);
     *nsplit_out = nsplit_eff;
@@ -740,11 +780,10 @@ gvs_status launch32(Ctx *c, float eps2, double **partial, int *nsplit, size_t *n
     for (const auto &e : c->tune_cache)
         if (e.first == bucket) c->tune = e.second;
     const Tune &t = c->tune;
-    if (t.nthreads == 128 && t.ipt == 4) return launch32_t<128, 2, MIXED, GUARD>(c, eps2, t.nsplit, partial, nsplit, npad);
-    if (t.nthreads == 128 && t.ipt == 8) return launch32_t<128, 4, MIXED, GUARD>(c, eps2, t.nsplit, partial, nsplit, npad);
-    if (t.nthreads == 256 && t.ipt == 8) return launch32_t<256, 4, MIXED, GUARD>(c, eps2, t.nsplit, partial, nsplit, npad);
+    if (t.nthreads == 256 && t.ipt == 4) return launch32_t<256, 2, MIXED, GUARD>(c, eps2, t.nsplit, partial, nsplit, npad);
     if (t.nthreads == 256 && t.ipt == 2) return launch32_t<256, 1, MIXED, GUARD>(c, eps2, t.nsplit, partial, nsplit, npad);
-    return launch32_t<256, 2, MIXED, GUARD>(c, eps2, t.nsplit, partial, nsplit, npad);
+    if (t.nthreads == 128 && t.ipt == 2) return launch32_t<128, 1, MIXED, GUARD>(c, eps2, t.nsplit, partial, nsplit, npad);
+    return launch32_t<128, 2, MIXED, GUARD>(c, eps2, t.nsplit, partial, nsplit, npad);
 }
 
 gvs_status launch64(Ctx *c, double eps2, double **partial_out, int *nsplit_out, size_t *npad_out) {
@@ -837,7 +876,7 @@ gvs_status direct_forces(Ctx *c, int precision, double eps, bool accumulate) {
 // Times every compiled (block size, targets per thread) variant of the f32
 // pair kernel on the resident state and keeps the fastest for this N bucket.
 gvs_status autotune_direct(Ctx *c, int precision, double eps, int *best_nt, int *best_ipt, double *best_ms) {
-    static const int cand[][2] = {{256, 4}, {256, 2}, {256, 8}, {128, 4}, {128, 8}};
+    static const int cand[][2] = {{128, 4}, {128, 2}, {256, 4}, {256, 2}};
     const bool was_on = c->prof.on;
     Tune best = c->tune;
     double best_t = 1e300;

@@ -431,6 +431,8 @@ gvs_status gvs_profile_enable(gvs_ctx *c, int on) {
     c->prof.launches = 0;
     c->prof.force_flops = 0.0;
     c->prof.force_bytes = 0.0;
+    c->prof.tile_visits = 0.0;
+    GVS_CUDA(c, cudaMemsetAsync(err_ptr(c) + 8, 0, sizeof(unsigned long long), c->stream));
     return GVS_OK;
 }
 
@@ -443,6 +445,10 @@ gvs_status gvs_profile_read(gvs_ctx *c, gvs_profile *out) {
     out->launches = c->prof.launches;
     out->force_flops = c->prof.force_flops;
     out->force_bytes = c->prof.force_bytes;
+    unsigned long long nearc = 0;
+    GVS_CUDA(c, cudaMemcpy(&nearc, err_ptr(c) + 8, sizeof nearc, cudaMemcpyDeviceToHost));
+    out->near_tile_visits = (double)nearc;
+    out->tile_visits = c->prof.tile_visits;
     return GVS_OK;
 }
 

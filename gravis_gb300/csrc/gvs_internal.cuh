@@ -54,11 +54,12 @@ struct Prof {
     long long launches = 0;  // every kernel this context launched
     double force_bytes = 0;  // algorithmic bytes moved by timed force kernels
     double force_flops = 0;  // algorithmic flops (20 per pair interaction)
+    double tile_visits = 0;  // (target block, source tile) visits of the f32 pair kernel
 };
 
 struct Tune {
     int ipt = 4;       // i-particles per thread
-    int nthreads = 256;
+    int nthreads = 128;
     int nsplit = 0;    // 0 = automatic
 };
 
