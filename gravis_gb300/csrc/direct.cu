@@ -343,8 +343,8 @@ __device__ __forceinline__ void ff_rel(float cih, float cil, float cjh, float cj
 // Per source tile J and pair p: d = (c_I - c_J) from the hi/lo pairs, then
 // -(x_i - c_J) = -(d + off_i) as one f32x2 vector; per source particle j:
 // 3 ADD2 + 3 FMA2 (r^2) + 2 MUFU.RSQ + 3 MUL2 + 3 FMA2 (accumulate).
-template <int NT, int NP, int NSTAGE, bool MIXED, bool GUARD>
-__global__ void __launch_bounds__(NT) k_direct32(const float4 *__restrict__ pack, int ntiles, int tiles_per_split,
+template <int NT, int NP, int NSTAGE, bool MIXED, bool GUARD, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_direct32(const float4 *__restrict__ pack, int ntiles, int tiles_per_split,
                                                  float eps2, double *__restrict__ partial, size_t npad,
                                                  unsigned *__restrict__ err,
                                                  unsigned long long *__restrict__ near_count) {
@@ -712,15 +712,25 @@ struct Launch32 {
     int nt, np, nsplit;
 };
 
-// Chooses the j-split so that the grid covers every SM several times.
+// Chooses the j-split: at least ~4 waves of resident blocks, then the split
+// whose last wave is fullest (every block costs the same, so a ragged last
+// wave idles SMs), preferring fewer splits on ties.
 int auto_split(Ctx *c, int iblocks, int ntiles, int blocks_per_sm) {
-    int want = c->num_sms * blocks_per_sm * 4;
-    int ns = std::max(1, (want + iblocks - 1) / iblocks);
-    ns = std::min(ns, std::max(1, ntiles / 2));
-    return std::min(ns, 64);
+    const long long conc = (long long)c->num_sms * std::max(1, blocks_per_sm);
+    const int lo = std::max(1, (int)((4 * conc + iblocks - 1) / iblocks));
+    int best = std::min(lo, std::max(1, ntiles / 4));
+    double best_eff = -1.0;
+    for (int ns = best; ns <= std::min(64, std::max(best, ntiles / 4)); ++ns) {
+        const int tps = ceil_div(ntiles, ns);
+        const long long total = (long long)iblocks * ceil_div(ntiles, tps);
+        const double waves = (double)total / conc;
+        const double eff = waves / std::ceil(waves);
+        if (eff > best_eff + 1e-3) { best_eff = eff; best = ns; }
+    }
+    return best;
 }
 
-template <int NT, int NP, bool MIXED, bool GUARD>
+template <int NT, int NP, bool MIXED, bool GUARD, int MINB = 1>
 gvs_status launch32_t(Ctx *c, float eps2, int nsplit_req, double **partial_out, int *nsplit_out, size_t *npad_out) {
     constexpr int NSTAGE = 3;
     constexpr int TJ = NT;
@@ -741,7 +751,7 @@ gvs_status launch32_t(Ctx *c, float eps2, int nsplit_req, double **partial_out, 
         GVS_CUDA(c, cudaMemsetAsync(as<float4>(c->jpack32) + (size_t)ntiles * TF4, 0,
                                     (size_t)(ntiles_pad - ntiles) * TF4 * sizeof(float4), c->stream));
     const int smem = NSTAGE * TF4 * (int)sizeof(float4);
-    auto kern = k_direct32<NT, NP, NSTAGE, MIXED, GUARD>;
+    auto kern = k_direct32<NT, NP, NSTAGE, MIXED, GUARD, MINB>;
     set_smem(kern, smem);
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
@@ -780,10 +790,17 @@ gvs_status launch32(Ctx *c, float eps2, double **partial, int *nsplit, size_t *n
     for (const auto &e : c->tune_cache)
         if (e.first == bucket) c->tune = e.second;
     const Tune &t = c->tune;
-    if (t.nthreads == 256 && t.ipt == 4) return launch32_t<256, 2, MIXED, GUARD>(c, eps2, t.nsplit, partial, nsplit, npad);
-    if (t.nthreads == 256 && t.ipt == 2) return launch32_t<256, 1, MIXED, GUARD>(c, eps2, t.nsplit, partial, nsplit, npad);
-    if (t.nthreads == 128 && t.ipt == 2) return launch32_t<128, 1, MIXED, GUARD>(c, eps2, t.nsplit, partial, nsplit, npad);
-    return launch32_t<128, 2, MIXED, GUARD>(c, eps2, t.nsplit, partial, nsplit, npad);
+    if (t.nthreads == 128 && t.ipt == 4 && t.minb == 5)
+        return launch32_t<128, 2, MIXED, GUARD, 5>(c, eps2, t.nsplit, partial, nsplit, npad);
+    if (t.nthreads == 128 && t.ipt == 4 && t.minb == 6)
+        return launch32_t<128, 2, MIXED, GUARD, 6>(c, eps2, t.nsplit, partial, nsplit, npad);
+    if (t.nthreads == 256 && t.ipt == 4)
+        return launch32_t<256, 2, MIXED, GUARD, 2>(c, eps2, t.nsplit, partial, nsplit, npad);
+    if (t.nthreads == 256 && t.ipt == 2)
+        return launch32_t<256, 1, MIXED, GUARD, 4>(c, eps2, t.nsplit, partial, nsplit, npad);
+    if (t.nthreads == 128 && t.ipt == 2)
+        return launch32_t<128, 1, MIXED, GUARD, 8>(c, eps2, t.nsplit, partial, nsplit, npad);
+    return launch32_t<128, 2, MIXED, GUARD, 4>(c, eps2, t.nsplit, partial, nsplit, npad);
 }
 
 gvs_status launch64(Ctx *c, double eps2, double **partial_out, int *nsplit_out, size_t *npad_out) {
@@ -876,13 +893,14 @@ gvs_status direct_forces(Ctx *c, int precision, double eps, bool accumulate) {
 // Times every compiled (block size, targets per thread) variant of the f32
 // pair kernel on the resident state and keeps the fastest for this N bucket.
 gvs_status autotune_direct(Ctx *c, int precision, double eps, int *best_nt, int *best_ipt, double *best_ms) {
-    static const int cand[][2] = {{128, 4}, {128, 2}, {256, 4}, {256, 2}};
+    static const int cand[][3] = {{128, 4, 4}, {128, 4, 5}, {128, 4, 6}, {128, 2, 8}, {256, 4, 2}, {256, 2, 4}};
     const bool was_on = c->prof.on;
     Tune best = c->tune;
     double best_t = 1e300;
     for (const auto &cd : cand) {
         c->tune.nthreads = cd[0];
         c->tune.ipt = cd[1];
+        c->tune.minb = cd[2];
         c->tune.nsplit = 0;
         GVS_TRY(direct_forces(c, precision, eps, false));  // warm (also builds the order)
         c->prof.on = true;

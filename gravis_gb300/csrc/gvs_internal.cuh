@@ -61,6 +61,7 @@ struct Tune {
     int ipt = 4;       // i-particles per thread
     int nthreads = 128;
     int nsplit = 0;    // 0 = automatic
+    int minb = 4;      // __launch_bounds__ minimum blocks per SM (register cap)
 };
 
 struct Ctx {
