@@ -63,6 +63,8 @@ SIGNATURES = {
     "gvs_get_gas": (_ST, [_P] + [_P] * 7),
     "gvs_count": (_sz, [_P]),
     "gvs_gravity_direct": (_ST, [_P, _sz, _P, _P, _P, _P, _d, _i, _P, _P, _P]),
+    "gvs_gravity_bh": (_ST, [_P, _sz, _P, _P, _P, _P, _d, _d, _i, _P, _P, _P]),
+    "gvs_tree_export": (_ST, [_P, _sz, C.POINTER(_sz)] + [_P] * 8),
     "gvs_compute_forces": (_ST, [_P, _i, _i, _d, _d]),
     "gvs_kdk_steps": (_ST, [_P, _i, _i, _d, _d, _d, _ll]),
     "gvs_kdk_step_host": (_ST, [_P, _sz] + [_P] * 10 + [_i, _i, _d, _d, _d]),

@@ -1,10 +1,602 @@
-// bh.cu -- Barnes-Hut on the GPU (placeholder until the tree pipeline lands).
+// bh.cu -- octree build and Barnes-Hut walk on the GPU
+// (Octree: crates/sim-core/src/octree.rs:14-324; BarnesHut: crates/sim-core/src/barnes_hut.rs:21-192).
+//
+// The reference builds its octree by inserting particles one at a time into a
+// cubic root box (BoundingBox::containing, octree.rs:14-44) that is halved
+// level by level (child_bounds, octree.rs:52-64), each particle descending by
+// the octant test x >= centre (octree.rs:67-79), leaves holding one particle.
+// That tree does not depend on insertion order: a cell at depth L is a node
+// iff its parent holds >= 2 particles, and it is a leaf iff it holds exactly
+// one.  So the GPU builds the same tree from sorted keys:
+//
+//  1. Key: each particle replays the reference's f64 halving arithmetic for
+//     42 levels (centre +- hw/2, same rounding), recording 3 octant bits per
+//     level: a 126-bit octant-path key (two u64 words, 21 levels each).
+//  2. Sort: stable radix sort by (high word, low word).  Sorted order = the
+//     depth-first order of the reference tree with children 0..7.
+//  3. Nodes: with d_i = common prefix depth of sorted keys i-1 and i, particle
+//     i starts exactly the nodes at depths d_i+1 .. max(d_i, d_{i+1})+1 (the
+//     last is its leaf).  A prefix sum of those counts gives every node an
+//     index in pre-order; the node (i, L) covers particles [i, e) and its
+//     subtree covers node indices [idx, off[e]) -- the skip pointer.
+//     Particles that share all 42 levels (closer than 2^-42 of the box) form
+//     one bucket leaf; the reference would keep splitting down to depth 64.
+//  4. Moments: mass and centre of mass in f64, bottom-up one level at a time
+//     (a node sums its children in child order, so results are deterministic).
+//     The reference updates the COM incrementally in insertion order; the
+//     two agree to a few ulps.
+//  5. Walk: the reference's per-particle stack walk (barnes_hut.rs:44-108):
+//     skip empty, leaf != self -> direct term, internal -> accept if
+//     s^2 < theta^2 d^2 with s = 2*half_width and d = |com - p|, else open.
+//     Here each lane of a warp keeps its own "next node" pointer and the warp
+//     processes the smallest pointer among its lanes each step, so every lane
+//     visits exactly the nodes its own walk would (same accept decisions)
+//     while node loads are broadcast.  Children are visited 0..7 (pre-order)
+//     rather than the reference's LIFO 7..0: the same terms summed in another
+//     order (differences at the 1e-16 relative level).
 #include "gvs_internal.cuh"
 
 namespace gvs {
-gvs_status bh_forces(Ctx *c, double, double, int, bool) {
-    return fail(c, GVS_ERR_STATE, "Barnes-Hut path not available in this build");
+
+constexpr int MAXL = 42;
+
+struct Tree {
+    unsigned long long version = ~0ull;  // c->pos_version the tree was built for
+    size_t n = 0, nnodes = 0;
+    int precision = -1;
+    double root[4] = {0, 0, 0, 0};  // centre x, y, z, half width (host copy)
+    DevBuf bb, bbpart;              // device: min/max (6) then centre + hw (4)
+    DevBuf khi, klo, khi2, klo2, perm, perm2, iota, iota2;
+    DevBuf delta, nown, off, total;
+    DevBuf level, first, cnt, skip;  // per node
+    DevBuf mass, comx, comy, comz;   // per node (f64)
+    DevBuf boxx, boxy, boxz;         // per node cell centre (f64)
+    DevBuf sx, sy, sz, sm;           // sorted particle positions / masses (f64)
+    DevBuf pos32, cm32, cm64, meta, acc;
+};
+
+namespace {
+
+__device__ __forceinline__ int common_levels(uint64_t ah, uint64_t al, uint64_t bh, uint64_t bl) {
+    uint64_t x = ah ^ bh;
+    if (x) return (__clzll(x) - 1) / 3;
+    x = al ^ bl;
+    if (x) return 21 + (__clzll(x) - 1) / 3;
+    return MAXL;
 }
-gvs_status tree_build(Ctx *c) { return fail(c, GVS_ERR_STATE, "tree build not available in this build"); }
-void tree_free(Ctx *) {}
+
+// same cell at depth L (L in 0..42)?
+__device__ __forceinline__ bool same_prefix(uint64_t ah, uint64_t al, uint64_t bh, uint64_t bl, int L) {
+    if (L <= 21) return L == 0 || ((ah ^ bh) >> (63 - 3 * L)) == 0;
+    if (ah != bh) return false;
+    return ((al ^ bl) >> (63 - 3 * (L - 21))) == 0;
+}
+
+__device__ __forceinline__ int octant_at(uint64_t hi, uint64_t lo, int L) {  // L in 1..42
+    return L <= 21 ? (int)((hi >> (63 - 3 * L)) & 7u) : (int)((lo >> (63 - 3 * (L - 21))) & 7u);
+}
+
+// Root cube: BoundingBox::containing (octree.rs:29-43), f64 without contraction.
+__global__ void k_root(double *bb) {
+    if (threadIdx.x || blockIdx.x) return;
+    double c[3];
+    for (int d = 0; d < 3; ++d) c[d] = __dmul_rn(0.5, __dadd_rn(bb[d], bb[3 + d]));
+    double e = fmax(fmax(__dsub_rn(bb[3], bb[0]), __dsub_rn(bb[4], bb[1])), __dsub_rn(bb[5], bb[2]));
+    double hw = __dadd_rn(__dmul_rn(__dmul_rn(0.5, e), 1.001), 1e-10);
+    bb[6] = c[0]; bb[7] = c[1]; bb[8] = c[2]; bb[9] = hw;
+}
+
+// Octant-path key (octant, child_bounds: octree.rs:52-79), 42 levels.
+__global__ void k_keys(const double *__restrict__ X, const double *__restrict__ Y, const double *__restrict__ Z,
+                       size_t n, const double *__restrict__ bb, uint64_t *__restrict__ khi,
+                       uint64_t *__restrict__ klo, uint32_t *__restrict__ perm) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double x = X[i], y = Y[i], z = Z[i];
+    double cx = bb[6], cy = bb[7], cz = bb[8], hw = bb[9];
+    uint64_t hi = 0, lo = 0;
+    for (int L = 1; L <= MAXL; ++L) {
+        const int oct = (x >= cx ? 1 : 0) | (y >= cy ? 2 : 0) | (z >= cz ? 4 : 0);
+        const double q = __dmul_rn(hw, 0.5);
+        cx = __dadd_rn(cx, (oct & 1) ? q : -q);
+        cy = __dadd_rn(cy, (oct & 2) ? q : -q);
+        cz = __dadd_rn(cz, (oct & 4) ? q : -q);
+        hw = q;
+        if (L <= 21) hi = (hi << 3) | (uint64_t)oct;
+        else lo = (lo << 3) | (uint64_t)oct;
+    }
+    khi[i] = hi;
+    klo[i] = lo;
+    perm[i] = (uint32_t)i;
+}
+
+__global__ void k_iota(uint32_t *a, size_t n) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = (uint32_t)i;
+}
+
+template <class T>
+__global__ void k_gather(const T *__restrict__ src, const uint32_t *__restrict__ idx, T *__restrict__ dst, size_t n) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[idx[i]];
+}
+
+// delta[i] = common depth of sorted keys i-1 and i (delta[0] = delta[n] = -1);
+// nown[i] = number of nodes particle i starts; nown[n] = 0.
+__global__ void k_delta(const uint64_t *__restrict__ khi, const uint64_t *__restrict__ klo, size_t n,
+                        int *__restrict__ delta) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n) return;
+    delta[i] = (i == 0 || i == n) ? -1 : common_levels(khi[i - 1], klo[i - 1], khi[i], klo[i]);
+}
+
+__global__ void k_nown(const int *__restrict__ delta, size_t n, uint32_t *__restrict__ nown) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n) return;
+    if (i == n) { nown[i] = 0; return; }
+    const int a = delta[i] + 1;
+    const int b = min(max(delta[i], delta[i + 1]) + 1, MAXL);
+    nown[i] = b >= a ? (uint32_t)(b - a + 1) : 0u;
+}
+
+// One thread per particle: writes the nodes it starts.
+__global__ void k_nodes(const uint64_t *__restrict__ khi, const uint64_t *__restrict__ klo,
+                        const int *__restrict__ delta, const uint32_t *__restrict__ off, size_t n,
+                        const double *__restrict__ bb, uint8_t *__restrict__ level, uint32_t *__restrict__ first,
+                        uint32_t *__restrict__ cnt, uint32_t *__restrict__ skip, double *__restrict__ bx,
+                        double *__restrict__ by, double *__restrict__ bz) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int a = delta[i] + 1;
+    const int b = min(max(delta[i], delta[i + 1]) + 1, MAXL);
+    if (b < a) return;
+    const uint64_t hi = khi[i], lo = klo[i];
+    double cx = bb[6], cy = bb[7], cz = bb[8], hw = bb[9];
+    for (int L = 1; L < a; ++L) {  // descend to depth a
+        const int oct = octant_at(hi, lo, L);
+        const double q = __dmul_rn(hw, 0.5);
+        cx = __dadd_rn(cx, (oct & 1) ? q : -q);
+        cy = __dadd_rn(cy, (oct & 2) ? q : -q);
+        cz = __dadd_rn(cz, (oct & 4) ? q : -q);
+        hw = q;
+    }
+    const uint32_t base = off[i];
+    for (int L = a; L <= b; ++L) {
+        if (L >= 1) {
+            const int oct = octant_at(hi, lo, L);
+            const double q = __dmul_rn(hw, 0.5);
+            cx = __dadd_rn(cx, (oct & 1) ? q : -q);
+            cy = __dadd_rn(cy, (oct & 2) ? q : -q);
+            cz = __dadd_rn(cz, (oct & 4) ? q : -q);
+            hw = q;
+        }
+        // end of the depth-L cell of particle i
+        size_t e;
+        if (delta[i + 1] < L) {
+            e = i + 1;
+        } else {
+            size_t lo_j = i + 1, hi_j = n;
+            while (lo_j < hi_j) {
+                const size_t mid = (lo_j + hi_j) >> 1;
+                if (same_prefix(khi[mid], klo[mid], hi, lo, L)) lo_j = mid + 1;
+                else hi_j = mid;
+            }
+            e = lo_j;
+        }
+        const uint32_t idx = base + (uint32_t)(L - a);
+        const bool leaf = (e - i == 1) || L == MAXL;
+        level[idx] = (uint8_t)L;
+        first[idx] = (uint32_t)i;
+        cnt[idx] = leaf ? (uint32_t)(e - i) : 0u;
+        skip[idx] = off[e];
+        bx[idx] = cx; by[idx] = cy; bz[idx] = cz;
+    }
+}
+
+// Bottom-up moments for the nodes of depth L.
+__global__ void k_moments(int L, size_t nnodes, const uint8_t *__restrict__ level, const uint32_t *__restrict__ first,
+                          const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ skip,
+                          const double *__restrict__ sx, const double *__restrict__ sy, const double *__restrict__ sz,
+                          const double *__restrict__ sm, double *__restrict__ mass, double *__restrict__ cx,
+                          double *__restrict__ cy, double *__restrict__ cz) {
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nnodes || level[k] != L) return;
+    const uint32_t c0 = cnt[k];
+    if (c0 == 1) {
+        const uint32_t p = first[k];
+        mass[k] = sm[p]; cx[k] = sx[p]; cy[k] = sy[p]; cz[k] = sz[p];
+        return;
+    }
+    double M = 0.0, X = 0.0, Yv = 0.0, Zv = 0.0;
+    if (c0 > 1) {  // bucket leaf: members in order
+        for (uint32_t p = first[k]; p < first[k] + c0; ++p) {
+            const double m = sm[p];
+            M += m; X += m * sx[p]; Yv += m * sy[p]; Zv += m * sz[p];
+        }
+    } else {  // internal: children in order 0..7
+        const uint32_t end = skip[k];
+        for (uint32_t ch = (uint32_t)k + 1; ch < end; ch = skip[ch]) {
+            const double m = mass[ch];
+            M += m; X += m * cx[ch]; Yv += m * cy[ch]; Zv += m * cz[ch];
+        }
+    }
+    mass[k] = M;
+    if (M > 0.0) {
+        cx[k] = X / M; cy[k] = Yv / M; cz[k] = Zv / M;
+    } else {
+        cx[k] = cy[k] = cz[k] = 0.0;
+    }
+}
+
+__global__ void k_pack_nodes(size_t nnodes, const uint8_t *__restrict__ level, const uint32_t *__restrict__ first,
+                             const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ skip,
+                             const double *__restrict__ mass, const double *__restrict__ cx,
+                             const double *__restrict__ cy, const double *__restrict__ cz, float4 *__restrict__ cm32,
+                             double4 *__restrict__ cm64, int4 *__restrict__ meta) {
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nnodes) return;
+    meta[k] = make_int4((int)skip[k], (int)first[k], (int)cnt[k], (int)level[k]);
+    if (cm32) cm32[k] = make_float4((float)cx[k], (float)cy[k], (float)cz[k], (float)mass[k]);
+    if (cm64) cm64[k] = make_double4(cx[k], cy[k], cz[k], mass[k]);
+}
+
+__global__ void k_pack_particles(size_t n, const double *__restrict__ sx, const double *__restrict__ sy,
+                                 const double *__restrict__ sz, const double *__restrict__ sm, float4 *__restrict__ p32) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p32[i] = make_float4((float)sx[i], (float)sy[i], (float)sz[i], (float)sm[i]);
+}
+
+// ---- walk -------------------------------------------------------------------
+struct S2Table {
+    double s2[MAXL + 1];   // (2 * half_width_L)^2, half_width_L = hw0 * 2^-L
+    float s2f[MAXL + 1];
+};
+
+// BarnesHut::add_force (barnes_hut.rs:114-135), IEEE f64 with no contraction.
+__device__ __forceinline__ void add_force64(double px, double py, double pz, double sx, double sy, double sz,
+                                            double m, double eps2, double &ax, double &ay, double &az) {
+    const double dx = __dsub_rn(sx, px), dy = __dsub_rn(sy, py), dz = __dsub_rn(sz, pz);
+    const double r2 = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)), eps2);
+    const double inv_r3 = __ddiv_rn(1.0, __dmul_rn(r2, __dsqrt_rn(r2)));
+    const double f = __dmul_rn(m, inv_r3);
+    ax = __dadd_rn(ax, __dmul_rn(f, dx));
+    ay = __dadd_rn(ay, __dmul_rn(f, dy));
+    az = __dadd_rn(az, __dmul_rn(f, dz));
+}
+
+__device__ __forceinline__ void add_force32(float px, float py, float pz, float sx, float sy, float sz, float m,
+                                            float eps2, float &ax, float &ay, float &az) {
+    const float dx = sx - px, dy = sy - py, dz = sz - pz;
+    const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+    const float ri = rsqrt_approx(r2);
+    const float f = m * ri * ri * ri;
+    ax = fmaf(f, dx, ax);
+    ay = fmaf(f, dy, ay);
+    az = fmaf(f, dz, az);
+}
+
+template <bool F64>
+__global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int4 *__restrict__ meta,
+                                              const float4 *__restrict__ cm32, const double4 *__restrict__ cm64,
+                                              const float4 *__restrict__ p32, const double *__restrict__ sx,
+                                              const double *__restrict__ sy, const double *__restrict__ sz,
+                                              const double *__restrict__ sm, const S2Table tab, double theta2,
+                                              double eps2, double *__restrict__ acc) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = t < n;
+    double px = 0, py = 0, pz = 0;
+    float qx = 0, qy = 0, qz = 0;
+    if (active) {
+        if (F64) { px = sx[t]; py = sy[t]; pz = sz[t]; }
+        else { const float4 p = p32[t]; qx = p.x; qy = p.y; qz = p.z; }
+    }
+    const float theta2f = (float)theta2, eps2f = (float)eps2;
+    double ax = 0, ay = 0, az = 0;
+    float fx = 0, fy = 0, fz = 0;
+    uint32_t next = active ? 0u : 0xFFFFFFFFu;
+    for (;;) {
+        const uint32_t m = __reduce_min_sync(0xFFFFFFFFu, next);
+        if ((size_t)m >= nnodes) break;
+        if (next != m) continue;
+        const int4 mt = meta[m];
+        if (mt.z > 0) {  // leaf
+            if (mt.z == 1) {
+                if ((size_t)mt.y != t) {
+                    if (F64) {
+                        const double4 c = cm64[m];
+                        if (c.w != 0.0) add_force64(px, py, pz, c.x, c.y, c.z, c.w, eps2, ax, ay, az);
+                    } else {
+                        const float4 c = cm32[m];
+                        if (c.w != 0.f) add_force32(qx, qy, qz, c.x, c.y, c.z, c.w, eps2f, fx, fy, fz);
+                    }
+                }
+            } else {  // bucket of coincident-key particles: direct terms
+                for (int j = mt.y; j < mt.y + mt.z; ++j) {
+                    if ((size_t)j == t) continue;
+                    if (F64) {
+                        if (sm[j] != 0.0) add_force64(px, py, pz, sx[j], sy[j], sz[j], sm[j], eps2, ax, ay, az);
+                    } else {
+                        const float4 q = p32[j];
+                        if (q.w != 0.f) add_force32(qx, qy, qz, q.x, q.y, q.z, q.w, eps2f, fx, fy, fz);
+                    }
+                }
+            }
+            next = (uint32_t)mt.x;
+        } else if (F64) {
+            const double4 c = cm64[m];
+            if (c.w == 0.0) {
+                next = (uint32_t)mt.x;
+            } else {
+                const double dx = __dsub_rn(c.x, px), dy = __dsub_rn(c.y, py), dz = __dsub_rn(c.z, pz);
+                const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+                if (tab.s2[mt.w] < __dmul_rn(theta2, d2)) {
+                    add_force64(px, py, pz, c.x, c.y, c.z, c.w, eps2, ax, ay, az);
+                    next = (uint32_t)mt.x;
+                } else {
+                    next = m + 1;
+                }
+            }
+        } else {
+            const float4 c = cm32[m];
+            if (c.w == 0.f) {
+                next = (uint32_t)mt.x;
+            } else {
+                const float dx = c.x - qx, dy = c.y - qy, dz = c.z - qz;
+                const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                if (tab.s2f[mt.w] < theta2f * d2) {
+                    add_force32(qx, qy, qz, c.x, c.y, c.z, c.w, eps2f, fx, fy, fz);
+                    next = (uint32_t)mt.x;
+                } else {
+                    next = m + 1;
+                }
+            }
+        }
+    }
+    if (!active) return;
+    if (!F64) { ax = fx; ay = fy; az = fz; }
+    acc[t] = ax;
+    acc[n + t] = ay;
+    acc[2 * n + t] = az;
+}
+
+__global__ void k_scatter_acc(size_t n, const double *__restrict__ acc, const uint32_t *__restrict__ perm,
+                              double *__restrict__ AX, double *__restrict__ AY, double *__restrict__ AZ,
+                              int accumulate) {
+    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const uint32_t o = perm[s];
+    if (accumulate) {
+        AX[o] += acc[s]; AY[o] += acc[n + s]; AZ[o] += acc[2 * n + s];
+    } else {
+        AX[o] = acc[s]; AY[o] = acc[n + s]; AZ[o] = acc[2 * n + s];
+    }
+}
+
+inline int nblk(size_t n, int t = 256) { return (int)std::max<size_t>(1, (n + t - 1) / t); }
+
+}  // namespace
+
+Tree *tree_of(Ctx *c) {
+    if (!c->tree) c->tree = new Tree();
+    return static_cast<Tree *>(c->tree);
+}
+
+void tree_free(Ctx *c) {
+    Tree *t = static_cast<Tree *>(c->tree);
+    if (!t) return;
+    DevBuf *all[] = {&t->bb, &t->bbpart, &t->khi, &t->klo, &t->khi2, &t->klo2, &t->perm, &t->perm2, &t->iota,
+                     &t->iota2, &t->delta, &t->nown, &t->off, &t->total, &t->level, &t->first, &t->cnt, &t->skip,
+                     &t->mass, &t->comx, &t->comy, &t->comz, &t->boxx, &t->boxy, &t->boxz, &t->sx, &t->sy,
+                     &t->sz, &t->sm, &t->pos32, &t->cm32, &t->cm64, &t->meta, &t->acc};
+    for (DevBuf *b : all)
+        if (b->ptr) cudaFree(b->ptr);
+    delete t;
+    c->tree = nullptr;
+}
+
+// Builds (or reuses) the tree of the resident positions.
+gvs_status tree_build(Ctx *c) {
+    Tree *t = tree_of(c);
+    const size_t n = c->n;
+    if (n == 0) return fail(c, GVS_ERR_STATE, "tree build with no particles");
+    if (t->version == c->pos_version && t->n == n) return GVS_OK;
+    cudaStream_t st = c->stream;
+    GVS_CUDA(c, ensure(c, t->bb, 16 * sizeof(double)));
+    GVS_TRY(bbox_minmax(c, as<double>(t->bb), t->bbpart));
+    k_root<<<1, 1, 0, st>>>(as<double>(t->bb));
+    // keys, sorted by (hi, lo): lo first, then a stable sort by hi
+    const size_t b8 = n * 8, b4 = n * 4;
+    GVS_CUDA(c, ensure(c, t->khi, b8)); GVS_CUDA(c, ensure(c, t->klo, b8));
+    GVS_CUDA(c, ensure(c, t->khi2, b8)); GVS_CUDA(c, ensure(c, t->klo2, b8));
+    GVS_CUDA(c, ensure(c, t->perm, b4)); GVS_CUDA(c, ensure(c, t->perm2, b4));
+    GVS_CUDA(c, ensure(c, t->iota, b4)); GVS_CUDA(c, ensure(c, t->iota2, b4));
+    k_keys<<<nblk(n), 256, 0, st>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z), n, as<double>(t->bb),
+                                    as<uint64_t>(t->khi), as<uint64_t>(t->klo), as<uint32_t>(t->perm));
+    c->prof.launches += 2;
+    GVS_TRY(check_launch(c, "tree keys"));
+    uint64_t *klo_s;
+    uint32_t *perm1;
+    GVS_TRY(radix_sort_u64(c, as<uint64_t>(t->klo), as<uint32_t>(t->perm), as<uint64_t>(t->klo2),
+                           as<uint32_t>(t->perm2), n, 0, 64, &klo_s, &perm1));
+    // khi in lo-sorted order, then the stable sort by hi carrying lo-order slots
+    uint64_t *khi_g = as<uint64_t>(t->khi2);
+    k_gather<uint64_t><<<nblk(n), 256, 0, st>>>(as<uint64_t>(t->khi), perm1, khi_g, n);
+    k_iota<<<nblk(n), 256, 0, st>>>(as<uint32_t>(t->iota), n);
+    c->prof.launches += 2;
+    uint64_t *khi_s;
+    uint32_t *slot;
+    GVS_TRY(radix_sort_u64(c, khi_g, as<uint32_t>(t->iota), as<uint64_t>(t->khi), as<uint32_t>(t->iota2), n, 0, 64,
+                           &khi_s, &slot));
+    // khi_s lives in khi2 (even number of passes); final perm and lo keys
+    uint32_t *perm_final = (perm1 == as<uint32_t>(t->perm)) ? as<uint32_t>(t->perm2) : as<uint32_t>(t->perm);
+    uint64_t *klo_final = (klo_s == as<uint64_t>(t->klo)) ? as<uint64_t>(t->klo2) : as<uint64_t>(t->klo);
+    k_gather<uint32_t><<<nblk(n), 256, 0, st>>>(perm1, slot, perm_final, n);
+    k_gather<uint64_t><<<nblk(n), 256, 0, st>>>(klo_s, slot, klo_final, n);
+    c->prof.launches += 2;
+    // make the canonical buffers hold the final arrays
+    if (perm_final != as<uint32_t>(t->perm)) std::swap(t->perm, t->perm2);
+    if (klo_final != as<uint64_t>(t->klo)) std::swap(t->klo, t->klo2);
+    if (khi_s != as<uint64_t>(t->khi)) std::swap(t->khi, t->khi2);
+    uint64_t *KH = as<uint64_t>(t->khi), *KL = as<uint64_t>(t->klo);
+    uint32_t *P = as<uint32_t>(t->perm);
+    // node enumeration
+    GVS_CUDA(c, ensure(c, t->delta, (n + 1) * 4));
+    GVS_CUDA(c, ensure(c, t->nown, (n + 1) * 4));
+    GVS_CUDA(c, ensure(c, t->off, (n + 1) * 4));
+    GVS_CUDA(c, ensure(c, t->total, 16));
+    k_delta<<<nblk(n + 1), 256, 0, st>>>(KH, KL, n, as<int>(t->delta));
+    k_nown<<<nblk(n + 1), 256, 0, st>>>(as<int>(t->delta), n, as<uint32_t>(t->nown));
+    c->prof.launches += 2;
+    GVS_TRY(exclusive_scan_u32(c, as<uint32_t>(t->nown), as<uint32_t>(t->off), n + 1, as<uint32_t>(t->total)));
+    uint32_t nn = 0;
+    GVS_CUDA(c, cudaMemcpyAsync(&nn, t->total.ptr, 4, cudaMemcpyDeviceToHost, st));
+    GVS_CUDA(c, cudaMemcpyAsync(t->root, as<double>(t->bb) + 6, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    GVS_CUDA(c, cudaStreamSynchronize(st));
+    const size_t nnodes = nn;
+    t->nnodes = nnodes;
+    GVS_CUDA(c, ensure(c, t->level, nnodes));
+    GVS_CUDA(c, ensure(c, t->first, nnodes * 4)); GVS_CUDA(c, ensure(c, t->cnt, nnodes * 4));
+    GVS_CUDA(c, ensure(c, t->skip, nnodes * 4));
+    GVS_CUDA(c, ensure(c, t->mass, nnodes * 8)); GVS_CUDA(c, ensure(c, t->comx, nnodes * 8));
+    GVS_CUDA(c, ensure(c, t->comy, nnodes * 8)); GVS_CUDA(c, ensure(c, t->comz, nnodes * 8));
+    GVS_CUDA(c, ensure(c, t->boxx, nnodes * 8)); GVS_CUDA(c, ensure(c, t->boxy, nnodes * 8));
+    GVS_CUDA(c, ensure(c, t->boxz, nnodes * 8));
+    k_nodes<<<nblk(n), 256, 0, st>>>(KH, KL, as<int>(t->delta), as<uint32_t>(t->off), n, as<double>(t->bb),
+                                     as<uint8_t>(t->level), as<uint32_t>(t->first), as<uint32_t>(t->cnt),
+                                     as<uint32_t>(t->skip), as<double>(t->boxx), as<double>(t->boxy),
+                                     as<double>(t->boxz));
+    // sorted particle data
+    GVS_CUDA(c, ensure(c, t->sx, b8)); GVS_CUDA(c, ensure(c, t->sy, b8));
+    GVS_CUDA(c, ensure(c, t->sz, b8)); GVS_CUDA(c, ensure(c, t->sm, b8));
+    k_gather<double><<<nblk(n), 256, 0, st>>>(as<double>(c->x), P, as<double>(t->sx), n);
+    k_gather<double><<<nblk(n), 256, 0, st>>>(as<double>(c->y), P, as<double>(t->sy), n);
+    k_gather<double><<<nblk(n), 256, 0, st>>>(as<double>(c->z), P, as<double>(t->sz), n);
+    k_gather<double><<<nblk(n), 256, 0, st>>>(as<double>(c->m), P, as<double>(t->sm), n);
+    c->prof.launches += 5;
+    GVS_TRY(check_launch(c, "tree nodes"));
+    for (int L = MAXL; L >= 0; --L) {
+        k_moments<<<nblk(nnodes), 256, 0, st>>>(L, nnodes, as<uint8_t>(t->level), as<uint32_t>(t->first),
+                                                 as<uint32_t>(t->cnt), as<uint32_t>(t->skip), as<double>(t->sx),
+                                                 as<double>(t->sy), as<double>(t->sz), as<double>(t->sm),
+                                                 as<double>(t->mass), as<double>(t->comx), as<double>(t->comy),
+                                                 as<double>(t->comz));
+    }
+    c->prof.launches += MAXL + 1;
+    GVS_TRY(check_launch(c, "tree moments"));
+    t->n = n;
+    t->version = c->pos_version;
+    t->precision = -1;
+    return GVS_OK;
+}
+
+gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accumulate) {
+    const size_t n = c->n;
+    if (n == 0) return GVS_OK;
+    GVS_TRY(tree_build(c));
+    Tree *t = tree_of(c);
+    cudaStream_t st = c->stream;
+    const size_t nnodes = t->nnodes;
+    const bool f64 = precision == GVS_PREC_FP64_EXACT || precision == GVS_PREC_FP64;
+    GVS_CUDA(c, ensure(c, t->meta, nnodes * sizeof(int4)));
+    if (f64) GVS_CUDA(c, ensure(c, t->cm64, nnodes * sizeof(double4)));
+    else {
+        GVS_CUDA(c, ensure(c, t->cm32, nnodes * sizeof(float4)));
+        GVS_CUDA(c, ensure(c, t->pos32, n * sizeof(float4)));
+    }
+    if (t->precision != (f64 ? 1 : 0)) {
+        k_pack_nodes<<<nblk(nnodes), 256, 0, st>>>(nnodes, as<uint8_t>(t->level), as<uint32_t>(t->first),
+                                                    as<uint32_t>(t->cnt), as<uint32_t>(t->skip), as<double>(t->mass),
+                                                    as<double>(t->comx), as<double>(t->comy), as<double>(t->comz),
+                                                    f64 ? nullptr : as<float4>(t->cm32),
+                                                    f64 ? as<double4>(t->cm64) : nullptr, as<int4>(t->meta));
+        if (!f64)
+            k_pack_particles<<<nblk(n), 256, 0, st>>>(n, as<double>(t->sx), as<double>(t->sy), as<double>(t->sz),
+                                                      as<double>(t->sm), as<float4>(t->pos32));
+        c->prof.launches += f64 ? 1 : 2;
+        t->precision = f64 ? 1 : 0;
+    }
+    S2Table tab;
+    for (int L = 0; L <= MAXL; ++L) {
+        const double hw = ldexp(t->root[3], -L);  // exact: child half width = parent * 0.5
+        const double s = hw * 2.0;
+        tab.s2[L] = s * s;
+        tab.s2f[L] = (float)(s * s);
+    }
+    GVS_CUDA(c, ensure(c, t->acc, 3 * n * sizeof(double)));
+    if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], st));
+    if (f64)
+        k_walk<true><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, as<int4>(t->meta), nullptr, as<double4>(t->cm64),
+                                                   nullptr, as<double>(t->sx), as<double>(t->sy), as<double>(t->sz),
+                                                   as<double>(t->sm), tab, theta * theta, eps * eps,
+                                                   as<double>(t->acc));
+    else
+        k_walk<false><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, as<int4>(t->meta), as<float4>(t->cm32), nullptr,
+                                                    as<float4>(t->pos32), as<double>(t->sx), as<double>(t->sy),
+                                                    as<double>(t->sz), as<double>(t->sm), tab, theta * theta,
+                                                    eps * eps, as<double>(t->acc));
+    c->prof.launches += 1;
+    GVS_TRY(check_launch(c, "tree walk"));
+    if (c->prof.on) {
+        GVS_CUDA(c, cudaEventRecord(c->prof.ev[1], st));
+        GVS_CUDA(c, cudaEventSynchronize(c->prof.ev[1]));
+        float ms = 0.f;
+        GVS_CUDA(c, cudaEventElapsedTime(&ms, c->prof.ev[0], c->prof.ev[1]));
+        c->prof.force_ms += ms;
+        c->prof.force_launches += 1;
+    }
+    k_scatter_acc<<<nblk(n), 256, 0, st>>>(n, as<double>(t->acc), as<uint32_t>(t->perm), as<double>(c->ax),
+                                           as<double>(c->ay), as<double>(c->az), accumulate ? 1 : 0);
+    c->prof.launches += 1;
+    return check_launch(c, "tree scatter");
+}
+
+// ---- accessors used by the SPH neighbour search and the tests ------------------
+gvs_status tree_view(Ctx *c, TreeView *v) {
+    GVS_TRY(tree_build(c));
+    Tree *t = tree_of(c);
+    v->n = t->n;
+    v->nnodes = t->nnodes;
+    v->level = as<uint8_t>(t->level);
+    v->first = as<uint32_t>(t->first);
+    v->cnt = as<uint32_t>(t->cnt);
+    v->skip = as<uint32_t>(t->skip);
+    v->perm = as<uint32_t>(t->perm);
+    v->bx = as<double>(t->boxx);
+    v->by = as<double>(t->boxy);
+    v->bz = as<double>(t->boxz);
+    v->sx = as<double>(t->sx);
+    v->sy = as<double>(t->sy);
+    v->sz = as<double>(t->sz);
+    v->root_hw = t->root[3];
+    return GVS_OK;
+}
+
+// Host copy of the tree arrays (for tests): returns node count.
+gvs_status tree_export(Ctx *c, size_t cap, uint8_t *level, uint32_t *first, uint32_t *cnt, uint32_t *skip,
+                       double *mass, double *com, uint32_t *perm, uint64_t *keys, size_t *nnodes) {
+    GVS_TRY(tree_build(c));
+    Tree *t = tree_of(c);
+    *nnodes = t->nnodes;
+    if (cap < t->nnodes) return GVS_OK;
+    cudaStream_t st = c->stream;
+    const size_t nn = t->nnodes, n = t->n;
+    if (level) GVS_CUDA(c, cudaMemcpyAsync(level, t->level.ptr, nn, cudaMemcpyDeviceToHost, st));
+    if (first) GVS_CUDA(c, cudaMemcpyAsync(first, t->first.ptr, nn * 4, cudaMemcpyDeviceToHost, st));
+    if (cnt) GVS_CUDA(c, cudaMemcpyAsync(cnt, t->cnt.ptr, nn * 4, cudaMemcpyDeviceToHost, st));
+    if (skip) GVS_CUDA(c, cudaMemcpyAsync(skip, t->skip.ptr, nn * 4, cudaMemcpyDeviceToHost, st));
+    if (mass) GVS_CUDA(c, cudaMemcpyAsync(mass, t->mass.ptr, nn * 8, cudaMemcpyDeviceToHost, st));
+    if (com) {
+        GVS_CUDA(c, cudaMemcpyAsync(com, t->comx.ptr, nn * 8, cudaMemcpyDeviceToHost, st));
+        GVS_CUDA(c, cudaMemcpyAsync(com + nn, t->comy.ptr, nn * 8, cudaMemcpyDeviceToHost, st));
+        GVS_CUDA(c, cudaMemcpyAsync(com + 2 * nn, t->comz.ptr, nn * 8, cudaMemcpyDeviceToHost, st));
+    }
+    if (perm) GVS_CUDA(c, cudaMemcpyAsync(perm, t->perm.ptr, n * 4, cudaMemcpyDeviceToHost, st));
+    if (keys) {
+        GVS_CUDA(c, cudaMemcpyAsync(keys, t->khi.ptr, n * 8, cudaMemcpyDeviceToHost, st));
+        GVS_CUDA(c, cudaMemcpyAsync(keys + n, t->klo.ptr, n * 8, cudaMemcpyDeviceToHost, st));
+    }
+    GVS_CUDA(c, cudaStreamSynchronize(st));
+    return GVS_OK;
+}
+
 }  // namespace gvs

@@ -678,6 +678,21 @@ void set_smem(T kernel, int bytes) {
 // host side
 // ---------------------------------------------------------------------------
 
+// f64 min/max of the resident positions into dev_out6 = (min x, min y, min z, max x, max y, max z).
+// min/max are exact, so the result equals the reference's sequential scan
+// (BoundingBox::containing, crates/sim-core/src/octree.rs:14-44).
+gvs_status bbox_minmax(Ctx *c, double *dev_out6, DevBuf &part_buf) {
+    const size_t n = c->n;
+    const int nb = std::min(c->num_sms * 4, std::max(1, ceil_div((long long)n, 256)));
+    GVS_CUDA(c, ensure(c, part_buf, (size_t)nb * 6 * sizeof(double)));
+    double *bb = as<double>(part_buf);
+    k_bbox_part<<<nb, 256, 0, c->stream>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z), n, bb);
+    k_bbox_final<<<1, 32, 0, c->stream>>>(bb, nb);
+    c->prof.launches += 2;
+    GVS_CUDA(c, cudaMemcpyAsync(dev_out6, bb, 6 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    return check_launch(c, "bounding box");
+}
+
 // Hilbert order of the resident positions: c->perm[s] = caller index of sorted slot s.
 gvs_status spatial_order(Ctx *c) {
     const size_t n = c->n;

@@ -99,6 +99,7 @@ static gvs_status download(Ctx *c, void *dst, DevBuf &b, size_t bytes) {
 }
 
 static gvs_status alloc_state(Ctx *c, size_t n) {
+    c->pos_version++;
     const size_t b = std::max<size_t>(n, 1) * sizeof(double);
     DevBuf *f64s[] = {&c->x, &c->y, &c->z, &c->vx, &c->vy, &c->vz, &c->ax, &c->ay, &c->az, &c->m,
                       &c->u, &c->h, &c->alpha, &c->rho, &c->pres, &c->cs, &c->du_dt, &c->omega,
@@ -254,6 +255,7 @@ gvs_status gvs_set_state(gvs_ctx *c, size_t n, const double *x, const double *y,
     GVS_TRY(upload(c, c->x, x, b)); GVS_TRY(upload(c, c->y, y, b)); GVS_TRY(upload(c, c->z, z, b));
     GVS_TRY(upload(c, c->vx, vx, b)); GVS_TRY(upload(c, c->vy, vy, b)); GVS_TRY(upload(c, c->vz, vz, b));
     GVS_TRY(upload(c, c->m, mass, b));
+    c->pos_version++;
     GVS_TRY(clear_acc(c));
     c->has_gas = ptype != nullptr;
     if (ptype) GVS_CUDA(c, cudaMemcpyAsync(c->ptype.ptr, ptype, n, cudaMemcpyHostToDevice, c->stream));
@@ -310,11 +312,12 @@ static gvs_status check_prec_algo(gvs_ctx *c, int algo, int precision, double ep
     return GVS_OK;
 }
 
-gvs_status gvs_gravity_direct(gvs_ctx *c, size_t n, const double *x, const double *y, const double *z,
-                              const double *mass, double eps, int precision, double *ax, double *ay, double *az) {
+static gvs_status gravity_host(gvs_ctx *c, int algo, size_t n, const double *x, const double *y, const double *z,
+                               const double *mass, double eps, double theta, int precision, double *ax, double *ay,
+                               double *az) {
     GVS_TRY(check_ctx(c));
     if (!x || !y || !z || !mass || !ax || !ay || !az) return fail(c, GVS_ERR_INVALID_ARG, "null array");
-    GVS_TRY(check_prec_algo(c, GVS_ALGO_DIRECT, precision, eps, 0.0));
+    GVS_TRY(check_prec_algo(c, algo, precision, eps, theta));
     if (n > 0xFFFFFFF0ull) return fail(c, GVS_ERR_INVALID_ARG, "n too large");
     if (n == 0) return GVS_OK;
     cudaSetDevice(c->device);
@@ -322,11 +325,33 @@ gvs_status gvs_gravity_direct(gvs_ctx *c, size_t n, const double *x, const doubl
     const size_t b = n * sizeof(double);
     GVS_TRY(upload(c, c->x, x, b)); GVS_TRY(upload(c, c->y, y, b)); GVS_TRY(upload(c, c->z, z, b));
     GVS_TRY(upload(c, c->m, mass, b));
+    c->pos_version++;
     // accumulate semantics: upload the caller's a, add forces, download
     GVS_TRY(upload(c, c->ax, ax, b)); GVS_TRY(upload(c, c->ay, ay, b)); GVS_TRY(upload(c, c->az, az, b));
-    GVS_TRY(gravity(c, GVS_ALGO_DIRECT, precision, eps, 0.0, true));
+    GVS_TRY(gravity(c, algo, precision, eps, theta, true));
     GVS_TRY(download(c, ax, c->ax, b)); GVS_TRY(download(c, ay, c->ay, b)); GVS_TRY(download(c, az, c->az, b));
     GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return read_device_errors(c);
+}
+
+gvs_status gvs_gravity_direct(gvs_ctx *c, size_t n, const double *x, const double *y, const double *z,
+                              const double *mass, double eps, int precision, double *ax, double *ay, double *az) {
+    return gravity_host(c, GVS_ALGO_DIRECT, n, x, y, z, mass, eps, 0.0, precision, ax, ay, az);
+}
+
+gvs_status gvs_gravity_bh(gvs_ctx *c, size_t n, const double *x, const double *y, const double *z,
+                          const double *mass, double eps, double theta, int precision, double *ax, double *ay,
+                          double *az) {
+    return gravity_host(c, GVS_ALGO_BH, n, x, y, z, mass, eps, theta, precision, ax, ay, az);
+}
+
+gvs_status gvs_tree_export(gvs_ctx *c, size_t cap, size_t *nnodes, uint8_t *level, uint32_t *first, uint32_t *count,
+                           uint32_t *skip, double *mass, double *com, uint32_t *order, uint64_t *keys) {
+    GVS_TRY(check_ctx(c));
+    if (!nnodes) return fail(c, GVS_ERR_INVALID_ARG, "nnodes is NULL");
+    if (c->n == 0) return fail(c, GVS_ERR_STATE, "no particles");
+    cudaSetDevice(c->device);
+    GVS_TRY(tree_export(c, cap, level, first, count, skip, mass, com, order, keys, nnodes));
     return read_device_errors(c);
 }
 
@@ -368,6 +393,7 @@ gvs_status gvs_kdk_step_host(gvs_ctx *c, size_t n, double *x, double *y, double 
     GVS_TRY(upload(c, c->vx, vx, b)); GVS_TRY(upload(c, c->vy, vy, b)); GVS_TRY(upload(c, c->vz, vz, b));
     GVS_TRY(upload(c, c->ax, ax, b)); GVS_TRY(upload(c, c->ay, ay, b)); GVS_TRY(upload(c, c->az, az, b));
     GVS_TRY(upload(c, c->m, mass, b));
+    c->pos_version++;
     if (nan_fault_due(c)) return fail(c, GVS_ERR_INJECTED, "injected non-finite fault");
     GVS_TRY(kdk_one(c, algo, precision, eps, theta, dt));
     GVS_TRY(download(c, x, c->x, b)); GVS_TRY(download(c, y, c->y, b)); GVS_TRY(download(c, z, c->z, b));

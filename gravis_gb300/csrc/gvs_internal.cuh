@@ -100,6 +100,7 @@ struct Ctx {
     int fault_kind = 0;  // 0 none, 1 alloc, 2 launch, 3 nan
     long long fault_step = -1;
     long long step_counter = 0;
+    unsigned long long pos_version = 0;  // bumped whenever resident positions change
 };
 
 // Records an error message on the context and returns the status.
@@ -196,11 +197,13 @@ gvs_status radix_sort_u32(Ctx *c, uint32_t *keys, uint32_t *vals, uint32_t *keys
                           int begin_bit, int end_bit, uint32_t **keys_out, uint32_t **vals_out);
 gvs_status radix_sort_u64(Ctx *c, uint64_t *keys, uint32_t *vals, uint64_t *keys_alt, uint32_t *vals_alt, size_t n,
                           int begin_bit, int end_bit, uint64_t **keys_out, uint32_t **vals_out);
+gvs_status exclusive_scan_u32(Ctx *c, const uint32_t *in, uint32_t *out, size_t n, uint32_t *total_dev);
 // direct.cu
 gvs_status direct_forces(Ctx *c, int precision, double eps, bool accumulate);
 gvs_status direct_forces_subset(Ctx *c, int precision, double eps, const int64_t *idx_dev, size_t nidx,
                                 double *out_dev);
 gvs_status spatial_order(Ctx *c);
+gvs_status bbox_minmax(Ctx *c, double *dev_out6, DevBuf &part_buf);
 gvs_status autotune_direct(Ctx *c, int precision, double eps, int *best_nt, int *best_ipt, double *best_ms);
 // kdk.cu
 gvs_status kick(Ctx *c, double half_dt);
@@ -213,6 +216,19 @@ gvs_status diagnostics(Ctx *c, double eps, int with_potential, gvs_diag *out);
 gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accumulate);
 gvs_status tree_build(Ctx *c);
 void tree_free(Ctx *c);
+// Read-only view of the octree of the resident positions (device pointers).
+// Nodes are in depth-first pre-order; node k covers sorted slots
+// [first[k], first[k] + count) and its subtree ends at node skip[k].
+struct TreeView {
+    size_t n, nnodes;
+    const uint8_t *level;
+    const uint32_t *first, *cnt, *skip, *perm;
+    const double *bx, *by, *bz, *sx, *sy, *sz;  // cell centres; sorted positions
+    double root_hw;                              // half width at depth 0 (depth L: root_hw * 2^-L)
+};
+gvs_status tree_view(Ctx *c, TreeView *v);
+gvs_status tree_export(Ctx *c, size_t cap, uint8_t *level, uint32_t *first, uint32_t *cnt, uint32_t *skip,
+                       double *mass, double *com, uint32_t *perm, uint64_t *keys, size_t *nnodes);
 // sph.cu
 gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm);
 gvs_status sph_timestep(Ctx *c, const gvs_sph_params *prm, double *dt_out);

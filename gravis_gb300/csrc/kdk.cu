@@ -67,6 +67,7 @@ gvs_status kick(Ctx *c, double half_dt) {
 
 gvs_status drift(Ctx *c, double dt) {
     if (c->n == 0) return GVS_OK;
+    c->pos_version++;
     k_drift<<<grid_for(c, c->n), 256, 0, c->stream>>>(c->n, dt, as<double>(c->vx), as<double>(c->vy),
                                                       as<double>(c->vz), as<double>(c->x), as<double>(c->y),
                                                       as<double>(c->z));
@@ -76,6 +77,7 @@ gvs_status drift(Ctx *c, double dt) {
 
 gvs_status kick_drift(Ctx *c, double half_dt, double dt) {
     if (c->n == 0) return GVS_OK;
+    c->pos_version++;
     k_kick_drift<<<grid_for(c, c->n), 256, 0, c->stream>>>(
         c->n, half_dt, dt, as<double>(c->ax), as<double>(c->ay), as<double>(c->az), as<double>(c->vx),
         as<double>(c->vy), as<double>(c->vz), as<double>(c->x), as<double>(c->y), as<double>(c->z));

@@ -1,7 +1,7 @@
 // sort.cu -- stable LSD radix sort of (key, u32 value) pairs on the device.
 //
 // Used to put particles in space-filling-curve order: the direct sum sorts
-// 30-bit Morton keys so that consecutive particles form compact tiles (the
+// 63-bit Hilbert keys so that consecutive particles form compact tiles (the
 // tile-centre split of the mixed-precision kernel needs that), and the
 // Barnes-Hut build sorts 126-bit octant-path keys (two u64 words, sorted as
 // low word then high word) so that the sorted order is the depth-first order
@@ -60,6 +60,8 @@ __global__ void __launch_bounds__(1024) k_scan1(uint32_t *a, int m) {
         run += v;
     }
 }
+
+__global__ void k_add_u32(uint32_t *a, const uint32_t *b) { a[0] += b[0]; }
 
 template <class K>
 __global__ void __launch_bounds__(NT) k_scatter(const K *__restrict__ keys, const uint32_t *__restrict__ vals,
@@ -138,4 +140,94 @@ gvs_status radix_sort_u64(Ctx *c, uint64_t *keys, uint32_t *vals, uint64_t *keys
     return radix_sort_impl<uint64_t>(c, keys, vals, keys_alt, vals_alt, n, begin_bit, end_bit, keys_out, vals_out);
 }
 
+}  // namespace gvs
+
+// ---------------------------------------------------------------------------
+// exclusive prefix sum of u32 counts (three phases: block sums, one-block scan
+// of the block sums, block-local scan plus offset).  out may alias in.
+// ---------------------------------------------------------------------------
+namespace gvs {
+namespace {
+constexpr int SCAN_NT = 512;
+constexpr int SCAN_IPT = 8;
+constexpr int SCAN_TILE = SCAN_NT * SCAN_IPT;
+
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *total) {
+    __shared__ uint32_t ws[SCAN_NT / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t s = lane < SCAN_NT / 32 ? ws[lane] : 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xFFFFFFFFu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < SCAN_NT / 32) ws[lane] = s;
+    }
+    __syncthreads();
+    const uint32_t before = (w > 0 ? ws[w - 1] : 0u) + x - v;
+    if (total) *total = ws[SCAN_NT / 32 - 1];
+    __syncthreads();
+    return before;
+}
+
+__global__ void __launch_bounds__(SCAN_NT) k_scan_blocksum(const uint32_t *__restrict__ in, size_t n,
+                                                           uint32_t *__restrict__ bsum) {
+    const size_t base = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_IPT;
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_IPT; ++k)
+        if (base + k < n) s += in[base + k];
+    uint32_t tot;
+    block_excl_scan(s, &tot);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(SCAN_NT) k_scan_apply(const uint32_t *in, size_t n, const uint32_t *__restrict__ boff,
+                                                        uint32_t *out) {
+    const size_t base = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_IPT;
+    uint32_t v[SCAN_IPT];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_IPT; ++k) {
+        v[k] = base + k < n ? in[base + k] : 0u;
+        s += v[k];
+    }
+    uint32_t run = block_excl_scan(s, nullptr) + boff[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < SCAN_IPT; ++k)
+        if (base + k < n) {
+            out[base + k] = run;
+            run += v[k];
+        }
+}
+}  // namespace
+
+// out[i] = sum_{k<i} in[i], for i in [0, n); also returns the total in *total_dev[0] (device).
+gvs_status exclusive_scan_u32(Ctx *c, const uint32_t *in, uint32_t *out, size_t n, uint32_t *total_dev) {
+    if (n == 0) return GVS_OK;
+    const int nb = ceil_div((long long)n, SCAN_TILE);
+    GVS_CUDA(c, ensure(c, c->sort_hist, ((size_t)nb + 1) * sizeof(uint32_t) * 2));
+    uint32_t *bsum = as<uint32_t>(c->sort_hist);
+    uint32_t *boff = bsum + nb + 1;
+    k_scan_blocksum<<<nb, SCAN_NT, 0, c->stream>>>(in, n, bsum);
+    GVS_CUDA(c, cudaMemcpyAsync(boff, bsum, nb * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c->stream));
+    k_scan1<<<1, 1024, 0, c->stream>>>(boff, nb);
+    k_scan_apply<<<nb, SCAN_NT, 0, c->stream>>>(in, n, boff, out);
+    c->prof.launches += 3;
+    GVS_TRY(check_launch(c, "exclusive scan"));
+    if (total_dev) {
+        // total = offset of the last block + its sum
+        GVS_CUDA(c, cudaMemcpyAsync(total_dev, boff + nb - 1, sizeof(uint32_t), cudaMemcpyDeviceToDevice, c->stream));
+        k_add_u32<<<1, 1, 0, c->stream>>>(total_dev, bsum + nb - 1);
+        c->prof.launches += 1;
+    }
+    return GVS_OK;
+}
 }  // namespace gvs

@@ -181,6 +181,20 @@ class Context:
                                              _ptr(out[1]), _ptr(out[2])))
         return out.T.copy()
 
+    def tree_export(self) -> dict:
+        """The octree of the resident positions (depth-first pre-order)."""
+        nn = C.c_size_t()
+        self._ck(self._lib.gvs_tree_export(self.h, 0, C.byref(nn), None, None, None, None, None, None, None, None))
+        k, n = nn.value, self._lib.gvs_count(self.h)
+        out = {"level": np.zeros(k, np.uint8), "first": np.zeros(k, np.uint32), "count": np.zeros(k, np.uint32),
+               "skip": np.zeros(k, np.uint32), "mass": np.zeros(k), "com": np.zeros((3, k)),
+               "order": np.zeros(n, np.uint32), "keys": np.zeros((2, n), np.uint64)}
+        self._ck(self._lib.gvs_tree_export(self.h, k, C.byref(nn), *(_ptr(out[f]) for f in
+                                                                      ("level", "first", "count", "skip", "mass",
+                                                                       "com", "order", "keys"))))
+        out["nnodes"] = k
+        return out
+
     def autotune(self, precision: int, softening: float) -> dict:
         nt, ipt, ms = C.c_int(), C.c_int(), C.c_double()
         self._ck(self._lib.gvs_autotune_direct(self.h, precision, softening, C.byref(nt), C.byref(ipt),
@@ -287,13 +301,8 @@ class BarnesHut(GravitySolver):
 
     def compute_accelerations(self, p: Particles):
         c = self.context()
-        c.set_state(p)
-        c.compute_forces(L.ALGO_BH, self.precision, self.softening, self.theta)
-        a = np.zeros((3, p.count))
-        c._ck(c._lib.gvs_get_state(c.h, None, None, None, None, None, None, _ptr(a[0]), _ptr(a[1]), _ptr(a[2])))
-        p.ax += a[0]
-        p.ay += a[1]
-        p.az += a[2]
+        c._ck(c._lib.gvs_gravity_bh(c.h, p.count, _ptr(p.x), _ptr(p.y), _ptr(p.z), _ptr(p.mass), self.softening,
+                                    self.theta, self.precision, _ptr(p.ax), _ptr(p.ay), _ptr(p.az)))
 
 
 class LeapfrogKDK:

@@ -119,6 +119,23 @@ gvs_status gvs_gravity_direct(gvs_ctx *ctx, size_t n, const double *x, const dou
                               const double *mass, double softening, int precision, double *ax, double *ay,
                               double *az);
 
+/* BarnesHut::compute_accelerations (crates/sim-core/src/barnes_hut.rs:139-192): octree
+ * of the given positions, opening test s^2 < theta^2 d^2, monopoles.  precision
+ * GVS_PREC_FP64 / FP64_EXACT walks in f64 (the reference's arithmetic per term),
+ * GVS_PREC_FP32 / MIXED walks on f32 positions and f32 moments.  Accumulates. */
+gvs_status gvs_gravity_bh(gvs_ctx *ctx, size_t n, const double *x, const double *y, const double *z,
+                          const double *mass, double softening, double theta, int precision, double *ax, double *ay,
+                          double *az);
+/* Octree of the resident positions (Octree::rebuild, crates/sim-core/src/octree.rs:156-239),
+ * in depth-first pre-order (children 0..7).  Always sets *nnodes; fills the arrays only
+ * if cap >= *nnodes (any may be NULL): depth, first sorted slot, leaf particle count (0
+ * for internal nodes), skip (index after the subtree), mass, com (x[nn], y[nn], z[nn]),
+ * order (sorted slot -> caller index, length n) and keys (126-bit octant paths of the
+ * sorted particles: high words [n] then low words [n]). */
+gvs_status gvs_tree_export(gvs_ctx *ctx, size_t cap, size_t *nnodes, uint8_t *level, uint32_t *first,
+                           uint32_t *count, uint32_t *skip, double *mass, double *com, uint32_t *order,
+                           uint64_t *keys);
+
 /* ---- device-resident force / integration --------------------------------------- */
 /* clear_accelerations + compute_accelerations on the resident state
  * (integrator.rs:67-68): a = forces (overwrites the resident a). */

@@ -103,6 +103,8 @@ def lib():
             "orc_sph_timestep": (d, [C.POINTER(_CSph), P]),
             "orc_sph_step": (d, [P, G, C.POINTER(_CSph), d]),
             "orc_max_threads": (i32, []),
+            "orc_octree_build_leaves": (i64, [P, C.POINTER(i64), C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.c_void_p, i64]),
             "orc_rng_seed_u64": (None, [C.c_void_p, u64]),
             "orc_rng_next_u64": (u64, [C.c_void_p]),
             "orc_rng_f64": (d, [C.c_void_p]),
@@ -237,6 +239,21 @@ def diagnostics(p: Particles, softening: float, compute_potential: bool = True) 
 def octant(center, x, y, z) -> int:
     c = (C.c_double * 3)(*center)
     return lib().orc_octant(c, x, y, z)
+
+
+def octree_leaves(p: Particles) -> dict:
+    """Reference octree of p: node count and leaves in DFS pre-order (children 0..7)
+    with their depth and octant path (126-bit, left-aligned, truncated at the leaf)."""
+    nn = C.c_int64()
+    cap = p.n
+    pidx = np.zeros(cap, np.uint32)
+    depth = np.zeros(cap, np.int32)
+    hi = np.zeros(cap, np.uint64)
+    lo = np.zeros(cap, np.uint64)
+    nl = lib().orc_octree_build_leaves(p.c(), C.byref(nn), pidx.ctypes.data, depth.ctypes.data, hi.ctypes.data,
+                                       lo.ctypes.data, cap)
+    return {"nnodes": nn.value, "nleaves": nl, "order": pidx[:nl], "depth": depth[:nl], "path_hi": hi[:nl],
+            "path_lo": lo[:nl]}
 
 
 def bbox_containing(p: Particles):

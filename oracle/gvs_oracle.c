@@ -487,6 +487,57 @@ void orc_octree_rebuild(orc_octree *t, const orc_particles *p) {
         tree_insert(t, 0, (uint32_t)i, p->x[i], p->y[i], p->z[i], p->mass[i], 0);
 }
 
+/* Depth-first pre-order walk of the tree (children 0..7, the order of
+ * query_ball_walk, octree.rs:285-289): for each leaf, its particle index,
+ * depth and octant path (3 bits per level, levels 1..21 in path_hi, 22..42
+ * in path_lo, left-aligned as in a 126-bit key truncated at the leaf).
+ * Returns the number of leaves (fills at most cap). */
+int64_t orc_octree_leaves(const orc_octree *t, uint32_t *pidx, int32_t *depth, uint64_t *path_hi,
+                          uint64_t *path_lo, int64_t cap) {
+    if (t->count == 0) return 0;
+    typedef struct { uint32_t node; int32_t d; uint64_t hi, lo; } item;
+    item *stack = (item *)malloc(sizeof(item) * (size_t)(t->count + 8));
+    int64_t sp = 0, nl = 0;
+    stack[sp++] = (item){0, 0, 0, 0};
+    while (sp > 0) {
+        item it = stack[--sp];
+        const orc_node *nd = &t->nodes[it.node];
+        if (nd->particle_index != ORC_NONE) {
+            if (nl < cap) {
+                pidx[nl] = nd->particle_index;
+                depth[nl] = it.d;
+                path_hi[nl] = it.hi;
+                path_lo[nl] = it.lo;
+            }
+            nl++;
+            continue;
+        }
+        for (int k = 7; k >= 0; --k) {
+            if (nd->children[k] == ORC_NONE) continue;
+            item ch = {nd->children[k], it.d + 1, it.hi, it.lo};
+            int L = it.d + 1;
+            if (L <= 21) ch.hi |= (uint64_t)k << (63 - 3 * L);
+            else if (L <= 42) ch.lo |= (uint64_t)k << (63 - 3 * (L - 21));
+            stack[sp++] = ch;
+        }
+    }
+    free(stack);
+    return nl;
+}
+
+int64_t orc_octree_count(const orc_octree *t) { return t->count; }
+
+/* Builds the reference octree of p and returns its node count and leaves. */
+int64_t orc_octree_build_leaves(const orc_particles *p, int64_t *nnodes, uint32_t *pidx, int32_t *depth,
+                                uint64_t *path_hi, uint64_t *path_lo, int64_t cap) {
+    orc_octree t = {0};
+    orc_octree_rebuild(&t, p);
+    *nnodes = t.count;
+    int64_t nl = orc_octree_leaves(&t, pidx, depth, path_hi, path_lo, cap);
+    orc_octree_free(&t);
+    return nl;
+}
+
 void orc_octree_free(orc_octree *t) {
     free(t->nodes);
     t->nodes = NULL;

@@ -116,6 +116,11 @@ void orc_octree_free(orc_octree *t);
 int64_t orc_octree_query_ball(const orc_octree *t, const orc_particles *p, const double pos[3], double radius,
                               uint32_t *out, int64_t cap);
 void orc_bbox_containing(const orc_particles *p, double center[3], double *half_width);
+int64_t orc_octree_leaves(const orc_octree *t, uint32_t *pidx, int32_t *depth, uint64_t *path_hi,
+                          uint64_t *path_lo, int64_t cap);
+int64_t orc_octree_count(const orc_octree *t);
+int64_t orc_octree_build_leaves(const orc_particles *p, int64_t *nnodes, uint32_t *pidx, int32_t *depth,
+                                uint64_t *path_hi, uint64_t *path_lo, int64_t cap);
 int  orc_octant(const double center[3], double x, double y, double z);
 
 /* ---- SPH ---------------------------------------------------------------- */

@@ -1,0 +1,185 @@
+"""GPU octree + Barnes-Hut against the oracle's restatement of the reference.
+
+Tree: bit-exact.  The node count, the depth-first leaf order (= the GPU sort
+order) and every particle's octant path down to its leaf must equal the
+reference tree's (Octree::rebuild, crates/sim-core/src/octree.rs:156-239).
+Forces: the f64 walk makes the reference's accept decisions on a bottom-up
+centre of mass (a few ulps from the reference's incremental one) and sums
+children 0..7 instead of 7..0, so it agrees with the oracle's BarnesHut to
+<= 1e-12 relative RMS; the f32 walk within 1e-5 of the f64 walk.
+"""
+import numpy as np
+import pytest
+
+import gravis_gb300 as G
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = G.Context(0)
+    yield c
+    c.close()
+
+
+def rel_rms(a, ref):
+    return float(np.sqrt(((a - ref) ** 2).sum() / (ref ** 2).sum()))
+
+
+def to_oracle(p):
+    q = O.Particles(p.count)
+    for a, b in (("x", "x"), ("y", "y"), ("z", "z"), ("vx", "vx"), ("vy", "vy"), ("vz", "vz"), ("mass", "mass")):
+        getattr(q, b)[:] = getattr(p, a)
+    return q
+
+
+def lattice(n_side, spacing):
+    p = G.Particles(n_side ** 3)
+    k = 0
+    for ix in range(n_side):
+        for iy in range(n_side):
+            for iz in range(n_side):
+                p.x[k], p.y[k], p.z[k], p.mass[k] = ix * spacing, iy * spacing, iz * spacing, 1.0
+                k += 1
+    return p
+
+
+def cases():
+    return {
+        "plummer1000": G.PlummerSphere(1000, seed=42).generate(),
+        "plummer20000": G.PlummerSphere(20000, seed=3).generate(),
+        "collision4096": G.collision(4096, seed=7),
+        "lattice8": lattice(8, 0.5),  # exact octant-boundary ties
+        "two": G.TwoBody(0.5, 0.5, 1.0).generate(),
+        "one": G.PlummerSphere(1, seed=1).generate(),
+    }
+
+
+@pytest.mark.parametrize("name", list(cases().keys()))
+def test_tree_matches_reference(ctx, name):
+    p = cases()[name]
+    ctx.set_state(p)
+    t = ctx.tree_export()
+    ref = O.octree_leaves(to_oracle(p))
+    assert t["nnodes"] == ref["nnodes"]
+    leaves = t["count"] > 0
+    assert int(leaves.sum()) == ref["nleaves"] == p.count
+    # depth-first leaf order == sorted order of the GPU
+    assert np.array_equal(t["order"][t["first"][leaves]], ref["order"])
+    assert np.array_equal(t["level"][leaves].astype(np.int32), ref["depth"])
+    # octant paths, bit-exact, truncated at each leaf's depth
+    hi, lo = t["keys"][0][t["first"][leaves]], t["keys"][1][t["first"][leaves]]
+    def masks(k):
+        k = int(k)
+        if k <= 21:
+            return ((1 << (3 * k)) - 1) << (63 - 3 * k), 0
+        return (1 << 63) - 1, ((1 << (3 * (k - 21))) - 1) << (63 - 3 * (k - 21))
+    mk = [masks(k) for k in ref["depth"]]
+    mask_hi = np.array([a for a, _ in mk], dtype=np.uint64)
+    mask_lo = np.array([b for _, b in mk], dtype=np.uint64)
+    assert np.array_equal(hi & mask_hi, ref["path_hi"])
+    assert np.array_equal(lo & mask_lo, ref["path_lo"])
+    # moments: the root holds the total mass and centre of mass
+    m = p.mass
+    assert abs(t["mass"][0] - m.sum()) <= 1e-12 * m.sum()
+    com = np.array([(m * p.x).sum(), (m * p.y).sum(), (m * p.z).sum()]) / m.sum()
+    assert np.allclose(t["com"][:, 0], com, rtol=0, atol=1e-12 * max(1.0, np.abs(p.x).max()))
+
+
+@pytest.mark.parametrize("theta", [0.0, 0.3, 0.5, 0.7, 1.0])
+@pytest.mark.parametrize("name", ["plummer1000", "collision4096", "lattice8"])
+def test_bh_f64_vs_oracle(ctx, name, theta):
+    p = cases()[name]
+    eps = 0.05
+    q = p.copy()
+    q.clear_accelerations()
+    G.BarnesHut(eps, theta, G.PREC_FP64, ctx).compute_accelerations(q)
+    r = to_oracle(p)
+    O.bh(r, eps, theta)
+    assert rel_rms(q.acc(), r.acc()) <= 1e-12, rel_rms(q.acc(), r.acc())
+
+
+def test_bh_theta_zero_is_bf(ctx):
+    """barnes_hut.rs:219-265 on the GPU: theta = 0 equals BruteForce within 1e-12."""
+    pts = [(0.0, 0.0, 0.0, 1.0), (1.0, 0.0, 0.0, 2.0), (0.0, 1.0, 0.0, 1.5), (-1.0, -1.0, 0.5, 0.5),
+           (0.5, 0.5, -0.5, 3.0)]
+    p = G.Particles(5)
+    for i, (x, y, z, m) in enumerate(pts):
+        p.x[i], p.y[i], p.z[i], p.mass[i] = x, y, z, m
+    a = p.copy()
+    G.BarnesHut(0.05, 0.0, G.PREC_FP64, ctx).compute_accelerations(a)
+    b = p.copy()
+    G.BruteForce(0.05, G.PREC_FP64_EXACT, ctx).compute_accelerations(b)
+    assert np.max(np.abs(a.acc() - b.acc())) < 1e-12
+
+
+def test_bh_accuracy_table(ctx, golden):
+    """m3_accuracy.csv from the GPU walk: BH vs BF relative error at N=1000, seed 42, eps 0.05."""
+    p = G.PlummerSphere(1000, seed=42).generate()
+    bf = p.copy()
+    G.BruteForce(0.05, G.PREC_FP64_EXACT, ctx).compute_accelerations(bf)
+    a = bf.acc()
+    for row in golden["m3_accuracy.csv"]["rows"]:
+        q = p.copy()
+        G.BarnesHut(0.05, row[0], G.PREC_FP64, ctx).compute_accelerations(q)
+        m2 = (a * a).sum(1)
+        rel = ((q.acc() - a) ** 2).sum(1) / m2
+        rms, mx = np.sqrt(rel.sum() / 1000), np.sqrt(rel.max())
+        assert f"{rms:.5e}" == f"{row[2]:.5e}", (row[0], rms, row[2])
+        assert f"{mx:.5e}" == f"{row[3]:.5e}", (row[0], mx, row[3])
+
+
+@pytest.mark.parametrize("theta", [0.5, 0.7])
+def test_bh_f32_walk(ctx, theta):
+    p = G.collision(1 << 16, seed=7)
+    eps = 1e-3
+    a64 = p.copy()
+    G.BarnesHut(eps, theta, G.PREC_FP64, ctx).compute_accelerations(a64)
+    a32 = p.copy()
+    G.BarnesHut(eps, theta, G.PREC_FP32, ctx).compute_accelerations(a32)
+    err = rel_rms(a32.acc(), a64.acc())
+    print(f"theta={theta} f32 walk vs f64 walk rel RMS {err:.2e}")
+    assert err <= 1e-5
+
+
+def test_bh_vs_direct_subset(ctx):
+    """Accuracy of the walk against the exact f64 direct sum on a random subset."""
+    n = 1 << 17
+    p = G.collision(n, seed=7)
+    eps = 1e-3
+    ctx.set_state(p)
+    idx = np.sort(np.random.default_rng(1).choice(n, 2048, replace=False))
+    ref = ctx.direct_subset(idx, eps)
+    for theta, bound in ((0.5, 0.01), (0.7, 0.03)):
+        q = p.copy()
+        G.BarnesHut(eps, theta, G.PREC_FP32, ctx).compute_accelerations(q)
+        rel = np.sqrt((((q.acc()[idx] - ref) ** 2).sum(1) / (ref ** 2).sum(1)).mean())
+        print(f"theta={theta} BH f32 vs direct f64 per-particle RMS {rel:.3e}")
+        assert rel < bound
+
+
+def test_bh_deterministic_and_resident_steps(ctx):
+    p = G.PlummerSphere(5000, seed=9).generate()
+    outs = []
+    for _ in range(2):
+        ctx.set_state(p)
+        ctx.compute_forces(G.ALGO_BH, G.PREC_FP32, 0.01, 0.5)
+        ctx.kdk_steps(G.ALGO_BH, G.PREC_FP32, 0.01, 0.5, 1e-3, 20)
+        q = G.Particles(p.count)
+        ctx.get_state(q)
+        outs.append(q.x.copy())
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_bh_kdk_energy(ctx):
+    """Plummer N=2000 with BH theta=0.5: 500 steps at dt=1e-3 keep |dE/E| small (tests/barnes_hut.rs)."""
+    p = G.PlummerSphere(2000, seed=42).generate()
+    eps = 0.05
+    ctx.set_state(p)
+    ctx.compute_forces(G.ALGO_BH, G.PREC_FP64, eps, 0.5)
+    e0 = ctx.diagnostics(eps).total_energy
+    ctx.kdk_steps(G.ALGO_BH, G.PREC_FP64, eps, 0.5, 1e-3, 500)
+    e1 = ctx.diagnostics(eps).total_energy
+    assert abs(e1 - e0) / abs(e0) < 1e-3
