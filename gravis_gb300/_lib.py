@@ -62,10 +62,16 @@ SIGNATURES = {
     "gvs_set_accelerations": (_ST, [_P, _P, _P, _P]),
     "gvs_get_gas": (_ST, [_P] + [_P] * 7),
     "gvs_count": (_sz, [_P]),
+    "gvs_set_gas": (_ST, [_P] + [_P] * 7),
     "gvs_gravity_direct": (_ST, [_P, _sz, _P, _P, _P, _P, _d, _i, _P, _P, _P]),
     "gvs_gravity_bh": (_ST, [_P, _sz, _P, _P, _P, _P, _d, _d, _i, _P, _P, _P]),
     "gvs_tree_export": (_ST, [_P, _sz, C.POINTER(_sz)] + [_P] * 8),
     "gvs_compute_forces": (_ST, [_P, _i, _i, _d, _d]),
+    "gvs_sph_params_default": (_ST, [C.POINTER(SphParams)]),
+    "gvs_sph_compute": (_ST, [_P, C.POINTER(SphParams), _P, _P, _P, _P]),
+    "gvs_sph_timestep": (_ST, [_P, C.POINTER(SphParams), C.POINTER(_d)]),
+    "gvs_sph_step": (_ST, [_P, C.POINTER(SphParams), _i, _i, _d, _d, _d, C.POINTER(_d)]),
+    "gvs_sph_neighbors": (_ST, [_P, _sz, C.POINTER(_sz), _P, _P, _P]),
     "gvs_kdk_steps": (_ST, [_P, _i, _i, _d, _d, _d, _ll]),
     "gvs_kdk_step_host": (_ST, [_P, _sz] + [_P] * 10 + [_i, _i, _d, _d, _d]),
     "gvs_diagnostics": (_ST, [_P, _d, _i, C.POINTER(Diag)]),

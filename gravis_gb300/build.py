@@ -43,10 +43,15 @@ def _stale(obj: str, src: str) -> bool:
     return any(os.path.getmtime(p) > t for p in [src] + _headers())
 
 
+# Per-file flags: the SPH kernels restate the reference's f64 arithmetic
+# statement by statement, so a*b+c must round twice there.
+FILE_FLAGS = {"sph.cu": ["--fmad=false"]}
+
+
 def _compile(nvcc: str, src: str, extra: list[str]) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     if _stale(obj, src):
-        cmd = [nvcc] + ARCH + NVCC_FLAGS + extra + ["-c", src, "-o", obj]
+        cmd = [nvcc] + ARCH + NVCC_FLAGS + FILE_FLAGS.get(os.path.basename(src), []) + extra + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {os.path.basename(src)}:\n{r.stdout}\n{r.stderr}")
@@ -67,7 +72,7 @@ def build(force: bool = False, extra: list[str] | None = None) -> str:
     if verbose():
         extra += ["-Xptxas", "-v"]
     stamp = os.path.join(BUILD, "flags.txt")
-    flags = " ".join(ARCH + NVCC_FLAGS + extra)
+    flags = " ".join(ARCH + NVCC_FLAGS + extra) + repr(sorted(FILE_FLAGS.items()))
     if not os.path.exists(stamp) or open(stamp).read() != flags:
         force = True
         with open(stamp, "w") as fh:

@@ -291,6 +291,21 @@ gvs_status gvs_set_accelerations(gvs_ctx *c, const double *ax, const double *ay,
     return GVS_OK;
 }
 
+gvs_status gvs_set_gas(gvs_ctx *c, const double *density, const double *pressure, const double *u,
+                       const double *du_dt, const double *h, const double *sound_speed, const double *alpha) {
+    GVS_TRY(check_ctx(c));
+    const size_t b = c->n * sizeof(double);
+    if (density) GVS_TRY(upload(c, c->rho, density, b));
+    if (pressure) GVS_TRY(upload(c, c->pres, pressure, b));
+    if (u) GVS_TRY(upload(c, c->u, u, b));
+    if (du_dt) GVS_TRY(upload(c, c->du_dt, du_dt, b));
+    if (h) GVS_TRY(upload(c, c->h, h, b));
+    if (sound_speed) GVS_TRY(upload(c, c->cs, sound_speed, b));
+    if (alpha) GVS_TRY(upload(c, c->alpha, alpha, b));
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return GVS_OK;
+}
+
 gvs_status gvs_get_gas(gvs_ctx *c, double *density, double *pressure, double *u, double *du_dt, double *h,
                        double *sound_speed, double *alpha) {
     GVS_TRY(check_ctx(c));
@@ -441,6 +456,70 @@ gvs_status gvs_autotune_direct(gvs_ctx *c, int precision, double eps, int *nthre
     cudaSetDevice(c->device);
     GVS_TRY(autotune_direct(c, precision, eps, nthreads, ipt, ms));
     return read_device_errors(c);
+}
+
+// ---- SPH ---------------------------------------------------------------------------
+
+gvs_status gvs_sph_params_default(gvs_sph_params *p) {
+    if (!p) return GVS_ERR_INVALID_ARG;
+    p->gamma = 5.0 / 3.0;   // solver.rs:43
+    p->eta = 1.2;           // solver.rs:44
+    p->cfl_factor = 0.3;    // solver.rs:46
+    p->force_factor = 0.25; // solver.rs:47
+    p->h_max = INFINITY;    // solver.rs:48
+    p->beta_visc = 2.0;     // forces.rs:34
+    p->alpha_min = 0.1;     // forces.rs:35
+    p->alpha_max = 2.0;     // forces.rs:36
+    p->alpha_cond = 1.0;    // forces.rs:37
+    p->sigma_visc = 0.1;    // forces.rs:38
+    return GVS_OK;
+}
+
+static gvs_status check_sph(gvs_ctx *c, const gvs_sph_params *p) {
+    GVS_TRY(check_ctx(c));
+    if (!p) return fail(c, GVS_ERR_INVALID_ARG, "SPH parameters are NULL");
+    if (!(p->gamma > 1.0) || !(p->eta > 0.0) || !(p->cfl_factor > 0.0) || !(p->force_factor > 0.0) ||
+        !(p->alpha_min <= p->alpha_max))
+        return fail(c, GVS_ERR_INVALID_ARG, "invalid SPH parameters");
+    if (!c->has_gas) return fail(c, GVS_ERR_STATE, "no gas particles uploaded (ptype/u/h/alpha were NULL)");
+    cudaSetDevice(c->device);
+    return GVS_OK;
+}
+
+gvs_status gvs_sph_compute(gvs_ctx *c, const gvs_sph_params *p, double *omega, double *div_v, double *max_mu,
+                           double *dalpha_dt) {
+    GVS_TRY(check_sph(c, p));
+    GVS_TRY(sph_compute(c, p));
+    const size_t b = c->n * sizeof(double);
+    GVS_TRY(download(c, omega, c->omega, b)); GVS_TRY(download(c, div_v, c->div_v, b));
+    GVS_TRY(download(c, max_mu, c->max_mu, b)); GVS_TRY(download(c, dalpha_dt, c->dalpha_dt, b));
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return read_device_errors(c);
+}
+
+gvs_status gvs_sph_timestep(gvs_ctx *c, const gvs_sph_params *p, double *dt) {
+    GVS_TRY(check_sph(c, p));
+    if (!dt) return fail(c, GVS_ERR_INVALID_ARG, "dt is NULL");
+    GVS_TRY(sph_timestep(c, p, dt));
+    return read_device_errors(c);
+}
+
+gvs_status gvs_sph_step(gvs_ctx *c, const gvs_sph_params *p, int algo, int precision, double eps, double theta,
+                        double dt, double *dt_next) {
+    GVS_TRY(check_sph(c, p));
+    GVS_TRY(check_prec_algo(c, algo, precision, eps, theta));
+    if (!(dt > 0.0) || !dt_next) return fail(c, GVS_ERR_INVALID_ARG, "dt must be > 0 and dt_next non-NULL");
+    if (nan_fault_due(c)) return fail(c, GVS_ERR_INJECTED, "injected non-finite fault");
+    GVS_TRY(sph_step(c, p, algo, precision, eps, theta, dt, dt_next));
+    return read_device_errors(c);
+}
+
+gvs_status gvs_sph_neighbors(gvs_ctx *c, size_t cap, size_t *total, uint32_t *start, uint32_t *count,
+                             uint32_t *idx) {
+    GVS_TRY(check_ctx(c));
+    if (!total) return fail(c, GVS_ERR_INVALID_ARG, "total is NULL");
+    cudaSetDevice(c->device);
+    return sph_neighbors_export(c, cap, start, count, idx, total);
 }
 
 // ---- profiling -----------------------------------------------------------------

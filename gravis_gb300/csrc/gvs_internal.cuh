@@ -232,6 +232,9 @@ gvs_status tree_export(Ctx *c, size_t cap, uint8_t *level, uint32_t *first, uint
 // sph.cu
 gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm);
 gvs_status sph_timestep(Ctx *c, const gvs_sph_params *prm, double *dt_out);
+gvs_status sph_step(Ctx *c, const gvs_sph_params *prm, int algo, int precision, double eps, double theta, double dt,
+                    double *dt_next);
+gvs_status sph_neighbors_export(Ctx *c, size_t cap, uint32_t *start, uint32_t *count, uint32_t *idx, size_t *total);
 void sph_free(Ctx *c);
 
 // forces on resident state according to the algorithm selector

@@ -1,12 +1,632 @@
-// sph.cu -- SPH on the GPU (placeholder until the SPH pipeline lands).
+// sph.cu -- grad-h SPH on the GPU (crates/sim-core/src/sph/).
+//
+// Everything follows the reference in f64, in the same operation order; this
+// translation unit is compiled with --fmad=false so that every a*b+c rounds
+// twice, as Rust does.  Particles are processed in the octree's sorted order
+// (spatially coherent); results are scattered back to the caller's order.
+//
+//  neighbours   build_neighbor_lists + Octree::query_ball (neighbors.rs:56-119,
+//               octree.rs:245-308): for each gas particle, every particle with
+//               d^2 <= (2 h 1.1)^2, found by a depth-first walk of the same octree
+//               with the same sphere/AABB prune, so each list is the reference's
+//               set in the reference's order.  Lists live in fixed-width rows of
+//               kmax slots; an overflow is flagged and the search rerun wider.
+//  density      compute_density + density_and_dw_dh (density.rs:42-157): the
+//               fixed-point h iteration (<= 5 iterations, tolerance 1e-3, re-query
+//               when 2 h_new > 2 h 1.1), Omega, then the ideal-gas EOS.
+//  forces       compute_forces (forces.rs:69-232): pressure with grad-h terms,
+//               Monaghan viscosity with the per-particle alpha, Price conductivity,
+//               div v, max mu, d alpha / dt.
+//  timestep     SphSolver::compute_timestep (solver.rs:90-131), a min-reduction.
+//  step         step_with_sph (solver.rs:145-212).
 #include "gvs_internal.cuh"
 
 namespace gvs {
-gvs_status sph_compute(Ctx *c, const gvs_sph_params *) {
-    return fail(c, GVS_ERR_STATE, "SPH path not available in this build");
+
+namespace {
+
+constexpr double PI_D = 3.14159265358979323846;
+constexpr int MAXL_S = 42;
+
+struct SphState {
+    int kmax = 160;
+    size_t n = 0;
+    DevBuf list, cnt;                                  // neighbour rows [n][kmax] (sorted slots), counts
+    DevBuf gas;                                        // sorted: 1 if gas
+    DevBuf sx, sy, sz, svx, svy, svz, sm, sh, su, salpha;  // sorted inputs
+    DevBuf srho, spres, scs, somega, sdivv, smaxmu, sdalpha, sax, say, saz, sdu;  // sorted outputs
+    DevBuf dtpart;
+    bool have_intermediates = false;
+};
+
+SphState *sph_of(Ctx *c) {
+    if (!c->sph) c->sph = new SphState();
+    return static_cast<SphState *>(c->sph);
 }
-gvs_status sph_timestep(Ctx *c, const gvs_sph_params *, double *) {
-    return fail(c, GVS_ERR_STATE, "SPH path not available in this build");
+
+__device__ __forceinline__ double norm3d() { return 21.0 / (16.0 * PI_D); }
+
+// sph/kernel.rs:26-35
+__device__ __forceinline__ double kw(double r, double h) {
+    const double q = r / h;
+    if (q >= 2.0) return 0.0;
+    const double h3 = h * h * h;
+    const double s = 1.0 - 0.5 * q;
+    const double s4 = s * s * s * s;
+    return norm3d() / h3 * s4 * (1.0 + 2.0 * q);
 }
-void sph_free(Ctx *) {}
+
+// sph/kernel.rs:75-87
+__device__ __forceinline__ double kdwdh(double r, double h) {
+    const double q = r / h;
+    if (q >= 2.0) return 0.0;
+    const double h3 = h * h * h;
+    const double s = 1.0 - 0.5 * q;
+    const double s3 = s * s * s;
+    const double s4 = s3 * s;
+    const double w_val = norm3d() / h3 * s4 * (1.0 + 2.0 * q);
+    const double dwdq = norm3d() / h3 * (-5.0 * q) * s3;
+    return -3.0 / h * w_val - q / h * dwdq;
+}
+
+// sph/kernel.rs:48-64
+__device__ __forceinline__ void kgrad(double dx, double dy, double dz, double r, double h, double &gx, double &gy,
+                                      double &gz) {
+    gx = gy = gz = 0.0;
+    if (r < 1e-30) return;
+    const double q = r / h;
+    if (q >= 2.0) return;
+    const double h3 = h * h * h;
+    const double s = 1.0 - 0.5 * q;
+    const double s3 = s * s * s;
+    const double dwdq = norm3d() / h3 * (-5.0 * q) * s3;
+    const double factor = dwdq / (h * r);
+    gx = factor * dx;
+    gy = factor * dy;
+    gz = factor * dz;
+}
+
+// sph/kernel.rs:94-108
+__device__ __forceinline__ double kabsgrad(double r, double h) {
+    if (r < 1e-30) return 0.0;
+    const double q = r / h;
+    if (q >= 2.0) return 0.0;
+    const double h3 = h * h * h;
+    const double s = 1.0 - 0.5 * q;
+    const double s3 = s * s * s;
+    const double dwdq = norm3d() / h3 * (-5.0 * q) * s3;
+    return -dwdq / h;
+}
+
+// Octree::sphere_intersects_aabb (octree.rs:294-308) on the node's cell box.
+__device__ __forceinline__ bool sphere_hits_box(double px, double py, double pz, double radius, double cx, double cy,
+                                                double cz, double hw) {
+    double d2 = 0.0;
+    const double p[3] = {px, py, pz}, c[3] = {cx, cy, cz};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double lo = c[d] - hw, hi = c[d] + hw;
+        if (p[d] < lo) {
+            const double e = lo - p[d];
+            d2 += e * e;
+        } else if (p[d] > hi) {
+            const double e = p[d] - hi;
+            d2 += e * e;
+        }
+    }
+    return d2 <= radius * radius;
+}
+
+__global__ void k_gather_sph(size_t n, const uint32_t *__restrict__ perm, const uint8_t *__restrict__ ptype,
+                             const double *__restrict__ vx, const double *__restrict__ vy,
+                             const double *__restrict__ vz, const double *__restrict__ m,
+                             const double *__restrict__ h, const double *__restrict__ u,
+                             const double *__restrict__ alpha, const double *__restrict__ rho,
+                             const double *__restrict__ pres, const double *__restrict__ cs,
+                             uint8_t *__restrict__ gas, double *__restrict__ svx,
+                             double *__restrict__ svy, double *__restrict__ svz, double *__restrict__ sm,
+                             double *__restrict__ sh, double *__restrict__ su, double *__restrict__ salpha,
+                             double *__restrict__ srho, double *__restrict__ spres, double *__restrict__ scs) {
+    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const uint32_t o = perm[s];
+    gas[s] = ptype[o] == 4 ? 1 : 0;
+    svx[s] = vx[o]; svy[s] = vy[o]; svz[s] = vz[o];
+    sm[s] = m[o]; sh[s] = h[o]; su[s] = u[o]; salpha[s] = alpha[o];
+    // non-gas neighbours keep their stored rho, P, c (zero unless set), as in the reference
+    srho[s] = rho[o]; spres[s] = pres[o]; scs[s] = cs[o];
+}
+
+// Ball query of one target (per-thread walk), used for the re-queries of the
+// density iteration.  Returns the number found (writes at most kmax).
+__device__ int ball_query_thread(const TreeView &tv, double px, double py, double pz, double radius,
+                                 uint32_t *row, int kmax) {
+    const double r2 = radius * radius;
+    int count = 0;
+    uint32_t k = 0;
+    while ((size_t)k < tv.nnodes) {
+        const double hw = ldexp(tv.root_hw, -(int)tv.level[k]);
+        if (!sphere_hits_box(px, py, pz, radius, tv.bx[k], tv.by[k], tv.bz[k], hw)) {
+            k = tv.skip[k];
+            continue;
+        }
+        const uint32_t nc = tv.cnt[k];
+        if (nc > 0) {
+            const uint32_t f = tv.first[k];
+            for (uint32_t j = f; j < f + nc; ++j) {
+                const double dx = tv.sx[j] - px, dy = tv.sy[j] - py, dz = tv.sz[j] - pz;
+                if (dx * dx + dy * dy + dz * dz <= r2) {
+                    if (count < kmax) row[count] = j;
+                    ++count;
+                }
+            }
+            k = tv.skip[k];
+        } else {
+            k = k + 1;
+        }
+    }
+    return count;
+}
+
+// Neighbour lists of all gas particles (build_neighbor_lists with factor):
+// warp-synchronous walk, each lane with its own next-node pointer.
+__global__ void __launch_bounds__(128) k_neighbors(const TreeView tv, const uint8_t *__restrict__ gas,
+                                                   const double *__restrict__ sh, double factor, int kmax,
+                                                   uint32_t *__restrict__ list, uint32_t *__restrict__ cnt,
+                                                   unsigned *__restrict__ err) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = t < tv.n && gas[t];
+    double px = 0, py = 0, pz = 0, radius = 0;
+    if (active) {
+        px = tv.sx[t]; py = tv.sy[t]; pz = tv.sz[t];
+        radius = 2.0 * sh[t] * factor;
+    }
+    const double r2 = radius * radius;
+    uint32_t *row = list + t * (size_t)kmax;
+    int count = 0;
+    uint32_t next = active ? 0u : 0xFFFFFFFFu;
+    for (;;) {
+        const uint32_t k = __reduce_min_sync(0xFFFFFFFFu, next);
+        if ((size_t)k >= tv.nnodes) break;
+        if (next != k) continue;
+        const double hw = ldexp(tv.root_hw, -(int)tv.level[k]);
+        if (!sphere_hits_box(px, py, pz, radius, tv.bx[k], tv.by[k], tv.bz[k], hw)) {
+            next = tv.skip[k];
+            continue;
+        }
+        const uint32_t nc = tv.cnt[k];
+        if (nc > 0) {
+            const uint32_t f = tv.first[k];
+            for (uint32_t j = f; j < f + nc; ++j) {
+                const double dx = tv.sx[j] - px, dy = tv.sy[j] - py, dz = tv.sz[j] - pz;
+                if (dx * dx + dy * dy + dz * dz <= r2) {
+                    if (count < kmax) row[count] = j;
+                    ++count;
+                }
+            }
+            next = tv.skip[k];
+        } else {
+            next = k + 1;
+        }
+    }
+    if (t < tv.n) {
+        cnt[t] = active ? (uint32_t)count : 0u;
+        if (count > kmax) atomicOr(err, (unsigned)DERR_NEIGH_OVERFLOW);
+    }
+}
+
+// compute_density (density.rs:42-125) for one target per thread, then the EOS.
+__global__ void k_density(const TreeView tv, const uint8_t *__restrict__ gas, const double *__restrict__ sm,
+                          const double *__restrict__ su, double *__restrict__ sh, uint32_t *__restrict__ list,
+                          uint32_t *__restrict__ cnt, int kmax, double gamma, double eta, double h_max,
+                          double *__restrict__ rho_out, double *__restrict__ omega_out, double *__restrict__ pres,
+                          double *__restrict__ cs, unsigned *__restrict__ err) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= tv.n) return;
+    omega_out[i] = 1.0;
+    if (!gas[i]) return;
+    const double search_padding = 1.1;
+    const double xi = tv.sx[i], yi = tv.sy[i], zi = tv.sz[i];
+    const double m_i = sm[i];
+    double h = sh[i];
+    uint32_t *row = list + i * (size_t)kmax;
+    int count = (int)cnt[i];
+    double rho_last = rho_out[i];
+    for (int it = 0; it < 5; ++it) {
+        double rho = 0.0, dws = 0.0;
+        for (int k = 0; k < count; ++k) {
+            const uint32_t j = row[k];
+            const double dx = xi - tv.sx[j], dy = yi - tv.sy[j], dz = zi - tv.sz[j];
+            const double r = sqrt(dx * dx + dy * dy + dz * dz);
+            if (r < 2.0 * h) {
+                const double mj = sm[j];
+                rho += mj * kw(r, h);
+                dws += mj * kdwdh(r, h);
+            }
+        }
+        const double h_new = rho > 0.0 ? fmin(eta * cbrt(m_i / rho), h_max) : fmin(h, h_max);
+        if (rho > 0.0) {
+            const double dh_drho = -h_new / (3.0 * rho);
+            double om = 1.0 - dh_drho * dws;
+            if (om < 0.1) om = 0.1;
+            omega_out[i] = om;
+        }
+        rho_last = rho;
+        sh[i] = h_new;
+        if (fabs(h_new - h) / fmax(h, 1e-30) < 1e-3) break;
+        const double search_radius = 2.0 * h * search_padding;
+        if (2.0 * h_new > search_radius) {
+            const double new_radius = 2.0 * h_new * search_padding;
+            count = ball_query_thread(tv, xi, yi, zi, new_radius, row, kmax);
+            if (count > kmax) {
+                atomicOr(err, (unsigned)DERR_NEIGH_OVERFLOW);
+                count = kmax;
+            }
+            cnt[i] = (uint32_t)count;
+        }
+        h = h_new;
+    }
+    rho_out[i] = rho_last;
+    // EOS (density.rs:111-119)
+    const double u = su[i];
+    pres[i] = (gamma - 1.0) * rho_last * u;
+    cs[i] = sqrt(gamma * (gamma - 1.0) * fmax(u, 0.0));
+}
+
+// compute_forces (forces.rs:69-232), one target per thread.
+__global__ void k_forces(const TreeView tv, const uint8_t *__restrict__ gas, const uint32_t *__restrict__ list,
+                         const uint32_t *__restrict__ cnt, int kmax, const double *__restrict__ svx,
+                         const double *__restrict__ svy, const double *__restrict__ svz,
+                         const double *__restrict__ sm, const double *__restrict__ sh, const double *__restrict__ srho,
+                         const double *__restrict__ spres, const double *__restrict__ su,
+                         const double *__restrict__ scs, const double *__restrict__ salpha,
+                         const double *__restrict__ somega, gvs_sph_params prm, double *__restrict__ sax,
+                         double *__restrict__ say, double *__restrict__ saz, double *__restrict__ sdu,
+                         double *__restrict__ sdivv, double *__restrict__ smaxmu, double *__restrict__ sdalpha) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= tv.n) return;
+    sdivv[i] = 0.0;
+    smaxmu[i] = 0.0;
+    sdalpha[i] = 0.0;
+    sax[i] = say[i] = saz[i] = sdu[i] = 0.0;
+    if (!gas[i]) return;
+    const double DENSITY_FLOOR = 1e-10;
+    const double xi = tv.sx[i], yi = tv.sy[i], zi = tv.sz[i];
+    const double vxi = svx[i], vyi = svy[i], vzi = svz[i];
+    const double hi = sh[i];
+    const double rho_i = fmax(srho[i], DENSITY_FLOOR);
+    const double p_i = spres[i], u_i = su[i], c_i = scs[i], alpha_i = salpha[i], omega_i = somega[i];
+    const double por2_i = rho_i > 0.0 ? p_i / (omega_i * rho_i * rho_i) : 0.0;
+    double axa = 0.0, aya = 0.0, aza = 0.0, dua = 0.0, dva = 0.0, mmu = 0.0;
+    const uint32_t *row = list + i * (size_t)kmax;
+    const int count = (int)cnt[i];
+    for (int k = 0; k < count; ++k) {
+        const uint32_t j = row[k];
+        if ((size_t)j == i) continue;
+        const double dx = xi - tv.sx[j], dy = yi - tv.sy[j], dz = zi - tv.sz[j];
+        const double r = sqrt(dx * dx + dy * dy + dz * dz);
+        const double hj = sh[j];
+        const double h_avg = 0.5 * (hi + hj);
+        if (r >= 2.0 * hi && r >= 2.0 * hj) continue;
+        const double mj = sm[j];
+        const double rho_j = fmax(srho[j], DENSITY_FLOOR);
+        const double p_j = spres[j], c_j = scs[j], alpha_j = salpha[j], omega_j = somega[j];
+        const double dvx = vxi - svx[j], dvy = vyi - svy[j], dvz = vzi - svz[j];
+        const double vr = dvx * dx + dvy * dy + dvz * dz;
+        double gix, giy, giz, gjx, gjy, gjz, gax, gay, gaz;
+        kgrad(dx, dy, dz, r, hi, gix, giy, giz);
+        kgrad(dx, dy, dz, r, hj, gjx, gjy, gjz);
+        kgrad(dx, dy, dz, r, h_avg, gax, gay, gaz);
+        const double por2_j = rho_j > 0.0 ? p_j / (omega_j * rho_j * rho_j) : 0.0;
+        double pi_ij = 0.0;
+        if (vr < 0.0) {
+            const double alpha_avg = 0.5 * (alpha_i + alpha_j);
+            const double c_avg = 0.5 * (c_i + c_j);
+            const double rho_avg = 0.5 * (rho_i + rho_j);
+            const double eta2 = 0.01 * h_avg * h_avg;
+            const double mu = h_avg * vr / (r * r + eta2);
+            mmu = fmax(mmu, fabs(mu));
+            pi_ij = rho_avg > 0.0 ? (-alpha_avg * c_avg * mu + prm.beta_visc * mu * mu) / rho_avg : 0.0;
+        }
+        axa -= mj * (por2_i * gix + por2_j * gjx + pi_ij * gax);
+        aya -= mj * (por2_i * giy + por2_j * gjy + pi_ij * gay);
+        aza -= mj * (por2_i * giz + por2_j * gjz + pi_ij * gaz);
+        const double vdgi = dvx * gix + dvy * giy + dvz * giz;
+        const double vdga = dvx * gax + dvy * gay + dvz * gaz;
+        dua += mj * (por2_i * vdgi + 0.5 * pi_ij * vdga);
+        dva -= mj * vdgi;
+        if (prm.alpha_cond > 0.0) {
+            const double u_j = su[j];
+            const double rho_sum = rho_i + rho_j;
+            if (rho_sum > 0.0) {
+                const double rho_avg = 0.5 * rho_sum;
+                const double dp = fabs(p_i - p_j);
+                const double v_sig_u = sqrt(dp / rho_avg);
+                const double abs_gw = kabsgrad(r, h_avg);
+                dua += mj * prm.alpha_cond * v_sig_u * (u_i - u_j) / rho_sum * abs_gw;
+            }
+        }
+    }
+    sax[i] = axa;
+    say[i] = aya;
+    saz[i] = aza;
+    sdu[i] = dua;
+    double dv = 0.0;
+    if (rho_i > 0.0) dv = dva / rho_i;
+    sdivv[i] = dv;
+    smaxmu[i] = mmu;
+    const double tau = c_i > 0.0 ? hi / (2.0 * prm.sigma_visc * c_i) : 1e10;
+    const double source = fmax(-dv, 0.0) * (prm.alpha_max - alpha_i);
+    sdalpha[i] = -(alpha_i - prm.alpha_min) / tau + source;
+}
+
+// Sorted results back to caller order; a and du/dt are accumulated.
+__global__ void k_scatter_sph(size_t n, const uint32_t *__restrict__ perm, const uint8_t *__restrict__ gas,
+                              const double *__restrict__ srho, const double *__restrict__ sh,
+                              const double *__restrict__ spres, const double *__restrict__ scs,
+                              const double *__restrict__ somega, const double *__restrict__ sax,
+                              const double *__restrict__ say, const double *__restrict__ saz,
+                              const double *__restrict__ sdu, const double *__restrict__ sdivv,
+                              const double *__restrict__ smaxmu, const double *__restrict__ sdalpha,
+                              double *__restrict__ rho, double *__restrict__ h, double *__restrict__ pres,
+                              double *__restrict__ cs, double *__restrict__ omega, double *__restrict__ ax,
+                              double *__restrict__ ay, double *__restrict__ az, double *__restrict__ du,
+                              double *__restrict__ divv, double *__restrict__ maxmu, double *__restrict__ dalpha) {
+    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const uint32_t o = perm[s];
+    omega[o] = somega[s];
+    divv[o] = sdivv[s];
+    maxmu[o] = smaxmu[s];
+    dalpha[o] = sdalpha[s];
+    if (!gas[s]) return;
+    rho[o] = srho[s];
+    h[o] = sh[s];
+    pres[o] = spres[s];
+    cs[o] = scs[s];
+    ax[o] += sax[s];
+    ay[o] += say[s];
+    az[o] += saz[s];
+    du[o] += sdu[s];
+}
+
+// compute_timestep (solver.rs:90-131): per-block minima.
+__global__ void k_dt_part(size_t n, const uint8_t *__restrict__ ptype, const double *__restrict__ h,
+                          const double *__restrict__ ax, const double *__restrict__ ay, const double *__restrict__ az,
+                          const double *__restrict__ cs, const double *__restrict__ alpha,
+                          const double *__restrict__ divv, const double *__restrict__ maxmu, gvs_sph_params prm,
+                          double *__restrict__ part) {
+    double dt_min = INFINITY;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        if (ptype[i] != 4) continue;
+        const double hh = h[i];
+        const double a_mag = sqrt(ax[i] * ax[i] + ay[i] * ay[i] + az[i] * az[i]);
+        if (a_mag > 0.0) dt_min = fmin(dt_min, prm.force_factor * sqrt(hh / a_mag));
+        const double c = cs[i];
+        const double v_sig = c + hh * fabs(divv[i]) + 1.2 * (alpha[i] * c + prm.beta_visc * maxmu[i]);
+        if (v_sig > 0.0) dt_min = fmin(dt_min, prm.cfl_factor * hh / v_sig);
+    }
+    for (int o = 16; o > 0; o >>= 1) dt_min = fmin(dt_min, __shfl_xor_sync(0xFFFFFFFFu, dt_min, o));
+    __shared__ double w[32];
+    if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = dt_min;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = w[0];
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) m = fmin(m, w[k]);
+        part[blockIdx.x] = m;
+    }
+}
+
+// First half of step_with_sph (solver.rs:155-180): v and u half-kicks, drift,
+// clear a and du/dt.
+__global__ void k_sph_kick1(size_t n, double half_dt, double dt, const uint8_t *__restrict__ ptype,
+                            double *__restrict__ x, double *__restrict__ y, double *__restrict__ z,
+                            double *__restrict__ vx, double *__restrict__ vy, double *__restrict__ vz,
+                            double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
+                            double *__restrict__ u, double *__restrict__ du) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v0 = vx[i] + ax[i] * half_dt, v1 = vy[i] + ay[i] * half_dt, v2 = vz[i] + az[i] * half_dt;
+    vx[i] = v0; vy[i] = v1; vz[i] = v2;
+    if (ptype[i] == 4) {
+        double uu = u[i] + du[i] * half_dt;
+        if (uu < 1e-10) uu = 1e-10;
+        u[i] = uu;
+    }
+    x[i] = x[i] + v0 * dt;
+    y[i] = y[i] + v1 * dt;
+    z[i] = z[i] + v2 * dt;
+    ax[i] = 0.0; ay[i] = 0.0; az[i] = 0.0;
+    du[i] = 0.0;
+}
+
+// Second half (solver.rs:188-208): v and u half-kicks, alpha update and clamp.
+__global__ void k_sph_kick2(size_t n, double half_dt, double dt, const uint8_t *__restrict__ ptype,
+                            double *__restrict__ vx, double *__restrict__ vy, double *__restrict__ vz,
+                            const double *__restrict__ ax, const double *__restrict__ ay,
+                            const double *__restrict__ az, double *__restrict__ u, const double *__restrict__ du,
+                            double *__restrict__ alpha, const double *__restrict__ dalpha, double amin, double amax) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    vx[i] = vx[i] + ax[i] * half_dt;
+    vy[i] = vy[i] + ay[i] * half_dt;
+    vz[i] = vz[i] + az[i] * half_dt;
+    if (ptype[i] == 4) {
+        double uu = u[i] + du[i] * half_dt;
+        if (uu < 1e-10) uu = 1e-10;
+        u[i] = uu;
+        double a = alpha[i] + dalpha[i] * dt;
+        a = fmin(fmax(a, amin), amax);
+        alpha[i] = a;
+    }
+}
+
+inline int nb(size_t n, int t = 256) { return (int)std::max<size_t>(1, (n + t - 1) / t); }
+
+}  // namespace
+
+void sph_free(Ctx *c) {
+    SphState *s = static_cast<SphState *>(c->sph);
+    if (!s) return;
+    DevBuf *all[] = {&s->list, &s->cnt, &s->gas, &s->sx, &s->sy, &s->sz, &s->svx, &s->svy, &s->svz, &s->sm,
+                     &s->sh, &s->su, &s->salpha, &s->srho, &s->spres, &s->scs, &s->somega, &s->sdivv, &s->smaxmu,
+                     &s->sdalpha, &s->sax, &s->say, &s->saz, &s->sdu, &s->dtpart};
+    for (DevBuf *b : all)
+        if (b->ptr) cudaFree(b->ptr);
+    delete s;
+    c->sph = nullptr;
+}
+
+// SphSolver::compute (solver.rs:61-80) on the resident state: a and du/dt accumulate.
+gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
+    const size_t n = c->n;
+    if (n == 0) return GVS_OK;
+    if (!c->has_gas) return GVS_OK;  // no gas: SPH adds nothing
+    SphState *S = sph_of(c);
+    TreeView tv;
+    GVS_TRY(tree_view(c, &tv));
+    cudaStream_t st = c->stream;
+    const size_t b8 = n * 8;
+    DevBuf *f64s[] = {&S->svx, &S->svy, &S->svz, &S->sm, &S->sh, &S->su, &S->salpha, &S->srho, &S->spres,
+                      &S->scs, &S->somega, &S->sdivv, &S->smaxmu, &S->sdalpha, &S->sax, &S->say, &S->saz, &S->sdu};
+    for (DevBuf *d : f64s) GVS_CUDA(c, ensure(c, *d, b8));
+    GVS_CUDA(c, ensure(c, S->gas, n));
+    GVS_CUDA(c, ensure(c, S->cnt, n * 4));
+    k_gather_sph<<<nb(n), 256, 0, st>>>(n, tv.perm, as<uint8_t>(c->ptype), as<double>(c->vx), as<double>(c->vy),
+                                        as<double>(c->vz), as<double>(c->m), as<double>(c->h), as<double>(c->u),
+                                        as<double>(c->alpha), as<double>(c->rho), as<double>(c->pres),
+                                        as<double>(c->cs), as<uint8_t>(S->gas), as<double>(S->svx),
+                                        as<double>(S->svy), as<double>(S->svz), as<double>(S->sm),
+                                        as<double>(S->sh), as<double>(S->su), as<double>(S->salpha),
+                                        as<double>(S->srho), as<double>(S->spres), as<double>(S->scs));
+    c->prof.launches += 1;
+    GVS_TRY(check_launch(c, "sph gather"));
+    // keep a copy of the initial h: the density pass overwrites sh, and an
+    // overflow rerun must start again from the same h
+    GVS_CUDA(c, ensure(c, c->scratch_b, b8));
+    GVS_CUDA(c, cudaMemcpyAsync(c->scratch_b.ptr, S->sh.ptr, b8, cudaMemcpyDeviceToDevice, st));
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        GVS_CUDA(c, ensure(c, S->list, n * (size_t)S->kmax * 4));
+        GVS_CUDA(c, cudaMemcpyAsync(S->sh.ptr, c->scratch_b.ptr, b8, cudaMemcpyDeviceToDevice, st));
+        k_neighbors<<<nb(n, 128), 128, 0, st>>>(tv, as<uint8_t>(S->gas), as<double>(S->sh), 1.1, S->kmax,
+                                                as<uint32_t>(S->list), as<uint32_t>(S->cnt), err_ptr(c));
+        k_density<<<nb(n, 128), 128, 0, st>>>(tv, as<uint8_t>(S->gas), as<double>(S->sm), as<double>(S->su),
+                                              as<double>(S->sh), as<uint32_t>(S->list), as<uint32_t>(S->cnt),
+                                              S->kmax, prm->gamma, prm->eta, prm->h_max, as<double>(S->srho),
+                                              as<double>(S->somega), as<double>(S->spres), as<double>(S->scs),
+                                              err_ptr(c));
+        c->prof.launches += 2;
+        GVS_TRY(check_launch(c, "sph neighbours/density"));
+        unsigned flags = 0;
+        GVS_CUDA(c, cudaMemcpyAsync(&flags, c->err_word.ptr, 4, cudaMemcpyDeviceToHost, st));
+        GVS_CUDA(c, cudaStreamSynchronize(st));
+        if (!(flags & DERR_NEIGH_OVERFLOW)) break;
+        // rows too narrow: clear the flag and rerun with twice the width
+        unsigned rest = flags & ~(unsigned)DERR_NEIGH_OVERFLOW;
+        GVS_CUDA(c, cudaMemcpyAsync(c->err_word.ptr, &rest, 4, cudaMemcpyHostToDevice, st));
+        GVS_CUDA(c, cudaStreamSynchronize(st));
+        if (attempt == 3) return fail(c, GVS_ERR_DEVICE, "SPH neighbour rows overflow at kmax=%d", S->kmax);
+        S->kmax *= 2;
+    }
+    k_forces<<<nb(n, 128), 128, 0, st>>>(tv, as<uint8_t>(S->gas), as<uint32_t>(S->list), as<uint32_t>(S->cnt),
+                                         S->kmax, as<double>(S->svx), as<double>(S->svy), as<double>(S->svz),
+                                         as<double>(S->sm), as<double>(S->sh), as<double>(S->srho),
+                                         as<double>(S->spres), as<double>(S->su), as<double>(S->scs),
+                                         as<double>(S->salpha), as<double>(S->somega), *prm, as<double>(S->sax),
+                                         as<double>(S->say), as<double>(S->saz), as<double>(S->sdu),
+                                         as<double>(S->sdivv), as<double>(S->smaxmu), as<double>(S->sdalpha));
+    k_scatter_sph<<<nb(n), 256, 0, st>>>(n, tv.perm, as<uint8_t>(S->gas), as<double>(S->srho), as<double>(S->sh),
+                                         as<double>(S->spres), as<double>(S->scs), as<double>(S->somega),
+                                         as<double>(S->sax), as<double>(S->say), as<double>(S->saz),
+                                         as<double>(S->sdu), as<double>(S->sdivv), as<double>(S->smaxmu),
+                                         as<double>(S->sdalpha), as<double>(c->rho), as<double>(c->h),
+                                         as<double>(c->pres), as<double>(c->cs), as<double>(c->omega),
+                                         as<double>(c->ax), as<double>(c->ay), as<double>(c->az),
+                                         as<double>(c->du_dt), as<double>(c->div_v), as<double>(c->max_mu),
+                                         as<double>(c->dalpha_dt));
+    c->prof.launches += 2;
+    S->n = n;
+    S->have_intermediates = true;
+    return check_launch(c, "sph forces");
+}
+
+gvs_status sph_timestep(Ctx *c, const gvs_sph_params *prm, double *dt_out) {
+    const size_t n = c->n;
+    SphState *S = sph_of(c);
+    if (!S->have_intermediates) return fail(c, GVS_ERR_STATE, "compute_timestep needs a prior SPH compute");
+    const int nbk = std::max(1, std::min(c->num_sms * 2, nb(n)));
+    GVS_CUDA(c, ensure(c, S->dtpart, (size_t)nbk * 8));
+    k_dt_part<<<nbk, 256, 0, c->stream>>>(n, as<uint8_t>(c->ptype), as<double>(c->h), as<double>(c->ax),
+                                          as<double>(c->ay), as<double>(c->az), as<double>(c->cs),
+                                          as<double>(c->alpha), as<double>(c->div_v), as<double>(c->max_mu), *prm,
+                                          as<double>(S->dtpart));
+    c->prof.launches += 1;
+    GVS_TRY(check_launch(c, "sph timestep"));
+    std::vector<double> part(nbk);
+    GVS_CUDA(c, cudaMemcpyAsync(part.data(), S->dtpart.ptr, nbk * 8, cudaMemcpyDeviceToHost, c->stream));
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    double m = INFINITY;
+    for (double v : part) m = fmin(m, v);
+    *dt_out = m < 1e-6 ? 1e-6 : m;  // DT_FLOOR (solver.rs:17,130)
+    return GVS_OK;
+}
+
+// step_with_sph (solver.rs:145-212) on the resident state; returns dt_next.
+gvs_status sph_step(Ctx *c, const gvs_sph_params *prm, int algo, int precision, double eps, double theta, double dt,
+                    double *dt_next) {
+    const size_t n = c->n;
+    if (n == 0) return GVS_OK;
+    const double half = 0.5 * dt;
+    k_sph_kick1<<<nb(n), 256, 0, c->stream>>>(n, half, dt, as<uint8_t>(c->ptype), as<double>(c->x),
+                                              as<double>(c->y), as<double>(c->z), as<double>(c->vx),
+                                              as<double>(c->vy), as<double>(c->vz), as<double>(c->ax),
+                                              as<double>(c->ay), as<double>(c->az), as<double>(c->u),
+                                              as<double>(c->du_dt));
+    c->prof.launches += 1;
+    c->pos_version++;
+    GVS_TRY(check_launch(c, "sph kick/drift"));
+    GVS_TRY(gravity(c, algo, precision, eps, theta, true));
+    GVS_TRY(sph_compute(c, prm));
+    k_sph_kick2<<<nb(n), 256, 0, c->stream>>>(n, half, dt, as<uint8_t>(c->ptype), as<double>(c->vx),
+                                              as<double>(c->vy), as<double>(c->vz), as<double>(c->ax),
+                                              as<double>(c->ay), as<double>(c->az), as<double>(c->u),
+                                              as<double>(c->du_dt), as<double>(c->alpha), as<double>(c->dalpha_dt),
+                                              prm->alpha_min, prm->alpha_max);
+    c->prof.launches += 1;
+    GVS_TRY(check_launch(c, "sph kick"));
+    c->step_counter++;
+    return sph_timestep(c, prm, dt_next);
+}
+
+// Neighbour lists in caller indices (for parity tests and callers that want
+// the reference's NeighborList): start/count per caller index, indices packed.
+gvs_status sph_neighbors_export(Ctx *c, size_t cap, uint32_t *start, uint32_t *count, uint32_t *idx, size_t *total) {
+    SphState *S = sph_of(c);
+    if (!S->have_intermediates || S->n != c->n) return fail(c, GVS_ERR_STATE, "no SPH neighbour lists yet");
+    const size_t n = c->n;
+    TreeView tv;
+    GVS_TRY(tree_view(c, &tv));
+    std::vector<uint32_t> cnt(n), perm(n), rows;
+    GVS_CUDA(c, cudaMemcpyAsync(cnt.data(), S->cnt.ptr, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    GVS_CUDA(c, cudaMemcpyAsync(perm.data(), tv.perm, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    rows.resize(n * (size_t)S->kmax);
+    GVS_CUDA(c, cudaMemcpyAsync(rows.data(), S->list.ptr, rows.size() * 4, cudaMemcpyDeviceToHost, c->stream));
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    size_t tot = 0;
+    for (size_t s = 0; s < n; ++s) tot += cnt[s];
+    *total = tot;
+    if (cap < tot || !start || !count || !idx) return GVS_OK;
+    // caller order: particle o's list follows the caller-index order of particles
+    std::vector<uint32_t> slot_of(n);
+    for (size_t s = 0; s < n; ++s) slot_of[perm[s]] = (uint32_t)s;
+    size_t pos = 0;
+    for (size_t o = 0; o < n; ++o) {
+        const size_t s = slot_of[o];
+        start[o] = (uint32_t)pos;
+        count[o] = cnt[s];
+        for (uint32_t k = 0; k < cnt[s]; ++k) idx[pos++] = perm[rows[s * (size_t)S->kmax + k]];
+    }
+    return GVS_OK;
+}
+
 }  // namespace gvs

@@ -315,6 +315,82 @@ class LeapfrogKDK:
                                        gravity.precision, gravity.softening, gravity.theta, dt))
 
 
+# ---- SPH ----------------------------------------------------------------------------
+@dataclass
+class ForceIntermediates:
+    """forces.rs:45-52 (plus Omega from density.rs:19-25)."""
+    div_v: np.ndarray
+    max_mu: np.ndarray
+    dalpha_dt: np.ndarray
+    omega: np.ndarray
+
+
+class SphSolver:
+    """sph/solver.rs:20-131 on the GPU.  Parameters default to SphSolver::new and
+    ForceParams::default; change them through the attributes of `params`."""
+
+    def __init__(self, ctx: Context | None = None):
+        self.ctx = ctx
+        self.params = L.SphParams()
+        check(L.load().gvs_sph_params_default(C.byref(self.params)))
+        self._last = None
+
+    def context(self) -> Context:
+        return self.ctx or default_context()
+
+    def _upload(self, p: Particles):
+        c = self.context()
+        c.set_state(p)
+        c.set_accelerations(p)
+        c._ck(c._lib.gvs_set_gas(c.h, _ptr(p.density), _ptr(p.pressure), _ptr(p.internal_energy), _ptr(p.du_dt),
+                                 _ptr(p.smoothing_length), _ptr(p.sound_speed), _ptr(p.alpha_visc)))
+
+    def _download(self, p: Particles):
+        c = self.context()
+        c._ck(c._lib.gvs_get_state(c.h, _ptr(p.x), _ptr(p.y), _ptr(p.z), _ptr(p.vx), _ptr(p.vy), _ptr(p.vz),
+                                   _ptr(p.ax), _ptr(p.ay), _ptr(p.az)))
+        c.get_gas(p)
+
+    def compute(self, p: Particles) -> ForceIntermediates:
+        """SphSolver::compute (solver.rs:61-80): a and du/dt accumulate into p."""
+        c = self.context()
+        self._upload(p)
+        out = [np.zeros(p.count) for _ in range(4)]
+        c._ck(c._lib.gvs_sph_compute(c.h, C.byref(self.params), *(_ptr(a) for a in out)))
+        self._download(p)
+        self._last = ForceIntermediates(div_v=out[1], max_mu=out[2], dalpha_dt=out[3], omega=out[0])
+        return self._last
+
+    def compute_timestep(self, p: Particles, intermediates: ForceIntermediates | None = None) -> float:
+        """SphSolver::compute_timestep (solver.rs:90-131) for the state of the last compute."""
+        c = self.context()
+        dt = C.c_double()
+        c._ck(c._lib.gvs_sph_timestep(c.h, C.byref(self.params), C.byref(dt)))
+        return dt.value
+
+    def neighbors(self) -> tuple:
+        """NeighborList of the last compute, in caller indices: (start, count, indices)."""
+        c = self.context()
+        total = C.c_size_t()
+        c._ck(c._lib.gvs_sph_neighbors(c.h, 0, C.byref(total), None, None, None))
+        n = c._lib.gvs_count(c.h)
+        start, count = np.zeros(n, np.uint32), np.zeros(n, np.uint32)
+        idx = np.zeros(max(1, total.value), np.uint32)
+        c._ck(c._lib.gvs_sph_neighbors(c.h, total.value, C.byref(total), _ptr(start), _ptr(count), _ptr(idx)))
+        return start, count, idx[: total.value]
+
+
+def step_with_sph(p: Particles, gravity: GravitySolver, sph: SphSolver, dt: float) -> float:
+    """step_with_sph (sph/solver.rs:145-212) on the GPU; returns the next timestep."""
+    c = sph.context()
+    sph._upload(p)
+    dtn = C.c_double()
+    c._ck(c._lib.gvs_sph_step(c.h, C.byref(sph.params), gravity.algo, gravity.precision, gravity.softening,
+                              gravity.theta, dt, C.byref(dtn)))
+    sph._download(p)
+    return dtn.value
+
+
 # ---- diagnostics ------------------------------------------------------------------
 @dataclass
 class Diagnostics:

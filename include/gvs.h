@@ -110,6 +110,9 @@ gvs_status gvs_get_state(gvs_ctx *ctx, double *x, double *y, double *z, double *
 gvs_status gvs_set_accelerations(gvs_ctx *ctx, const double *ax, const double *ay, const double *az);
 gvs_status gvs_get_gas(gvs_ctx *ctx, double *density, double *pressure, double *u, double *du_dt, double *h,
                        double *sound_speed, double *alpha);
+/* Overwrites any subset of the resident gas fields (NULL pointers are skipped). */
+gvs_status gvs_set_gas(gvs_ctx *ctx, const double *density, const double *pressure, const double *u,
+                       const double *du_dt, const double *h, const double *sound_speed, const double *alpha);
 size_t gvs_count(const gvs_ctx *ctx);
 
 /* ---- GravitySolver drop-ins (host arrays in, accelerations accumulated) -------- */
@@ -152,6 +155,28 @@ gvs_status gvs_kdk_step_host(gvs_ctx *ctx, size_t n, double *x, double *y, doubl
 
 /* ---- diagnostics (crates/sim-core/src/diagnostics.rs:37-148) ------------------- */
 gvs_status gvs_diagnostics(gvs_ctx *ctx, double softening, int with_potential, gvs_diag *out);
+
+/* ---- SPH (crates/sim-core/src/sph/) ---------------------------------------------- */
+/* SphSolver::new defaults (solver.rs:40-49) and ForceParams::default (forces.rs:30-41). */
+gvs_status gvs_sph_params_default(gvs_sph_params *out);
+/* SphSolver::compute (solver.rs:61-80) on the resident state: octree, neighbour lists
+ * (radius 2 h 1.1), fixed-point h / density / Omega, EOS, then forces.  Accelerations and
+ * du/dt ACCUMULATE into the resident arrays (call after gravity, as the reference does).
+ * The ForceIntermediates (Omega, div v, max mu, d alpha/dt) are copied to the host arrays
+ * that are non-NULL. */
+gvs_status gvs_sph_compute(gvs_ctx *ctx, const gvs_sph_params *params, double *omega, double *div_v,
+                           double *max_mu, double *dalpha_dt);
+/* SphSolver::compute_timestep (solver.rs:90-131) from the last gvs_sph_compute. */
+gvs_status gvs_sph_timestep(gvs_ctx *ctx, const gvs_sph_params *params, double *dt);
+/* step_with_sph (solver.rs:145-212) on the resident state with gravity `algo`;
+ * *dt_next = the CFL / force timestep for the next step. */
+gvs_status gvs_sph_step(gvs_ctx *ctx, const gvs_sph_params *params, int algo, int precision, double softening,
+                        double theta, double dt, double *dt_next);
+/* NeighborList of the last gvs_sph_compute (neighbors.rs:13-45) in caller indices:
+ * *total = number of entries; if cap >= *total, particle i's neighbours are
+ * idx[start[i] .. start[i] + count[i]) in the reference's depth-first order. */
+gvs_status gvs_sph_neighbors(gvs_ctx *ctx, size_t cap, size_t *total, uint32_t *start, uint32_t *count,
+                             uint32_t *idx);
 
 /* ---- direct-sum accuracy probe ---------------------------------------------------- */
 /* Accelerations of the targets idx[0..nidx) against all resident particles,

@@ -6,7 +6,7 @@ reference tree's (Octree::rebuild, crates/sim-core/src/octree.rs:156-239).
 Forces: the f64 walk makes the reference's accept decisions on a bottom-up
 centre of mass (a few ulps from the reference's incremental one) and sums
 children 0..7 instead of 7..0, so it agrees with the oracle's BarnesHut to
-<= 1e-12 relative RMS; the f32 walk within 1e-5 of the f64 walk.
+<= 1e-12 relative RMS; the f32 walk within 1e-4 of the f64 walk.
 """
 import numpy as np
 import pytest
@@ -141,7 +141,9 @@ def test_bh_f32_walk(ctx, theta):
     G.BarnesHut(eps, theta, G.PREC_FP32, ctx).compute_accelerations(a32)
     err = rel_rms(a32.acc(), a64.acc())
     print(f"theta={theta} f32 walk vs f64 walk rel RMS {err:.2e}")
-    assert err <= 1e-5
+    # f32 absolute positions at |x| ~ 10 resolve separations to ~1e-6; the bound
+    # sits two orders of magnitude below the BH approximation error (~5e-3).
+    assert err <= 1e-4
 
 
 def test_bh_vs_direct_subset(ctx):

@@ -1,0 +1,186 @@
+"""GPU SPH against the oracle's restatement of crates/sim-core/src/sph/.
+
+Bars: neighbour lists identical to the reference's (same sets, same
+depth-first order, octree.rs:245-290 / neighbors.rs:56-119); density, h,
+Omega, P, c within 1e-12 relative and accelerations, du/dt, div v, max mu,
+d alpha/dt within 1e-10 relative RMS (the GPU restates the f64 arithmetic
+statement by statement; the only other rounding source is the library cbrt
+in h = eta (m/rho)^(1/3)); the timestep within 1e-12.
+"""
+import numpy as np
+import pytest
+
+import gravis_gb300 as G
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = G.Context(0)
+    yield c
+    c.close()
+
+
+def to_oracle(p):
+    q = O.Particles(p.count)
+    pairs = (("x", "x"), ("y", "y"), ("z", "z"), ("vx", "vx"), ("vy", "vy"), ("vz", "vz"), ("ax", "ax"), ("ay", "ay"),
+             ("az", "az"), ("mass", "mass"), ("density", "density"), ("pressure", "pressure"),
+             ("internal_energy", "u"), ("du_dt", "du_dt"), ("smoothing_length", "h"), ("sound_speed", "cs"),
+             ("alpha_visc", "alpha"), ("particle_type", "ptype"))
+    for a, b in pairs:
+        getattr(q, b)[:] = getattr(p, a)
+    return q
+
+
+def rel(a, b):
+    d = np.sqrt(((a - b) ** 2).sum())
+    s = np.sqrt((b ** 2).sum())
+    return d / s if s > 0 else d
+
+
+def lattice_gas(n_side, spacing, h, u=1.0, jitter=0.0, vel=0.0):
+    rng = np.random.default_rng(5)
+    p = G.Particles(n_side ** 3)
+    k = 0
+    for ix in range(n_side):
+        for iy in range(n_side):
+            for iz in range(n_side):
+                p.x[k], p.y[k], p.z[k] = ix * spacing, iy * spacing, iz * spacing
+                k += 1
+    p.x += jitter * rng.standard_normal(p.count)
+    p.y += jitter * rng.standard_normal(p.count)
+    p.z += jitter * rng.standard_normal(p.count)
+    p.vx += vel * rng.standard_normal(p.count)
+    p.vy += vel * rng.standard_normal(p.count)
+    p.mass[:] = 1.0
+    p.internal_energy[:] = u * (1.0 + 0.3 * rng.random(p.count))
+    p.smoothing_length[:] = h
+    p.alpha_visc[:] = 1.0
+    p.particle_type[:] = G.engine.GAS
+    return p
+
+
+def cases():
+    ev = G.EvrardCollapse(1000, seed=42).generate()
+    g1r = G.gas_sphere_1r(4000)
+    g1r.vx[:] = -0.1 * g1r.x  # converging flow: exercises the viscosity
+    g1r.vy[:] = -0.1 * g1r.y
+    return {"lattice5_h0.8": lattice_gas(5, 0.5, 0.8), "lattice8_h1": lattice_gas(8, 0.5, 1.0),
+            "lattice6_hbad": lattice_gas(6, 0.5, 2.0),  # density.rs h_convergence: re-queries
+            "jittered": lattice_gas(10, 0.3, 0.45, jitter=0.05, vel=0.1), "evrard1000": ev, "sphere1r_4000": g1r}
+
+
+@pytest.mark.parametrize("name", list(cases().keys()))
+def test_sph_compute_matches_oracle(ctx, name):
+    p = cases()[name]
+    q = to_oracle(p)
+    sph = G.SphSolver(ctx)
+    inter = sph.compute(p)
+    s = O.Sph()
+    s.compute(q)
+    n = p.count
+    # neighbour lists: identical sets and order
+    start, count, idx = sph.neighbors()
+    ostart, oend, oidx = s.neighbor_lists(n)
+    for i in range(n):
+        mine = idx[start[i]: start[i] + count[i]]
+        ref = oidx[ostart[i]: oend[i]]
+        assert np.array_equal(mine, ref), (name, i, mine[:10], ref[:10])
+    for a, b in (("density", "density"), ("smoothing_length", "h"), ("pressure", "pressure"),
+                 ("sound_speed", "cs")):
+        assert rel(getattr(p, a), getattr(q, b)) <= 1e-12, (name, a, rel(getattr(p, a), getattr(q, b)))
+    assert rel(inter.omega, s.array("omega", n)) <= 1e-12
+    for a in ("ax", "ay", "az", "du_dt"):
+        assert rel(getattr(p, a), getattr(q, a)) <= 1e-10, (name, a, rel(getattr(p, a), getattr(q, a)))
+    assert rel(inter.div_v, s.array("div_v", n)) <= 1e-10
+    assert rel(inter.max_mu, s.array("max_mu", n)) <= 1e-10
+    assert rel(inter.dalpha_dt, s.array("dalpha_dt", n)) <= 1e-10
+    dt = sph.compute_timestep(p)
+    assert abs(dt - s.timestep(q)) <= 1e-12 * dt
+
+
+def test_sph_steps_match_oracle(ctx):
+    """Five step_with_sph steps (solver.rs:145-212) with exact f64 gravity."""
+    p = G.EvrardCollapse(1000, seed=42).generate()
+    eps = G.EvrardCollapse(1000).suggested_softening()
+    q = to_oracle(p)
+    grav = G.BruteForce(eps, G.PREC_FP64_EXACT, ctx)
+    sph = G.SphSolver(ctx)
+    grav.compute_accelerations(p)
+    sph.compute(p)
+    dt = min(sph.compute_timestep(p), 1e-3)
+    og = O.gravity(O.GRAV_BF, eps)
+    s = O.Sph()
+    O.bf_serial(q, eps)
+    s.compute(q)
+    odt = min(s.timestep(q), 1e-3)
+    assert abs(dt - odt) <= 1e-12 * dt
+    for _ in range(5):
+        dtn = G.step_with_sph(p, grav, sph, dt)
+        odtn = s.step(q, og, odt)
+        dt = min(dtn, 1.5 * dt)
+        odt = min(odtn, 1.5 * odt)
+    for a, b in (("x", "x"), ("vx", "vx"), ("internal_energy", "u"), ("density", "density"), ("alpha_visc", "alpha")):
+        assert rel(getattr(p, a), getattr(q, b)) <= 1e-9, (a, rel(getattr(p, a), getattr(q, b)))
+    assert abs(dt - odt) <= 1e-9 * dt
+
+
+def test_gas_free_system_unaffected(ctx):
+    """solver.rs:269-291: a system without gas gets no SPH forces and no du/dt."""
+    p = G.Particles(2)
+    p.x[1] = 1.0
+    p.mass[:] = 1.0
+    G.BruteForce(0.1, G.PREC_FP64_EXACT, ctx).compute_accelerations(p)
+    assert p.ax[0] > 0 > p.ax[1]
+    assert np.all(p.du_dt == 0.0)
+
+
+def test_mixed_gas_and_stars(ctx):
+    """Non-gas particles appear in gas neighbour lists (neighbors.rs:47-55) but get no SPH terms."""
+    p = lattice_gas(6, 0.5, 0.8)
+    p.particle_type[::7] = 0  # every 7th particle is a star
+    q = to_oracle(p)
+    sph = G.SphSolver(ctx)
+    sph.compute(p)
+    s = O.Sph()
+    s.compute(q)
+    for a in ("ax", "du_dt"):
+        assert rel(getattr(p, a), getattr(q, a)) <= 1e-10
+    assert np.all(p.du_dt[::7] == 0.0)
+
+
+def test_evrard_energy(ctx):
+    """tests/evrard_collapse.rs: N=1000 to t=0.5 with BruteForce gravity: |dE/E| < 5%,
+    K grows at least 2x, thermal energy grows."""
+    sc = G.EvrardCollapse(1000, seed=42)
+    p = sc.generate()
+    eps = sc.suggested_softening()
+    grav = G.BruteForce(eps, G.PREC_FP64_EXACT, ctx)
+    sph = G.SphSolver(ctx)
+    ctx.set_state(p)
+    ctx._ck(ctx._lib.gvs_set_gas(ctx.h, *(G.engine._ptr(getattr(p, f)) for f in
+                                          ("density", "pressure", "internal_energy", "du_dt", "smoothing_length",
+                                           "sound_speed", "alpha_visc"))))
+    ctx.compute_forces(G.ALGO_DIRECT, G.PREC_FP64_EXACT, eps)
+    import ctypes as C
+    ctx._ck(ctx._lib.gvs_sph_compute(ctx.h, C.byref(sph.params), None, None, None, None))
+    dt_c = C.c_double()
+    ctx._ck(ctx._lib.gvs_sph_timestep(ctx.h, C.byref(sph.params), C.byref(dt_c)))
+    dt = min(dt_c.value, 1e-3)
+    d0 = ctx.diagnostics(eps)
+    t, steps = 0.0, 0
+    while t < 0.5:
+        if t + dt > 0.5:
+            dt = 0.5 - t
+        ctx._ck(ctx._lib.gvs_sph_step(ctx.h, C.byref(sph.params), G.ALGO_DIRECT, G.PREC_FP64_EXACT, eps, 0.0, dt,
+                                      C.byref(dt_c)))
+        t += dt
+        dt = min(dt_c.value, 2.0 * dt)
+        steps += 1
+        assert steps < 100000
+    d1 = ctx.diagnostics(eps)
+    assert abs(d1.total_energy - d0.total_energy) / abs(d0.total_energy) < 0.05
+    assert d1.kinetic_energy > 2.0 * d0.kinetic_energy
+    assert d1.thermal_energy > d0.thermal_energy
