@@ -75,6 +75,7 @@ SIGNATURES = {
     "gvs_kdk_steps": (_ST, [_P, _i, _i, _d, _d, _d, _ll]),
     "gvs_kdk_step_host": (_ST, [_P, _sz] + [_P] * 10 + [_i, _i, _d, _d, _d]),
     "gvs_diagnostics": (_ST, [_P, _d, _i, C.POINTER(Diag)]),
+    "gvs_diagnostics_noalloc": (_ST, [_i, _P, _sz] + [_P] * 9 + [_d, _i, C.POINTER(Diag)]),
     "gvs_direct_subset": (_ST, [_P, _i, _d, _P, _sz, _P, _P, _P]),
     "gvs_ic_plummer": (_ST, [_sz, _u64, _d, _d] + [_P] * 7),
     "gvs_ic_two_body": (_ST, [_d, _d, _d] + [_P] * 7),

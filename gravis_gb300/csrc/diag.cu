@@ -136,3 +136,113 @@ gvs_status diagnostics(Ctx *c, double eps, int with_potential, gvs_diag *out) {
 }
 
 }  // namespace gvs
+
+// ---------------------------------------------------------------------------
+// Diagnostics without any allocation (gvs_diagnostics_noalloc).
+//
+// Some callers cannot allocate device memory: a host that owns every device
+// byte through its own allocator (a game or visualisation engine, an ML
+// framework's caching allocator, a Rust host with an arena), code that runs
+// while a CUDA graph is being captured (cudaMalloc is not allowed during
+// capture), or a real-time loop where an allocation's implicit device
+// synchronisation is not acceptable.  For them the reductions below use a
+// fixed scratch array that lives in the library image: a file-scope
+// __device__ array that every GPU which loads the library holds until the
+// process exits.  The caller passes device pointers for the inputs; nothing
+// is allocated, freed or resized, on the device or in the library.
+// ---------------------------------------------------------------------------
+namespace gvs {
+namespace {
+
+constexpr size_t NOALLOC_MAX_N = (size_t)1 << 22;    // largest particle count accepted
+constexpr int NOALLOC_MAX_SUM_BLOCKS = 1024;          // O(N) reduction blocks
+constexpr size_t NOALLOC_SCRATCH_DOUBLES =
+    (size_t)NOALLOC_MAX_SUM_BLOCKS * NQ + NOALLOC_MAX_N / RNT + NQ + 1;  // about 270 KB
+
+// Shared by every call on a device; holds the last call's partial sums.
+static __device__ __align__(256) double g_diag_scratch[NOALLOC_SCRATCH_DOUBLES];
+
+// Device address of g_diag_scratch per device, looked up once per device.
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static double *g_diag_scratch_ptr[NOALLOC_MAX_DEVICES] = {nullptr};
+static int g_diag_sms[NOALLOC_MAX_DEVICES] = {0};
+
+// Adds the partial sums in the same order as gvs_diagnostics does on the host
+// (blocks in order, then potential blocks in order), so both agree bit for bit.
+__global__ void k_sums_final(const double *__restrict__ part, int nb, int npb, double *__restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int k = 0; k < NQ; ++k) {
+        double q = 0.0;
+        for (int b = 0; b < nb; ++b) q += part[(size_t)b * NQ + k];
+        out[k] = q;
+    }
+    double pe = 0.0;
+    for (int b = 0; b < npb; ++b) pe += part[(size_t)nb * NQ + b];
+    out[NQ] = pe;
+}
+
+}  // namespace
+}  // namespace gvs
+
+extern "C" gvs_status gvs_diagnostics_noalloc(int device, void *stream, size_t n, const double *x, const double *y,
+                                              const double *z, const double *vx, const double *vy, const double *vz,
+                                              const double *mass, const uint8_t *ptype, const double *u,
+                                              double softening, int with_potential, gvs_diag *out) {
+    using namespace gvs;
+    if (!out || !x || !y || !z || !vx || !vy || !vz || !mass || (ptype && !u))
+        return fail(nullptr, GVS_ERR_INVALID_ARG, "gvs_diagnostics_noalloc: null pointer");
+    if (!(softening >= 0.0)) return fail(nullptr, GVS_ERR_INVALID_ARG, "softening must be >= 0");
+    if (n > NOALLOC_MAX_N)
+        return fail(nullptr, GVS_ERR_INVALID_ARG,
+                    "gvs_diagnostics_noalloc: n = %zu exceeds the fixed scratch limit of %zu particles", n,
+                    NOALLOC_MAX_N);
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES)
+        return fail(nullptr, GVS_ERR_INVALID_ARG, "gvs_diagnostics_noalloc: device %d out of range", device);
+    memset(out, 0, sizeof(*out));
+    if (n == 0) return GVS_OK;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
+    if (!g_diag_scratch_ptr[device]) {  // one-time set-up on this device (run it before any stream capture)
+        double *p = nullptr;
+        e = cudaGetSymbolAddress((void **)&p, g_diag_scratch);
+        if (e != cudaSuccess || !p) return cuda_fail(nullptr, e, "cudaGetSymbolAddress(g_diag_scratch)");
+        int sms = 0;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaDeviceGetAttribute");
+        g_diag_sms[device] = sms;
+        g_diag_scratch_ptr[device] = p;
+    }
+    double *part = g_diag_scratch_ptr[device];
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int nb = std::max(1, std::min(std::min(g_diag_sms[device] * 2, NOALLOC_MAX_SUM_BLOCKS),
+                                        ceil_div((long long)n, RNT)));
+    const int npb = with_potential ? ceil_div((long long)n, RNT) : 0;
+    double *result = part + (size_t)NOALLOC_MAX_SUM_BLOCKS * NQ + NOALLOC_MAX_N / RNT;  // NQ + 1 slots
+    // every slot read below is written by this call first, so nothing needs clearing
+    k_sums<<<nb, RNT, 0, st>>>(n, x, y, z, vx, vy, vz, mass, ptype, u, part);
+    if (with_potential) k_potential<<<npb, RNT, 0, st>>>(n, x, y, z, mass, softening * softening, part + (size_t)nb * NQ);
+    k_sums_final<<<1, 32, 0, st>>>(part, nb, npb, result);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "gvs_diagnostics_noalloc launch");
+    double q[NQ + 1];
+    e = cudaMemcpyAsync(q, result, sizeof q, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "gvs_diagnostics_noalloc result copy");
+    const double pe = q[NQ];
+    out->kinetic_energy = q[0];
+    out->thermal_energy = q[1];
+    out->potential_energy = pe;
+    out->total_energy = q[0] + pe + q[1];
+    for (int d = 0; d < 3; ++d) {
+        out->momentum[d] = q[2 + d];
+        out->angular_momentum[d] = q[5 + d];
+    }
+    const double mt = q[14];
+    if (mt > 0.0)
+        for (int d = 0; d < 3; ++d) {
+            out->center_of_mass[d] = q[8 + d] / mt;
+            out->center_of_mass_velocity[d] = q[11 + d] / mt;
+        }
+    out->virial_ratio = fabs(pe) > 0.0 ? 2.0 * q[0] / fabs(pe) : 0.0;
+    return GVS_OK;
+}
