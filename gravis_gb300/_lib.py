@@ -42,7 +42,7 @@ class SphParams(C.Structure):
 class Profile(C.Structure):
     _fields_ = [("force_ms", C.c_double), ("force_launches", C.c_longlong), ("launches", C.c_longlong),
                 ("force_flops", C.c_double), ("force_bytes", C.c_double), ("tile_visits", C.c_double),
-                ("near_tile_visits", C.c_double)]
+                ("near_tile_visits", C.c_double), ("vjp_ms", C.c_double), ("vjp_launches", C.c_longlong)]
 
 
 _P = C.c_void_p  # every array argument is passed as a raw address
@@ -67,6 +67,8 @@ SIGNATURES = {
     "gvs_gravity_bh": (_ST, [_P, _sz, _P, _P, _P, _P, _d, _d, _i, _P, _P, _P]),
     "gvs_tree_export": (_ST, [_P, _sz, C.POINTER(_sz)] + [_P] * 8),
     "gvs_compute_forces": (_ST, [_P, _i, _i, _d, _d]),
+    "gvs_adjoint_forward": (_ST, [_P, _i, _d, _d, _ll, _ll]),
+    "gvs_adjoint_backward": (_ST, [_P] + [_P] * 13),
     "gvs_sph_params_default": (_ST, [C.POINTER(SphParams)]),
     "gvs_sph_compute": (_ST, [_P, C.POINTER(SphParams), _P, _P, _P, _P]),
     "gvs_sph_timestep": (_ST, [_P, C.POINTER(SphParams), C.POINTER(_d)]),

@@ -621,6 +621,369 @@ __global__ void k_reduce(const double *__restrict__ partial, int nsplit, size_t 
 }
 
 // ---------------------------------------------------------------------------
+// fused force + vector-Jacobian product (the adjoint's all-pairs kernel)
+// ---------------------------------------------------------------------------
+// For the softened force a_i = sum_j m_j d_ij s^-3/2 (d_ij = x_j - x_i,
+// s = |d|^2 + eps^2) and an adjoint vector w (one 3-vector per particle):
+//   g_k  = sum_i (da_i/dx_k)^T w_i = sum_j T(d_kj) (m_k w_j - m_j w_k),
+//          T(d) = s^-3/2 I - 3 s^-5/2 d d^T          (symmetric, even in d)
+//   gm_k = sum_i w_i . da_i/dm_k = - sum_j (w_j . d_kj) s^-3/2
+// Per source j and target k (packed by pairs of targets) the kernel forms
+// r3 = s^-3/2, r5 = s^-5/2 once and accumulates
+//   a  += m_j r3 d,  S += m_j r3,  A += r3 w_j,  B += r5 (w_j.d) d,
+//   C  += m_j r5 (w_k.d) d,  gm -= r3 (w_j.d)
+// then g = m_k (A - 3 B) - w_k S + 3 C per tile (linear in the sums), folded
+// into two-sum accumulators with a.  The forces come out of the same pass
+// because the reverse-time sweep needs a(x) at exactly the points where it
+// applies the VJP.  Tiles, near-field path and bulk-copy ring as k_direct32;
+// the adjoint vectors stream in a second tile of (wx,wx,wy,wy)(wz,wz,0,0).
+__host__ __device__ constexpr int wtile_f4(int tj) { return 2 * tj; }
+
+// OWN: the source tile is one of the block's own target tiles; there the
+// explicit u = m_k w_j - m_j w_k form is used, which is exactly zero for the
+// self pair (the split A/S form would leave the rounding of two large
+// self terms, m_k eps^-3 w_k, that should cancel).
+template <int TJ, int NP, int MASK, bool GUARD, bool OWN>
+__device__ __forceinline__ void tile_vjp(const float4 *__restrict__ tile, const float4 *__restrict__ wt,
+                                         const f2 *nx, const f2 *ny, const f2 *nz, const f2 *nxl, const f2 *nyl,
+                                         const f2 *nzl, const f2 *wkx, const f2 *wky, const f2 *wkz, const f2 *mk,
+                                         f2 e2, f2 *ax, f2 *ay, f2 *az, f2 *S, f2 *Ax, f2 *Ay, f2 *Az, f2 *Bx,
+                                         f2 *By, f2 *Bz, f2 *Cx, f2 *Cy, f2 *Cz, f2 *Gx, f2 *Gy, f2 *Gz, f2 *gm) {
+    const f2 mthree = pk(-3.f, -3.f);
+    const f2 *jd = reinterpret_cast<const f2 *>(tile + 2);
+    const f2 *jl = reinterpret_cast<const f2 *>(tile + 2 + 2 * TJ);
+    const f2 *jw = reinterpret_cast<const f2 *>(wt);
+#pragma unroll 2
+    for (int j = 0; j < TJ; ++j) {
+        const f2 xj = jd[4 * j + 0], yj = jd[4 * j + 1], zj = jd[4 * j + 2], mj = jd[4 * j + 3];
+        const f2 wx = jw[4 * j + 0], wy = jw[4 * j + 1], wz = jw[4 * j + 2];
+        f2 xl = 0ull, yl = 0ull, zl = 0ull;
+        if (MASK) { xl = jl[4 * j + 0]; yl = jl[4 * j + 1]; zl = jl[4 * j + 2]; }
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            f2 dx = add2(xj, nx[p]), dy = add2(yj, ny[p]), dz = add2(zj, nz[p]);
+            if ((MASK >> p) & 1) {
+                dx = add2(dx, add2(xl, nxl[p]));
+                dy = add2(dy, add2(yl, nyl[p]));
+                dz = add2(dz, add2(zl, nzl[p]));
+            }
+            f2 r2 = fma2(dx, dx, e2);
+            r2 = fma2(dy, dy, r2);
+            r2 = fma2(dz, dz, r2);
+            float ra, rb;
+            upk(r2, ra, rb);
+            if (GUARD) { ra = fmaxf(ra, 1e-24f); rb = fmaxf(rb, 1e-24f); }
+            const f2 ri = pk(rsqrt_approx(ra), rsqrt_approx(rb));
+            const f2 ri2 = mul2(ri, ri);
+            const f2 r3 = mul2(ri, ri2);
+            const f2 r5 = mul2(r3, ri2);
+            const f2 mr3 = mul2(mj, r3);
+            ax[p] = fma2(mr3, dx, ax[p]);
+            ay[p] = fma2(mr3, dy, ay[p]);
+            az[p] = fma2(mr3, dz, az[p]);
+            const f2 dw = fma2(wz, dz, fma2(wy, dy, mul2(wx, dx)));
+            gm[p] = fma2(r3, dw, gm[p]);
+            if (OWN) {
+                const f2 ux = sub2(mul2(mk[p], wx), mul2(mj, wkx[p]));
+                const f2 uy = sub2(mul2(mk[p], wy), mul2(mj, wky[p]));
+                const f2 uz = sub2(mul2(mk[p], wz), mul2(mj, wkz[p]));
+                const f2 du = fma2(uz, dz, fma2(uy, dy, mul2(ux, dx)));
+                const f2 c = mul2(mthree, mul2(r5, du));
+                Gx[p] = fma2(c, dx, fma2(r3, ux, Gx[p]));
+                Gy[p] = fma2(c, dy, fma2(r3, uy, Gy[p]));
+                Gz[p] = fma2(c, dz, fma2(r3, uz, Gz[p]));
+            } else {
+                S[p] = add2(S[p], mr3);
+                Ax[p] = fma2(r3, wx, Ax[p]);
+                Ay[p] = fma2(r3, wy, Ay[p]);
+                Az[p] = fma2(r3, wz, Az[p]);
+                const f2 b = mul2(r5, dw);
+                Bx[p] = fma2(b, dx, Bx[p]);
+                By[p] = fma2(b, dy, By[p]);
+                Bz[p] = fma2(b, dz, Bz[p]);
+                const f2 dwk = fma2(wkz[p], dz, fma2(wky[p], dy, mul2(wkx[p], dx)));
+                const f2 cc = mul2(mul2(mj, r5), dwk);
+                Cx[p] = fma2(cc, dx, Cx[p]);
+                Cy[p] = fma2(cc, dy, Cy[p]);
+                Cz[p] = fma2(cc, dz, Cz[p]);
+            }
+        }
+    }
+}
+
+// Partials per split: [split][7][npad] = a (3), g (3), gm (1), in sorted order.
+template <int NT, int NP, int NSTAGE, bool GUARD>
+__global__ void __launch_bounds__(NT) k_force_vjp32(const float4 *__restrict__ pack, const float4 *__restrict__ wpack,
+                                                    int ntiles, int tiles_per_split, float eps2,
+                                                    double *__restrict__ partial, size_t npad,
+                                                    unsigned *__restrict__ err) {
+    constexpr int TJ = NT;
+    constexpr int IPT = 2 * NP;
+    constexpr int TF4 = tile_f4(TJ);
+    constexpr int WF4 = wtile_f4(TJ);
+    constexpr unsigned TILE_BYTES = TF4 * 16, WTILE_BYTES = WF4 * 16;
+    extern __shared__ __align__(128) float4 smem_v[];
+    float4 *spos = smem_v;                  // NSTAGE position tiles
+    float4 *sw = smem_v + NSTAGE * TF4;     // NSTAGE adjoint-vector tiles
+    __shared__ __align__(8) uint64_t bar[NSTAGE];
+    __shared__ float4 ci[IPT][2];
+
+    const int tid = threadIdx.x;
+    const size_t ibase = (size_t)blockIdx.x * NT * IPT;
+    const int t0 = blockIdx.y * tiles_per_split;
+    const int nt = max(0, min(ntiles, t0 + tiles_per_split) - t0);
+    if (tid == 0) {
+        for (int s = 0; s < NSTAGE; ++s) mbar_init(&bar[s], 1);
+        fence_mbar_init();
+    }
+    if (tid < IPT) {
+        const float4 *tp = pack + ((size_t)blockIdx.x * IPT + tid) * TF4;
+        ci[tid][0] = __ldg(tp);
+        ci[tid][1] = __ldg(tp + 1);
+    }
+    __syncthreads();
+    if (tid == 0)
+        for (int s = 0; s < NSTAGE && s < nt; ++s) {
+            mbar_arrive_expect_tx(&bar[s], TILE_BYTES + WTILE_BYTES);
+            bulk_g2s(spos + s * TF4, pack + (size_t)(t0 + s) * TF4, TILE_BYTES, &bar[s]);
+            bulk_g2s(sw + s * WF4, wpack + (size_t)(t0 + s) * WF4, WTILE_BYTES, &bar[s]);
+        }
+    // target data: offsets (hi, lo), own adjoint vector, mass
+    f2 ox[NP], oy[NP], oz[NP], oxl[NP], oyl[NP], ozl[NP], wkx[NP], wky[NP], wkz[NP], mk[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        float v[2][10];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const size_t tile = (size_t)blockIdx.x * IPT + 2 * p + q;
+            const float4 *tp = pack + tile * TF4;
+            const float4 a = __ldg(tp + 2 + 2 * tid), b = __ldg(tp + 3 + 2 * tid);
+            const float4 al = __ldg(tp + 2 + 2 * TJ + 2 * tid), bl = __ldg(tp + 3 + 2 * TJ + 2 * tid);
+            const float4 wa = __ldg(wpack + tile * WF4 + 2 * tid), wb = __ldg(wpack + tile * WF4 + 2 * tid + 1);
+            v[q][0] = a.x; v[q][1] = a.z; v[q][2] = b.x; v[q][3] = al.x; v[q][4] = al.z; v[q][5] = bl.x;
+            v[q][6] = wa.x; v[q][7] = wa.z; v[q][8] = wb.x; v[q][9] = b.z;
+        }
+        ox[p] = pk(v[0][0], v[1][0]); oy[p] = pk(v[0][1], v[1][1]); oz[p] = pk(v[0][2], v[1][2]);
+        oxl[p] = pk(v[0][3], v[1][3]); oyl[p] = pk(v[0][4], v[1][4]); ozl[p] = pk(v[0][5], v[1][5]);
+        wkx[p] = pk(v[0][6], v[1][6]); wky[p] = pk(v[0][7], v[1][7]); wkz[p] = pk(v[0][8], v[1][8]);
+        mk[p] = pk(v[0][9], v[1][9]);
+    }
+    f2 ax[NP], ay[NP], az[NP], S[NP], Ax[NP], Ay[NP], Az[NP], Bx[NP], By[NP], Bz[NP], Cx[NP], Cy[NP], Cz[NP], gm[NP];
+    f2 Gx[NP], Gy[NP], Gz[NP];
+    f2 hi[NP][7], lo[NP][7];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        ax[p] = ay[p] = az[p] = S[p] = Ax[p] = Ay[p] = Az[p] = Bx[p] = By[p] = Bz[p] = Cx[p] = Cy[p] = Cz[p] = gm[p] =
+            0ull;
+        Gx[p] = Gy[p] = Gz[p] = 0ull;
+#pragma unroll
+        for (int k = 0; k < 7; ++k) hi[p][k] = lo[p][k] = 0ull;
+    }
+    const f2 e2 = pk(eps2, eps2);
+    const f2 three = pk(3.f, 3.f);
+    int it = 0;
+    bool bail = false;
+    for (; it < nt; ++it) {
+        const int s = it % NSTAGE;
+        const bool ok = mbar_wait_bounded(&bar[s], (unsigned)(it / NSTAGE) & 1u, err);
+        if (__syncthreads_or(!ok)) { bail = true; break; }
+        const float4 *tile = spos + s * TF4;
+        const float4 jh = tile[0], jo = tile[1];
+        f2 nx[NP], ny[NP], nz[NP], nxl[NP], nyl[NP], nzl[NP];
+        int mask = 0;
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const float4 h = ci[2 * p + q][0];
+                const float dist = fmaxf(fabsf(h.x - jh.x), fmaxf(fabsf(h.y - jh.y), fabsf(h.z - jh.z)));
+                if (dist < 0.5f * (h.w + jh.w)) mask |= 1 << p;
+            }
+            if ((mask >> p) & 1) {
+                float o[2][6], hh[2][3], ll[2][3];
+                upk(ox[p], o[0][0], o[1][0]); upk(oy[p], o[0][1], o[1][1]); upk(oz[p], o[0][2], o[1][2]);
+                upk(oxl[p], o[0][3], o[1][3]); upk(oyl[p], o[0][4], o[1][4]); upk(ozl[p], o[0][5], o[1][5]);
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const float4 h = ci[2 * p + q][0], l = ci[2 * p + q][1];
+                    ff_rel(h.x, l.x, jh.x, jo.x, o[q][0], o[q][3], hh[q][0], ll[q][0]);
+                    ff_rel(h.y, l.y, jh.y, jo.y, o[q][1], o[q][4], hh[q][1], ll[q][1]);
+                    ff_rel(h.z, l.z, jh.z, jo.z, o[q][2], o[q][5], hh[q][2], ll[q][2]);
+                }
+                nx[p] = pk(hh[0][0], hh[1][0]); nxl[p] = pk(ll[0][0], ll[1][0]);
+                ny[p] = pk(hh[0][1], hh[1][1]); nyl[p] = pk(ll[0][1], ll[1][1]);
+                nz[p] = pk(hh[0][2], hh[1][2]); nzl[p] = pk(ll[0][2], ll[1][2]);
+            } else {
+                const float4 h0 = ci[2 * p][0], l0 = ci[2 * p][1], h1 = ci[2 * p + 1][0], l1 = ci[2 * p + 1][1];
+                nx[p] = sub2(pk(-((h0.x - jh.x) + (l0.x - jo.x)), -((h1.x - jh.x) + (l1.x - jo.x))), ox[p]);
+                ny[p] = sub2(pk(-((h0.y - jh.y) + (l0.y - jo.y)), -((h1.y - jh.y) + (l1.y - jo.y))), oy[p]);
+                nz[p] = sub2(pk(-((h0.z - jh.z) + (l0.z - jo.z)), -((h1.z - jh.z) + (l1.z - jo.z))), oz[p]);
+                nxl[p] = nyl[p] = nzl[p] = 0ull;
+            }
+        }
+        const float4 *wt = sw + s * WF4;
+        constexpr int ALL = NP == 1 ? 1 : 3;
+        const int J = t0 + it;
+        const bool own = J >= (int)blockIdx.x * IPT && J < ((int)blockIdx.x + 1) * IPT;
+        if (own) {
+            if (mask != ALL) {  // every lane is near its own tile: switch all pairs to float-float
+#pragma unroll
+                for (int p = 0; p < NP; ++p)
+                    if (!((mask >> p) & 1)) {
+                        float o[2][6], hh[2][3], ll[2][3];
+                        upk(ox[p], o[0][0], o[1][0]); upk(oy[p], o[0][1], o[1][1]); upk(oz[p], o[0][2], o[1][2]);
+                        upk(oxl[p], o[0][3], o[1][3]); upk(oyl[p], o[0][4], o[1][4]); upk(ozl[p], o[0][5], o[1][5]);
+#pragma unroll
+                        for (int q = 0; q < 2; ++q) {
+                            const float4 h = ci[2 * p + q][0], l = ci[2 * p + q][1];
+                            ff_rel(h.x, l.x, jh.x, jo.x, o[q][0], o[q][3], hh[q][0], ll[q][0]);
+                            ff_rel(h.y, l.y, jh.y, jo.y, o[q][1], o[q][4], hh[q][1], ll[q][1]);
+                            ff_rel(h.z, l.z, jh.z, jo.z, o[q][2], o[q][5], hh[q][2], ll[q][2]);
+                        }
+                        nx[p] = pk(hh[0][0], hh[1][0]); nxl[p] = pk(ll[0][0], ll[1][0]);
+                        ny[p] = pk(hh[0][1], hh[1][1]); nyl[p] = pk(ll[0][1], ll[1][1]);
+                        nz[p] = pk(hh[0][2], hh[1][2]); nzl[p] = pk(ll[0][2], ll[1][2]);
+                    }
+            }
+            tile_vjp<TJ, NP, ALL, GUARD, true>(tile, wt, nx, ny, nz, nxl, nyl, nzl, wkx, wky, wkz, mk, e2, ax, ay, az,
+                                               S, Ax, Ay, Az, Bx, By, Bz, Cx, Cy, Cz, Gx, Gy, Gz, gm);
+        } else if (mask == 0) {
+            tile_vjp<TJ, NP, 0, GUARD, false>(tile, wt, nx, ny, nz, nxl, nyl, nzl, wkx, wky, wkz, mk, e2, ax, ay, az,
+                                              S, Ax, Ay, Az, Bx, By, Bz, Cx, Cy, Cz, Gx, Gy, Gz, gm);
+        } else {
+            tile_vjp<TJ, NP, ALL, GUARD, false>(tile, wt, nx, ny, nz, nxl, nyl, nzl, wkx, wky, wkz, mk, e2, ax, ay,
+                                                az, S, Ax, Ay, Az, Bx, By, Bz, Cx, Cy, Cz, Gx, Gy, Gz, gm);
+        }
+        // g = m_k (A - 3 B) - w_k S + 3 C for this tile, then fold into (hi, lo)
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            const f2 gx = add2(Gx[p], fma2(three, Cx[p], sub2(mul2(mk[p], sub2(Ax[p], mul2(three, Bx[p]))),
+                                                               mul2(wkx[p], S[p]))));
+            const f2 gy = add2(Gy[p], fma2(three, Cy[p], sub2(mul2(mk[p], sub2(Ay[p], mul2(three, By[p]))),
+                                                               mul2(wky[p], S[p]))));
+            const f2 gz = add2(Gz[p], fma2(three, Cz[p], sub2(mul2(mk[p], sub2(Az[p], mul2(three, Bz[p]))),
+                                                               mul2(wkz[p], S[p]))));
+            const f2 v[7] = {ax[p], ay[p], az[p], gx, gy, gz, sub2(0ull, gm[p])};
+#pragma unroll
+            for (int k = 0; k < 7; ++k) two_sum2(hi[p][k], lo[p][k], v[k]);
+            ax[p] = ay[p] = az[p] = S[p] = Ax[p] = Ay[p] = Az[p] = Bx[p] = By[p] = Bz[p] = Cx[p] = Cy[p] = Cz[p] =
+                gm[p] = 0ull;
+            Gx[p] = Gy[p] = Gz[p] = 0ull;
+        }
+        __syncthreads();
+        if (tid == 0 && it + NSTAGE < nt) {
+            mbar_arrive_expect_tx(&bar[s], TILE_BYTES + WTILE_BYTES);
+            bulk_g2s(spos + s * TF4, pack + (size_t)(t0 + it + NSTAGE) * TF4, TILE_BYTES, &bar[s]);
+            bulk_g2s(sw + s * WF4, wpack + (size_t)(t0 + it + NSTAGE) * WF4, WTILE_BYTES, &bar[s]);
+        }
+    }
+    if (bail) {
+        if (tid == 0)
+            for (int j = it; j < nt && j < it + NSTAGE; ++j)
+                mbar_wait_bounded(&bar[j % NSTAGE], (unsigned)(j / NSTAGE) & 1u, err);
+        return;
+    }
+    double *dst = partial + (size_t)blockIdx.y * 7 * npad;
+#pragma unroll
+    for (int p = 0; p < NP; ++p)
+#pragma unroll
+        for (int k = 0; k < 7; ++k) {
+            float h0, h1, l0, l1;
+            upk(hi[p][k], h0, h1);
+            upk(lo[p][k], l0, l1);
+            dst[(size_t)k * npad + ibase + (size_t)(2 * p) * NT + tid] = (double)h0 + (double)l0;
+            dst[(size_t)k * npad + ibase + (size_t)(2 * p + 1) * NT + tid] = (double)h1 + (double)l1;
+        }
+}
+
+// Adjoint vectors in sorted tile order: slot s of tile t at [t*WF4 + 2k].
+template <int TJ>
+__global__ void k_pack_w(const double *__restrict__ wx, const double *__restrict__ wy, const double *__restrict__ wz,
+                         double scale, const uint32_t *__restrict__ perm, size_t n, size_t nslots,
+                         float4 *__restrict__ wpack) {
+    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nslots) return;
+    float a = 0.f, b = 0.f, c = 0.f;
+    if (s < n) {
+        const uint32_t o = perm[s];
+        a = (float)(scale * wx[o]); b = (float)(scale * wy[o]); c = (float)(scale * wz[o]);
+    }
+    const size_t t = s / TJ, k = s % TJ;
+    wpack[t * wtile_f4(TJ) + 2 * k] = make_float4(a, a, b, b);
+    wpack[t * wtile_f4(TJ) + 2 * k + 1] = make_float4(c, c, 0.f, 0.f);
+}
+
+// f64 form of the fused kernel (reference gradients): double4 tiles of (x, y, z, m)
+// and (wx, wy, wz, 0), one target per thread pair of accumulator sets.
+template <int NT, int NSTAGE>
+__global__ void __launch_bounds__(NT) k_force_vjp64(const double4 *__restrict__ pack, const double4 *__restrict__ wpack,
+                                                    int ntiles, int tiles_per_split, double eps2,
+                                                    double *__restrict__ partial, size_t npad) {
+    __shared__ double4 sp[TJ64], sw[TJ64];
+    const int tid = threadIdx.x;
+    const size_t i = (size_t)blockIdx.x * NT + tid;
+    const int t0 = blockIdx.y * tiles_per_split;
+    const int t1 = min(ntiles, t0 + tiles_per_split);
+    const double4 me = pack[i], wme = wpack[i];
+    double a[3] = {0, 0, 0}, g[3] = {0, 0, 0}, gm = 0.0;
+    for (int t = t0; t < t1; ++t) {
+        __syncthreads();
+        for (int k = tid; k < TJ64; k += NT) {
+            sp[k] = pack[(size_t)t * TJ64 + k];
+            sw[k] = wpack[(size_t)t * TJ64 + k];
+        }
+        __syncthreads();
+        for (int j = 0; j < TJ64; ++j) {
+            const double4 q = sp[j], w = sw[j];
+            const double dx = q.x - me.x, dy = q.y - me.y, dz = q.z - me.z;
+            const double s = fma(dz, dz, fma(dy, dy, fma(dx, dx, eps2)));
+            if (s <= 0.0) continue;  // only the self pair at eps = 0
+            const double ri = rsqrt(s), r3 = ri * ri * ri, r5 = r3 * ri * ri;
+            const double mr3 = q.w * r3;
+            a[0] = fma(mr3, dx, a[0]); a[1] = fma(mr3, dy, a[1]); a[2] = fma(mr3, dz, a[2]);
+            const double ux = me.w * w.x - q.w * wme.x, uy = me.w * w.y - q.w * wme.y, uz = me.w * w.z - q.w * wme.z;
+            const double du = ux * dx + uy * dy + uz * dz;
+            const double c = 3.0 * r5 * du;
+            g[0] += r3 * ux - c * dx; g[1] += r3 * uy - c * dy; g[2] += r3 * uz - c * dz;
+            gm -= r3 * (w.x * dx + w.y * dy + w.z * dz);
+        }
+    }
+    double *dst = partial + (size_t)blockIdx.y * 7 * npad;
+    const double v[7] = {a[0], a[1], a[2], g[0], g[1], g[2], gm};
+    for (int k = 0; k < 7; ++k) dst[(size_t)k * npad + i] = v[k];
+}
+
+__global__ void k_pack_w64(const double *__restrict__ wx, const double *__restrict__ wy, const double *__restrict__ wz,
+                           double scale, const uint32_t *__restrict__ perm, size_t n, size_t nslots,
+                           double4 *__restrict__ wpack) {
+    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nslots) return;
+    double a = 0, b = 0, c = 0;
+    if (s < n) {
+        const uint32_t o = perm[s];
+        a = scale * wx[o]; b = scale * wy[o]; c = scale * wz[o];
+    }
+    wpack[s] = make_double4(a, b, c, 0.0);
+}
+
+// Sums the split partials of the fused kernel: a overwrites, g and gm accumulate (scaled).
+__global__ void k_reduce_vjp(const double *__restrict__ partial, int nsplit, size_t npad, size_t n,
+                             const uint32_t *__restrict__ perm, double *__restrict__ AX, double *__restrict__ AY,
+                             double *__restrict__ AZ, double *__restrict__ GX, double *__restrict__ GY,
+                             double *__restrict__ GZ, double *__restrict__ GM) {
+    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    double r[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int js = 0; js < nsplit; ++js)
+#pragma unroll
+        for (int k = 0; k < 7; ++k) r[k] += partial[((size_t)js * 7 + k) * npad + s];
+    const uint32_t o = perm[s];
+    AX[o] = r[0]; AY[o] = r[1]; AZ[o] = r[2];
+    GX[o] += r[3]; GY[o] += r[4]; GZ[o] += r[5];
+    GM[o] += r[6];
+}
+
+// ---------------------------------------------------------------------------
 // FP64_EXACT: the reference's arithmetic, one target per thread
 // ---------------------------------------------------------------------------
 constexpr int EX_NT = 128;
@@ -903,6 +1266,93 @@ gvs_status direct_forces(Ctx *c, int precision, double eps, bool accumulate) {
                                                                   as<double>(c->az), accumulate ? 1 : 0);
     c->prof.launches += 1;
     return check_launch(c, "direct reduce");
+}
+
+// Fused forces + VJP on the resident positions with adjoint vectors scale * w
+// (device arrays in caller order): a <- forces (overwrites the resident
+// accelerations), g += VJP_x, gm += VJP_m.  MIXED / FP32 use the f32 tile
+// kernel, FP64 / FP64_EXACT the f64 one.
+gvs_status direct_force_vjp(Ctx *c, int precision, double eps, const double *wx, const double *wy, const double *wz,
+                            double scale, double *gx, double *gy, double *gz, double *gm) {
+    const size_t n = c->n;
+    if (n == 0) return GVS_OK;
+    GVS_TRY(spatial_order(c));
+    cudaStream_t st = c->stream;
+    const double eps2 = eps * eps;
+    double *partial = nullptr;
+    int nsplit_eff = 1;
+    size_t npad = 0;
+    if (precision == GVS_PREC_MIXED || precision == GVS_PREC_FP32) {
+        constexpr int NT = 128, NP = 1, NSTAGE = 3, TJ = NT, IPT = 2 * NP;
+        constexpr int TF4 = tile_f4(TJ), WF4 = wtile_f4(TJ);
+        const int ntiles = ceil_div((long long)n, TJ);
+        const int iblocks = ceil_div((long long)n, (long long)NT * IPT);
+        npad = (size_t)iblocks * NT * IPT;
+        const int ntiles_pad = (int)(npad / TJ);
+        GVS_CUDA(c, ensure(c, c->jpack32, (size_t)ntiles_pad * TF4 * sizeof(float4)));
+        GVS_CUDA(c, ensure(c, c->scratch_a, (size_t)ntiles_pad * WF4 * sizeof(float4)));
+        k_pack32<TJ, true><<<ntiles, TJ, 0, st>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z),
+                                                  as<double>(c->m), as<uint32_t>(c->perm), n, as<float4>(c->jpack32));
+        if (ntiles_pad > ntiles)
+            GVS_CUDA(c, cudaMemsetAsync(as<float4>(c->jpack32) + (size_t)ntiles * TF4, 0,
+                                        (size_t)(ntiles_pad - ntiles) * TF4 * sizeof(float4), st));
+        k_pack_w<TJ><<<ceil_div((long long)npad, 256), 256, 0, st>>>(wx, wy, wz, scale, as<uint32_t>(c->perm), n,
+                                                                     npad, as<float4>(c->scratch_a));
+        c->prof.launches += 2;
+        const int smem = NSTAGE * (TF4 + WF4) * (int)sizeof(float4);
+        const float e2 = (float)eps2;
+        const bool guard = !(e2 > 0.f);
+        auto kern = guard ? k_force_vjp32<NT, NP, NSTAGE, true> : k_force_vjp32<NT, NP, NSTAGE, false>;
+        set_smem(kern, smem);
+        int per_sm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
+        const int nsplit = auto_split(c, iblocks, ntiles, std::max(1, per_sm));
+        const int tps = ceil_div(ntiles, nsplit);
+        nsplit_eff = ceil_div(ntiles, tps);
+        GVS_CUDA(c, ensure(c, c->partial, (size_t)nsplit_eff * 7 * npad * sizeof(double)));
+        partial = as<double>(c->partial);
+        if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], st));
+        kern<<<dim3(iblocks, nsplit_eff), NT, smem, st>>>(as<float4>(c->jpack32), as<float4>(c->scratch_a), ntiles,
+                                                          tps, e2, partial, npad, err_ptr(c));
+    } else {
+        constexpr int NT = 128, NSTAGE = 1;
+        const int ntiles = ceil_div((long long)n, TJ64);
+        const int iblocks = ceil_div((long long)n, NT);
+        npad = (size_t)iblocks * NT;
+        const size_t nslots = std::max(npad, (size_t)ntiles * TJ64);
+        GVS_CUDA(c, ensure(c, c->jpack64, nslots * sizeof(double4)));
+        GVS_CUDA(c, ensure(c, c->scratch_a, nslots * sizeof(double4)));
+        k_pack64<<<ceil_div((long long)nslots, 256), 256, 0, st>>>(as<double>(c->x), as<double>(c->y),
+                                                                   as<double>(c->z), as<double>(c->m),
+                                                                   as<uint32_t>(c->perm), n, nslots,
+                                                                   as<double4>(c->jpack64));
+        k_pack_w64<<<ceil_div((long long)nslots, 256), 256, 0, st>>>(wx, wy, wz, scale, as<uint32_t>(c->perm), n,
+                                                                     nslots, as<double4>(c->scratch_a));
+        c->prof.launches += 2;
+        const int nsplit = auto_split(c, iblocks, ntiles, 4);
+        const int tps = ceil_div(ntiles, nsplit);
+        nsplit_eff = ceil_div(ntiles, tps);
+        GVS_CUDA(c, ensure(c, c->partial, (size_t)nsplit_eff * 7 * npad * sizeof(double)));
+        partial = as<double>(c->partial);
+        if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], st));
+        k_force_vjp64<NT, NSTAGE><<<dim3(iblocks, nsplit_eff), NT, 0, st>>>(
+            as<double4>(c->jpack64), as<double4>(c->scratch_a), ntiles, tps, eps2, partial, npad);
+    }
+    c->prof.launches += 1;
+    GVS_TRY(check_launch(c, "force+VJP kernel"));
+    if (c->prof.on) {
+        GVS_CUDA(c, cudaEventRecord(c->prof.ev[1], st));
+        GVS_CUDA(c, cudaEventSynchronize(c->prof.ev[1]));
+        float ms = 0.f;
+        GVS_CUDA(c, cudaEventElapsedTime(&ms, c->prof.ev[0], c->prof.ev[1]));
+        c->prof.vjp_ms += ms;
+        c->prof.vjp_launches += 1;
+    }
+    k_reduce_vjp<<<ceil_div((long long)n, 256), 256, 0, st>>>(partial, nsplit_eff, npad, n, as<uint32_t>(c->perm),
+                                                              as<double>(c->ax), as<double>(c->ay), as<double>(c->az),
+                                                              gx, gy, gz, gm);
+    c->prof.launches += 1;
+    return check_launch(c, "force+VJP reduce");
 }
 
 // Times every compiled (block size, targets per thread) variant of the f32

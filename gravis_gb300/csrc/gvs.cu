@@ -181,6 +181,7 @@ gvs_status gvs_destroy(gvs_ctx *c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     tree_free(c);
     sph_free(c);
+    adj_free(c);
     DevBuf *all[] = {&c->x, &c->y, &c->z, &c->vx, &c->vy, &c->vz, &c->ax, &c->ay, &c->az, &c->m,
                      &c->ptype, &c->u, &c->h, &c->alpha, &c->rho, &c->pres, &c->cs, &c->du_dt, &c->omega,
                      &c->div_v, &c->max_mu, &c->dalpha_dt, &c->keys, &c->keys_alt, &c->perm, &c->perm_alt,
@@ -537,6 +538,8 @@ gvs_status gvs_profile_enable(gvs_ctx *c, int on) {
     c->prof.force_flops = 0.0;
     c->prof.force_bytes = 0.0;
     c->prof.tile_visits = 0.0;
+    c->prof.vjp_ms = 0.0;
+    c->prof.vjp_launches = 0;
     GVS_CUDA(c, cudaMemsetAsync(err_ptr(c) + 8, 0, sizeof(unsigned long long), c->stream));
     return GVS_OK;
 }
@@ -550,6 +553,8 @@ gvs_status gvs_profile_read(gvs_ctx *c, gvs_profile *out) {
     out->launches = c->prof.launches;
     out->force_flops = c->prof.force_flops;
     out->force_bytes = c->prof.force_bytes;
+    out->vjp_ms = c->prof.vjp_ms;
+    out->vjp_launches = c->prof.vjp_launches;
     unsigned long long nearc = 0;
     GVS_CUDA(c, cudaMemcpy(&nearc, err_ptr(c) + 8, sizeof nearc, cudaMemcpyDeviceToHost));
     out->near_tile_visits = (double)nearc;

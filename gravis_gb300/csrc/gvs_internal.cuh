@@ -55,6 +55,8 @@ struct Prof {
     double force_bytes = 0;  // algorithmic bytes moved by timed force kernels
     double force_flops = 0;  // algorithmic flops (20 per pair interaction)
     double tile_visits = 0;  // (target block, source tile) visits of the f32 pair kernel
+    double vjp_ms = 0;       // device time of the fused force + VJP kernels
+    long long vjp_launches = 0;
 };
 
 struct Tune {
@@ -200,6 +202,8 @@ gvs_status radix_sort_u64(Ctx *c, uint64_t *keys, uint32_t *vals, uint64_t *keys
 gvs_status exclusive_scan_u32(Ctx *c, const uint32_t *in, uint32_t *out, size_t n, uint32_t *total_dev);
 // direct.cu
 gvs_status direct_forces(Ctx *c, int precision, double eps, bool accumulate);
+gvs_status direct_force_vjp(Ctx *c, int precision, double eps, const double *wx, const double *wy, const double *wz,
+                            double scale, double *gx, double *gy, double *gz, double *gm);
 gvs_status direct_forces_subset(Ctx *c, int precision, double eps, const int64_t *idx_dev, size_t nidx,
                                 double *out_dev);
 gvs_status spatial_order(Ctx *c);
@@ -236,6 +240,9 @@ gvs_status sph_step(Ctx *c, const gvs_sph_params *prm, int algo, int precision, 
                     double *dt_next);
 gvs_status sph_neighbors_export(Ctx *c, size_t cap, uint32_t *start, uint32_t *count, uint32_t *idx, size_t *total);
 void sph_free(Ctx *c);
+
+// adjoint.cu
+void adj_free(Ctx *c);
 
 // forces on resident state according to the algorithm selector
 gvs_status gravity(Ctx *c, int algo, int precision, double eps, double theta, bool accumulate);

@@ -195,6 +195,21 @@ class Context:
         out["nnodes"] = k
         return out
 
+    def adjoint_forward(self, precision: int, softening: float, dt: float, nsteps: int, checkpoint_every: int = 100):
+        self._ck(self._lib.gvs_adjoint_forward(self.h, precision, softening, dt, nsteps, checkpoint_every))
+
+    def adjoint_backward(self, dl_dx: np.ndarray, dl_dv: np.ndarray | None = None) -> dict:
+        """dl_dx, dl_dv: (n, 3) arrays.  Returns dL/dx0, dL/dv0 (n, 3) and dL/dm (n,) through the dynamics."""
+        n = self._lib.gvs_count(self.h)
+        lx = np.ascontiguousarray(np.asarray(dl_dx, dtype=np.float64).T)
+        lv = None if dl_dv is None else np.ascontiguousarray(np.asarray(dl_dv, dtype=np.float64).T)
+        gx, gv, gm = np.zeros((3, n)), np.zeros((3, n)), np.zeros(n)
+        self._ck(self._lib.gvs_adjoint_backward(
+            self.h, _ptr(lx[0]), _ptr(lx[1]), _ptr(lx[2]), *((_ptr(lv[0]), _ptr(lv[1]), _ptr(lv[2])) if lv is not None
+                                                            else (None, None, None)),
+            _ptr(gx[0]), _ptr(gx[1]), _ptr(gx[2]), _ptr(gv[0]), _ptr(gv[1]), _ptr(gv[2]), _ptr(gm)))
+        return {"x": gx.T.copy(), "v": gv.T.copy(), "m": gm}
+
     def autotune(self, precision: int, softening: float) -> dict:
         nt, ipt, ms = C.c_int(), C.c_int(), C.c_double()
         self._ck(self._lib.gvs_autotune_direct(self.h, precision, softening, C.byref(nt), C.byref(ipt),
@@ -221,7 +236,7 @@ class Context:
         self._ck(self._lib.gvs_profile_read(self.h, C.byref(pr)))
         return {"force_ms": pr.force_ms, "force_launches": pr.force_launches, "launches": pr.launches,
                 "force_flops": pr.force_flops, "force_bytes": pr.force_bytes, "tile_visits": pr.tile_visits,
-                "near_tile_visits": pr.near_tile_visits}
+                "near_tile_visits": pr.near_tile_visits, "vjp_ms": pr.vjp_ms, "vjp_launches": pr.vjp_launches}
 
     def event(self, slot: int):
         self._ck(self._lib.gvs_event_record(self.h, slot))

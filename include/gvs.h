@@ -81,6 +81,8 @@ typedef struct gvs_profile {
     double force_bytes;       /* algorithmic bytes of those launches */
     double tile_visits;       /* (target block, source tile) visits of the f32 pair kernel */
     double near_tile_visits;  /* of which took the float-float near-field path */
+    double vjp_ms;            /* device time of the fused force + VJP kernels (adjoint) */
+    long long vjp_launches;
 } gvs_profile;
 
 /* ---- library / context ---------------------------------------------------- */
@@ -94,7 +96,9 @@ gvs_status gvs_last_error(const gvs_ctx *ctx, char *buf, size_t len);
 gvs_status gvs_set_fault(gvs_ctx *ctx, const char *spec);
 /* Waits for the context stream; returns GVS_ERR_DEVICE if a kernel flagged an error. */
 gvs_status gvs_sync(gvs_ctx *ctx);
-/* Reads and clears the device error word (bit flags). */
+/* Reads and clears the device error word.  Bits: 1 an mbarrier wait hit its cap,
+ * 2 tree-walk stack overflow, 4 SPH neighbour row overflow, 8 non-finite value,
+ * 16 tree invariant violated, 32 index out of range, 64 work-queue wait hit its cap. */
 gvs_status gvs_device_errors(gvs_ctx *ctx, unsigned *flags);
 
 /* ---- state transfer (Particles <-> device) ------------------------------------ */
@@ -155,6 +159,23 @@ gvs_status gvs_kdk_step_host(gvs_ctx *ctx, size_t n, double *x, double *y, doubl
 
 /* ---- diagnostics (crates/sim-core/src/diagnostics.rs:37-148) ------------------- */
 gvs_status gvs_diagnostics(gvs_ctx *ctx, double softening, int with_potential, gvs_diag *out);
+
+/* ---- adjoint (no reference counterpart; differentiates LeapfrogKDK::step,
+ * crates/sim-core/src/integrator.rs:42-76, with BruteForce forces) ---------------- */
+/* Runs nsteps KDK steps from the resident state (direct-sum forces at `precision`),
+ * keeping the f64 state every checkpoint_every steps (and the last) on the device.
+ * The resident state ends at the final time T. */
+gvs_status gvs_adjoint_forward(gvs_ctx *ctx, int precision, double softening, double dt, long long nsteps,
+                               long long checkpoint_every);
+/* Reverse-mode sweep of the last gvs_adjoint_forward: given dL/dx(T), dL/dv(T) (host
+ * arrays, NULL = zero), returns dL/dx(0), dL/dv(0) and the mass gradient through the
+ * dynamics (host arrays, NULL = skip).  One fused force + VJP all-pairs launch per step;
+ * states are recomputed backward by time reversibility and reset at every checkpoint.
+ * A loss that depends on the masses directly adds its own dL/dm.  The resident state
+ * is the initial state again on return. */
+gvs_status gvs_adjoint_backward(gvs_ctx *ctx, const double *dl_dx, const double *dl_dy, const double *dl_dz,
+                                const double *dl_dvx, const double *dl_dvy, const double *dl_dvz, double *g_x,
+                                double *g_y, double *g_z, double *g_vx, double *g_vy, double *g_vz, double *g_m);
 
 /* ---- SPH (crates/sim-core/src/sph/) ---------------------------------------------- */
 /* SphSolver::new defaults (solver.rs:40-49) and ForceParams::default (forces.rs:30-41). */
