@@ -67,6 +67,9 @@ SIGNATURES = {
     "gvs_gravity_bh": (_ST, [_P, _sz, _P, _P, _P, _P, _d, _d, _i, _P, _P, _P]),
     "gvs_tree_export": (_ST, [_P, _sz, C.POINTER(_sz)] + [_P] * 8),
     "gvs_compute_forces": (_ST, [_P, _i, _i, _d, _d]),
+    "gvs_ensemble_setup": (_ST, [_P, _i, _P, _d]),
+    "gvs_ensemble_forces": (_ST, [_P]),
+    "gvs_ensemble_kdk_steps": (_ST, [_P, _d, _ll, _i]),
     "gvs_adjoint_forward": (_ST, [_P, _i, _d, _d, _ll, _ll]),
     "gvs_adjoint_backward": (_ST, [_P] + [_P] * 13),
     "gvs_sph_params_default": (_ST, [C.POINTER(SphParams)]),

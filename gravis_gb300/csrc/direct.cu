@@ -89,41 +89,6 @@ __global__ void k_bbox_final(double *part, int nparts) {
         }
 }
 
-// 63-bit Hilbert key of a point quantised to 21 bits per axis (Skilling's
-// transpose method, "Programming the Hilbert curve", AIP Conf. Proc. 707, 2004).
-// The bounding box of a Plummer sphere is set by a few outliers (r ~ 1e3 at
-// N = 2^20), so 21 bits are needed to resolve the core; Hilbert rather than
-// Morton order because consecutive runs of a Hilbert curve stay contiguous,
-// which keeps the 128-particle tiles (and their f32 offsets) small.
-__device__ __forceinline__ uint64_t hilbert_key(uint32_t x0, uint32_t x1, uint32_t x2) {
-    uint32_t X[3] = {x0, x1, x2};
-    const uint32_t M = 1u << 20;
-    for (uint32_t Q = M; Q > 1; Q >>= 1) {
-        const uint32_t P = Q - 1;
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            if (X[i] & Q) {
-                X[0] ^= P;
-            } else {
-                const uint32_t t = (X[0] ^ X[i]) & P;
-                X[0] ^= t;
-                X[i] ^= t;
-            }
-        }
-    }
-    X[1] ^= X[0];
-    X[2] ^= X[1];
-    uint32_t t = 0;
-    for (uint32_t Q = M; Q > 1; Q >>= 1)
-        if (X[2] & Q) t ^= Q - 1;
-    X[0] ^= t; X[1] ^= t; X[2] ^= t;
-    uint64_t key = 0;
-    for (int b = 20; b >= 0; --b)
-#pragma unroll
-        for (int i = 0; i < 3; ++i) key = (key << 1) | ((X[i] >> b) & 1u);
-    return key;
-}
-
 __global__ void k_hilbert(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
                           size_t n, const double *__restrict__ bb, uint64_t *__restrict__ keys,
                           uint32_t *__restrict__ idx) {
@@ -160,18 +125,30 @@ __global__ void k_hilbert(const double *__restrict__ x, const double *__restrict
 // broadcast pairs.  Padding slots sit at the centre with zero mass.
 __host__ __device__ constexpr int tile_f4(int tj) { return 2 + 4 * tj; }
 
+// map (optional, batched ensembles): slot -> caller index, or PAD_FLAG | anchor
+// for padding (the slot then takes the position of the tile's first slot).
+constexpr uint32_t PAD_FLAG = 0x80000000u;
+
 template <int TJ, bool MIXED>
 __global__ void __launch_bounds__(TJ) k_pack32(const double *__restrict__ X, const double *__restrict__ Y,
                                                const double *__restrict__ Z, const double *__restrict__ M,
                                                const uint32_t *__restrict__ perm, size_t n,
-                                               float4 *__restrict__ pack) {
+                                               float4 *__restrict__ pack, const uint32_t *__restrict__ map) {
     constexpr int TF4 = tile_f4(TJ);
     __shared__ double red[TJ / 32][6];
     __shared__ float rred[TJ / 32];
     const int t = blockIdx.x, tid = threadIdx.x;
     const size_t s = (size_t)t * TJ + tid;
-    const bool valid = s < n;
-    const uint32_t o = perm[valid ? s : (size_t)t * TJ];
+    bool valid;
+    uint32_t o;
+    if (map) {
+        const uint32_t raw = map[s];
+        valid = !(raw & PAD_FLAG);
+        o = valid ? raw : (map[(size_t)t * TJ] & ~PAD_FLAG);
+    } else {
+        valid = s < n;
+        o = perm[valid ? s : (size_t)t * TJ];
+    }
     double p[3] = {X[o], Y[o], Z[o]};
     const double mass = valid ? M[o] : 0.0;
     double c[3] = {0.0, 0.0, 0.0};
@@ -343,39 +320,33 @@ __device__ __forceinline__ void ff_rel(float cih, float cil, float cjh, float cj
 // Per source tile J and pair p: d = (c_I - c_J) from the hi/lo pairs, then
 // -(x_i - c_J) = -(d + off_i) as one f32x2 vector; per source particle j:
 // 3 ADD2 + 3 FMA2 (r^2) + 2 MUFU.RSQ + 3 MUL2 + 3 FMA2 (accumulate).
-template <int NT, int NP, int NSTAGE, bool MIXED, bool GUARD, int MINB>
-__global__ void __launch_bounds__(NT, MINB) k_direct32(const float4 *__restrict__ pack, int ntiles, int tiles_per_split,
-                                                 float eps2, double *__restrict__ partial, size_t npad,
-                                                 unsigned *__restrict__ err,
-                                                 unsigned long long *__restrict__ near_count) {
+// One work item of the tiled f32 kernel: the IPT target tiles starting at
+// tile tgt0 against the source tiles [t0, t0 + nt); writes the item's partial
+// sums to dst[c * npad + slot].  The mbarrier ring is shared by all items of
+// a CTA: `phase` counts the tiles the CTA has consumed so far, so stage and
+// parity continue across items.  Returns false if a bounded wait gave up.
+template <int NT, int NP, int NSTAGE, bool MIXED, bool GUARD>
+__device__ __forceinline__ bool direct_item(const float4 *__restrict__ pack, int tgt0, int t0, int nt, float eps2,
+                                            double *__restrict__ dst, size_t npad, unsigned *__restrict__ err,
+                                            float4 *smem, uint64_t *bar, float4 (*ci)[2], unsigned &phase,
+                                            unsigned &near_tiles) {
     constexpr int TJ = NT;
     constexpr int IPT = 2 * NP;
     constexpr int TF4 = tile_f4(TJ);
     constexpr unsigned TILE_BYTES = TF4 * 16;
-    extern __shared__ __align__(128) float4 smem[];
-    __shared__ __align__(8) uint64_t bar[NSTAGE];
-    __shared__ float4 ci[IPT][2];  // target-tile centres (hi, lo)
-
     const int tid = threadIdx.x;
-    const size_t ibase = (size_t)blockIdx.x * NT * IPT;
-    const int t0 = blockIdx.y * tiles_per_split;
-    const int t1 = min(ntiles, t0 + tiles_per_split);
-    const int nt = max(0, t1 - t0);
-
-    if (tid == 0) {
-        for (int s = 0; s < NSTAGE; ++s) mbar_init(&bar[s], 1);
-        fence_mbar_init();
-    }
+    const size_t ibase = (size_t)tgt0 * TJ;
     if (tid < IPT) {
-        const float4 *tp = pack + ((size_t)blockIdx.x * IPT + tid) * TF4;
+        const float4 *tp = pack + ((size_t)tgt0 + tid) * TF4;
         ci[tid][0] = __ldg(tp);
         ci[tid][1] = __ldg(tp + 1);
     }
     __syncthreads();
     if (tid == 0) {
         for (int s = 0; s < NSTAGE && s < nt; ++s) {
-            mbar_arrive_expect_tx(&bar[s], TILE_BYTES);
-            bulk_g2s(smem + s * TF4, pack + (size_t)(t0 + s) * TF4, TILE_BYTES, &bar[s]);
+            const unsigned st = (phase + s) % NSTAGE;
+            mbar_arrive_expect_tx(&bar[st], TILE_BYTES);
+            bulk_g2s(smem + st * TF4, pack + (size_t)(t0 + s) * TF4, TILE_BYTES, &bar[st]);
         }
     }
 
@@ -386,7 +357,7 @@ __global__ void __launch_bounds__(NT, MINB) k_direct32(const float4 *__restrict_
         float v[2][6];
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
-            const float4 *tp = pack + ((size_t)blockIdx.x * IPT + 2 * p + q) * TF4;
+            const float4 *tp = pack + ((size_t)tgt0 + 2 * p + q) * TF4;
             const float4 a = __ldg(tp + 2 + 2 * tid), b = __ldg(tp + 3 + 2 * tid);
             v[q][0] = a.x; v[q][1] = a.z; v[q][2] = b.x;
             if (MIXED) {
@@ -410,11 +381,10 @@ __global__ void __launch_bounds__(NT, MINB) k_direct32(const float4 *__restrict_
     const f2 e2 = pk(eps2, eps2);
 
     int it = 0;
-    unsigned near_tiles = 0;
     bool bail = false;
     for (; it < nt; ++it) {
-        const int s = it % NSTAGE;
-        const unsigned parity = (unsigned)(it / NSTAGE) & 1u;
+        const int s = (int)((phase + it) % NSTAGE);
+        const unsigned parity = ((phase + it) / NSTAGE) & 1u;
         const bool ok = mbar_wait_bounded(&bar[s], parity, err);
         if (__syncthreads_or(!ok)) { bail = true; break; }
         const float4 *tile = smem + s * TF4;
@@ -499,11 +469,10 @@ __global__ void __launch_bounds__(NT, MINB) k_direct32(const float4 *__restrict_
         // drain copies still in flight before the CTA exits (bounded)
         if (tid == 0)
             for (int j = it; j < nt && j < it + NSTAGE; ++j)
-                mbar_wait_bounded(&bar[j % NSTAGE], (unsigned)(j / NSTAGE) & 1u, err);
-        return;
+                mbar_wait_bounded(&bar[(phase + j) % NSTAGE], ((phase + j) / NSTAGE) & 1u, err);
+        return false;
     }
-    if (tid == 0 && near_count) atomicAdd(near_count, (unsigned long long)near_tiles);
-    double *dst = partial + (size_t)blockIdx.y * 3 * npad;
+    phase += (unsigned)nt;
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
         float v[3][2][2];  // component, lane, (hi, lo)
@@ -524,6 +493,64 @@ __global__ void __launch_bounds__(NT, MINB) k_direct32(const float4 *__restrict_
             for (int c = 0; c < 3; ++c) dst[(size_t)c * npad + i] = (double)v[c][q][0] + (double)v[c][q][1];
         }
     }
+    return true;
+}
+
+template <int NT, int NP, int NSTAGE, bool MIXED, bool GUARD, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_direct32(const float4 *__restrict__ pack, int ntiles, int tiles_per_split,
+                                                 float eps2, double *__restrict__ partial, size_t npad,
+                                                 unsigned *__restrict__ err,
+                                                 unsigned long long *__restrict__ near_count) {
+    constexpr int IPT = 2 * NP;
+    extern __shared__ __align__(128) float4 smem[];
+    __shared__ __align__(8) uint64_t bar[NSTAGE];
+    __shared__ float4 ci[IPT][2];  // target-tile centres (hi, lo)
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NSTAGE; ++s) mbar_init(&bar[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const int t0 = blockIdx.y * tiles_per_split;
+    const int nt = max(0, min(ntiles, t0 + tiles_per_split) - t0);
+    unsigned phase = 0, near_tiles = 0;
+    const bool ok = direct_item<NT, NP, NSTAGE, MIXED, GUARD>(pack, (int)blockIdx.x * IPT, t0, nt, eps2,
+                                                             partial + (size_t)blockIdx.y * 3 * npad, npad, err,
+                                                             smem, bar, ci, phase, near_tiles);
+    if (ok && threadIdx.x == 0 && near_count) atomicAdd(near_count, (unsigned long long)near_tiles);
+}
+
+// Persistent form for batched ensembles: each CTA takes work items
+// (target tile, first source tile, source tile count, partial slot) from a
+// queue counter until it is empty.  Items never wait on each other.
+template <int NT, int NP, int NSTAGE, bool MIXED, bool GUARD, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_direct32_items(const float4 *__restrict__ pack,
+                                                       const int4 *__restrict__ items, int nitems,
+                                                       unsigned *__restrict__ counter, float eps2,
+                                                       double *__restrict__ partial, size_t npad,
+                                                       unsigned *__restrict__ err,
+                                                       unsigned long long *__restrict__ near_count) {
+    constexpr int IPT = 2 * NP;
+    extern __shared__ __align__(128) float4 smem[];
+    __shared__ __align__(8) uint64_t bar[NSTAGE];
+    __shared__ float4 ci[IPT][2];
+    __shared__ int item_s;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NSTAGE; ++s) mbar_init(&bar[s], 1);
+        fence_mbar_init();
+    }
+    unsigned phase = 0, near_tiles = 0;
+    for (;;) {
+        if (threadIdx.x == 0) item_s = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int k = item_s;
+        __syncthreads();
+        if (k >= nitems) break;
+        const int4 w = items[k];
+        if (!direct_item<NT, NP, NSTAGE, MIXED, GUARD>(pack, w.x, w.y, w.z, eps2, partial + (size_t)w.w * 3 * npad,
+                                                       npad, err, smem, bar, ci, phase, near_tiles))
+            return;
+    }
+    if (threadIdx.x == 0 && near_count) atomicAdd(near_count, (unsigned long long)near_tiles);
 }
 
 // ---------------------------------------------------------------------------
@@ -1123,7 +1150,7 @@ gvs_status launch32_t(Ctx *c, float eps2, int nsplit_req, double **partial_out, 
     GVS_CUDA(c, ensure(c, c->jpack32, (size_t)ntiles_pad * TF4 * sizeof(float4)));
     k_pack32<TJ, MIXED><<<ntiles, TJ, 0, c->stream>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z),
                                                        as<double>(c->m), as<uint32_t>(c->perm), n,
-                                                       as<float4>(c->jpack32));
+                                                       as<float4>(c->jpack32), nullptr);
     c->prof.launches += 1;
     if (ntiles_pad > ntiles)  // target-side padding tiles: zero mass at the origin, never reduced
         GVS_CUDA(c, cudaMemsetAsync(as<float4>(c->jpack32) + (size_t)ntiles * TF4, 0,
@@ -1292,7 +1319,8 @@ gvs_status direct_force_vjp(Ctx *c, int precision, double eps, const double *wx,
         GVS_CUDA(c, ensure(c, c->jpack32, (size_t)ntiles_pad * TF4 * sizeof(float4)));
         GVS_CUDA(c, ensure(c, c->scratch_a, (size_t)ntiles_pad * WF4 * sizeof(float4)));
         k_pack32<TJ, true><<<ntiles, TJ, 0, st>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z),
-                                                  as<double>(c->m), as<uint32_t>(c->perm), n, as<float4>(c->jpack32));
+                                                  as<double>(c->m), as<uint32_t>(c->perm), n, as<float4>(c->jpack32),
+                                                  nullptr);
         if (ntiles_pad > ntiles)
             GVS_CUDA(c, cudaMemsetAsync(as<float4>(c->jpack32) + (size_t)ntiles * TF4, 0,
                                         (size_t)(ntiles_pad - ntiles) * TF4 * sizeof(float4), st));
@@ -1353,6 +1381,38 @@ gvs_status direct_force_vjp(Ctx *c, int precision, double eps, const double *wx,
                                                               gx, gy, gz, gm);
     c->prof.launches += 1;
     return check_launch(c, "force+VJP reduce");
+}
+
+// ---- batched ensembles: map-driven packing and the persistent item kernel ----
+// (tile size 128 = block size, 2 target pairs per thread, as the default single-system shape)
+constexpr int ENS_TJ = 128, ENS_NP = 2, ENS_NSTAGE = 3;
+
+gvs_status ens_pack(Ctx *c, int ntiles, const uint32_t *map, float4 *pack) {
+    k_pack32<ENS_TJ, true><<<ntiles, ENS_TJ, 0, c->stream>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z),
+                                                            as<double>(c->m), nullptr, 0, pack, map);
+    c->prof.launches += 1;
+    return check_launch(c, "ensemble pack");
+}
+
+int ens_tile_float4s() { return tile_f4(ENS_TJ); }
+int ens_tile() { return ENS_TJ; }
+int ens_targets_per_block() { return ENS_TJ * 2 * ENS_NP; }
+
+gvs_status ens_pairs(Ctx *c, const float4 *pack, const int4 *items, int nitems, unsigned *counter, float eps2,
+                     double *partial, size_t npad) {
+    const int smem = ENS_NSTAGE * tile_f4(ENS_TJ) * (int)sizeof(float4);
+    const bool guard = !(eps2 > 0.f);
+    auto kern = guard ? k_direct32_items<ENS_TJ, ENS_NP, ENS_NSTAGE, true, true, 4>
+                      : k_direct32_items<ENS_TJ, ENS_NP, ENS_NSTAGE, true, false, 4>;
+    set_smem(kern, smem);
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, ENS_TJ, smem);
+    const int grid = std::max(1, std::min(nitems, c->num_sms * std::max(1, per_sm)));
+    GVS_CUDA(c, cudaMemsetAsync(counter, 0, sizeof(unsigned), c->stream));
+    unsigned long long *nearc = reinterpret_cast<unsigned long long *>(err_ptr(c) + 8);
+    kern<<<grid, ENS_TJ, smem, c->stream>>>(pack, items, nitems, counter, eps2, partial, npad, err_ptr(c), nearc);
+    c->prof.launches += 1;
+    return check_launch(c, "ensemble pair kernel");
 }
 
 // Times every compiled (block size, targets per thread) variant of the f32

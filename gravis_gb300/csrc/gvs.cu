@@ -182,6 +182,7 @@ gvs_status gvs_destroy(gvs_ctx *c) {
     tree_free(c);
     sph_free(c);
     adj_free(c);
+    ens_free(c);
     DevBuf *all[] = {&c->x, &c->y, &c->z, &c->vx, &c->vy, &c->vz, &c->ax, &c->ay, &c->az, &c->m,
                      &c->ptype, &c->u, &c->h, &c->alpha, &c->rho, &c->pres, &c->cs, &c->du_dt, &c->omega,
                      &c->div_v, &c->max_mu, &c->dalpha_dt, &c->keys, &c->keys_alt, &c->perm, &c->perm_alt,

@@ -191,6 +191,42 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// 63-bit Hilbert key of a point quantised to 21 bits per axis (Skilling's
+// transpose method, "Programming the Hilbert curve", AIP Conf. Proc. 707, 2004).
+// The bounding box of a Plummer sphere is set by a few outliers (r ~ 1e3 at
+// N = 2^20), so 21 bits are needed to resolve the core; Hilbert rather than
+// Morton order because consecutive runs of a Hilbert curve stay contiguous,
+// which keeps the 128-particle tiles (and their f32 offsets) small.
+__device__ __forceinline__ uint64_t hilbert_key(uint32_t x0, uint32_t x1, uint32_t x2) {
+    uint32_t X[3] = {x0, x1, x2};
+    const uint32_t M = 1u << 20;
+    for (uint32_t Q = M; Q > 1; Q >>= 1) {
+        const uint32_t P = Q - 1;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            if (X[i] & Q) {
+                X[0] ^= P;
+            } else {
+                const uint32_t t = (X[0] ^ X[i]) & P;
+                X[0] ^= t;
+                X[i] ^= t;
+            }
+        }
+    }
+    X[1] ^= X[0];
+    X[2] ^= X[1];
+    uint32_t t = 0;
+    for (uint32_t Q = M; Q > 1; Q >>= 1)
+        if (X[2] & Q) t ^= Q - 1;
+    X[0] ^= t; X[1] ^= t; X[2] ^= t;
+    uint64_t key = 0;
+    for (int b = 20; b >= 0; --b)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) key = (key << 1) | ((X[i] >> b) & 1u);
+    return key;
+}
+
+
 // ---------------------------------------------------------------------------
 // subsystem entry points (defined in the .cu files)
 // ---------------------------------------------------------------------------
@@ -243,6 +279,8 @@ void sph_free(Ctx *c);
 
 // adjoint.cu
 void adj_free(Ctx *c);
+// ensemble.cu
+void ens_free(Ctx *c);
 
 // forces on resident state according to the algorithm selector
 gvs_status gravity(Ctx *c, int algo, int precision, double eps, double theta, bool accumulate);

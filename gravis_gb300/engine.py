@@ -195,6 +195,17 @@ class Context:
         out["nnodes"] = k
         return out
 
+    def ensemble_setup(self, sizes, softening: float):
+        """The resident state holds len(sizes) independent systems back to back."""
+        self._ens_sizes = np.ascontiguousarray(sizes, dtype=np.int64)
+        self._ck(self._lib.gvs_ensemble_setup(self.h, len(self._ens_sizes), _ptr(self._ens_sizes), softening))
+
+    def ensemble_forces(self):
+        self._ck(self._lib.gvs_ensemble_forces(self.h))
+
+    def ensemble_kdk_steps(self, dt: float, nsteps: int, use_graph: bool = True):
+        self._ck(self._lib.gvs_ensemble_kdk_steps(self.h, dt, nsteps, 1 if use_graph else 0))
+
     def adjoint_forward(self, precision: int, softening: float, dt: float, nsteps: int, checkpoint_every: int = 100):
         self._ck(self._lib.gvs_adjoint_forward(self.h, precision, softening, dt, nsteps, checkpoint_every))
 
@@ -557,3 +568,15 @@ def ensemble_sizes(count: int, seed: int, lo: float = 256, hi: float = 16384) ->
     out = np.zeros(count, dtype=np.int64)
     check(L.load().gvs_ic_ensemble_sizes(count, seed, lo, hi, _ptr(out)))
     return out
+
+
+def plummer_ensemble(sizes, seed0: int = 1000) -> Particles:
+    """Plummer spheres with N = sizes[i] and seed seed0 + i, concatenated (each in its own COM frame)."""
+    parts = [PlummerSphere(int(n), seed=seed0 + i).generate() for i, n in enumerate(sizes)]
+    p = Particles(int(np.sum(sizes)))
+    o = 0
+    for q in parts:
+        for f in _F64 + ("particle_type",):
+            getattr(p, f)[o:o + q.count] = getattr(q, f)
+        o += q.count
+    return p

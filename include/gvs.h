@@ -177,6 +177,19 @@ gvs_status gvs_adjoint_backward(gvs_ctx *ctx, const double *dl_dx, const double 
                                 const double *dl_dvx, const double *dl_dvy, const double *dl_dvz, double *g_x,
                                 double *g_y, double *g_z, double *g_vx, double *g_vy, double *g_vz, double *g_m);
 
+/* ---- batched ensembles (no reference counterpart; each system is the reference's
+ * BruteForce + LeapfrogKDK problem, gravity.rs:47-80, integrator.rs:42-76) ----------- */
+/* The resident state (gvs_set_state) holds nsys independent systems back to back:
+ * system s owns particles [sizes[0] + .. + sizes[s-1], .. + sizes[s]).  Forces act only
+ * within a system, mixed precision (f32 pairs on f64 tile centres), softening shared.
+ * Builds the static tile layout and work list; call again after a new upload. */
+gvs_status gvs_ensemble_setup(gvs_ctx *ctx, int nsys, const int64_t *sizes, double softening);
+/* a = forces of every system (one persistent launch of the pair kernel for all systems). */
+gvs_status gvs_ensemble_forces(gvs_ctx *ctx);
+/* nsteps KDK steps of every system; use_graph != 0 captures one step into a CUDA graph
+ * (on the first call for this dt) and replays it.  Needs valid accelerations first. */
+gvs_status gvs_ensemble_kdk_steps(gvs_ctx *ctx, double dt, long long nsteps, int use_graph);
+
 /* ---- SPH (crates/sim-core/src/sph/) ---------------------------------------------- */
 /* SphSolver::new defaults (solver.rs:40-49) and ForceParams::default (forces.rs:30-41). */
 gvs_status gvs_sph_params_default(gvs_sph_params *out);
