@@ -147,8 +147,11 @@ __global__ void __launch_bounds__(TJ) k_pack32(const double *__restrict__ X, con
         o = valid ? raw : (map[(size_t)t * TJ] & ~PAD_FLAG);
     } else {
         valid = s < n;
-        o = perm[valid ? s : (size_t)t * TJ];
+        o = perm[valid ? s : std::min((size_t)t * TJ, n - 1)];
     }
+    // tiles without any member (target-side padding) get a negative radius,
+    // so they never trigger the near-field path of the real tile they are paired with
+    const int nvalid = __syncthreads_count(valid);
     double p[3] = {X[o], Y[o], Z[o]};
     const double mass = valid ? M[o] : 0.0;
     double c[3] = {0.0, 0.0, 0.0};
@@ -190,7 +193,7 @@ __global__ void __launch_bounds__(TJ) k_pack32(const double *__restrict__ X, con
     if (tid == 0) {
         float r = rred[0];
         for (int w = 1; w < TJ / 32; ++w) r = fmaxf(r, rred[w]);
-        tile[0] = make_float4(chi[0], chi[1], chi[2], r * 1.0001f);
+        tile[0] = make_float4(chi[0], chi[1], chi[2], nvalid > 0 ? r * 1.0001f : -1e30f);
         tile[1] = make_float4(clo[0], clo[1], clo[2], 0.f);
     }
     const float mf = (float)mass;
@@ -1148,13 +1151,11 @@ gvs_status launch32_t(Ctx *c, float eps2, int nsplit_req, double **partial_out, 
     const size_t npad = (size_t)iblocks * per_block;
     const int ntiles_pad = (int)(npad / TJ);  // >= ntiles
     GVS_CUDA(c, ensure(c, c->jpack32, (size_t)ntiles_pad * TF4 * sizeof(float4)));
-    k_pack32<TJ, MIXED><<<ntiles, TJ, 0, c->stream>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z),
-                                                       as<double>(c->m), as<uint32_t>(c->perm), n,
-                                                       as<float4>(c->jpack32), nullptr);
+    // target-side padding tiles (beyond ntiles) are packed too: zero mass, never reduced
+    k_pack32<TJ, MIXED><<<ntiles_pad, TJ, 0, c->stream>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z),
+                                                           as<double>(c->m), as<uint32_t>(c->perm), n,
+                                                           as<float4>(c->jpack32), nullptr);
     c->prof.launches += 1;
-    if (ntiles_pad > ntiles)  // target-side padding tiles: zero mass at the origin, never reduced
-        GVS_CUDA(c, cudaMemsetAsync(as<float4>(c->jpack32) + (size_t)ntiles * TF4, 0,
-                                    (size_t)(ntiles_pad - ntiles) * TF4 * sizeof(float4), c->stream));
     const int smem = NSTAGE * TF4 * (int)sizeof(float4);
     auto kern = k_direct32<NT, NP, NSTAGE, MIXED, GUARD, MINB>;
     set_smem(kern, smem);
@@ -1318,12 +1319,9 @@ gvs_status direct_force_vjp(Ctx *c, int precision, double eps, const double *wx,
         const int ntiles_pad = (int)(npad / TJ);
         GVS_CUDA(c, ensure(c, c->jpack32, (size_t)ntiles_pad * TF4 * sizeof(float4)));
         GVS_CUDA(c, ensure(c, c->scratch_a, (size_t)ntiles_pad * WF4 * sizeof(float4)));
-        k_pack32<TJ, true><<<ntiles, TJ, 0, st>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z),
-                                                  as<double>(c->m), as<uint32_t>(c->perm), n, as<float4>(c->jpack32),
-                                                  nullptr);
-        if (ntiles_pad > ntiles)
-            GVS_CUDA(c, cudaMemsetAsync(as<float4>(c->jpack32) + (size_t)ntiles * TF4, 0,
-                                        (size_t)(ntiles_pad - ntiles) * TF4 * sizeof(float4), st));
+        k_pack32<TJ, true><<<ntiles_pad, TJ, 0, st>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z),
+                                                      as<double>(c->m), as<uint32_t>(c->perm), n,
+                                                      as<float4>(c->jpack32), nullptr);
         k_pack_w<TJ><<<ceil_div((long long)npad, 256), 256, 0, st>>>(wx, wy, wz, scale, as<uint32_t>(c->perm), n,
                                                                      npad, as<float4>(c->scratch_a));
         c->prof.launches += 2;
