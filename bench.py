@@ -49,6 +49,11 @@ def parse():
     ap.add_argument("--cpu-targets", type=int, default=1024, help="targets in the bounded CPU sample")
     ap.add_argument("--no-extras", action="store_true", help="skip FP64 / accuracy / CPU side measurements")
     ap.add_argument("--no-autotune", action="store_true", help="use the default kernel shape (profiling runs)")
+    ap.add_argument("--workload", default="direct", choices=["direct", "bh", "sph", "ensemble", "adjoint"],
+                    help="direct (default headline); the others print their own line")
+    ap.add_argument("--theta", type=float, default=0.5)
+    ap.add_argument("--nsys", type=int, default=512, help="systems in the ensemble workload")
+    ap.add_argument("--adjoint-steps", type=int, default=200, help="steps of the adjoint side measurement")
     return ap.parse_args()
 
 
@@ -294,6 +299,7 @@ def run_engine(a, d: Dist):
         got = full.acc()[idx]
         extras["force_rel_rms_mixed_vs_fp64"] = float(np.sqrt(((got - ref) ** 2).sum() / (ref ** 2).sum()))
         extras["force_rel_err_subset"] = "1024 random targets, exact f64 reference on the GPU"
+        extras["adjoint"] = adjoint_ratio(ctx, G, n=16384, steps=a.adjoint_steps, every=100)
         line["extras"] = extras
         try:
             v, cores, secs, sample = cpu_sample(a.n, a.seed, eps, a.cpu_targets)
@@ -307,12 +313,191 @@ def run_engine(a, d: Dist):
         print(json.dumps(line), flush=True)
 
 
+def adjoint_ratio(ctx, G, n=16384, steps=200, every=100, seed=42, eps=0.01, dt=1e-3, check_fp64=True):
+    """Adjoint workload: L = sum m |x(T) - x*|^2 for a Plummer sphere; cost of the
+    backward sweep over the cost of the plain forward run, and the relative error
+    of the mixed-precision gradient against the f64 adjoint."""
+    p = G.PlummerSphere(n, seed=seed).generate()
+    rng = np.random.default_rng(seed)
+
+    def run(prec):
+        ctx.set_state(p)
+        ctx.compute_forces(G.ALGO_DIRECT, prec, eps)
+        ctx.sync()
+        ctx.event(2)
+        ctx.kdk_steps(G.ALGO_DIRECT, prec, eps, 0.0, dt, steps)
+        ctx.event(3)
+        fwd_plain = ctx.elapsed(2, 3)
+        ctx.set_state(p)
+        ctx.event(4)
+        ctx.adjoint_forward(prec, eps, dt, steps, every)
+        ctx.event(5)
+        fwd_ck = ctx.elapsed(4, 5)
+        q = G.Particles(n)
+        ctx.get_state(q)
+        x = np.stack([q.x, q.y, q.z], 1)
+        xstar = x + 0.01 * np.random.default_rng(seed + 1).standard_normal(x.shape)
+        ctx.event(6)
+        g = ctx.adjoint_backward(2.0 * p.mass[:, None] * (x - xstar))
+        ctx.event(7)
+        return fwd_plain, fwd_ck, ctx.elapsed(6, 7), g
+
+    f_plain, f_ck, bwd, g = run(G.PREC_MIXED)
+    out = {"workload": f"Plummer N={n} seed {seed}, eps={eps}, dt={dt}, {steps} steps, f64 checkpoints every {every}",
+           "forward_ms": f_plain, "forward_with_checkpoints_ms": f_ck, "backward_ms": bwd,
+           "adjoint_over_forward": bwd / f_plain}
+    if check_fp64:
+        _, _, bwd64, g64 = run(G.PREC_FP64)
+        out["grad_rel_err_mixed_vs_fp64_adjoint"] = {
+            k: float(np.linalg.norm(g[k] - g64[k]) / np.linalg.norm(g64[k])) for k in ("x", "v", "m")}
+        out["fp64_backward_ms"] = bwd64
+    del rng
+    return out
+
+
+def run_workload(a, d):
+    """Secondary workloads (one JSON line each; the default run is the direct sum)."""
+    import gravis_gb300 as G
+    ctx = G.Context(d.local)
+    res = {"metric": METRIC, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic"}
+    if a.workload == "bh":
+        n = a.n
+        p = G.collision(n, seed=7)
+        eps, theta, dt = 1e-3, a.theta, 5e-4
+        prec = G.PREC_FP32 if a.precision in ("mixed", "fp32") else G.PREC_FP64
+        ctx.set_state(p)
+        ctx.compute_forces(G.ALGO_BH, prec, eps, theta)
+        for _ in range(a.warmup):
+            ctx.kdk_steps(G.ALGO_BH, prec, eps, theta, dt, 1)
+        ctx.profile(True)
+        ms = []
+        with Clocks(d.local) as clk:
+            for _ in range(a.steps):
+                ctx.l2_flush()
+                ctx.event(0)
+                ctx.kdk_steps(G.ALGO_BH, prec, eps, theta, dt, 1)
+                ctx.event(1)
+                ms.append(ctx.elapsed(0, 1))
+        prof = ctx.profile_read()
+        ctx.profile(False)
+        t = sum(ms)
+        idx = np.sort(np.random.default_rng(1).choice(n, 4096, replace=False))
+        ref = ctx.direct_subset(idx, eps)
+        q = G.Particles(n)
+        ctx.get_state(q)
+        ctx.compute_forces(G.ALGO_BH, prec, eps, theta)
+        ctx.get_state(q)
+        rel = np.sqrt((((q.acc()[idx] - ref) ** 2).sum(1) / (ref ** 2).sum(1)).mean())
+        res.update({"value": n * a.steps / (t * 1e-3), "ms_per_step": t / a.steps, "dtype": "f32 walk / f64 state",
+                    "config": {"workload": f"Barnes-Hut KDK, two Plummer spheres N={n} seed 7, theta={theta}, "
+                                           f"eps={eps}, dt={dt}", "n": n, "theta": theta},
+                    "walk_ms_per_step": prof["force_ms"] / max(1, prof["force_launches"]),
+                    "gpu_launches": int(prof["launches"]),
+                    "accuracy": {"per_particle_rms_rel_err_vs_exact_f64_direct": float(rel),
+                                 "subset": "4096 random particles"},
+                    "clocks": clk.summary()})
+    elif a.workload == "sph":
+        n = a.n
+        p = G.gas_sphere_1r(n)
+        eps = 0.3 * (4.0 / 3.0 * np.pi / n) ** (1.0 / 3.0)
+        theta = a.theta
+        sph = G.SphSolver(ctx)
+        import ctypes as C
+        ctx.set_state(p)
+        ctx._ck(ctx._lib.gvs_set_gas(ctx.h, *(G.engine._ptr(getattr(p, f)) for f in (
+            "density", "pressure", "internal_energy", "du_dt", "smoothing_length", "sound_speed", "alpha_visc"))))
+        ctx.compute_forces(G.ALGO_BH, G.PREC_FP32, eps, theta)
+        ctx._ck(ctx._lib.gvs_sph_compute(ctx.h, C.byref(sph.params), None, None, None, None))
+        dtc = C.c_double()
+        ctx._ck(ctx._lib.gvs_sph_timestep(ctx.h, C.byref(sph.params), C.byref(dtc)))
+        dt = dtc.value
+
+        def step(dt):
+            ctx._ck(ctx._lib.gvs_sph_step(ctx.h, C.byref(sph.params), G.ALGO_BH, G.PREC_FP32, eps, theta, dt,
+                                          C.byref(dtc)))
+            return min(dtc.value, 1.5 * dt)
+
+        for _ in range(a.warmup):
+            dt = step(dt)
+        ms = []
+        with Clocks(d.local) as clk:
+            for _ in range(a.steps):
+                ctx.l2_flush()
+                ctx.event(0)
+                dt = step(dt)
+                ctx.event(1)
+                ms.append(ctx.elapsed(0, 1))
+        t = sum(ms)
+        res.update({"value": n * a.steps / (t * 1e-3), "ms_per_step": t / a.steps, "dtype": "f64 SPH / f32 walk",
+                    "config": {"workload": f"grad-h SPH + BH gravity, rho~1/r gas sphere N={n}, u=0.05, "
+                                           f"Wendland C2, eta=1.2, theta={theta}, eps={eps:.3g}, CFL 0.3",
+                               "n": n}, "clocks": clk.summary()})
+    elif a.workload == "ensemble":
+        from gravis_gb300.engine import plummer_ensemble
+        sizes = G.ensemble_sizes(a.nsys, seed=2024)
+        p = plummer_ensemble(sizes)
+        n, eps, dt = p.count, 0.01, 1e-3
+        ctx.set_state(p)
+        ctx.ensemble_setup(sizes, eps)
+        ctx.ensemble_forces()
+        ctx.ensemble_kdk_steps(dt, max(1, a.warmup), True)
+        ctx.sync()
+        ctx.event(0)
+        ctx.ensemble_kdk_steps(dt, a.steps, True)
+        ctx.event(1)
+        t = ctx.elapsed(0, 1)
+        # the same systems, one single-system context each, stepped one after another
+        ctxs, subs, o = [], [], 0
+        for m in sizes:
+            q = G.Particles(int(m))
+            for f in ("x", "y", "z", "vx", "vy", "vz", "mass"):
+                getattr(q, f)[:] = getattr(p, f)[o:o + m]
+            o += m
+            c = G.Context(d.local)
+            c.set_state(q)
+            c.compute_forces(G.ALGO_DIRECT, G.PREC_MIXED, eps)
+            ctxs.append(c)
+        for c in ctxs:
+            c.kdk_steps(G.ALGO_DIRECT, G.PREC_MIXED, eps, 0.0, dt, 1)
+        for c in ctxs:
+            c.sync()
+        kb = 2
+        t0 = time.perf_counter()
+        for _ in range(kb):
+            for c in ctxs:
+                c.kdk_steps(G.ALGO_DIRECT, G.PREC_MIXED, eps, 0.0, dt, 1)
+        for c in ctxs:
+            c.sync()
+        tb = (time.perf_counter() - t0) * 1e3
+        for c in ctxs:
+            c.close()
+        v = n * a.steps / (t * 1e-3)
+        vb = n * kb / (tb * 1e-3)
+        res.update({"value": v, "ms_per_step": t / a.steps, "dtype": "f32 pairs / f64 state",
+                    "config": {"workload": f"{a.nsys} Plummer systems, N_i log-uniform [256, 16384] (seed 2024), "
+                                           f"seeds 1000+i, eps={eps}, dt={dt}, CUDA-graph steps",
+                               "n_total": n, "sum_n2": float((sizes.astype(np.float64) ** 2).sum())},
+                    "separate_systems": {"value": vb, "ms_per_step": tb / kb,
+                                         "how": "one single-system context per system, stepped in turn"},
+                    "batched_over_separate": v / vb})
+    elif a.workload == "adjoint":
+        r = adjoint_ratio(ctx, G, n=a.n, steps=a.steps, every=100)
+        res.update({"value": r["adjoint_over_forward"], "unit": "backward/forward", "higher_is_better": False,
+                    "adjoint": r})
+    ctx.close()
+    if d.rank == 0:
+        print(json.dumps(res), flush=True)
+
+
 def main():
     a = parse()
     d = Dist()
     try:
         if a.impl == "reference":
             run_reference(a, d)
+        elif a.workload != "direct":
+            run_workload(a, d)
         else:
             run_engine(a, d)
     finally:
