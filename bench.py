@@ -196,6 +196,8 @@ def run_engine(a, d: Dist):
     eps, dt = w["eps"], a.dt
     ctx.set_state(p)
     tune = ctx.autotune(prec, eps) if prec in (2, 3) and not a.no_autotune else None
+    if tune is not None:
+        tune["candidates"] = ctx.autotune_report()
     ctx.set_state(p)
     ctx.compute_forces(G.ALGO_DIRECT, prec, eps)
     for _ in range(a.warmup):

@@ -89,12 +89,16 @@ SIGNATURES = {
     "gvs_ic_gas_sphere_1r": (_ST, [_sz, _d, _d, _d, _d] + [_P] * 6),
     "gvs_ic_ensemble_sizes": (_ST, [_sz, _u64, _d, _d, _P]),
     "gvs_autotune_direct": (_ST, [_P, _i, _d, C.POINTER(_i), C.POINTER(_i), C.POINTER(_d)]),
+    "gvs_set_direct_shape": (_ST, [_P, _i, _i, _i, _i]),
+    "gvs_autotune_report": (_ST, [_P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                  C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "gvs_profile_enable": (_ST, [_P, _i]),
     "gvs_profile_read": (_ST, [_P, C.POINTER(Profile)]),
     "gvs_event_record": (_ST, [_P, _i]),
     "gvs_event_elapsed": (_ST, [_P, _i, _i, C.POINTER(C.c_float)]),
     "gvs_l2_flush": (_ST, [_P]),
     "gvs_measure_fp32_peak": (_ST, [_P, C.POINTER(C.c_double)]),
+    "gvs_fp32_peak_variants": (_ST, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 }
 
 _lib = None

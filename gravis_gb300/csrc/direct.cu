@@ -260,17 +260,22 @@ __device__ __forceinline__ void two_sum2(f2 &hi, f2 &lo, f2 v) {
 // Pairs whose bit is set in MASK also add the f32 lo parts of both sides
 // (float-float separations): tiles close to the targets, where f32 offsets
 // alone would lose relative accuracy.
-template <int TJ, int NP, int MASK, bool GUARD>
+template <int TJ, int NP, int MASK, bool GUARD, int UNR = 4>
 __device__ __forceinline__ void tile_pairs(const float4 *__restrict__ tile, const f2 *nx, const f2 *ny, const f2 *nz,
                                            const f2 *nxl, const f2 *nyl, const f2 *nzl, f2 e2, f2 *accx,
                                            f2 *accy, f2 *accz) {
-    const f2 *jd = reinterpret_cast<const f2 *>(tile + 2);
-    const f2 *jl = reinterpret_cast<const f2 *>(tile + 2 + 2 * TJ);
-#pragma unroll 4
+    const float4 *jd = tile + 2;
+    const float4 *jl = tile + 2 + 2 * TJ;
+#pragma unroll (UNR)
     for (int j = 0; j < TJ; ++j) {
-        const f2 xj = jd[4 * j + 0], yj = jd[4 * j + 1], zj = jd[4 * j + 2], mj = jd[4 * j + 3];
+        // two 16-byte broadcast loads per source; each float4 holds two ready f32x2 pairs
+        const float4 a = jd[2 * j], b = jd[2 * j + 1];
+        const f2 xj = pk(a.x, a.y), yj = pk(a.z, a.w), zj = pk(b.x, b.y), mj = pk(b.z, b.w);
         f2 xl = 0ull, yl = 0ull, zl = 0ull;
-        if (MASK) { xl = jl[4 * j + 0]; yl = jl[4 * j + 1]; zl = jl[4 * j + 2]; }
+        if (MASK) {
+            const float4 c = jl[2 * j], d = jl[2 * j + 1];
+            xl = pk(c.x, c.y); yl = pk(c.z, c.w); zl = pk(d.x, d.y);
+        }
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
             f2 dx = add2(xj, nx[p]);
@@ -328,7 +333,7 @@ __device__ __forceinline__ void ff_rel(float cih, float cil, float cjh, float cj
 // sums to dst[c * npad + slot].  The mbarrier ring is shared by all items of
 // a CTA: `phase` counts the tiles the CTA has consumed so far, so stage and
 // parity continue across items.  Returns false if a bounded wait gave up.
-template <int NT, int NP, int NSTAGE, bool MIXED, bool GUARD>
+template <int NT, int NP, int NSTAGE, bool MIXED, bool GUARD, int UNR = 4>
 __device__ __forceinline__ bool direct_item(const float4 *__restrict__ pack, int tgt0, int t0, int nt, float eps2,
                                             double *__restrict__ dst, size_t npad, unsigned *__restrict__ err,
                                             float4 *smem, uint64_t *bar, float4 (*ci)[2], unsigned &phase,
@@ -388,8 +393,9 @@ __device__ __forceinline__ bool direct_item(const float4 *__restrict__ pack, int
     for (; it < nt; ++it) {
         const int s = (int)((phase + it) % NSTAGE);
         const unsigned parity = ((phase + it) / NSTAGE) & 1u;
+        // A thread whose wait gave up still runs the tile (on stale data, discarded):
+        // the one barrier at the end of the tile both frees stage s and spreads the bail.
         const bool ok = mbar_wait_bounded(&bar[s], parity, err);
-        if (__syncthreads_or(!ok)) { bail = true; break; }
         const float4 *tile = smem + s * TF4;
         f2 nx[NP], ny[NP], nz[NP], nxl[NP], nyl[NP], nzl[NP];
         int mask = 0;
@@ -444,14 +450,16 @@ __device__ __forceinline__ bool direct_item(const float4 *__restrict__ pack, int
             }
         }
         near_tiles += (unsigned)__popc(mask);
+        // near tiles of two-pair threads take the exact mask; otherwise every pair
+        // takes the float-float path (unflagged pairs have zero target lo parts)
         if (!MIXED || mask == 0) {
-            tile_pairs<TJ, NP, 0, GUARD>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
-        } else if (NP == 1 || mask == 3) {
-            tile_pairs<TJ, NP, (NP == 1 ? 1 : 3), GUARD>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
-        } else if (mask == 1) {
-            tile_pairs<TJ, NP, 1, GUARD>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
+            tile_pairs<TJ, NP, 0, GUARD, UNR>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
+        } else if (NP == 2 && mask == 1) {
+            tile_pairs<TJ, NP, 1, GUARD, UNR>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
+        } else if (NP == 2 && mask == 2) {
+            tile_pairs<TJ, NP, 2, GUARD, UNR>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
         } else {
-            tile_pairs<TJ, NP, 2, GUARD>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
+            tile_pairs<TJ, NP, (1 << NP) - 1, GUARD, UNR>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
         }
         if (MIXED) {
 #pragma unroll
@@ -462,7 +470,7 @@ __device__ __forceinline__ bool direct_item(const float4 *__restrict__ pack, int
                 accx[p] = accy[p] = accz[p] = 0ull;
             }
         }
-        __syncthreads();  // every thread is done with stage s
+        if (__syncthreads_or(!ok)) { bail = true; break; }  // every thread is done with stage s
         if (tid == 0 && it + NSTAGE < nt) {
             mbar_arrive_expect_tx(&bar[s], TILE_BYTES);
             bulk_g2s(smem + s * TF4, pack + (size_t)(t0 + it + NSTAGE) * TF4, TILE_BYTES, &bar[s]);
@@ -499,7 +507,7 @@ __device__ __forceinline__ bool direct_item(const float4 *__restrict__ pack, int
     return true;
 }
 
-template <int NT, int NP, int NSTAGE, bool MIXED, bool GUARD, int MINB>
+template <int NT, int NP, int NSTAGE, bool MIXED, bool GUARD, int MINB, int UNR>
 __global__ void __launch_bounds__(NT, MINB) k_direct32(const float4 *__restrict__ pack, int ntiles, int tiles_per_split,
                                                  float eps2, double *__restrict__ partial, size_t npad,
                                                  unsigned *__restrict__ err,
@@ -516,7 +524,7 @@ __global__ void __launch_bounds__(NT, MINB) k_direct32(const float4 *__restrict_
     const int t0 = blockIdx.y * tiles_per_split;
     const int nt = max(0, min(ntiles, t0 + tiles_per_split) - t0);
     unsigned phase = 0, near_tiles = 0;
-    const bool ok = direct_item<NT, NP, NSTAGE, MIXED, GUARD>(pack, (int)blockIdx.x * IPT, t0, nt, eps2,
+    const bool ok = direct_item<NT, NP, NSTAGE, MIXED, GUARD, UNR>(pack, (int)blockIdx.x * IPT, t0, nt, eps2,
                                                              partial + (size_t)blockIdx.y * 3 * npad, npad, err,
                                                              smem, bar, ci, phase, near_tiles);
     if (ok && threadIdx.x == 0 && near_count) atomicAdd(near_count, (unsigned long long)near_tiles);
@@ -525,7 +533,7 @@ __global__ void __launch_bounds__(NT, MINB) k_direct32(const float4 *__restrict_
 // Persistent form for batched ensembles: each CTA takes work items
 // (target tile, first source tile, source tile count, partial slot) from a
 // queue counter until it is empty.  Items never wait on each other.
-template <int NT, int NP, int NSTAGE, bool MIXED, bool GUARD, int MINB>
+template <int NT, int NP, int NSTAGE, bool MIXED, bool GUARD, int MINB, int UNR>
 __global__ void __launch_bounds__(NT, MINB) k_direct32_items(const float4 *__restrict__ pack,
                                                        const int4 *__restrict__ items, int nitems,
                                                        unsigned *__restrict__ counter, float eps2,
@@ -549,7 +557,7 @@ __global__ void __launch_bounds__(NT, MINB) k_direct32_items(const float4 *__res
         __syncthreads();
         if (k >= nitems) break;
         const int4 w = items[k];
-        if (!direct_item<NT, NP, NSTAGE, MIXED, GUARD>(pack, w.x, w.y, w.z, eps2, partial + (size_t)w.w * 3 * npad,
+        if (!direct_item<NT, NP, NSTAGE, MIXED, GUARD, UNR>(pack, w.x, w.y, w.z, eps2, partial + (size_t)w.w * 3 * npad,
                                                        npad, err, smem, bar, ci, phase, near_tiles))
             return;
     }
@@ -680,15 +688,18 @@ __device__ __forceinline__ void tile_vjp(const float4 *__restrict__ tile, const 
                                          f2 e2, f2 *ax, f2 *ay, f2 *az, f2 *S, f2 *Ax, f2 *Ay, f2 *Az, f2 *Bx,
                                          f2 *By, f2 *Bz, f2 *Cx, f2 *Cy, f2 *Cz, f2 *Gx, f2 *Gy, f2 *Gz, f2 *gm) {
     const f2 mthree = pk(-3.f, -3.f);
-    const f2 *jd = reinterpret_cast<const f2 *>(tile + 2);
-    const f2 *jl = reinterpret_cast<const f2 *>(tile + 2 + 2 * TJ);
-    const f2 *jw = reinterpret_cast<const f2 *>(wt);
+    const float4 *jd = tile + 2;
+    const float4 *jl = tile + 2 + 2 * TJ;
 #pragma unroll 2
     for (int j = 0; j < TJ; ++j) {
-        const f2 xj = jd[4 * j + 0], yj = jd[4 * j + 1], zj = jd[4 * j + 2], mj = jd[4 * j + 3];
-        const f2 wx = jw[4 * j + 0], wy = jw[4 * j + 1], wz = jw[4 * j + 2];
+        const float4 a = jd[2 * j], b = jd[2 * j + 1], wa = wt[2 * j], wb = wt[2 * j + 1];
+        const f2 xj = pk(a.x, a.y), yj = pk(a.z, a.w), zj = pk(b.x, b.y), mj = pk(b.z, b.w);
+        const f2 wx = pk(wa.x, wa.y), wy = pk(wa.z, wa.w), wz = pk(wb.x, wb.y);
         f2 xl = 0ull, yl = 0ull, zl = 0ull;
-        if (MASK) { xl = jl[4 * j + 0]; yl = jl[4 * j + 1]; zl = jl[4 * j + 2]; }
+        if (MASK) {
+            const float4 c = jl[2 * j], d = jl[2 * j + 1];
+            xl = pk(c.x, c.y); yl = pk(c.z, c.w); zl = pk(d.x, d.y);
+        }
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
             f2 dx = add2(xj, nx[p]), dy = add2(yj, ny[p]), dz = add2(zj, nz[p]);
@@ -1138,7 +1149,7 @@ int auto_split(Ctx *c, int iblocks, int ntiles, int blocks_per_sm) {
     return best;
 }
 
-template <int NT, int NP, bool MIXED, bool GUARD, int MINB = 1>
+template <int NT, int NP, bool MIXED, bool GUARD, int MINB = 1, int UNR = 4>
 gvs_status launch32_t(Ctx *c, float eps2, int nsplit_req, double **partial_out, int *nsplit_out, size_t *npad_out) {
     constexpr int NSTAGE = 3;
     constexpr int TJ = NT;
@@ -1157,7 +1168,7 @@ gvs_status launch32_t(Ctx *c, float eps2, int nsplit_req, double **partial_out, 
                                                            as<float4>(c->jpack32), nullptr);
     c->prof.launches += 1;
     const int smem = NSTAGE * TF4 * (int)sizeof(float4);
-    auto kern = k_direct32<NT, NP, NSTAGE, MIXED, GUARD, MINB>;
+    auto kern = k_direct32<NT, NP, NSTAGE, MIXED, GUARD, MINB, UNR>;
     set_smem(kern, smem);
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
@@ -1195,18 +1206,25 @@ gvs_status launch32(Ctx *c, float eps2, double **partial, int *nsplit, size_t *n
     const long long bucket = 63 - __builtin_clzll((unsigned long long)std::max<size_t>(c->n, 1));
     for (const auto &e : c->tune_cache)
         if (e.first == bucket) c->tune = e.second;
-    const Tune &t = c->tune;
-    if (t.nthreads == 128 && t.ipt == 4 && t.minb == 5)
-        return launch32_t<128, 2, MIXED, GUARD, 5>(c, eps2, t.nsplit, partial, nsplit, npad);
-    if (t.nthreads == 128 && t.ipt == 4 && t.minb == 6)
-        return launch32_t<128, 2, MIXED, GUARD, 6>(c, eps2, t.nsplit, partial, nsplit, npad);
-    if (t.nthreads == 256 && t.ipt == 4)
-        return launch32_t<256, 2, MIXED, GUARD, 2>(c, eps2, t.nsplit, partial, nsplit, npad);
-    if (t.nthreads == 256 && t.ipt == 2)
-        return launch32_t<256, 1, MIXED, GUARD, 4>(c, eps2, t.nsplit, partial, nsplit, npad);
-    if (t.nthreads == 128 && t.ipt == 2)
-        return launch32_t<128, 1, MIXED, GUARD, 8>(c, eps2, t.nsplit, partial, nsplit, npad);
-    return launch32_t<128, 2, MIXED, GUARD, 4>(c, eps2, t.nsplit, partial, nsplit, npad);
+    Tune t = c->tune;
+    if (!direct_shape_eligible(c->n, t.nthreads)) {
+        t.nthreads = 128;  // every unroll of the 128-thread, 4-target shape is compiled
+        t.minb = 4;
+    }
+#define GVS_L32(NT_, NP_, MB_, U_)                                                        \
+    if (t.nthreads == NT_ && t.ipt == 2 * NP_ && t.minb == MB_ && t.unroll == U_)          \
+        return launch32_t<NT_, NP_, MIXED, GUARD, MB_, U_>(c, eps2, t.nsplit, partial, nsplit, npad);
+    GVS_L32(128, 2, 4, 2)
+    GVS_L32(128, 2, 4, 4)
+    GVS_L32(128, 2, 4, 8)
+    GVS_L32(128, 2, 4, 16)
+    GVS_L32(256, 2, 2, 2)
+    GVS_L32(256, 2, 2, 4)
+    GVS_L32(256, 2, 2, 16)
+    GVS_L32(512, 2, 1, 8)
+#undef GVS_L32
+    // default shape (Tune's defaults)
+    return launch32_t<256, 2, MIXED, GUARD, 2, 8>(c, eps2, t.nsplit, partial, nsplit, npad);
 }
 
 gvs_status launch64(Ctx *c, double eps2, double **partial_out, int *nsplit_out, size_t *npad_out) {
@@ -1383,7 +1401,7 @@ gvs_status direct_force_vjp(Ctx *c, int precision, double eps, const double *wx,
 
 // ---- batched ensembles: map-driven packing and the persistent item kernel ----
 // (tile size 128 = block size, 2 target pairs per thread, as the default single-system shape)
-constexpr int ENS_TJ = 128, ENS_NP = 2, ENS_NSTAGE = 3;
+constexpr int ENS_TJ = 128, ENS_NP = 2, ENS_NSTAGE = 3, ENS_UNR = 8;
 
 gvs_status ens_pack(Ctx *c, int ntiles, const uint32_t *map, float4 *pack) {
     k_pack32<ENS_TJ, true><<<ntiles, ENS_TJ, 0, c->stream>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z),
@@ -1400,8 +1418,8 @@ gvs_status ens_pairs(Ctx *c, const float4 *pack, const int4 *items, int nitems, 
                      double *partial, size_t npad) {
     const int smem = ENS_NSTAGE * tile_f4(ENS_TJ) * (int)sizeof(float4);
     const bool guard = !(eps2 > 0.f);
-    auto kern = guard ? k_direct32_items<ENS_TJ, ENS_NP, ENS_NSTAGE, true, true, 4>
-                      : k_direct32_items<ENS_TJ, ENS_NP, ENS_NSTAGE, true, false, 4>;
+    auto kern = guard ? k_direct32_items<ENS_TJ, ENS_NP, ENS_NSTAGE, true, true, 4, ENS_UNR>
+                      : k_direct32_items<ENS_TJ, ENS_NP, ENS_NSTAGE, true, false, 4, ENS_UNR>;
     set_smem(kern, smem);
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, ENS_TJ, smem);
@@ -1415,15 +1433,45 @@ gvs_status ens_pairs(Ctx *c, const float4 *pack, const int4 *items, int nitems, 
 
 // Times every compiled (block size, targets per thread) variant of the f32
 // pair kernel on the resident state and keeps the fastest for this N bucket.
+// Compiled shapes of the f32 pair kernel: (block size, targets per thread, min blocks per
+// SM, source-loop unroll).  The first is the default.
+static const int kShapes[][4] = {{256, 4, 2, 8},  {128, 4, 4, 4},  {128, 4, 4, 2},  {128, 4, 4, 8}, {128, 4, 4, 16},
+                                 {256, 4, 2, 4},  {256, 4, 2, 2},  {256, 4, 2, 16}, {512, 4, 1, 8}};
+
+// Mixed-precision accuracy needs tiles that are small against the system: a tile
+// size above n/64 (fewer than 64 tiles) let the f32 offsets of close pairs in
+// tiles that are not flagged near lose up to 1e-5 relative in measurements on
+// Plummer spheres, so such shapes fall back to 128-particle tiles.
+bool direct_shape_eligible(size_t n, int nthreads) { return nthreads <= 128 || n >= (size_t)nthreads * 64; }
+
+bool direct_shape_compiled(int nthreads, int ipt, int minb, int unroll) {
+    for (const auto &cd : kShapes)
+        if (cd[0] == nthreads && cd[1] == ipt && cd[2] == minb && cd[3] == unroll) return true;
+    return false;
+}
+
+void set_direct_shape(Ctx *c, int nthreads, int ipt, int minb, int unroll) {
+    c->tune.nthreads = nthreads;
+    c->tune.ipt = ipt;
+    c->tune.minb = minb;
+    c->tune.unroll = unroll;
+    c->tune.nsplit = 0;
+    c->tune_cache.clear();  // a fixed shape overrides earlier autotune choices
+}
+
 gvs_status autotune_direct(Ctx *c, int precision, double eps, int *best_nt, int *best_ipt, double *best_ms) {
-    static const int cand[][3] = {{128, 4, 4}, {128, 4, 5}, {128, 4, 6}, {128, 2, 8}, {256, 4, 2}, {256, 2, 4}};
+    // (block size, targets per thread, min blocks per SM, source-loop unroll)
+    const auto &cand = kShapes;
     const bool was_on = c->prof.on;
     Tune best = c->tune;
     double best_t = 1e300;
+    c->tune_report.clear();
     for (const auto &cd : cand) {
+        if (!direct_shape_eligible(c->n, cd[0])) continue;
         c->tune.nthreads = cd[0];
         c->tune.ipt = cd[1];
         c->tune.minb = cd[2];
+        c->tune.unroll = cd[3];
         c->tune.nsplit = 0;
         GVS_TRY(direct_forces(c, precision, eps, false));  // warm (also builds the order)
         c->prof.on = true;
@@ -1431,6 +1479,7 @@ gvs_status autotune_direct(Ctx *c, int precision, double eps, int *best_nt, int 
         for (int r = 0; r < 2; ++r) GVS_TRY(direct_forces(c, precision, eps, false));
         const double t = (c->prof.force_ms - ms0) / 2.0;
         c->prof.on = was_on;
+        c->tune_report.push_back({c->tune, t});
         if (t < best_t) {
             best_t = t;
             best = c->tune;

@@ -460,6 +460,32 @@ gvs_status gvs_autotune_direct(gvs_ctx *c, int precision, double eps, int *nthre
     return read_device_errors(c);
 }
 
+gvs_status gvs_set_direct_shape(gvs_ctx *c, int nthreads, int ipt, int min_blocks, int unroll) {
+    GVS_TRY(check_ctx(c));
+    if (!direct_shape_compiled(nthreads, ipt, min_blocks, unroll))
+        return fail(c, GVS_ERR_INVALID_ARG, "pair-kernel shape (%d, %d, %d, %d) is not compiled", nthreads, ipt,
+                    min_blocks, unroll);
+    set_direct_shape(c, nthreads, ipt, min_blocks, unroll);
+    return GVS_OK;
+}
+
+gvs_status gvs_autotune_report(gvs_ctx *c, int cap, int *count, int *nthreads, int *ipt, int *min_blocks,
+                               int *unroll, double *ms) {
+    GVS_TRY(check_ctx(c));
+    if (!count) return fail(c, GVS_ERR_INVALID_ARG, "count is NULL");
+    *count = (int)c->tune_report.size();
+    if (cap < *count) return GVS_OK;
+    for (int k = 0; k < *count; ++k) {
+        const auto &e = c->tune_report[(size_t)k];
+        if (nthreads) nthreads[k] = e.first.nthreads;
+        if (ipt) ipt[k] = e.first.ipt;
+        if (min_blocks) min_blocks[k] = e.first.minb;
+        if (unroll) unroll[k] = e.first.unroll;
+        if (ms) ms[k] = e.second;
+    }
+    return GVS_OK;
+}
+
 // ---- SPH ---------------------------------------------------------------------------
 
 gvs_status gvs_sph_params_default(gvs_sph_params *p) {
@@ -639,6 +665,38 @@ __global__ void k_fp32_peak_packed(float *out, float a, float b) {
     }
     if (s == 12345.678f) out[0] = s;
 }
+
+// Packed and scalar chains interleaved one to one: on sm_10x the packed FMA runs
+// on the heavy FP32 pipe and a scalar FMA can go to the lite pipe in the same
+// cycles, so this stream can exceed either pure form.  The scalar chains use
+// distinct multipliers so they cannot be merged into packed instructions.
+__global__ void k_fp32_peak_mixed(float *out, float a, float b) {
+    unsigned long long r[8], av, bv;
+    float s_[8], m_[8];
+    asm("mov.b64 %0, {%1, %1};" : "=l"(av) : "f"(a));
+    asm("mov.b64 %0, {%1, %1};" : "=l"(bv) : "f"(b));
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        float x = (float)(threadIdx.x + k), y = x + 0.5f;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(r[k]) : "f"(x), "f"(y));
+        s_[k] = x + 0.25f;
+        m_[k] = a - 1e-4f * (float)k;
+    }
+    for (int it = 0; it < PEAK_ITERS; ++it)
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            asm volatile("fma.rn.f32x2 %0, %0, %1, %2;" : "+l"(r[k]) : "l"(av), "l"(bv));
+            asm volatile("fma.rn.f32 %0, %0, %1, %2;" : "+f"(s_[k]) : "f"(m_[k]), "f"(b));
+        }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        float x, y;
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(r[k]));
+        s += x + y + s_[k];
+    }
+    if (s == 12345.678f) out[0] = s;
+}
 }  // namespace
 
 extern "C" gvs_status gvs_measure_fp32_peak(gvs_ctx *c, double *tflops) {
@@ -648,22 +706,36 @@ extern "C" gvs_status gvs_measure_fp32_peak(gvs_ctx *c, double *tflops) {
     GVS_CUDA(c, ensure(c, c->scratch_b, 64));
     const int blocks = c->num_sms * 8, threads = 256;
     double best = 0.0;
-    for (int variant = 0; variant < 2; ++variant) {
+    for (int variant = 0; variant < 3; ++variant) {
         for (int rep = 0; rep < 3; ++rep) {
             GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], c->stream));
             if (variant == 0)
                 k_fp32_peak_scalar<<<blocks, threads, 0, c->stream>>>(as<float>(c->scratch_b), 0.999f, 0.001f);
-            else
+            else if (variant == 1)
                 k_fp32_peak_packed<<<blocks, threads, 0, c->stream>>>(as<float>(c->scratch_b), 0.999f, 0.001f);
+            else
+                k_fp32_peak_mixed<<<blocks, threads, 0, c->stream>>>(as<float>(c->scratch_b), 0.999f, 0.001f);
             GVS_CUDA(c, cudaEventRecord(c->prof.ev[1], c->stream));
             GVS_TRY(check_launch(c, "fp32 peak probe"));
             GVS_CUDA(c, cudaEventSynchronize(c->prof.ev[1]));
             float ms = 0.f;
             GVS_CUDA(c, cudaEventElapsedTime(&ms, c->prof.ev[0], c->prof.ev[1]));
-            const double flops = 2.0 * 16.0 * PEAK_ITERS * (double)blocks * threads;
-            if (ms > 0.f) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+            // lane FMAs per thread per iteration: 16 scalar, 8 x 2 packed, 8 x 2 + 8 mixed
+            const double fmas = variant == 2 ? 24.0 : 16.0;
+            const double flops = 2.0 * fmas * PEAK_ITERS * (double)blocks * threads;
+            const double tf = ms > 0.f ? flops / (ms * 1e-3) / 1e12 : 0.0;
+            c->peak_by_variant[variant] = std::max(rep == 0 ? 0.0 : c->peak_by_variant[variant], tf);
+            best = std::max(best, tf);
         }
     }
     *tflops = best;
+    return GVS_OK;
+}
+
+extern "C" gvs_status gvs_fp32_peak_variants(gvs_ctx *c, double *scalar, double *packed, double *mixed) {
+    GVS_TRY(check_ctx(c));
+    if (scalar) *scalar = c->peak_by_variant[0];
+    if (packed) *packed = c->peak_by_variant[1];
+    if (mixed) *mixed = c->peak_by_variant[2];
     return GVS_OK;
 }

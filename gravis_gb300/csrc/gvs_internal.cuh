@@ -61,9 +61,10 @@ struct Prof {
 
 struct Tune {
     int ipt = 4;       // i-particles per thread
-    int nthreads = 128;
+    int nthreads = 256;
     int nsplit = 0;    // 0 = automatic
-    int minb = 4;      // __launch_bounds__ minimum blocks per SM (register cap)
+    int minb = 2;      // __launch_bounds__ minimum blocks per SM (register cap)
+    int unroll = 8;    // source-loop unroll of the pair kernel
 };
 
 struct Ctx {
@@ -97,12 +98,14 @@ struct Ctx {
     Prof prof;
     Tune tune;
     std::vector<std::pair<long long, Tune>> tune_cache;  // (n bucket, choice)
+    std::vector<std::pair<Tune, double>> tune_report;   // last autotune: every candidate and its ms
 
     // fault injection: GVS_FAULT / gvs_set_fault ("alloc", "launch", "nan@K")
     int fault_kind = 0;  // 0 none, 1 alloc, 2 launch, 3 nan
     long long fault_step = -1;
     long long step_counter = 0;
     unsigned long long pos_version = 0;  // bumped whenever resident positions change
+    double peak_by_variant[3] = {0.0, 0.0, 0.0};  // FP32 probe: scalar, packed, mixed (TFLOP/s)
 };
 
 // Records an error message on the context and returns the status.
@@ -244,6 +247,9 @@ gvs_status direct_forces_subset(Ctx *c, int precision, double eps, const int64_t
                                 double *out_dev);
 gvs_status spatial_order(Ctx *c);
 gvs_status bbox_minmax(Ctx *c, double *dev_out6, DevBuf &part_buf);
+bool direct_shape_compiled(int nthreads, int ipt, int minb, int unroll);
+bool direct_shape_eligible(size_t n, int nthreads);
+void set_direct_shape(Ctx *c, int nthreads, int ipt, int minb, int unroll);
 gvs_status autotune_direct(Ctx *c, int precision, double eps, int *best_nt, int *best_ipt, double *best_ms);
 // kdk.cu
 gvs_status kick(Ctx *c, double half_dt);

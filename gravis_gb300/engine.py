@@ -227,6 +227,22 @@ class Context:
                                                C.byref(ms)))
         return {"nthreads": nt.value, "ipt": ipt.value, "ms": ms.value}
 
+    def set_direct_shape(self, nthreads: int, ipt: int, min_blocks: int, unroll: int):
+        """Fixes the pair-kernel shape (one of autotune_report's candidates)."""
+        self._ck(self._lib.gvs_set_direct_shape(self.h, nthreads, ipt, min_blocks, unroll))
+
+    def autotune_report(self) -> list:
+        """Every candidate of the last autotune: block size, targets per thread, minimum
+        resident blocks per SM and ms per force evaluation."""
+        cnt = C.c_int()
+        self._ck(self._lib.gvs_autotune_report(self.h, 0, C.byref(cnt), None, None, None, None, None))
+        k = cnt.value
+        nt, ipt, mb, un = ((C.c_int * max(k, 1))() for _ in range(4))
+        ms = (C.c_double * max(k, 1))()
+        self._ck(self._lib.gvs_autotune_report(self.h, k, C.byref(cnt), nt, ipt, mb, un, ms))
+        return [{"nthreads": nt[i], "ipt": ipt[i], "min_blocks": mb[i], "unroll": un[i], "ms": ms[i]}
+                for i in range(k)]
+
     def sync(self):
         self._ck(self._lib.gvs_sync(self.h))
 
@@ -264,6 +280,12 @@ class Context:
         v = C.c_double()
         self._ck(self._lib.gvs_measure_fp32_peak(self.h, C.byref(v)))
         return v.value
+
+    def fp32_peak_variants(self) -> dict:
+        """TFLOP/s of the probe's scalar, packed and interleaved forms (after fp32_peak_tflops)."""
+        v = [C.c_double() for _ in range(3)]
+        self._ck(self._lib.gvs_fp32_peak_variants(self.h, *(C.byref(x) for x in v)))
+        return {"scalar": v[0].value, "packed": v[1].value, "mixed": v[2].value}
 
 
 _default_ctx: Context | None = None

@@ -241,6 +241,20 @@ gvs_status gvs_direct_subset(gvs_ctx *ctx, int precision, double softening, cons
  * thread) variants of the f32 pair kernel on the resident state, keeps the fastest
  * for this N (power-of-two bucket) and reports it. */
 gvs_status gvs_autotune_direct(gvs_ctx *ctx, int precision, double softening, int *nthreads, int *ipt, double *ms);
+/* Fixes the shape of the f32 pair kernel (block size = source tile size, targets per
+ * thread, minimum resident blocks per SM, source-loop unroll) instead of the autotuned or
+ * default one; GVS_ERR_INVALID_ARG unless the shape is one gvs_autotune_report lists.
+ * The tile size changes the f32 rounding, so a fixed shape gives run-to-run identical
+ * forces across processes; the unroll does not change results.  A shape whose tile
+ * holds more than n/64 particles runs with 128-particle tiles (mixed-precision accuracy
+ * needs tiles that are small against the system); the autotuner skips such shapes. */
+gvs_status gvs_set_direct_shape(gvs_ctx *ctx, int nthreads, int ipt, int min_blocks, int unroll);
+/* Every candidate of the last gvs_autotune_direct with its kernel time (ms per force
+ * evaluation).  Always sets *count; fills the arrays (any may be NULL) if cap >= *count.
+ * min_blocks is the kernel's minimum resident blocks per SM (its register budget),
+ * unroll the unroll depth of its source loop. */
+gvs_status gvs_autotune_report(gvs_ctx *ctx, int cap, int *count, int *nthreads, int *ipt, int *min_blocks,
+                               int *unroll, double *ms);
 
 /* ---- initial conditions (crates/sim-core/src/scenarios/) --------------------------- */
 /* PlummerSphere::generate (plummer_sphere.rs:106-133): ChaCha20Rng::seed_from_u64(seed),
@@ -277,6 +291,9 @@ gvs_status gvs_event_elapsed(gvs_ctx *ctx, int slot_a, int slot_b, float *ms);
 gvs_status gvs_l2_flush(gvs_ctx *ctx);
 /* Measured FP32 FMA throughput of this GPU (TFLOP/s, 2 flop per FMA). */
 gvs_status gvs_measure_fp32_peak(gvs_ctx *ctx, double *tflops);
+/* The three probe forms of the last gvs_measure_fp32_peak: scalar FMA, packed f32x2 FMA,
+ * and both interleaved (TFLOP/s; NULL pointers are skipped). */
+gvs_status gvs_fp32_peak_variants(gvs_ctx *ctx, double *scalar, double *packed, double *mixed);
 
 #ifdef __cplusplus
 }

@@ -2,7 +2,7 @@
 
 Bars: FP64_EXACT is bit-identical to the reference arithmetic (integer-like
 bar); FP64 (tiled, FMA) within 1e-13 relative RMS; MIXED within 1e-6 relative
-RMS (the spec precision target); FP32 within 1e-4.  Relative RMS is
+RMS (the precision target of the mixed form); FP32 within 1e-4.  Relative RMS is
 sqrt(sum |a - a_ref|^2 / sum |a_ref|^2).
 """
 import numpy as np
@@ -204,3 +204,44 @@ def test_fault_injection(ctx):
     ctx.sync()
     with pytest.raises(G.GvsError):
         ctx.set_fault("bogus")
+
+
+SHAPES = [(256, 4, 2, 8), (128, 4, 4, 4), (128, 4, 4, 2), (128, 4, 4, 8), (128, 4, 4, 16), (256, 4, 2, 4),
+          (256, 4, 2, 2), (256, 4, 2, 16), (512, 4, 1, 8)]
+
+
+def test_every_shape_within_mixed_bar(ctx):
+    """Each compiled pair-kernel shape meets the mixed bar against the exact f64 sum,
+    and shapes that differ only in the loop unroll give identical forces.  n is
+    large enough (>= 64 tiles of 512) that no shape falls back to 128 tiles."""
+    n, eps = 40000, 0.005
+    p = G.PlummerSphere(n=n, seed=11).generate()
+    exact = gpu_acc(ctx, p, eps, G.PREC_FP64_EXACT)
+    by_tile = {}
+    try:
+        for sh in SHAPES:
+            ctx.set_direct_shape(*sh)
+            a = gpu_acc(ctx, p, eps, G.PREC_MIXED)
+            assert rel_rms(a, exact) <= 1e-6, sh
+            if sh[0] in by_tile:
+                assert np.array_equal(a, by_tile[sh[0]]), sh
+            else:
+                by_tile[sh[0]] = a
+        with pytest.raises(G.GvsError):
+            ctx.set_direct_shape(96, 4, 2, 8)
+    finally:
+        ctx.set_direct_shape(*SHAPES[0])
+
+
+def test_large_tiles_fall_back_on_small_systems(ctx):
+    """Below 64 tiles a larger shape runs with 128-particle tiles: same forces."""
+    p = G.PlummerSphere(n=3000, seed=12).generate()
+    try:
+        ctx.set_direct_shape(128, 4, 4, 8)
+        a128 = gpu_acc(ctx, p, 0.01, G.PREC_MIXED)
+        ctx.set_direct_shape(256, 4, 2, 8)
+        a256 = gpu_acc(ctx, p, 0.01, G.PREC_MIXED)
+        assert np.array_equal(a128, a256)
+    finally:
+        ctx.set_direct_shape(*SHAPES[0])
+

@@ -1,9 +1,10 @@
 """Batched ensembles: many independent systems in one persistent launch.
 
 Each system of the ensemble must evolve exactly as it does on its own through
-the single-system mixed-precision path (same Hilbert order, same tiles; only
-the grouping of source chunks in the f64 reduce differs), so the bar is
-1e-10 relative; against the exact f64 direct sum the mixed bar 1e-6 holds.
+the single-system mixed-precision path with the same 128-particle tiles (same
+Hilbert order, same tiles; only the grouping of source chunks in the f64 reduce
+differs), so the bar is 1e-10 relative; against the exact f64 direct sum the
+mixed bar 1e-6 holds.
 """
 import numpy as np
 import pytest
@@ -34,6 +35,12 @@ def split(p, sizes):
     return out
 
 
+def single_context():
+    c = G.Context(0)
+    c.set_direct_shape(128, 4, 4, 4)  # the ensemble's tile size
+    return c
+
+
 def rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
@@ -51,7 +58,7 @@ def test_ensemble_forces_match_single_systems(ctx, ens):
     ctx.ensemble_forces()
     q = G.Particles(p.count)
     ctx.get_state(q)
-    single = G.Context(0)
+    single = single_context()
     try:
         for k, s in enumerate(split(q, sizes)):
             r = split(p, sizes)[k]
@@ -80,7 +87,7 @@ def test_graph_equals_eager_and_single_runs(ctx, ens):
         ctx.get_state(q)
         runs.append(q)
     assert np.array_equal(runs[0].x, runs[1].x) and np.array_equal(runs[0].vz, runs[1].vz)
-    single = G.Context(0)
+    single = single_context()
     try:
         for k, (s, r) in enumerate(zip(split(runs[1], sizes), split(p, sizes))):
             single.set_state(r)
