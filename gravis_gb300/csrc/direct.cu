@@ -116,14 +116,27 @@ __global__ void k_hilbert(const double *__restrict__ x, const double *__restrict
 //   [1]            centre lo (x, y, z, 0)
 //   [2+2k, 3+2k]   member k offset hi: (x,x,y,y) (z,z,m,m)
 //   [2+2TJ+2k, ..] member k offset lo: (x,x,y,y) (z,z,0,0)
-// MIXED: the centre is the midpoint of the members' bounding box in f64, kept
-// as an f32 hi + lo pair whose exact f64 sum is the canonical centre c; each
-// member stores off = x - c as f32 hi + f32 lo (hi + lo = x - c to ~2^-48).
+//   [2+4TJ+c]      chunk c (members 32c .. 32c+31) box of the hi offsets:
+//                  (centre x, y, z, half-extent), Chebyshev; half-extent -1e30
+//                  when the chunk has no member (padding only)
+// MIXED: the centre c is an f32 value, the midpoint of the members' f32-rounded
+// bounding box (its lo word is 0; the pair kernel still reads hi + lo, so a
+// centre that needs both words would work unchanged); each member stores
+// off = x - c, taken in f64, as f32 hi + f32 lo (hi + lo = x - c to ~2^-48).
 // The fast path reads only hi; tiles close to the targets also use lo.
 // FP32: centre 0, members as rounded absolute positions, lo = 0.
 // Components are stored twice so the pair kernel reads ready-made f32x2
 // broadcast pairs.  Padding slots sit at the centre with zero mass.
-__host__ __device__ constexpr int tile_f4(int tj) { return 2 + 4 * tj; }
+__host__ __device__ constexpr int tile_f4(int tj) { return 2 + 4 * tj + tj / 32; }
+__host__ __device__ constexpr int chunk_box(int tj) { return 2 + 4 * tj; }
+
+// A (32 targets, 32 sources) block takes the float-float path when the
+// Chebyshev distance of the two boxes' centres is below NEAR_KAPPA times the sum
+// of their half-extents.  In f32 the separation of a far pair carries an error
+// of about 2^-24 (|x_i - c_J| + |off_j|); below this distance that is no longer
+// small against the separation itself.  1.5 keeps every tested Plummer system
+// (N = 100 .. 2^20, softening down to 0.01) at or below 3e-7 relative RMS.
+constexpr float NEAR_KAPPA = 1.5f;
 
 // map (optional, batched ensembles): slot -> caller index, or PAD_FLAG | anchor
 // for padding (the slot then takes the position of the tile's first slot).
@@ -135,7 +148,7 @@ __global__ void __launch_bounds__(TJ) k_pack32(const double *__restrict__ X, con
                                                const uint32_t *__restrict__ perm, size_t n,
                                                float4 *__restrict__ pack, const uint32_t *__restrict__ map) {
     constexpr int TF4 = tile_f4(TJ);
-    __shared__ double red[TJ / 32][6];
+    __shared__ float red[TJ / 32][6];
     __shared__ float rred[TJ / 32];
     const int t = blockIdx.x, tid = threadIdx.x;
     const size_t s = (size_t)t * TJ + tid;
@@ -157,24 +170,28 @@ __global__ void __launch_bounds__(TJ) k_pack32(const double *__restrict__ X, con
     double c[3] = {0.0, 0.0, 0.0};
     float chi[3] = {0.f, 0.f, 0.f}, clo[3] = {0.f, 0.f, 0.f};
     if (MIXED) {
-        double mn[3] = {p[0], p[1], p[2]}, mx[3] = {p[0], p[1], p[2]};
+        // The centre only has to lie near the middle of the tile: it is the f32
+        // midpoint of the f32-rounded extent (f32 arithmetic; f64 throughput is a
+        // small fraction of f32 on this part), and the offsets below are taken
+        // from it exactly in f64.  Its lo part is therefore zero.
+        float mn[3], mx[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) mn[d] = mx[d] = __double2float_rn(p[d]);
 #pragma unroll
         for (int d = 0; d < 3; ++d)
             for (int off = 16; off > 0; off >>= 1) {
-                mn[d] = fmin(mn[d], __shfl_xor_sync(0xFFFFFFFFu, mn[d], off));
-                mx[d] = fmax(mx[d], __shfl_xor_sync(0xFFFFFFFFu, mx[d], off));
+                mn[d] = fminf(mn[d], __shfl_xor_sync(0xFFFFFFFFu, mn[d], off));
+                mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xFFFFFFFFu, mx[d], off));
             }
         if ((tid & 31) == 0)
             for (int d = 0; d < 3; ++d) { red[tid >> 5][d] = mn[d]; red[tid >> 5][3 + d] = mx[d]; }
         __syncthreads();
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            double lo = red[0][d], hi = red[0][3 + d];
-            for (int w = 1; w < TJ / 32; ++w) { lo = fmin(lo, red[w][d]); hi = fmax(hi, red[w][3 + d]); }
-            const double mid = 0.5 * (lo + hi);
-            chi[d] = __double2float_rn(mid);
-            clo[d] = __double2float_rn(mid - (double)chi[d]);
-            c[d] = (double)chi[d] + (double)clo[d];  // exact: the canonical centre
+            float lo = red[0][d], hi = red[0][3 + d];
+            for (int w = 1; w < TJ / 32; ++w) { lo = fminf(lo, red[w][d]); hi = fmaxf(hi, red[w][3 + d]); }
+            chi[d] = 0.5f * lo + 0.5f * hi;  // no overflow for any finite extent
+            c[d] = (double)chi[d];
         }
     }
     float oh[3], ol[3];
@@ -195,6 +212,34 @@ __global__ void __launch_bounds__(TJ) k_pack32(const double *__restrict__ X, con
         for (int w = 1; w < TJ / 32; ++w) r = fmaxf(r, rred[w]);
         tile[0] = make_float4(chi[0], chi[1], chi[2], nvalid > 0 ? r * 1.0001f : -1e30f);
         tile[1] = make_float4(clo[0], clo[1], clo[2], 0.f);
+    }
+    {
+        // box of this warp's chunk: members only (padding slots carry no mass)
+        float bmn[3], bmx[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            bmn[d] = valid ? oh[d] : 3.0e38f;
+            bmx[d] = valid ? oh[d] : -3.0e38f;
+            for (int off = 16; off > 0; off >>= 1) {
+                bmn[d] = fminf(bmn[d], __shfl_xor_sync(0xFFFFFFFFu, bmn[d], off));
+                bmx[d] = fmaxf(bmx[d], __shfl_xor_sync(0xFFFFFFFFu, bmx[d], off));
+            }
+        }
+        const bool any = __any_sync(0xFFFFFFFFu, valid);
+        if ((tid & 31) == 0) {
+            float4 box = make_float4(0.f, 0.f, 0.f, -1e30f);
+            if (any) {
+                float h = 0.f;
+                float cb[3];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    cb[d] = 0.5f * bmn[d] + 0.5f * bmx[d];
+                    h = fmaxf(h, fmaxf(bmx[d] - cb[d], cb[d] - bmn[d]));
+                }
+                box = make_float4(cb[0], cb[1], cb[2], h * 1.0001f + 1e-30f);
+            }
+            tile[chunk_box(TJ) + (tid >> 5)] = box;
+        }
     }
     const float mf = (float)mass;
     tile[2 + 2 * tid] = make_float4(oh[0], oh[0], oh[1], oh[1]);
@@ -256,18 +301,18 @@ __device__ __forceinline__ void two_sum2(f2 &hi, f2 &lo, f2 v) {
     hi = s;
 }
 
-// One source tile against NP target pairs.  nx.. hold -(x_i - c_J) per pair.
-// Pairs whose bit is set in MASK also add the f32 lo parts of both sides
-// (float-float separations): tiles close to the targets, where f32 offsets
-// alone would lose relative accuracy.
-template <int TJ, int NP, int MASK, bool GUARD, int UNR = 4>
+// Sources [j0, j0 + NJ) of a tile against NP target pairs.  nx.. hold
+// -(x_i - c_J) per pair.  Pairs whose bit is set in MASK also add the f32 lo
+// parts of both sides (float-float separations): sources close to the
+// targets, where f32 offsets alone would lose relative accuracy.
+template <int TJ, int NP, int MASK, bool GUARD, int UNR = 4, int NJ = TJ>
 __device__ __forceinline__ void tile_pairs(const float4 *__restrict__ tile, const f2 *nx, const f2 *ny, const f2 *nz,
                                            const f2 *nxl, const f2 *nyl, const f2 *nzl, f2 e2, f2 *accx,
-                                           f2 *accy, f2 *accz) {
-    const float4 *jd = tile + 2;
-    const float4 *jl = tile + 2 + 2 * TJ;
+                                           f2 *accy, f2 *accz, int j0 = 0) {
+    const float4 *jd = tile + 2 + 2 * j0;
+    const float4 *jl = tile + 2 + 2 * TJ + 2 * j0;
 #pragma unroll (UNR)
-    for (int j = 0; j < TJ; ++j) {
+    for (int j = 0; j < NJ; ++j) {
         // two 16-byte broadcast loads per source; each float4 holds two ready f32x2 pairs
         const float4 a = jd[2 * j], b = jd[2 * j + 1];
         const f2 xj = pk(a.x, a.y), yj = pk(a.z, a.w), zj = pk(b.x, b.y), mj = pk(b.z, b.w);
@@ -336,19 +381,24 @@ __device__ __forceinline__ void ff_rel(float cih, float cil, float cjh, float cj
 template <int NT, int NP, int NSTAGE, bool MIXED, bool GUARD, int UNR = 4>
 __device__ __forceinline__ bool direct_item(const float4 *__restrict__ pack, int tgt0, int t0, int nt, float eps2,
                                             double *__restrict__ dst, size_t npad, unsigned *__restrict__ err,
-                                            float4 *smem, uint64_t *bar, float4 (*ci)[2], unsigned &phase,
-                                            unsigned &near_tiles) {
+                                            float4 *smem, uint64_t *bar, float4 (*ci)[2], float4 (*wbox)[2 * NP],
+                                            unsigned &phase, unsigned &near_tiles) {
     constexpr int TJ = NT;
     constexpr int IPT = 2 * NP;
     constexpr int TF4 = tile_f4(TJ);
+    constexpr int NCH = TJ / 32;  // source chunks per tile
+    static_assert(NCH * NP <= 32, "one lane per (source chunk, target pair)");
     constexpr unsigned TILE_BYTES = TF4 * 16;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const size_t ibase = (size_t)tgt0 * TJ;
     if (tid < IPT) {
         const float4 *tp = pack + ((size_t)tgt0 + tid) * TF4;
         ci[tid][0] = __ldg(tp);
         ci[tid][1] = __ldg(tp + 1);
     }
+    // warp w's targets in target tile k are that tile's chunk w: its box is stored there
+    if (tid < (NT / 32) * IPT)
+        wbox[tid / IPT][tid % IPT] = __ldg(pack + ((size_t)tgt0 + tid % IPT) * TF4 + chunk_box(TJ) + tid / IPT);
     __syncthreads();
     if (tid == 0) {
         for (int s = 0; s < NSTAGE && s < nt; ++s) {
@@ -398,23 +448,29 @@ __device__ __forceinline__ bool direct_item(const float4 *__restrict__ pack, int
         const bool ok = mbar_wait_bounded(&bar[s], parity, err);
         const float4 *tile = smem + s * TF4;
         f2 nx[NP], ny[NP], nz[NP], nxl[NP], nyl[NP], nzl[NP];
-        int mask = 0;
+        unsigned mask = 0;  // bit p * NCH + c: target pair p against source chunk c is near
         if (MIXED) {
             const float4 jh = tile[0], jo = tile[1];
-            // near-field test per pair (block-uniform): Chebyshev distance of the
-            // tile centres below half the sum of the two tile radii
-#pragma unroll
-            for (int p = 0; p < NP; ++p) {
+            // near-field test, one lane per (source chunk c, target pair p), on the
+            // boxes of this warp's 32 targets and of the chunk's 32 sources
+            bool near = false;
+            if (lane < NCH * NP) {
+                const int c = lane % NCH, p = lane / NCH;
+                const float4 sb = tile[chunk_box(TJ) + c];
 #pragma unroll
                 for (int q = 0; q < 2; ++q) {
-                    const float4 h = ci[2 * p + q][0];
-                    const float dist = fmaxf(fabsf(h.x - jh.x), fmaxf(fabsf(h.y - jh.y), fabsf(h.z - jh.z)));
-                    if (dist < 0.5f * (h.w + jh.w)) mask |= 1 << p;
+                    const float4 h = ci[2 * p + q][0], l = ci[2 * p + q][1], tb = wbox[warp][2 * p + q];
+                    const float ddx = ((h.x - jh.x) + (l.x - jo.x)) + (tb.x - sb.x);
+                    const float ddy = ((h.y - jh.y) + (l.y - jo.y)) + (tb.y - sb.y);
+                    const float ddz = ((h.z - jh.z) + (l.z - jo.z)) + (tb.z - sb.z);
+                    const float dist = fmaxf(fabsf(ddx), fmaxf(fabsf(ddy), fabsf(ddz)));
+                    near = near || (dist < NEAR_KAPPA * (tb.w + sb.w));
                 }
             }
+            mask = __ballot_sync(0xFFFFFFFFu, near);
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
-                if ((mask >> p) & 1) {
+                if ((mask >> (p * NCH)) & ((1u << NCH) - 1u)) {
                     float o[2][6], hh[2][3], ll[2][3];
                     upk(ox[p], o[0][0], o[1][0]); upk(oy[p], o[0][1], o[1][1]); upk(oz[p], o[0][2], o[1][2]);
                     upk(oxl[p], o[0][3], o[1][3]); upk(oyl[p], o[0][4], o[1][4]); upk(ozl[p], o[0][5], o[1][5]);
@@ -449,17 +505,27 @@ __device__ __forceinline__ bool direct_item(const float4 *__restrict__ pack, int
                 nxl[p] = nyl[p] = nzl[p] = 0ull;
             }
         }
-        near_tiles += (unsigned)__popc(mask);
-        // near tiles of two-pair threads take the exact mask; otherwise every pair
-        // takes the float-float path (unflagged pairs have zero target lo parts)
+        if (lane == 0) near_tiles += (unsigned)__popc(mask);
         if (!MIXED || mask == 0) {
             tile_pairs<TJ, NP, 0, GUARD, UNR>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
-        } else if (NP == 2 && mask == 1) {
-            tile_pairs<TJ, NP, 1, GUARD, UNR>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
-        } else if (NP == 2 && mask == 2) {
-            tile_pairs<TJ, NP, 2, GUARD, UNR>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
         } else {
-            tile_pairs<TJ, NP, (1 << NP) - 1, GUARD, UNR>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz);
+            // chunk by chunk: far pairs on the plain path, near ones with the lo parts
+            // (a pair flagged in some chunk has its lo parts; they are zero otherwise)
+#pragma unroll 1
+            for (int c = 0; c < NCH; ++c) {
+                unsigned cm = 0;
+#pragma unroll
+                for (int p = 0; p < NP; ++p) cm |= ((mask >> (p * NCH + c)) & 1u) << p;
+                if (cm == 0)
+                    tile_pairs<TJ, NP, 0, GUARD, UNR, 32>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz, 32 * c);
+                else if (NP == 2 && cm == 1)
+                    tile_pairs<TJ, NP, 1, GUARD, UNR, 32>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz, 32 * c);
+                else if (NP == 2 && cm == 2)
+                    tile_pairs<TJ, NP, 2, GUARD, UNR, 32>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx, accy, accz, 32 * c);
+                else
+                    tile_pairs<TJ, NP, (1 << NP) - 1, GUARD, UNR, 32>(tile, nx, ny, nz, nxl, nyl, nzl, e2, accx,
+                                                                      accy, accz, 32 * c);
+            }
         }
         if (MIXED) {
 #pragma unroll
@@ -515,7 +581,8 @@ __global__ void __launch_bounds__(NT, MINB) k_direct32(const float4 *__restrict_
     constexpr int IPT = 2 * NP;
     extern __shared__ __align__(128) float4 smem[];
     __shared__ __align__(8) uint64_t bar[NSTAGE];
-    __shared__ float4 ci[IPT][2];  // target-tile centres (hi, lo)
+    __shared__ float4 ci[IPT][2];          // target-tile centres (hi, lo)
+    __shared__ float4 wbox[NT / 32][IPT];  // per warp: box of its targets in each target tile
     if (threadIdx.x == 0) {
         for (int s = 0; s < NSTAGE; ++s) mbar_init(&bar[s], 1);
         fence_mbar_init();
@@ -526,8 +593,8 @@ __global__ void __launch_bounds__(NT, MINB) k_direct32(const float4 *__restrict_
     unsigned phase = 0, near_tiles = 0;
     const bool ok = direct_item<NT, NP, NSTAGE, MIXED, GUARD, UNR>(pack, (int)blockIdx.x * IPT, t0, nt, eps2,
                                                              partial + (size_t)blockIdx.y * 3 * npad, npad, err,
-                                                             smem, bar, ci, phase, near_tiles);
-    if (ok && threadIdx.x == 0 && near_count) atomicAdd(near_count, (unsigned long long)near_tiles);
+                                                             smem, bar, ci, wbox, phase, near_tiles);
+    if (ok && (threadIdx.x & 31) == 0 && near_count) atomicAdd(near_count, (unsigned long long)near_tiles);
 }
 
 // Persistent form for batched ensembles: each CTA takes work items
@@ -544,6 +611,7 @@ __global__ void __launch_bounds__(NT, MINB) k_direct32_items(const float4 *__res
     extern __shared__ __align__(128) float4 smem[];
     __shared__ __align__(8) uint64_t bar[NSTAGE];
     __shared__ float4 ci[IPT][2];
+    __shared__ float4 wbox[NT / 32][IPT];
     __shared__ int item_s;
     if (threadIdx.x == 0) {
         for (int s = 0; s < NSTAGE; ++s) mbar_init(&bar[s], 1);
@@ -558,10 +626,10 @@ __global__ void __launch_bounds__(NT, MINB) k_direct32_items(const float4 *__res
         if (k >= nitems) break;
         const int4 w = items[k];
         if (!direct_item<NT, NP, NSTAGE, MIXED, GUARD, UNR>(pack, w.x, w.y, w.z, eps2, partial + (size_t)w.w * 3 * npad,
-                                                       npad, err, smem, bar, ci, phase, near_tiles))
+                                                       npad, err, smem, bar, ci, wbox, phase, near_tiles))
             return;
     }
-    if (threadIdx.x == 0 && near_count) atomicAdd(near_count, (unsigned long long)near_tiles);
+    if ((threadIdx.x & 31) == 0 && near_count) atomicAdd(near_count, (unsigned long long)near_tiles);
 }
 
 // ---------------------------------------------------------------------------
@@ -1193,7 +1261,8 @@ gvs_status launch32_t(Ctx *c, float eps2, int nsplit_req, double **partial_out, 
         c->prof.force_flops += 20.0 * (double)n * (double)n;
         c->prof.force_bytes += (double)nsplit_eff * (double)npad * 24.0 + (double)iblocks * nsplit_eff * tps *
                                                                               (double)TF4 * 16.0;
-        c->prof.tile_visits += (double)iblocks * (double)ntiles;
+        // near-field decisions: per warp, source tile, 32-source chunk and target pair
+        c->prof.tile_visits += (double)iblocks * (double)ntiles * (NT / 32) * (TJ / 32) * NP;
     }
     *partial_out = as<double>(c->partial);
     *nsplit_out = nsplit_eff;
@@ -1218,13 +1287,14 @@ gvs_status launch32(Ctx *c, float eps2, double **partial, int *nsplit, size_t *n
     GVS_L32(128, 2, 4, 4)
     GVS_L32(128, 2, 4, 8)
     GVS_L32(128, 2, 4, 16)
-    GVS_L32(256, 2, 2, 2)
     GVS_L32(256, 2, 2, 4)
+    GVS_L32(256, 2, 2, 8)
     GVS_L32(256, 2, 2, 16)
     GVS_L32(512, 2, 1, 8)
+    GVS_L32(512, 2, 1, 2)
 #undef GVS_L32
     // default shape (Tune's defaults)
-    return launch32_t<256, 2, MIXED, GUARD, 2, 8>(c, eps2, t.nsplit, partial, nsplit, npad);
+    return launch32_t<256, 2, MIXED, GUARD, 2, 2>(c, eps2, t.nsplit, partial, nsplit, npad);
 }
 
 gvs_status launch64(Ctx *c, double eps2, double **partial_out, int *nsplit_out, size_t *npad_out) {
@@ -1401,7 +1471,7 @@ gvs_status direct_force_vjp(Ctx *c, int precision, double eps, const double *wx,
 
 // ---- batched ensembles: map-driven packing and the persistent item kernel ----
 // (tile size 128 = block size, 2 target pairs per thread, as the default single-system shape)
-constexpr int ENS_TJ = 128, ENS_NP = 2, ENS_NSTAGE = 3, ENS_UNR = 8;
+constexpr int ENS_TJ = 128, ENS_NP = 2, ENS_NSTAGE = 3, ENS_UNR = 2;
 
 gvs_status ens_pack(Ctx *c, int ntiles, const uint32_t *map, float4 *pack) {
     k_pack32<ENS_TJ, true><<<ntiles, ENS_TJ, 0, c->stream>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z),
@@ -1435,8 +1505,8 @@ gvs_status ens_pairs(Ctx *c, const float4 *pack, const int4 *items, int nitems, 
 // pair kernel on the resident state and keeps the fastest for this N bucket.
 // Compiled shapes of the f32 pair kernel: (block size, targets per thread, min blocks per
 // SM, source-loop unroll).  The first is the default.
-static const int kShapes[][4] = {{256, 4, 2, 8},  {128, 4, 4, 4},  {128, 4, 4, 2},  {128, 4, 4, 8}, {128, 4, 4, 16},
-                                 {256, 4, 2, 4},  {256, 4, 2, 2},  {256, 4, 2, 16}, {512, 4, 1, 8}};
+static const int kShapes[][4] = {{256, 4, 2, 2},  {128, 4, 4, 4},  {128, 4, 4, 2},  {128, 4, 4, 8}, {128, 4, 4, 16},
+                                 {256, 4, 2, 4},  {256, 4, 2, 8},  {256, 4, 2, 16}, {512, 4, 1, 8}, {512, 4, 1, 2}};
 
 // Mixed-precision accuracy needs tiles that are small against the system: a tile
 // size above n/64 (fewer than 64 tiles) let the f32 offsets of close pairs in

@@ -54,7 +54,7 @@ struct Prof {
     long long launches = 0;  // every kernel this context launched
     double force_bytes = 0;  // algorithmic bytes moved by timed force kernels
     double force_flops = 0;  // algorithmic flops (20 per pair interaction)
-    double tile_visits = 0;  // (target block, source tile) visits of the f32 pair kernel
+    double tile_visits = 0;  // (warp, source tile, 32-source chunk, target pair) blocks of the f32 pair kernel
     double vjp_ms = 0;       // device time of the fused force + VJP kernels
     long long vjp_launches = 0;
 };
@@ -64,7 +64,7 @@ struct Tune {
     int nthreads = 256;
     int nsplit = 0;    // 0 = automatic
     int minb = 2;      // __launch_bounds__ minimum blocks per SM (register cap)
-    int unroll = 8;    // source-loop unroll of the pair kernel
+    int unroll = 2;    // source-loop unroll of the pair kernel
 };
 
 struct Ctx {

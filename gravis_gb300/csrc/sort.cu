@@ -105,6 +105,12 @@ __global__ void __launch_bounds__(NT) k_scatter(const K *__restrict__ keys, cons
     }
 }
 
+}  // namespace
+
+// In-place exclusive scan of m counts; bsum holds ceil(m / 4096) + 1 words of scratch.
+void scan_counts_inplace(Ctx *c, uint32_t *a, size_t m, uint32_t *bsum);
+
+namespace {
 template <class K>
 gvs_status radix_sort_impl(Ctx *c, K *keys, uint32_t *vals, K *keys_alt, uint32_t *vals_alt, size_t n,
                            int begin_bit, int end_bit, K **keys_out, uint32_t **vals_out) {
@@ -112,13 +118,15 @@ gvs_status radix_sort_impl(Ctx *c, K *keys, uint32_t *vals, K *keys_alt, uint32_
     uint32_t *vin = vals, *vout = vals_alt;
     if (n > 1) {
         const int nblocks = ceil_div((long long)n, TILE);
-        GVS_CUDA(c, ensure(c, c->sort_hist, (size_t)RADIX * nblocks * sizeof(uint32_t)));
+        const size_t m = (size_t)RADIX * nblocks;
+        GVS_CUDA(c, ensure(c, c->sort_hist, (m + m / 1024 + 64) * sizeof(uint32_t)));
         uint32_t *hist = as<uint32_t>(c->sort_hist);
+        uint32_t *bsum = hist + m;
         for (int bit = begin_bit; bit < end_bit; bit += 8) {
             k_hist<K><<<nblocks, NT, 0, c->stream>>>(kin, n, bit, hist, nblocks);
-            k_scan1<<<1, 1024, 0, c->stream>>>(hist, RADIX * nblocks);
+            scan_counts_inplace(c, hist, m, bsum);
             k_scatter<K><<<nblocks, NT, 0, c->stream>>>(kin, vin, kout, vout, n, bit, hist, nblocks);
-            c->prof.launches += 3;
+            c->prof.launches += 2;
             GVS_TRY(check_launch(c, "radix sort pass"));
             K *tk = kin; kin = kout; kout = tk;
             uint32_t *tv = vin; vin = vout; vout = tv;
@@ -208,6 +216,22 @@ __global__ void __launch_bounds__(SCAN_NT) k_scan_apply(const uint32_t *in, size
         }
 }
 }  // namespace
+
+// Three launches, each wide: block sums, one-block scan of the (few) block sums,
+// then the block-local scans plus their offsets.  In place is safe: every thread
+// reads its own elements before writing them.
+void scan_counts_inplace(Ctx *c, uint32_t *a, size_t m, uint32_t *bsum) {
+    if (m <= 16 * 1024) {  // small tables: one launch of one block beats three launches
+        k_scan1<<<1, 1024, 0, c->stream>>>(a, (int)m);
+        c->prof.launches += 1;
+        return;
+    }
+    const int nb = ceil_div((long long)m, SCAN_TILE);
+    k_scan_blocksum<<<nb, SCAN_NT, 0, c->stream>>>(a, m, bsum);
+    k_scan1<<<1, 1024, 0, c->stream>>>(bsum, nb);
+    k_scan_apply<<<nb, SCAN_NT, 0, c->stream>>>(a, m, bsum, a);
+    c->prof.launches += 3;
+}
 
 // out[i] = sum_{k<i} in[i], for i in [0, n); also returns the total in *total_dev[0] (device).
 gvs_status exclusive_scan_u32(Ctx *c, const uint32_t *in, uint32_t *out, size_t n, uint32_t *total_dev) {

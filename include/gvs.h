@@ -79,7 +79,8 @@ typedef struct gvs_profile {
     long long launches;       /* all kernel launches since reset */
     double force_flops;       /* algorithmic flops of those launches (20 per pair) */
     double force_bytes;       /* algorithmic bytes of those launches */
-    double tile_visits;       /* (target block, source tile) visits of the f32 pair kernel */
+    double tile_visits;       /* (warp of 32 targets, source tile, 32-source chunk, target pair)
+                                 blocks of the f32 pair kernel */
     double near_tile_visits;  /* of which took the float-float near-field path */
     double vjp_ms;            /* device time of the fused force + VJP kernels (adjoint) */
     long long vjp_launches;

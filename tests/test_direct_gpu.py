@@ -206,8 +206,8 @@ def test_fault_injection(ctx):
         ctx.set_fault("bogus")
 
 
-SHAPES = [(256, 4, 2, 8), (128, 4, 4, 4), (128, 4, 4, 2), (128, 4, 4, 8), (128, 4, 4, 16), (256, 4, 2, 4),
-          (256, 4, 2, 2), (256, 4, 2, 16), (512, 4, 1, 8)]
+SHAPES = [(256, 4, 2, 2), (128, 4, 4, 4), (128, 4, 4, 2), (128, 4, 4, 8), (128, 4, 4, 16), (256, 4, 2, 4),
+          (256, 4, 2, 8), (256, 4, 2, 16), (512, 4, 1, 8), (512, 4, 1, 2)]
 
 
 def test_every_shape_within_mixed_bar(ctx):
@@ -239,7 +239,7 @@ def test_large_tiles_fall_back_on_small_systems(ctx):
     try:
         ctx.set_direct_shape(128, 4, 4, 8)
         a128 = gpu_acc(ctx, p, 0.01, G.PREC_MIXED)
-        ctx.set_direct_shape(256, 4, 2, 8)
+        ctx.set_direct_shape(256, 4, 2, 8)  # falls back to (128, 4, 4, 8)
         a256 = gpu_acc(ctx, p, 0.01, G.PREC_MIXED)
         assert np.array_equal(a128, a256)
     finally:
