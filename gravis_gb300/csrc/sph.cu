@@ -36,6 +36,7 @@ struct SphState {
     DevBuf sx, sy, sz, svx, svy, svz, sm, sh, su, salpha;  // sorted inputs
     DevBuf srho, spres, scs, somega, sdivv, smaxmu, sdalpha, sax, say, saz, sdu;  // sorted outputs
     DevBuf dtpart;
+    DevBuf pos4, node4;  // f32 copies for the neighbour-search prefilter
     bool have_intermediates = false;
 };
 
@@ -117,6 +118,65 @@ __device__ __forceinline__ bool sphere_hits_box(double px, double py, double pz,
     return d2 <= radius * radius;
 }
 
+// ---- f32 prefilter of the neighbour search ------------------------------------------
+// The ball query decides membership and pruning with the reference's f64 tests.
+// Most decisions are far from the boundary: an f32 test with a certified margin
+// settles them, and only the rare borderline case runs the f64 test, so lists
+// (set and order) are exactly the f64 ones.  With X bounding every coordinate,
+// node centre and half width (the root cell: max |c_root| + root half width),
+// f32 rounding moves a point-point or point-box distance by at most ~1.8 E with
+// E = 2^-21 X; the margin is 3 E, plus a relative 2^-19 on the squared bounds.
+struct Prefilter {
+    float px, py, pz, rin2, rout2;
+};
+
+__device__ __forceinline__ float prefilter_scale(const TreeView &tv) {
+    const double x = fmax(fabs(tv.bx[0]), fmax(fabs(tv.by[0]), fabs(tv.bz[0]))) + tv.root_hw;
+    return (float)(x * 0x1p-21);
+}
+
+__device__ __forceinline__ Prefilter prefilter(double px, double py, double pz, double radius, float E) {
+    Prefilter f;
+    f.px = (float)px; f.py = (float)py; f.pz = (float)pz;
+    const float rf = (float)radius, m = 3.0f * E;
+    const float rin = rf - m, rout = rf + m;
+    f.rin2 = rin > 0.f ? rin * rin * (1.0f - 0x1p-19f) : -1.0f;
+    f.rout2 = rout * rout * (1.0f + 0x1p-19f);
+    return f;
+}
+
+// 1 inside, 0 outside, -1 undecided (run the f64 test)
+__device__ __forceinline__ int pref_point(const Prefilter &f, float4 q) {
+    const float ex = q.x - f.px, ey = q.y - f.py, ez = q.z - f.pz;
+    const float d2 = ex * ex + ey * ey + ez * ez;
+    return d2 < f.rin2 ? 1 : (d2 > f.rout2 ? 0 : -1);
+}
+
+__device__ __forceinline__ int pref_box(const Prefilter &f, float4 b) {
+    float d2 = 0.f;
+    const float p[3] = {f.px, f.py, f.pz}, c[3] = {b.x, b.y, b.z};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float lo = c[d] - b.w, hi = c[d] + b.w;
+        if (p[d] < lo) {
+            const float e = lo - p[d];
+            d2 += e * e;
+        } else if (p[d] > hi) {
+            const float e = p[d] - hi;
+            d2 += e * e;
+        }
+    }
+    return d2 < f.rin2 ? 1 : (d2 > f.rout2 ? 0 : -1);
+}
+
+__global__ void k_sph_f32copies(const TreeView tv, float4 *__restrict__ pos4, float4 *__restrict__ node4) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < tv.n) pos4[i] = make_float4((float)tv.sx[i], (float)tv.sy[i], (float)tv.sz[i], 0.f);
+    if (i < tv.nnodes)
+        node4[i] = make_float4((float)tv.bx[i], (float)tv.by[i], (float)tv.bz[i],
+                               (float)ldexp(tv.root_hw, -(int)tv.level[i]));
+}
+
 __global__ void k_gather_sph(size_t n, const uint32_t *__restrict__ perm, const uint8_t *__restrict__ ptype,
                              const double *__restrict__ vx, const double *__restrict__ vy,
                              const double *__restrict__ vz, const double *__restrict__ m,
@@ -139,14 +199,20 @@ __global__ void k_gather_sph(size_t n, const uint32_t *__restrict__ perm, const 
 
 // Ball query of one target (per-thread walk), used for the re-queries of the
 // density iteration.  Returns the number found (writes at most kmax).
-__device__ int ball_query_thread(const TreeView &tv, double px, double py, double pz, double radius,
-                                 uint32_t *row, int kmax) {
+__device__ int ball_query_thread(const TreeView &tv, const float4 *__restrict__ pos4,
+                                 const float4 *__restrict__ node4, float E, double px, double py, double pz,
+                                 double radius, uint32_t *row, int kmax) {
     const double r2 = radius * radius;
+    const Prefilter pf = prefilter(px, py, pz, radius, E);
     int count = 0;
     uint32_t k = 0;
     while ((size_t)k < tv.nnodes) {
-        const double hw = ldexp(tv.root_hw, -(int)tv.level[k]);
-        if (!sphere_hits_box(px, py, pz, radius, tv.bx[k], tv.by[k], tv.bz[k], hw)) {
+        int hit = pref_box(pf, node4[k]);
+        if (hit < 0) {
+            const double hw = ldexp(tv.root_hw, -(int)tv.level[k]);
+            hit = sphere_hits_box(px, py, pz, radius, tv.bx[k], tv.by[k], tv.bz[k], hw);
+        }
+        if (!hit) {
             k = tv.skip[k];
             continue;
         }
@@ -154,8 +220,12 @@ __device__ int ball_query_thread(const TreeView &tv, double px, double py, doubl
         if (nc > 0) {
             const uint32_t f = tv.first[k];
             for (uint32_t j = f; j < f + nc; ++j) {
-                const double dx = tv.sx[j] - px, dy = tv.sy[j] - py, dz = tv.sz[j] - pz;
-                if (dx * dx + dy * dy + dz * dz <= r2) {
+                int in = pref_point(pf, pos4[j]);
+                if (in < 0) {
+                    const double dx = tv.sx[j] - px, dy = tv.sy[j] - py, dz = tv.sz[j] - pz;
+                    in = dx * dx + dy * dy + dz * dz <= r2;
+                }
+                if (in) {
                     if (count < kmax) row[count] = j;
                     ++count;
                 }
@@ -170,7 +240,8 @@ __device__ int ball_query_thread(const TreeView &tv, double px, double py, doubl
 
 // Neighbour lists of all gas particles (build_neighbor_lists with factor):
 // warp-synchronous walk, each lane with its own next-node pointer.
-__global__ void __launch_bounds__(128) k_neighbors(const TreeView tv, const uint8_t *__restrict__ gas,
+__global__ void __launch_bounds__(128) k_neighbors(const TreeView tv, const float4 *__restrict__ pos4,
+                                                   const float4 *__restrict__ node4, const uint8_t *__restrict__ gas,
                                                    const double *__restrict__ sh, double factor, int kmax,
                                                    uint32_t *__restrict__ list, uint32_t *__restrict__ cnt,
                                                    unsigned *__restrict__ err) {
@@ -182,6 +253,7 @@ __global__ void __launch_bounds__(128) k_neighbors(const TreeView tv, const uint
         radius = 2.0 * sh[t] * factor;
     }
     const double r2 = radius * radius;
+    const Prefilter pf = prefilter(px, py, pz, radius, prefilter_scale(tv));
     uint32_t *row = list + t * (size_t)kmax;
     int count = 0;
     uint32_t next = active ? 0u : 0xFFFFFFFFu;
@@ -189,8 +261,12 @@ __global__ void __launch_bounds__(128) k_neighbors(const TreeView tv, const uint
         const uint32_t k = __reduce_min_sync(0xFFFFFFFFu, next);
         if ((size_t)k >= tv.nnodes) break;
         if (next != k) continue;
-        const double hw = ldexp(tv.root_hw, -(int)tv.level[k]);
-        if (!sphere_hits_box(px, py, pz, radius, tv.bx[k], tv.by[k], tv.bz[k], hw)) {
+        int hit = pref_box(pf, node4[k]);
+        if (hit < 0) {
+            const double hw = ldexp(tv.root_hw, -(int)tv.level[k]);
+            hit = sphere_hits_box(px, py, pz, radius, tv.bx[k], tv.by[k], tv.bz[k], hw);
+        }
+        if (!hit) {
             next = tv.skip[k];
             continue;
         }
@@ -198,8 +274,12 @@ __global__ void __launch_bounds__(128) k_neighbors(const TreeView tv, const uint
         if (nc > 0) {
             const uint32_t f = tv.first[k];
             for (uint32_t j = f; j < f + nc; ++j) {
-                const double dx = tv.sx[j] - px, dy = tv.sy[j] - py, dz = tv.sz[j] - pz;
-                if (dx * dx + dy * dy + dz * dz <= r2) {
+                int in = pref_point(pf, pos4[j]);
+                if (in < 0) {
+                    const double dx = tv.sx[j] - px, dy = tv.sy[j] - py, dz = tv.sz[j] - pz;
+                    in = dx * dx + dy * dy + dz * dz <= r2;
+                }
+                if (in) {
                     if (count < kmax) row[count] = j;
                     ++count;
                 }
@@ -216,7 +296,8 @@ __global__ void __launch_bounds__(128) k_neighbors(const TreeView tv, const uint
 }
 
 // compute_density (density.rs:42-125) for one target per thread, then the EOS.
-__global__ void k_density(const TreeView tv, const uint8_t *__restrict__ gas, const double *__restrict__ sm,
+__global__ void k_density(const TreeView tv, const float4 *__restrict__ pos4, const float4 *__restrict__ node4,
+                          const uint8_t *__restrict__ gas, const double *__restrict__ sm,
                           const double *__restrict__ su, double *__restrict__ sh, uint32_t *__restrict__ list,
                           uint32_t *__restrict__ cnt, int kmax, double gamma, double eta, double h_max,
                           double *__restrict__ rho_out, double *__restrict__ omega_out, double *__restrict__ pres,
@@ -257,7 +338,7 @@ __global__ void k_density(const TreeView tv, const uint8_t *__restrict__ gas, co
         const double search_radius = 2.0 * h * search_padding;
         if (2.0 * h_new > search_radius) {
             const double new_radius = 2.0 * h_new * search_padding;
-            count = ball_query_thread(tv, xi, yi, zi, new_radius, row, kmax);
+            count = ball_query_thread(tv, pos4, node4, prefilter_scale(tv), xi, yi, zi, new_radius, row, kmax);
             if (count > kmax) {
                 atomicOr(err, (unsigned)DERR_NEIGH_OVERFLOW);
                 count = kmax;
@@ -470,7 +551,7 @@ void sph_free(Ctx *c) {
     if (!s) return;
     DevBuf *all[] = {&s->list, &s->cnt, &s->gas, &s->sx, &s->sy, &s->sz, &s->svx, &s->svy, &s->svz, &s->sm,
                      &s->sh, &s->su, &s->salpha, &s->srho, &s->spres, &s->scs, &s->somega, &s->sdivv, &s->smaxmu,
-                     &s->sdalpha, &s->sax, &s->say, &s->saz, &s->sdu, &s->dtpart};
+                     &s->sdalpha, &s->sax, &s->say, &s->saz, &s->sdu, &s->dtpart, &s->pos4, &s->node4};
     for (DevBuf *b : all)
         if (b->ptr) cudaFree(b->ptr);
     delete s;
@@ -492,6 +573,9 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
     for (DevBuf *d : f64s) GVS_CUDA(c, ensure(c, *d, b8));
     GVS_CUDA(c, ensure(c, S->gas, n));
     GVS_CUDA(c, ensure(c, S->cnt, n * 4));
+    GVS_CUDA(c, ensure(c, S->pos4, n * 16));
+    GVS_CUDA(c, ensure(c, S->node4, tv.nnodes * 16));
+    k_sph_f32copies<<<nb(std::max(n, tv.nnodes)), 256, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4));
     k_gather_sph<<<nb(n), 256, 0, st>>>(n, tv.perm, as<uint8_t>(c->ptype), as<double>(c->vx), as<double>(c->vy),
                                         as<double>(c->vz), as<double>(c->m), as<double>(c->h), as<double>(c->u),
                                         as<double>(c->alpha), as<double>(c->rho), as<double>(c->pres),
@@ -508,9 +592,11 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
     for (int attempt = 0; attempt < 4; ++attempt) {
         GVS_CUDA(c, ensure(c, S->list, n * (size_t)S->kmax * 4));
         GVS_CUDA(c, cudaMemcpyAsync(S->sh.ptr, c->scratch_b.ptr, b8, cudaMemcpyDeviceToDevice, st));
-        k_neighbors<<<nb(n, 128), 128, 0, st>>>(tv, as<uint8_t>(S->gas), as<double>(S->sh), 1.1, S->kmax,
+        k_neighbors<<<nb(n, 128), 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4), as<uint8_t>(S->gas),
+                                                as<double>(S->sh), 1.1, S->kmax,
                                                 as<uint32_t>(S->list), as<uint32_t>(S->cnt), err_ptr(c));
-        k_density<<<nb(n, 128), 128, 0, st>>>(tv, as<uint8_t>(S->gas), as<double>(S->sm), as<double>(S->su),
+        k_density<<<nb(n, 128), 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4), as<uint8_t>(S->gas),
+                                              as<double>(S->sm), as<double>(S->su),
                                               as<double>(S->sh), as<uint32_t>(S->list), as<uint32_t>(S->cnt),
                                               S->kmax, prm->gamma, prm->eta, prm->h_max, as<double>(S->srho),
                                               as<double>(S->somega), as<double>(S->spres), as<double>(S->scs),
