@@ -412,35 +412,67 @@ def run_workload(a, d):
         theta = a.theta
         sph = G.SphSolver(ctx)
         import ctypes as C
-        ctx.set_state(p)
-        ctx._ck(ctx._lib.gvs_set_gas(ctx.h, *(G.engine._ptr(getattr(p, f)) for f in (
-            "density", "pressure", "internal_energy", "du_dt", "smoothing_length", "sound_speed", "alpha_visc"))))
-        ctx.compute_forces(G.ALGO_BH, G.PREC_FP32, eps, theta)
-        ctx._ck(ctx._lib.gvs_sph_compute(ctx.h, C.byref(sph.params), None, None, None, None))
-        dtc = C.c_double()
-        ctx._ck(ctx._lib.gvs_sph_timestep(ctx.h, C.byref(sph.params), C.byref(dtc)))
-        dt = dtc.value
+        gas_fields = ("density", "pressure", "internal_energy", "du_dt", "smoothing_length", "sound_speed",
+                      "alpha_visc")
 
-        def step(dt):
-            ctx._ck(ctx._lib.gvs_sph_step(ctx.h, C.byref(sph.params), G.ALGO_BH, G.PREC_FP32, eps, theta, dt,
-                                          C.byref(dtc)))
-            return min(dtc.value, 1.5 * dt)
+        def upload():
+            ctx.set_state(p)
+            ctx._ck(ctx._lib.gvs_set_gas(ctx.h, *(G.engine._ptr(getattr(p, f)) for f in gas_fields)))
 
-        for _ in range(a.warmup):
-            dt = step(dt)
-        ms = []
-        with Clocks(d.local) as clk:
-            for _ in range(a.steps):
-                ctx.l2_flush()
-                ctx.event(0)
+        def sph_only(prec):
+            """one SphSolver::compute on the initial state, SPH terms only"""
+            upload()
+            sph.params.precision = prec
+            ctx._ck(ctx._lib.gvs_sph_compute(ctx.h, C.byref(sph.params), None, None, None, None))
+            q = G.Particles(n)
+            ctx.get_state(q)
+            ctx.get_gas(q)
+            return q
+
+        def timed(prec):
+            upload()
+            sph.params.precision = prec
+            ctx.compute_forces(G.ALGO_BH, G.PREC_FP32, eps, theta)
+            ctx._ck(ctx._lib.gvs_sph_compute(ctx.h, C.byref(sph.params), None, None, None, None))
+            dtc = C.c_double()
+            ctx._ck(ctx._lib.gvs_sph_timestep(ctx.h, C.byref(sph.params), C.byref(dtc)))
+            dt = dtc.value
+
+            def step(dt):
+                ctx._ck(ctx._lib.gvs_sph_step(ctx.h, C.byref(sph.params), G.ALGO_BH, G.PREC_FP32, eps, theta, dt,
+                                              C.byref(dtc)))
+                return min(dtc.value, 1.5 * dt)
+
+            for _ in range(a.warmup):
                 dt = step(dt)
-                ctx.event(1)
-                ms.append(ctx.elapsed(0, 1))
-        t = sum(ms)
-        res.update({"value": n * a.steps / (t * 1e-3), "ms_per_step": t / a.steps, "dtype": "f64 SPH / f32 walk",
+            ms = []
+            with Clocks(d.local) as clk:
+                for _ in range(a.steps):
+                    ctx.l2_flush()
+                    ctx.event(0)
+                    dt = step(dt)
+                    ctx.event(1)
+                    ms.append(ctx.elapsed(0, 1))
+            return sum(ms), clk.summary()
+
+        qe, qm = sph_only(G.PREC_FP64_EXACT), sph_only(G.PREC_MIXED)
+
+        def rel(f):
+            x, y = getattr(qm, f), getattr(qe, f)
+            return float(np.sqrt(((x - y) ** 2).sum() / max((y ** 2).sum(), 1e-300)))
+
+        errs = {f: rel(f) for f in ("density", "smoothing_length", "ax", "ay", "az", "du_dt")}
+        t_ex, _ = timed(G.PREC_FP64_EXACT)
+        t, clk = timed(G.PREC_MIXED)
+        res.update({"value": n * a.steps / (t * 1e-3), "ms_per_step": t / a.steps,
+                    "dtype": "f32 SPH pair terms (mixed) / f64 state / f32 BH walk",
                     "config": {"workload": f"grad-h SPH + BH gravity, rho~1/r gas sphere N={n}, u=0.05, "
                                            f"Wendland C2, eta=1.2, theta={theta}, eps={eps:.3g}, CFL 0.3",
-                               "n": n}, "clocks": clk.summary()})
+                               "n": n},
+                    "f64_exact": {"value": n * a.steps / (t_ex * 1e-3), "ms_per_step": t_ex / a.steps,
+                                  "what": "the same steps with the reference's f64 SPH arithmetic"},
+                    "mixed_over_f64": t_ex / t,
+                    "mixed_vs_f64_rel_rms": errs, "clocks": clk})
     elif a.workload == "ensemble":
         from gravis_gb300.engine import plummer_ensemble
         sizes = G.ensemble_sizes(a.nsys, seed=2024)

@@ -36,13 +36,15 @@ class Diag(C.Structure):
 
 class SphParams(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("gamma", "eta", "cfl_factor", "force_factor", "h_max", "beta_visc",
-                                          "alpha_min", "alpha_max", "alpha_cond", "sigma_visc")]
+                                          "alpha_min", "alpha_max", "alpha_cond", "sigma_visc")] + \
+               [("precision", C.c_int)]
 
 
 class Profile(C.Structure):
     _fields_ = [("force_ms", C.c_double), ("force_launches", C.c_longlong), ("launches", C.c_longlong),
                 ("force_flops", C.c_double), ("force_bytes", C.c_double), ("tile_visits", C.c_double),
-                ("near_tile_visits", C.c_double), ("vjp_ms", C.c_double), ("vjp_launches", C.c_longlong)]
+                ("near_tile_visits", C.c_double), ("vjp_ms", C.c_double), ("vjp_launches", C.c_longlong),
+                ("sph_f64_redo", C.c_longlong)]
 
 
 _P = C.c_void_p  # every array argument is passed as a raw address

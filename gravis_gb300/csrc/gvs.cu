@@ -500,6 +500,7 @@ gvs_status gvs_sph_params_default(gvs_sph_params *p) {
     p->alpha_max = 2.0;     // forces.rs:36
     p->alpha_cond = 1.0;    // forces.rs:37
     p->sigma_visc = 0.1;    // forces.rs:38
+    p->precision = GVS_PREC_FP64_EXACT;
     return GVS_OK;
 }
 
@@ -509,6 +510,8 @@ static gvs_status check_sph(gvs_ctx *c, const gvs_sph_params *p) {
     if (!(p->gamma > 1.0) || !(p->eta > 0.0) || !(p->cfl_factor > 0.0) || !(p->force_factor > 0.0) ||
         !(p->alpha_min <= p->alpha_max))
         return fail(c, GVS_ERR_INVALID_ARG, "invalid SPH parameters");
+    if (p->precision != GVS_PREC_FP64_EXACT && p->precision != GVS_PREC_FP64 && p->precision != GVS_PREC_MIXED)
+        return fail(c, GVS_ERR_INVALID_ARG, "SPH precision must be FP64_EXACT, FP64 or MIXED");
     if (!c->has_gas) return fail(c, GVS_ERR_STATE, "no gas particles uploaded (ptype/u/h/alpha were NULL)");
     cudaSetDevice(c->device);
     return GVS_OK;
@@ -567,7 +570,7 @@ gvs_status gvs_profile_enable(gvs_ctx *c, int on) {
     c->prof.tile_visits = 0.0;
     c->prof.vjp_ms = 0.0;
     c->prof.vjp_launches = 0;
-    GVS_CUDA(c, cudaMemsetAsync(err_ptr(c) + 8, 0, sizeof(unsigned long long), c->stream));
+    GVS_CUDA(c, cudaMemsetAsync(err_ptr(c) + 8, 0, sizeof(unsigned long long) + sizeof(unsigned), c->stream));
     return GVS_OK;
 }
 
@@ -586,6 +589,9 @@ gvs_status gvs_profile_read(gvs_ctx *c, gvs_profile *out) {
     GVS_CUDA(c, cudaMemcpy(&nearc, err_ptr(c) + 8, sizeof nearc, cudaMemcpyDeviceToHost));
     out->near_tile_visits = (double)nearc;
     out->tile_visits = c->prof.tile_visits;
+    unsigned redo = 0;
+    GVS_CUDA(c, cudaMemcpy(&redo, err_ptr(c) + 10, sizeof redo, cudaMemcpyDeviceToHost));
+    out->sph_f64_redo = redo;
     return GVS_OK;
 }
 

@@ -19,6 +19,12 @@
 //               div v, max mu, d alpha / dt.
 //  timestep     SphSolver::compute_timestep (solver.rs:90-131), a min-reduction.
 //  step         step_with_sph (solver.rs:145-212).
+//
+// The neighbour search settles its box and distance tests with an f32
+// prefilter and runs the f64 test only near the boundary (lists unchanged).
+// GVS_PREC_MIXED (opt-in) moves the density and force pair terms to f32 on
+// float-float separations with compensated sums; the f64 pipe is a small
+// fraction of the f32 one on this part, and those kernels were bound by it.
 #include "gvs_internal.cuh"
 
 namespace gvs {
@@ -37,6 +43,7 @@ struct SphState {
     DevBuf srho, spres, scs, somega, sdivv, smaxmu, sdalpha, sax, say, saz, sdu;  // sorted outputs
     DevBuf dtpart;
     DevBuf pos4, node4;  // f32 copies for the neighbour-search prefilter
+    DevBuf a4, b4, c4, d4, e4, f4;  // mixed precision: packed sources (see k_sph_src_*)
     bool have_intermediates = false;
 };
 
@@ -295,6 +302,24 @@ __global__ void __launch_bounds__(128) k_neighbors(const TreeView tv, const floa
     }
 }
 
+// The two sums of one density iteration (density.rs:60-75), f64, in list order.
+__device__ __forceinline__ void density_sums_f64(const TreeView &tv, const double *__restrict__ sm,
+                                                 const uint32_t *row, int count, double xi, double yi, double zi,
+                                                 double h, double &rho, double &dws) {
+    rho = 0.0;
+    dws = 0.0;
+    for (int k = 0; k < count; ++k) {
+        const uint32_t j = row[k];
+        const double dx = xi - tv.sx[j], dy = yi - tv.sy[j], dz = zi - tv.sz[j];
+        const double r = sqrt(dx * dx + dy * dy + dz * dz);
+        if (r < 2.0 * h) {
+            const double mj = sm[j];
+            rho += mj * kw(r, h);
+            dws += mj * kdwdh(r, h);
+        }
+    }
+}
+
 // compute_density (density.rs:42-125) for one target per thread, then the EOS.
 __global__ void k_density(const TreeView tv, const float4 *__restrict__ pos4, const float4 *__restrict__ node4,
                           const uint8_t *__restrict__ gas, const double *__restrict__ sm,
@@ -314,17 +339,8 @@ __global__ void k_density(const TreeView tv, const float4 *__restrict__ pos4, co
     int count = (int)cnt[i];
     double rho_last = rho_out[i];
     for (int it = 0; it < 5; ++it) {
-        double rho = 0.0, dws = 0.0;
-        for (int k = 0; k < count; ++k) {
-            const uint32_t j = row[k];
-            const double dx = xi - tv.sx[j], dy = yi - tv.sy[j], dz = zi - tv.sz[j];
-            const double r = sqrt(dx * dx + dy * dy + dz * dz);
-            if (r < 2.0 * h) {
-                const double mj = sm[j];
-                rho += mj * kw(r, h);
-                dws += mj * kdwdh(r, h);
-            }
-        }
+        double rho, dws;
+        density_sums_f64(tv, sm, row, count, xi, yi, zi, h, rho, dws);
         const double h_new = rho > 0.0 ? fmin(eta * cbrt(m_i / rho), h_max) : fmin(h, h_max);
         if (rho > 0.0) {
             const double dh_drho = -h_new / (3.0 * rho);
@@ -441,6 +457,269 @@ __global__ void k_forces(const TreeView tv, const uint8_t *__restrict__ gas, con
     sdalpha[i] = -(alpha_i - prm.alpha_min) / tau + source;
 }
 
+
+// ---- mixed precision (GVS_PREC_MIXED): f32 pair arithmetic ------------------------------
+// Positions and velocities as f32 hi + lo (their f64 value to ~2^-48), so a
+// neighbour separation (x_i hi - x_j hi) + (x_i lo - x_j lo) is good to an f32
+// ulp of the separation itself.  Pair terms in f32 (explicit FMA), sums in f32
+// (hi, lo) with two-sum, kernel constants factored out and applied in f64 per
+// target.  The h iteration, Omega, EOS and the per-target epilogues stay f64.
+// This translation unit is built without FMA contraction; the f32 code below
+// asks for its FMAs explicitly.
+
+__device__ __forceinline__ void tsum(float &hi, float &lo, float v) {
+    const float s = __fadd_rn(hi, v);
+    const float bp = __fsub_rn(s, hi);
+    lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(v, bp)));
+    hi = s;
+}
+
+__device__ __forceinline__ void split_ff(double v, float &hi, float &lo) {
+    hi = __double2float_rn(v);
+    lo = __double2float_rn(v - (double)hi);
+}
+
+// sources for the mixed density: (x hi, y hi, z hi, m), (x lo, y lo, z lo, 0)
+__global__ void k_sph_src_pos(const TreeView tv, const double *__restrict__ sm, float4 *__restrict__ a,
+                              float4 *__restrict__ b) {
+    const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= tv.n) return;
+    float xh, xl, yh, yl, zh, zl;
+    split_ff(tv.sx[j], xh, xl);
+    split_ff(tv.sy[j], yh, yl);
+    split_ff(tv.sz[j], zh, zl);
+    a[j] = make_float4(xh, yh, zh, (float)sm[j]);
+    b[j] = make_float4(xl, yl, zl, 0.f);
+}
+
+// sources for the mixed forces (after the density pass):
+//   c = (vx hi, vy hi, vz hi, 1/h)  d = (vx lo, vy lo, vz lo, -5 norm / h^5)
+//   e = (h, max(rho, floor), P / (Omega rho^2), c)  f = (alpha, P, u, 0)
+__global__ void k_sph_src_hydro(size_t n, const double *__restrict__ svx, const double *__restrict__ svy,
+                                const double *__restrict__ svz, const double *__restrict__ sh,
+                                const double *__restrict__ srho, const double *__restrict__ spres,
+                                const double *__restrict__ scs, const double *__restrict__ salpha,
+                                const double *__restrict__ somega, const double *__restrict__ su,
+                                float4 *__restrict__ c4, float4 *__restrict__ d4, float4 *__restrict__ e4,
+                                float4 *__restrict__ f4) {
+    const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    float vxh, vxl, vyh, vyl, vzh, vzl;
+    split_ff(svx[j], vxh, vxl);
+    split_ff(svy[j], vyh, vyl);
+    split_ff(svz[j], vzh, vzl);
+    const double h = sh[j];
+    const double rho = fmax(srho[j], 1e-10);
+    const double p = spres[j];
+    const double por2 = rho > 0.0 ? p / (somega[j] * rho * rho) : 0.0;
+    const double h2 = h * h;
+    c4[j] = make_float4(vxh, vyh, vzh, (float)(1.0 / h));
+    d4[j] = make_float4(vxl, vyl, vzl, (float)(-5.0 * norm3d() / (h2 * h2 * h)));
+    e4[j] = make_float4((float)h, (float)rho, (float)por2, (float)scs[j]);
+    f4[j] = make_float4((float)salpha[j], (float)p, (float)su[j], 0.f);
+}
+
+// Mixed sums of one density iteration: S1 = sum m f(q), S2 = sum m (5 q^2 s^3 - 3 f(q))
+// with f(q) = s^4 (1 + 2q), s = 1 - q/2; rho = norm/h^3 S1, dW/dh sum = norm/h^4 S2.
+__device__ __forceinline__ void density_sums_mixed(const float4 *__restrict__ a4, const float4 *__restrict__ b4,
+                                                   const uint32_t *row, int count, float4 pa, float4 pb, float ih,
+                                                   double &s1, double &s2) {
+    float h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;
+    for (int k = 0; k < count; ++k) {
+        const uint32_t j = row[k];
+        const float4 a = a4[j], b = b4[j];
+        const float dx = __fadd_rn(__fsub_rn(pa.x, a.x), __fsub_rn(pb.x, b.x));
+        const float dy = __fadd_rn(__fsub_rn(pa.y, a.y), __fsub_rn(pb.y, b.y));
+        const float dz = __fadd_rn(__fsub_rn(pa.z, a.z), __fsub_rn(pb.z, b.z));
+        const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+        const float r = d2 > 0.f ? __fmul_rn(d2, rsqrt_approx(d2)) : 0.f;
+        const float q = __fmul_rn(r, ih);
+        if (q < 2.0f) {
+            const float sq = __fmaf_rn(-0.5f, q, 1.0f);
+            const float s2q = __fmul_rn(sq, sq), s3 = __fmul_rn(s2q, sq);
+            const float f = __fmul_rn(__fmul_rn(s2q, s2q), __fmaf_rn(2.0f, q, 1.0f));
+            const float g = __fmaf_rn(5.0f * q * q, s3, -3.0f * f);
+            tsum(h1, l1, __fmul_rn(a.w, f));
+            tsum(h2, l2, __fmul_rn(a.w, g));
+        }
+    }
+    s1 = (double)h1 + (double)l1;
+    s2 = (double)h2 + (double)l2;
+}
+
+// compute_density with mixed sums.  A decision of the h iteration that lies
+// within 1e-6 of its threshold (convergence at 1e-3, re-query at a ratio of
+// 1.1) is taken again on the f64 sums of that iteration, so the iteration
+// path is the f64 one.
+__global__ void k_density_mixed(const TreeView tv, const float4 *__restrict__ pos4, const float4 *__restrict__ node4,
+                                const float4 *__restrict__ a4, const float4 *__restrict__ b4,
+                                const uint8_t *__restrict__ gas, const double *__restrict__ sm,
+                                const double *__restrict__ su, double *__restrict__ sh, uint32_t *__restrict__ list,
+                                uint32_t *__restrict__ cnt, int kmax, double gamma, double eta, double h_max,
+                                double *__restrict__ rho_out, double *__restrict__ omega_out,
+                                double *__restrict__ pres, double *__restrict__ cs, unsigned *__restrict__ err,
+                                unsigned *__restrict__ f64_redo) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= tv.n) return;
+    omega_out[i] = 1.0;
+    if (!gas[i]) return;
+    const double search_padding = 1.1;
+    const double xi = tv.sx[i], yi = tv.sy[i], zi = tv.sz[i];
+    const float4 pa = a4[i], pb = b4[i];
+    const double m_i = sm[i];
+    double h = sh[i];
+    uint32_t *row = list + i * (size_t)kmax;
+    int count = (int)cnt[i];
+    double rho_last = rho_out[i];
+    unsigned redo = 0;
+    for (int it = 0; it < 5; ++it) {
+        double s1, s2;
+        density_sums_mixed(a4, b4, row, count, pa, pb, (float)(1.0 / h), s1, s2);
+        const double nh3 = norm3d() / (h * h * h);
+        double rho = nh3 * s1, dws = nh3 / h * s2;
+        double h_new = rho > 0.0 ? fmin(eta * cbrt(m_i / rho), h_max) : fmin(h, h_max);
+        const double ratio = fabs(h_new - h) / fmax(h, 1e-30);
+        if (fabs(ratio - 1e-3) < 1e-6 || fabs(h_new / h - search_padding) < 1e-6) {
+            density_sums_f64(tv, sm, row, count, xi, yi, zi, h, rho, dws);
+            h_new = rho > 0.0 ? fmin(eta * cbrt(m_i / rho), h_max) : fmin(h, h_max);
+            ++redo;
+        }
+        if (rho > 0.0) {
+            const double dh_drho = -h_new / (3.0 * rho);
+            double om = 1.0 - dh_drho * dws;
+            if (om < 0.1) om = 0.1;
+            omega_out[i] = om;
+        }
+        rho_last = rho;
+        sh[i] = h_new;
+        if (fabs(h_new - h) / fmax(h, 1e-30) < 1e-3) break;
+        const double search_radius = 2.0 * h * search_padding;
+        if (2.0 * h_new > search_radius) {
+            const double new_radius = 2.0 * h_new * search_padding;
+            count = ball_query_thread(tv, pos4, node4, prefilter_scale(tv), xi, yi, zi, new_radius, row, kmax);
+            if (count > kmax) {
+                atomicOr(err, (unsigned)DERR_NEIGH_OVERFLOW);
+                count = kmax;
+            }
+            cnt[i] = (uint32_t)count;
+        }
+        h = h_new;
+    }
+    if (redo) atomicAdd(f64_redo, redo);
+    rho_out[i] = rho_last;
+    const double u = su[i];
+    pres[i] = (gamma - 1.0) * rho_last * u;
+    cs[i] = sqrt(gamma * (gamma - 1.0) * fmax(u, 0.0));
+}
+
+// compute_forces (forces.rs:69-232) with f32 pair terms.  With q/r = 1/h the
+// kernel gradient is dx * K(h) s^3, K(h) = -5 norm / h^5, and |grad W| =
+// -K(h) s^3 r.
+__global__ void __launch_bounds__(128) k_forces_mixed(
+    size_t n, const uint8_t *__restrict__ gas, const uint32_t *__restrict__ list, const uint32_t *__restrict__ cnt,
+    int kmax, const float4 *__restrict__ a4, const float4 *__restrict__ b4, const float4 *__restrict__ c4,
+    const float4 *__restrict__ d4, const float4 *__restrict__ e4, const float4 *__restrict__ f4,
+    const double *__restrict__ sh, const double *__restrict__ srho, const double *__restrict__ scs,
+    const double *__restrict__ salpha, gvs_sph_params prm, double *__restrict__ sax, double *__restrict__ say,
+    double *__restrict__ saz, double *__restrict__ sdu, double *__restrict__ sdivv, double *__restrict__ smaxmu,
+    double *__restrict__ sdalpha) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    sdivv[i] = 0.0;
+    smaxmu[i] = 0.0;
+    sdalpha[i] = 0.0;
+    sax[i] = say[i] = saz[i] = sdu[i] = 0.0;
+    if (!gas[i]) return;
+    const float4 pa = a4[i], pb = b4[i], pc = c4[i], pd = d4[i], pe = e4[i], pf = f4[i];
+    const float hi_f = pe.x, ih_i = pc.w, K_i = pd.w, rho_i = pe.y, por2_i = pe.z, c_i = pe.w;
+    const float alpha_i = pf.x, p_i = pf.y, u_i = pf.z;
+    const float beta = (float)prm.beta_visc, acond = (float)prm.alpha_cond;
+    const float cnorm5 = (float)(-5.0 * norm3d() * 32.0);  // K(h_avg) = cnorm5 / (hi + hj)^5
+    float axh = 0.f, axl = 0.f, ayh = 0.f, ayl = 0.f, azh = 0.f, azl = 0.f, duh = 0.f, dul = 0.f, dvh = 0.f,
+          dvl = 0.f, mmu = 0.f;
+    const uint32_t *row = list + i * (size_t)kmax;
+    const int count = (int)cnt[i];
+    for (int k = 0; k < count; ++k) {
+        const uint32_t j = row[k];
+        if ((size_t)j == i) continue;
+        const float4 a = a4[j], b = b4[j];
+        const float dx = __fadd_rn(__fsub_rn(pa.x, a.x), __fsub_rn(pb.x, b.x));
+        const float dy = __fadd_rn(__fsub_rn(pa.y, a.y), __fsub_rn(pb.y, b.y));
+        const float dz = __fadd_rn(__fsub_rn(pa.z, a.z), __fsub_rn(pb.z, b.z));
+        const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+        const float r = d2 > 0.f ? __fmul_rn(d2, rsqrt_approx(d2)) : 0.f;
+        const float4 e = e4[j];
+        const float hj = e.x;
+        if (r >= 2.0f * hi_f && r >= 2.0f * hj) continue;
+        const float4 c = c4[j], d = d4[j], f = f4[j];
+        const float mj = a.w;
+        const float dvx = __fadd_rn(__fsub_rn(pc.x, c.x), __fsub_rn(pd.x, d.x));
+        const float dvy = __fadd_rn(__fsub_rn(pc.y, c.y), __fsub_rn(pd.y, d.y));
+        const float dvz = __fadd_rn(__fsub_rn(pc.z, c.z), __fsub_rn(pd.z, d.z));
+        const float vr = __fmaf_rn(dvz, dz, __fmaf_rn(dvy, dy, __fmul_rn(dvx, dx)));
+        // kernel-gradient scalars (gradient = scalar * (dx, dy, dz)); zero at r = 0 or q >= 2
+        float fi = 0.f, fj = 0.f, fa = 0.f, sa3 = 0.f, Ka = 0.f;
+        const float hsum = __fadd_rn(hi_f, hj);
+        const float h_avg = 0.5f * hsum;
+        if (r >= 1e-30f) {
+            const float qi = __fmul_rn(r, ih_i), qj = __fmul_rn(r, c.w);
+            if (qi < 2.0f) { const float s = __fmaf_rn(-0.5f, qi, 1.0f); fi = __fmul_rn(K_i, __fmul_rn(__fmul_rn(s, s), s)); }
+            if (qj < 2.0f) { const float s = __fmaf_rn(-0.5f, qj, 1.0f); fj = __fmul_rn(d.w, __fmul_rn(__fmul_rn(s, s), s)); }
+            const float iha = __frcp_rn(h_avg);
+            const float qa = __fmul_rn(r, iha);
+            if (qa < 2.0f) {
+                const float s = __fmaf_rn(-0.5f, qa, 1.0f);
+                const float ih = __frcp_rn(hsum), ih2 = __fmul_rn(ih, ih);
+                Ka = __fmul_rn(cnorm5, __fmul_rn(__fmul_rn(ih2, ih2), ih));
+                sa3 = __fmul_rn(__fmul_rn(s, s), s);
+                fa = __fmul_rn(Ka, sa3);
+            }
+        }
+        const float rho_j = e.y, por2_j = e.z, c_j = e.w, alpha_j = f.x, p_j = f.y, u_j = f.z;
+        float pi_ij = 0.f;
+        if (vr < 0.f) {
+            const float alpha_avg = 0.5f * __fadd_rn(alpha_i, alpha_j);
+            const float c_avg = 0.5f * __fadd_rn(c_i, c_j);
+            const float rho_avg = 0.5f * __fadd_rn(rho_i, rho_j);
+            const float eta2 = 0.01f * __fmul_rn(h_avg, h_avg);
+            const float mu = __fdiv_rn(__fmul_rn(h_avg, vr), __fadd_rn(d2, eta2));
+            mmu = fmaxf(mmu, fabsf(mu));
+            if (rho_avg > 0.f)
+                pi_ij = __fdiv_rn(__fmaf_rn(beta * mu, mu, -__fmul_rn(__fmul_rn(alpha_avg, c_avg), mu)), rho_avg);
+        }
+        const float t = __fmul_rn(mj, __fmaf_rn(pi_ij, fa, __fmaf_rn(por2_j, fj, __fmul_rn(por2_i, fi))));
+        tsum(axh, axl, -__fmul_rn(t, dx));
+        tsum(ayh, ayl, -__fmul_rn(t, dy));
+        tsum(azh, azl, -__fmul_rn(t, dz));
+        const float vgi = __fmul_rn(fi, vr), vga = __fmul_rn(fa, vr);
+        float du = __fmul_rn(mj, __fmaf_rn(0.5f * pi_ij, vga, __fmul_rn(por2_i, vgi)));
+        if (acond > 0.f) {
+            const float rho_sum = __fadd_rn(rho_i, rho_j);
+            if (rho_sum > 0.f) {
+                const float v_sig = sqrtf(__fdiv_rn(fabsf(__fsub_rn(p_i, p_j)), 0.5f * rho_sum));
+                const float abs_gw = -__fmul_rn(__fmul_rn(Ka, sa3), r);
+                du = __fmaf_rn(__fmul_rn(mj, acond), __fmul_rn(__fdiv_rn(__fmul_rn(v_sig, __fsub_rn(u_i, u_j)), rho_sum), abs_gw), du);
+            }
+        }
+        tsum(duh, dul, du);
+        tsum(dvh, dvl, -__fmul_rn(mj, vgi));
+    }
+    sax[i] = (double)axh + (double)axl;
+    say[i] = (double)ayh + (double)ayl;
+    saz[i] = (double)azh + (double)azl;
+    sdu[i] = (double)duh + (double)dul;
+    const double rho_i64 = fmax(srho[i], 1e-10);
+    const double dva = (double)dvh + (double)dvl;
+    double dv = 0.0;
+    if (rho_i64 > 0.0) dv = dva / rho_i64;
+    sdivv[i] = dv;
+    smaxmu[i] = (double)mmu;
+    const double hi = sh[i], ci = scs[i], al = salpha[i];
+    const double tau = ci > 0.0 ? hi / (2.0 * prm.sigma_visc * ci) : 1e10;
+    const double source = fmax(-dv, 0.0) * (prm.alpha_max - al);
+    sdalpha[i] = -(al - prm.alpha_min) / tau + source;
+}
+
 // Sorted results back to caller order; a and du/dt are accumulated.
 __global__ void k_scatter_sph(size_t n, const uint32_t *__restrict__ perm, const uint8_t *__restrict__ gas,
                               const double *__restrict__ srho, const double *__restrict__ sh,
@@ -551,7 +830,8 @@ void sph_free(Ctx *c) {
     if (!s) return;
     DevBuf *all[] = {&s->list, &s->cnt, &s->gas, &s->sx, &s->sy, &s->sz, &s->svx, &s->svy, &s->svz, &s->sm,
                      &s->sh, &s->su, &s->salpha, &s->srho, &s->spres, &s->scs, &s->somega, &s->sdivv, &s->smaxmu,
-                     &s->sdalpha, &s->sax, &s->say, &s->saz, &s->sdu, &s->dtpart, &s->pos4, &s->node4};
+                     &s->sdalpha, &s->sax, &s->say, &s->saz, &s->sdu, &s->dtpart, &s->pos4, &s->node4,
+                     &s->a4, &s->b4, &s->c4, &s->d4, &s->e4, &s->f4};
     for (DevBuf *b : all)
         if (b->ptr) cudaFree(b->ptr);
     delete s;
@@ -576,6 +856,11 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
     GVS_CUDA(c, ensure(c, S->pos4, n * 16));
     GVS_CUDA(c, ensure(c, S->node4, tv.nnodes * 16));
     k_sph_f32copies<<<nb(std::max(n, tv.nnodes)), 256, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4));
+    const bool mixed = prm->precision == GVS_PREC_MIXED;
+    if (mixed) {
+        DevBuf *f4s[] = {&S->a4, &S->b4, &S->c4, &S->d4, &S->e4, &S->f4};
+        for (DevBuf *d : f4s) GVS_CUDA(c, ensure(c, *d, n * 16));
+    }
     k_gather_sph<<<nb(n), 256, 0, st>>>(n, tv.perm, as<uint8_t>(c->ptype), as<double>(c->vx), as<double>(c->vy),
                                         as<double>(c->vz), as<double>(c->m), as<double>(c->h), as<double>(c->u),
                                         as<double>(c->alpha), as<double>(c->rho), as<double>(c->pres),
@@ -589,18 +874,29 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
     // overflow rerun must start again from the same h
     GVS_CUDA(c, ensure(c, c->scratch_b, b8));
     GVS_CUDA(c, cudaMemcpyAsync(c->scratch_b.ptr, S->sh.ptr, b8, cudaMemcpyDeviceToDevice, st));
+    if (mixed) {
+        k_sph_src_pos<<<nb(n), 256, 0, st>>>(tv, as<double>(S->sm), as<float4>(S->a4), as<float4>(S->b4));
+        c->prof.launches += 1;
+    }
     for (int attempt = 0; attempt < 4; ++attempt) {
         GVS_CUDA(c, ensure(c, S->list, n * (size_t)S->kmax * 4));
         GVS_CUDA(c, cudaMemcpyAsync(S->sh.ptr, c->scratch_b.ptr, b8, cudaMemcpyDeviceToDevice, st));
         k_neighbors<<<nb(n, 128), 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4), as<uint8_t>(S->gas),
                                                 as<double>(S->sh), 1.1, S->kmax,
                                                 as<uint32_t>(S->list), as<uint32_t>(S->cnt), err_ptr(c));
-        k_density<<<nb(n, 128), 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4), as<uint8_t>(S->gas),
-                                              as<double>(S->sm), as<double>(S->su),
-                                              as<double>(S->sh), as<uint32_t>(S->list), as<uint32_t>(S->cnt),
-                                              S->kmax, prm->gamma, prm->eta, prm->h_max, as<double>(S->srho),
-                                              as<double>(S->somega), as<double>(S->spres), as<double>(S->scs),
-                                              err_ptr(c));
+        if (mixed)
+            k_density_mixed<<<nb(n, 128), 128, 0, st>>>(
+                tv, as<float4>(S->pos4), as<float4>(S->node4), as<float4>(S->a4), as<float4>(S->b4),
+                as<uint8_t>(S->gas), as<double>(S->sm), as<double>(S->su), as<double>(S->sh), as<uint32_t>(S->list),
+                as<uint32_t>(S->cnt), S->kmax, prm->gamma, prm->eta, prm->h_max, as<double>(S->srho),
+                as<double>(S->somega), as<double>(S->spres), as<double>(S->scs), err_ptr(c), err_ptr(c) + 10);
+        else
+            k_density<<<nb(n, 128), 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4), as<uint8_t>(S->gas),
+                                                  as<double>(S->sm), as<double>(S->su),
+                                                  as<double>(S->sh), as<uint32_t>(S->list), as<uint32_t>(S->cnt),
+                                                  S->kmax, prm->gamma, prm->eta, prm->h_max, as<double>(S->srho),
+                                                  as<double>(S->somega), as<double>(S->spres), as<double>(S->scs),
+                                                  err_ptr(c));
         c->prof.launches += 2;
         GVS_TRY(check_launch(c, "sph neighbours/density"));
         unsigned flags = 0;
@@ -614,13 +910,28 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
         if (attempt == 3) return fail(c, GVS_ERR_DEVICE, "SPH neighbour rows overflow at kmax=%d", S->kmax);
         S->kmax *= 2;
     }
-    k_forces<<<nb(n, 128), 128, 0, st>>>(tv, as<uint8_t>(S->gas), as<uint32_t>(S->list), as<uint32_t>(S->cnt),
+    if (mixed) {
+        k_sph_src_hydro<<<nb(n), 256, 0, st>>>(n, as<double>(S->svx), as<double>(S->svy), as<double>(S->svz),
+                                               as<double>(S->sh), as<double>(S->srho), as<double>(S->spres),
+                                               as<double>(S->scs), as<double>(S->salpha), as<double>(S->somega),
+                                               as<double>(S->su), as<float4>(S->c4), as<float4>(S->d4),
+                                               as<float4>(S->e4), as<float4>(S->f4));
+        k_forces_mixed<<<nb(n, 128), 128, 0, st>>>(
+            n, as<uint8_t>(S->gas), as<uint32_t>(S->list), as<uint32_t>(S->cnt), S->kmax, as<float4>(S->a4),
+            as<float4>(S->b4), as<float4>(S->c4), as<float4>(S->d4), as<float4>(S->e4), as<float4>(S->f4),
+            as<double>(S->sh), as<double>(S->srho), as<double>(S->scs), as<double>(S->salpha), *prm,
+            as<double>(S->sax), as<double>(S->say), as<double>(S->saz), as<double>(S->sdu), as<double>(S->sdivv),
+            as<double>(S->smaxmu), as<double>(S->sdalpha));
+        c->prof.launches += 1;
+    } else {
+        k_forces<<<nb(n, 128), 128, 0, st>>>(tv, as<uint8_t>(S->gas), as<uint32_t>(S->list), as<uint32_t>(S->cnt),
                                          S->kmax, as<double>(S->svx), as<double>(S->svy), as<double>(S->svz),
                                          as<double>(S->sm), as<double>(S->sh), as<double>(S->srho),
                                          as<double>(S->spres), as<double>(S->su), as<double>(S->scs),
                                          as<double>(S->salpha), as<double>(S->somega), *prm, as<double>(S->sax),
                                          as<double>(S->say), as<double>(S->saz), as<double>(S->sdu),
                                          as<double>(S->sdivv), as<double>(S->smaxmu), as<double>(S->sdalpha));
+    }
     k_scatter_sph<<<nb(n), 256, 0, st>>>(n, tv.perm, as<uint8_t>(S->gas), as<double>(S->srho), as<double>(S->sh),
                                          as<double>(S->spres), as<double>(S->scs), as<double>(S->somega),
                                          as<double>(S->sax), as<double>(S->say), as<double>(S->saz),

@@ -263,7 +263,8 @@ class Context:
         self._ck(self._lib.gvs_profile_read(self.h, C.byref(pr)))
         return {"force_ms": pr.force_ms, "force_launches": pr.force_launches, "launches": pr.launches,
                 "force_flops": pr.force_flops, "force_bytes": pr.force_bytes, "tile_visits": pr.tile_visits,
-                "near_tile_visits": pr.near_tile_visits, "vjp_ms": pr.vjp_ms, "vjp_launches": pr.vjp_launches}
+                "near_tile_visits": pr.near_tile_visits, "vjp_ms": pr.vjp_ms, "vjp_launches": pr.vjp_launches,
+                "sph_f64_redo": pr.sph_f64_redo}
 
     def event(self, slot: int):
         self._ck(self._lib.gvs_event_record(self.h, slot))

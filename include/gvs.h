@@ -70,6 +70,11 @@ typedef struct gvs_diag {
 typedef struct gvs_sph_params {
     double gamma, eta, cfl_factor, force_factor, h_max;
     double beta_visc, alpha_min, alpha_max, alpha_cond, sigma_visc;
+    /* GVS_PREC_FP64_EXACT (default): the reference's f64 arithmetic, statement by
+     * statement.  GVS_PREC_MIXED (no reference counterpart): density and force pair
+     * terms in f32 on float-float separations with compensated sums; neighbour lists,
+     * the h iteration's decisions, Omega, EOS and the epilogues stay the f64 ones. */
+    int precision;
 } gvs_sph_params;
 
 /* Kernel-time counters of one context (CUDA events on the context stream). */
@@ -84,6 +89,7 @@ typedef struct gvs_profile {
     double near_tile_visits;  /* of which took the float-float near-field path */
     double vjp_ms;            /* device time of the fused force + VJP kernels (adjoint) */
     long long vjp_launches;
+    long long sph_f64_redo;   /* mixed SPH: h-iteration steps redone on f64 sums (borderline) */
 } gvs_profile;
 
 /* ---- library / context ---------------------------------------------------- */

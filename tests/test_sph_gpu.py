@@ -184,3 +184,61 @@ def test_evrard_energy(ctx):
     assert abs(d1.total_energy - d0.total_energy) / abs(d0.total_energy) < 0.05
     assert d1.kinetic_energy > 2.0 * d0.kinetic_energy
     assert d1.thermal_energy > d0.thermal_energy
+
+
+# ---- mixed precision (GVS_PREC_MIXED) ---------------------------------------------------
+# Pair terms in f32 on float-float separations with compensated sums.  Bars: the
+# neighbour lists are still the reference's; rho, h, Omega, P, c, accelerations,
+# du/dt, div v and d alpha/dt within 1e-6 relative RMS of the reference (measured
+# 0.3-5e-7: every f32 pair term carries ~2^-22 relative error, and the sums are
+# compensated).
+
+@pytest.mark.parametrize("name", list(cases().keys()))
+def test_sph_mixed_matches_oracle(ctx, name):
+    p = cases()[name]
+    q = to_oracle(p)
+    sph = G.SphSolver(ctx)
+    sph.params.precision = G.PREC_MIXED
+    inter = sph.compute(p)
+    s = O.Sph()
+    s.compute(q)
+    n = p.count
+    start, count, idx = sph.neighbors()
+    ostart, oend, oidx = s.neighbor_lists(n)
+    for i in range(n):
+        assert np.array_equal(idx[start[i]: start[i] + count[i]], oidx[ostart[i]: oend[i]]), (name, i)
+    errs = {}
+    for a, b in (("density", "density"), ("smoothing_length", "h"), ("pressure", "pressure"),
+                 ("sound_speed", "cs")):
+        errs[a] = rel(getattr(p, a), getattr(q, b))
+    errs["omega"] = rel(inter.omega, s.array("omega", n))
+    for a in ("ax", "ay", "az", "du_dt"):
+        errs[a] = rel(getattr(p, a), getattr(q, a))
+    errs["div_v"] = rel(inter.div_v, s.array("div_v", n))
+    errs["dalpha_dt"] = rel(inter.dalpha_dt, s.array("dalpha_dt", n))
+    print(name, {k: f"{v:.1e}" for k, v in errs.items()})
+    for k in ("density", "smoothing_length", "pressure", "sound_speed", "omega"):
+        assert errs[k] <= 1e-6, (name, k, errs[k])
+    for k in ("ax", "ay", "az", "du_dt", "div_v", "dalpha_dt"):
+        assert errs[k] <= 1e-6, (name, k, errs[k])
+
+
+def test_sph_mixed_steps_track_f64(ctx):
+    """Five mixed step_with_sph steps stay within 1e-6 of the f64 ones (positions,
+    velocities, u, rho) on the Evrard collapse."""
+    runs = []
+    for prec in (G.PREC_FP64_EXACT, G.PREC_MIXED):
+        p = G.EvrardCollapse(1000, seed=42).generate()
+        eps = G.EvrardCollapse(1000).suggested_softening()
+        grav = G.BruteForce(eps, G.PREC_FP64_EXACT, ctx)
+        sph = G.SphSolver(ctx)
+        sph.params.precision = prec
+        grav.compute_accelerations(p)
+        sph.compute(p)
+        dt = 1e-3
+        for _ in range(5):
+            G.step_with_sph(p, grav, sph, dt)
+        runs.append(p)
+    a, b = runs
+    for f in ("x", "vx", "internal_energy", "density"):
+        assert rel(getattr(b, f), getattr(a, f)) <= 1e-6, (f, rel(getattr(b, f), getattr(a, f)))
