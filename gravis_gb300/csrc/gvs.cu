@@ -27,6 +27,7 @@ cudaError_t ensure(Ctx *c, DevBuf &b, size_t bytes) {
         b.bytes = 0;
     }
     size_t want = std::max<size_t>(bytes, 256);
+    c->alloc_gen++;
     cudaError_t e = cudaMalloc(&b.ptr, want);
     if (e != cudaSuccess) {
         b.ptr = nullptr;
@@ -130,6 +131,68 @@ using namespace gvs;
 
 struct gvs_ctx : public Ctx {};
 
+struct StepGraphKey {
+    int precision;
+    double eps, dt;
+    size_t n;
+    Tune tune;
+};
+
+static bool sgraph_valid(Ctx *c, const StepGraphKey &k) {
+    const auto &g = c->sgraph;
+    return g.exec && g.precision == k.precision && g.eps == k.eps && g.dt == k.dt && g.n == k.n &&
+           g.gen == c->alloc_gen && g.nt == k.tune.nthreads && g.ipt == k.tune.ipt && g.minb == k.tune.minb &&
+           g.unroll == k.tune.unroll;
+}
+
+// Captures one kdk_one into c->sgraph; on a capture error the context stays eager.
+static gvs_status sgraph_capture(Ctx *c, const StepGraphKey &k, int algo, double theta) {
+    auto &g = c->sgraph;
+    if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
+    const unsigned long long gen0 = c->alloc_gen;
+    const long long l0 = c->prof.launches;
+    const long long step0 = c->step_counter;
+    const unsigned long long pv0 = c->pos_version;
+    if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        g.disabled = true;
+        return GVS_OK;
+    }
+    const gvs_status st = kdk_one(c, algo, k.precision, k.eps, theta, k.dt);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    // the captured step has not run: undo its host-side bookkeeping
+    g.launches = c->prof.launches - l0;
+    c->prof.launches = l0;
+    c->step_counter = step0;
+    c->pos_version = pv0;
+    if (st != GVS_OK || e != cudaSuccess || c->alloc_gen != gen0) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        g.disabled = true;  // the eager loop takes over
+        return GVS_OK;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+        g.exec = nullptr;
+        cudaGetLastError();
+        g.disabled = true;
+        return GVS_OK;
+    }
+    g.precision = k.precision;
+    g.eps = k.eps;
+    g.dt = k.dt;
+    g.n = k.n;
+    g.gen = c->alloc_gen;
+    // the shape the step ran with (the per-n autotune choice may have replaced c->tune)
+    g.nt = c->tune.nthreads;
+    g.ipt = c->tune.ipt;
+    g.minb = c->tune.minb;
+    g.unroll = c->tune.unroll;
+    return GVS_OK;
+}
+
 static gvs_status check_ctx(const gvs_ctx *ctx) {
     if (!ctx) {
         snprintf(g_last_error, sizeof g_last_error, "null context");
@@ -179,6 +242,7 @@ gvs_status gvs_destroy(gvs_ctx *c) {
     if (!c) return GVS_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->sgraph.exec) cudaGraphExecDestroy(c->sgraph.exec);
     tree_free(c);
     sph_free(c);
     adj_free(c);
@@ -386,7 +450,29 @@ gvs_status gvs_kdk_steps(gvs_ctx *c, int algo, int precision, double eps, double
     GVS_TRY(check_prec_algo(c, algo, precision, eps, theta));
     if (!(dt > 0.0) || nsteps < 0) return fail(c, GVS_ERR_INVALID_ARG, "dt must be > 0 and nsteps >= 0");
     cudaSetDevice(c->device);
-    for (long long s = 0; s < nsteps; ++s) {
+    // Direct-sum steps replay one captured step: the step is a fixed chain of
+    // kernels with no host synchronisation (unless kernel timing is on).
+    const bool graph = algo == GVS_ALGO_DIRECT && !c->prof.on && c->fault_kind == 0 && !c->sgraph.disabled &&
+                       nsteps >= 2;
+    long long s = 0;
+    if (graph) {
+        StepGraphKey key{precision, eps, dt, c->n, c->tune};
+        if (!sgraph_valid(c, key)) {
+            GVS_TRY(kdk_one(c, algo, precision, eps, theta, dt));  // allocates what the step needs
+            ++s;
+            GVS_TRY(sgraph_capture(c, key, algo, theta));
+        }
+        if (c->sgraph.exec) {
+            for (; s < nsteps; ++s) {
+                GVS_CUDA(c, cudaGraphLaunch(c->sgraph.exec, c->stream));
+                c->prof.launches += c->sgraph.launches;
+                c->step_counter++;
+                c->pos_version++;
+            }
+            return GVS_OK;
+        }
+    }
+    for (; s < nsteps; ++s) {
         if (nan_fault_due(c)) return fail(c, GVS_ERR_INJECTED, "injected non-finite fault at step %lld", s);
         GVS_TRY(kdk_one(c, algo, precision, eps, theta, dt));
     }

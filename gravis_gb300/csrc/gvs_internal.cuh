@@ -97,6 +97,20 @@ struct Ctx {
 
     Prof prof;
     Tune tune;
+    unsigned long long alloc_gen = 0;  // bumped whenever ensure() (re)allocates a buffer
+
+    // One direct-sum KDK step captured as a CUDA graph, replayed by gvs_kdk_steps.
+    // Valid while the step's parameters, n, the kernel shape and every buffer
+    // address (alloc_gen) are the ones it was captured with.
+    struct StepGraph {
+        cudaGraphExec_t exec = nullptr;
+        int precision = -1, nt = 0, ipt = 0, minb = 0, unroll = 0;
+        double eps = 0.0, dt = 0.0;
+        size_t n = 0;
+        unsigned long long gen = 0;
+        long long launches = 0;  // kernel launches in one replay
+        bool disabled = false;   // capture failed once: stay eager
+    } sgraph;
     std::vector<std::pair<long long, Tune>> tune_cache;  // (n bucket, choice)
     std::vector<std::pair<Tune, double>> tune_report;   // last autotune: every candidate and its ms
 
