@@ -15,6 +15,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgvs.so")
@@ -90,7 +91,37 @@ def build(force: bool = False, extra: list[str] | None = None) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+    build_host()
     return LIB
+
+
+HOST = os.path.join(HERE, "host")
+HEADLESS = os.path.join(HERE, "gvs_headless")
+HOST_CHECK = os.path.join(HERE, "gvs_host_check")
+
+
+def _host_binary(out: str, main_src: str) -> str:
+    srcs = [os.path.join(HOST, "gravis.cpp"), os.path.join(HOST, main_src)]
+    deps = srcs + [os.path.join(HOST, "gravis.hpp"), os.path.join(ROOT, "include", "gvs.h"), LIB]
+    if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
+        return out
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    tmp = out + ".tmp"
+    cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", "-Wextra", "-o", tmp] + srcs + \
+          ["-L" + HERE, "-lgvs", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"host build failed ({main_src}):\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, out)
+    return out
+
+
+def build_host() -> str:
+    """The C++ host layer (host/gravis.cpp): the headless runner and the check
+    program of the drop-in classes, linked against libgvs.so (found next to the
+    binaries at run time)."""
+    _host_binary(HOST_CHECK, "host_check.cpp")
+    return _host_binary(HEADLESS, "headless.cpp")
 
 
 if __name__ == "__main__":

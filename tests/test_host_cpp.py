@@ -1,0 +1,103 @@
+"""The C++ host layer (gravis_gb300/host/): the headless runner gvs_headless and
+the drop-in class check gvs_host_check.
+
+CPU: the runner validates its arguments the way crates/headless/src/main.rs:66-95
+does, before touching a GPU.  GPU: the runner reproduces the reference's own
+diagnostics artifacts (m1_plummer_1k_diag.csv: N=1000 seed 42, suggested eps and
+dt, 1000 steps, a row every 100; m1_kepler_diag.csv: the e=0.5 two-body orbit, a
+row every 10^4 steps) to 1e-10 relative, and the per-call GravitySolver /
+Integrator / SphSolver classes give the device-resident path's results bit for bit.
+"""
+import csv
+import os
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADLESS = os.path.join(ROOT, "gravis_gb300", "gvs_headless")
+CHECK = os.path.join(ROOT, "gravis_gb300", "gvs_host_check")
+
+
+@pytest.fixture(scope="module")
+def built():
+    from gravis_gb300 import build
+    build.build()
+    assert os.path.exists(HEADLESS) and os.path.exists(CHECK)
+
+
+def run(*args, timeout=600):
+    return subprocess.run([HEADLESS, *args], capture_output=True, text=True, timeout=timeout)
+
+
+@pytest.mark.parametrize("args,msg", [
+    (["--eccentricity", "1.0"], "--eccentricity must be in [0, 1)"),
+    (["--particles", "0"], "--particles must be > 0"),
+    (["--dt", "-1e-3"], "--dt must be positive"),
+    (["--softening", "-0.1"], "--softening must be non-negative"),
+    (["--algorithm", "fmm"], "--algorithm must be brute-force or barnes-hut"),
+])
+def test_headless_validates_arguments(built, args, msg):
+    r = run(*args)
+    assert r.returncode == 1
+    assert msg in r.stderr
+
+
+def test_headless_help(built):
+    r = run("--help")
+    assert r.returncode == 0 and "--diag-csv" in r.stdout
+
+
+def read_csv(path):
+    with open(path) as fh:
+        rows = list(csv.DictReader(fh))
+    return rows
+
+
+@pytest.mark.gpu
+def test_headless_reproduces_plummer_artifact(built, golden, tmp_path):
+    out = tmp_path / "diag.csv"
+    r = run("--scenario", "plummer", "-n", "1000", "--seed", "42", "--steps", "1000", "--diag-interval", "100",
+            "--diag-csv", str(out))
+    assert r.returncode == 0, r.stderr
+    rows = read_csv(out)
+    ref = golden["m1_plummer_1k_diag.csv"]["rows"]  # step, time, K, U, E, |p|, |L|, com, virial
+    assert [int(x["step"]) for x in rows] == [int(v[0]) for v in ref]
+    for got, want in zip(rows, ref):
+        for col, k in (("kinetic_energy", 2), ("potential_energy", 3), ("total_energy", 4)):
+            assert abs(float(got[col]) - want[k]) <= 1e-10 * abs(want[k]), (got["step"], col, got[col], want[k])
+
+
+@pytest.mark.gpu
+def test_headless_reproduces_kepler_rows(built, golden, tmp_path):
+    out = tmp_path / "kepler.csv"
+    r = run("--scenario", "two-body", "--steps", "20000", "--diag-interval", "10000", "--diag-csv", str(out))
+    assert r.returncode == 0, r.stderr
+    rows = read_csv(out)
+    ref = golden["m1_kepler_diag.csv"]["rows"]
+    for got, want in zip(rows, ref[:3]):
+        assert int(got["step"]) == int(want[0])
+        for col, k in (("kinetic_energy", 2), ("total_energy", 4)):
+            assert abs(float(got[col]) - want[k]) <= 1e-10 * abs(want[k]), (got["step"], col)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64-exact", "mixed"])
+def test_headless_evrard_sph(built, tmp_path, precision):
+    out = tmp_path / "evrard.csv"
+    r = run("--scenario", "evrard-collapse", "-n", "1000", "--steps", "20", "--diag-interval", "10",
+            "--precision", precision, "--diag-csv", str(out))
+    assert r.returncode == 0, r.stderr
+    rows = read_csv(out)
+    assert [int(x["step"]) for x in rows] == [0, 10, 20]
+    e0, e1 = float(rows[0]["total_energy"]), float(rows[-1]["total_energy"])
+    assert float(rows[0]["thermal_energy"]) > 0.0
+    assert abs((e1 - e0) / e0) < 1e-2
+
+
+@pytest.mark.gpu
+def test_drop_in_classes_match_resident_path(built):
+    r = subprocess.run([CHECK], capture_output=True, text=True, timeout=600)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.count("ok  ") == 5
