@@ -397,7 +397,23 @@ def run_workload(a, d):
         ctx.compute_forces(G.ALGO_BH, prec, eps, theta)
         ctx.get_state(q)
         rel = np.sqrt((((q.acc()[idx] - ref) ** 2).sum(1) / (ref ** 2).sum(1)).mean())
+        # the walk forms side by side on the final state: time and distance to the f64 walk
+        walks = {}
+        for wname, wp in (("fp64", G.PREC_FP64), ("mixed", G.PREC_MIXED), ("fp32", G.PREC_FP32)):
+            ctx.compute_forces(G.ALGO_BH, wp, eps, theta)  # builds the packed node arrays
+            ctx.profile(True)
+            ctx.compute_forces(G.ALGO_BH, wp, eps, theta)
+            pw = ctx.profile_read()
+            ctx.profile(False)
+            qw = G.Particles(n)
+            ctx.get_state(qw)
+            walks[wname] = {"walk_ms": pw["force_ms"], "acc": qw.acc()}
+        a64 = walks["fp64"].pop("acc")
+        for wname in ("mixed", "fp32"):
+            aw = walks[wname].pop("acc")
+            walks[wname]["rel_rms_vs_fp64_walk"] = float(np.sqrt(((aw - a64) ** 2).sum() / (a64 ** 2).sum()))
         res.update({"value": n * a.steps / (t * 1e-3), "ms_per_step": t / a.steps, "dtype": "f32 walk / f64 state",
+                    "walk_forms": walks,
                     "config": {"workload": f"Barnes-Hut KDK, two Plummer spheres N={n} seed 7, theta={theta}, "
                                            f"eps={eps}, dt={dt}", "n": n, "theta": theta},
                     "walk_ms_per_step": prof["force_ms"] / max(1, prof["force_launches"]),

@@ -34,6 +34,9 @@
 //     while node loads are broadcast.  Children are visited 0..7 (pre-order)
 //     rather than the reference's LIFO 7..0: the same terms summed in another
 //     order (differences at the 1e-16 relative level).
+#include <algorithm>
+#include <cmath>
+
 #include "gvs_internal.cuh"
 
 namespace gvs {
@@ -53,6 +56,7 @@ struct Tree {
     DevBuf boxx, boxy, boxz;         // per node cell centre (f64)
     DevBuf sx, sy, sz, sm;           // sorted particle positions / masses (f64)
     DevBuf pos32, cm32, cm64, meta, acc;
+    DevBuf pos32lo, cm32lo;  // mixed walk: f32 lo words of positions and COMs
 };
 
 namespace {
@@ -232,24 +236,36 @@ __global__ void k_pack_nodes(size_t nnodes, const uint8_t *__restrict__ level, c
                              const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ skip,
                              const double *__restrict__ mass, const double *__restrict__ cx,
                              const double *__restrict__ cy, const double *__restrict__ cz, float4 *__restrict__ cm32,
-                             double4 *__restrict__ cm64, int4 *__restrict__ meta) {
+                             double4 *__restrict__ cm64, int4 *__restrict__ meta, float4 *__restrict__ cm32lo) {
     const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nnodes) return;
     meta[k] = make_int4((int)skip[k], (int)first[k], (int)cnt[k], (int)level[k]);
     if (cm32) cm32[k] = make_float4((float)cx[k], (float)cy[k], (float)cz[k], (float)mass[k]);
     if (cm64) cm64[k] = make_double4(cx[k], cy[k], cz[k], mass[k]);
+    if (cm32lo) {
+        const float hx = (float)cx[k], hy = (float)cy[k], hz = (float)cz[k];
+        cm32lo[k] = make_float4((float)(cx[k] - (double)hx), (float)(cy[k] - (double)hy), (float)(cz[k] - (double)hz), 0.f);
+    }
 }
 
 __global__ void k_pack_particles(size_t n, const double *__restrict__ sx, const double *__restrict__ sy,
-                                 const double *__restrict__ sz, const double *__restrict__ sm, float4 *__restrict__ p32) {
+                                 const double *__restrict__ sz, const double *__restrict__ sm, float4 *__restrict__ p32,
+                                 float4 *__restrict__ p32lo) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) p32[i] = make_float4((float)sx[i], (float)sy[i], (float)sz[i], (float)sm[i]);
+    if (i >= n) return;
+    const float hx = (float)sx[i], hy = (float)sy[i], hz = (float)sz[i];
+    p32[i] = make_float4(hx, hy, hz, (float)sm[i]);
+    if (p32lo)
+        p32lo[i] = make_float4((float)(sx[i] - (double)hx), (float)(sy[i] - (double)hy), (float)(sz[i] - (double)hz), 0.f);
 }
 
 // ---- walk -------------------------------------------------------------------
 struct S2Table {
     double s2[MAXL + 1];   // (2 * half_width_L)^2, half_width_L = hw0 * 2^-L
     float s2f[MAXL + 1];
+    // mixed walk: accept for sure if d^2 > hi2, open for sure if d^2 < lo2 (f32 d^2 of the
+    // hi words), else decide with the reference's f64 test (see bh_forces)
+    float lo2[MAXL + 1], hi2[MAXL + 1];
 };
 
 // BarnesHut::add_force (barnes_hut.rs:114-135), IEEE f64 with no contraction.
@@ -264,6 +280,26 @@ __device__ __forceinline__ void add_force64(double px, double py, double pz, dou
     az = __dadd_rn(az, __dmul_rn(f, dz));
 }
 
+// f32 monopole term on a float-float separation (hi - hi) + (lo - lo), summed into
+// (hi, lo) two-sum accumulators.
+__device__ __forceinline__ void tsum32(float &hi, float &lo, float v) {
+    const float s = hi + v;
+    const float bp = s - hi;
+    lo += (hi - (s - bp)) + (v - bp);
+    hi = s;
+}
+
+__device__ __forceinline__ void add_force_ff(float4 q, float4 ql, float sx, float sy, float sz, float sxl, float syl,
+                                             float szl, float m, float eps2, float *acc) {
+    const float dx = (sx - q.x) + (sxl - ql.x), dy = (sy - q.y) + (syl - ql.y), dz = (sz - q.z) + (szl - ql.z);
+    const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+    const float ri = rsqrt_approx(r2);
+    const float f = m * ri * ri * ri;
+    tsum32(acc[0], acc[3], f * dx);
+    tsum32(acc[1], acc[4], f * dy);
+    tsum32(acc[2], acc[5], f * dz);
+}
+
 __device__ __forceinline__ void add_force32(float px, float py, float pz, float sx, float sy, float sz, float m,
                                             float eps2, float &ax, float &ay, float &az) {
     const float dx = sx - px, dy = sy - py, dz = sz - pz;
@@ -275,24 +311,33 @@ __device__ __forceinline__ void add_force32(float px, float py, float pz, float 
     az = fmaf(f, dz, az);
 }
 
-template <bool F64>
+// MODE 0: f64, the reference's arithmetic per term.  MODE 1: f32 positions and
+// moments, f32 opening test.  MODE 2 (mixed): f32 terms on float-float
+// separations with compensated sums, and the reference's opening decisions --
+// an f32 test of the hi words with a certified margin, the f64 test in between.
+template <int MODE>
 __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int4 *__restrict__ meta,
                                               const float4 *__restrict__ cm32, const double4 *__restrict__ cm64,
                                               const float4 *__restrict__ p32, const double *__restrict__ sx,
                                               const double *__restrict__ sy, const double *__restrict__ sz,
                                               const double *__restrict__ sm, const S2Table tab, double theta2,
-                                              double eps2, double *__restrict__ acc) {
+                                              double eps2, double *__restrict__ acc, const float4 *__restrict__ cm32lo,
+                                              const float4 *__restrict__ p32lo) {
+    constexpr bool F64 = MODE == 0;
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = t < n;
     double px = 0, py = 0, pz = 0;
     float qx = 0, qy = 0, qz = 0;
+    float4 qh = make_float4(0.f, 0.f, 0.f, 0.f), ql = qh;
     if (active) {
-        if (F64) { px = sx[t]; py = sy[t]; pz = sz[t]; }
-        else { const float4 p = p32[t]; qx = p.x; qy = p.y; qz = p.z; }
+        if (MODE != 1) { px = sx[t]; py = sy[t]; pz = sz[t]; }
+        if (MODE != 0) { qh = p32[t]; qx = qh.x; qy = qh.y; qz = qh.z; }
+        if (MODE == 2) ql = p32lo[t];
     }
     const float theta2f = (float)theta2, eps2f = (float)eps2;
     double ax = 0, ay = 0, az = 0;
     float fx = 0, fy = 0, fz = 0;
+    float fa[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // mixed: (hi x, y, z, lo x, y, z)
     uint32_t next = active ? 0u : 0xFFFFFFFFu;
     for (;;) {
         const uint32_t m = __reduce_min_sync(0xFFFFFFFFu, next);
@@ -305,9 +350,15 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
                     if (F64) {
                         const double4 c = cm64[m];
                         if (c.w != 0.0) add_force64(px, py, pz, c.x, c.y, c.z, c.w, eps2, ax, ay, az);
-                    } else {
+                    } else if (MODE == 1) {
                         const float4 c = cm32[m];
                         if (c.w != 0.f) add_force32(qx, qy, qz, c.x, c.y, c.z, c.w, eps2f, fx, fy, fz);
+                    } else {
+                        const float4 c = cm32[m];
+                        if (c.w != 0.f) {
+                            const float4 cl = cm32lo[m];
+                            add_force_ff(qh, ql, c.x, c.y, c.z, cl.x, cl.y, cl.z, c.w, eps2f, fa);
+                        }
                     }
                 }
             } else {  // bucket of coincident-key particles: direct terms
@@ -315,9 +366,15 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
                     if ((size_t)j == t) continue;
                     if (F64) {
                         if (sm[j] != 0.0) add_force64(px, py, pz, sx[j], sy[j], sz[j], sm[j], eps2, ax, ay, az);
-                    } else {
+                    } else if (MODE == 1) {
                         const float4 q = p32[j];
                         if (q.w != 0.f) add_force32(qx, qy, qz, q.x, q.y, q.z, q.w, eps2f, fx, fy, fz);
+                    } else {
+                        const float4 q = p32[j];
+                        if (q.w != 0.f) {
+                            const float4 l = p32lo[j];
+                            add_force_ff(qh, ql, q.x, q.y, q.z, l.x, l.y, l.z, q.w, eps2f, fa);
+                        }
                     }
                 }
             }
@@ -343,8 +400,26 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
             } else {
                 const float dx = c.x - qx, dy = c.y - qy, dz = c.z - qz;
                 const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                if (tab.s2f[mt.w] < theta2f * d2) {
-                    add_force32(qx, qy, qz, c.x, c.y, c.z, c.w, eps2f, fx, fy, fz);
+                bool accept;
+                if (MODE == 1) {
+                    accept = tab.s2f[mt.w] < theta2f * d2;
+                } else if (d2 > tab.hi2[mt.w]) {
+                    accept = true;
+                } else if (d2 < tab.lo2[mt.w]) {
+                    accept = false;
+                } else {  // near the boundary: the reference's f64 test
+                    const double4 c64 = cm64[m];
+                    const double ex = __dsub_rn(c64.x, px), ey = __dsub_rn(c64.y, py), ez = __dsub_rn(c64.z, pz);
+                    const double e2 = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
+                    accept = tab.s2[mt.w] < __dmul_rn(theta2, e2);
+                }
+                if (accept) {
+                    if (MODE == 1) {
+                        add_force32(qx, qy, qz, c.x, c.y, c.z, c.w, eps2f, fx, fy, fz);
+                    } else {
+                        const float4 cl = cm32lo[m];
+                        add_force_ff(qh, ql, c.x, c.y, c.z, cl.x, cl.y, cl.z, c.w, eps2f, fa);
+                    }
                     next = (uint32_t)mt.x;
                 } else {
                     next = m + 1;
@@ -353,7 +428,12 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
         }
     }
     if (!active) return;
-    if (!F64) { ax = fx; ay = fy; az = fz; }
+    if (MODE == 1) { ax = fx; ay = fy; az = fz; }
+    if (MODE == 2) {
+        ax = (double)fa[0] + (double)fa[3];
+        ay = (double)fa[1] + (double)fa[4];
+        az = (double)fa[2] + (double)fa[5];
+    }
     acc[t] = ax;
     acc[n + t] = ay;
     acc[2 * n + t] = az;
@@ -387,7 +467,7 @@ void tree_free(Ctx *c) {
     DevBuf *all[] = {&t->bb, &t->bbpart, &t->khi, &t->klo, &t->khi2, &t->klo2, &t->perm, &t->perm2, &t->iota,
                      &t->iota2, &t->delta, &t->nown, &t->off, &t->total, &t->level, &t->first, &t->cnt, &t->skip,
                      &t->mass, &t->comx, &t->comy, &t->comz, &t->boxx, &t->boxy, &t->boxz, &t->sx, &t->sy,
-                     &t->sz, &t->sm, &t->pos32, &t->cm32, &t->cm64, &t->meta, &t->acc};
+                     &t->sz, &t->sm, &t->pos32, &t->cm32, &t->cm64, &t->meta, &t->acc, &t->pos32lo, &t->cm32lo};
     for (DevBuf *b : all)
         if (b->ptr) cudaFree(b->ptr);
     delete t;
@@ -496,44 +576,67 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
     Tree *t = tree_of(c);
     cudaStream_t st = c->stream;
     const size_t nnodes = t->nnodes;
-    const bool f64 = precision == GVS_PREC_FP64_EXACT || precision == GVS_PREC_FP64;
+    // walk mode: 0 f64 (FP64, FP64_EXACT), 1 f32 (FP32), 2 mixed (MIXED)
+    const int mode = (precision == GVS_PREC_FP64_EXACT || precision == GVS_PREC_FP64) ? 0
+                     : precision == GVS_PREC_FP32 ? 1 : 2;
     GVS_CUDA(c, ensure(c, t->meta, nnodes * sizeof(int4)));
-    if (f64) GVS_CUDA(c, ensure(c, t->cm64, nnodes * sizeof(double4)));
-    else {
+    if (mode != 1) GVS_CUDA(c, ensure(c, t->cm64, nnodes * sizeof(double4)));
+    if (mode != 0) {
         GVS_CUDA(c, ensure(c, t->cm32, nnodes * sizeof(float4)));
         GVS_CUDA(c, ensure(c, t->pos32, n * sizeof(float4)));
     }
-    if (t->precision != (f64 ? 1 : 0)) {
+    if (mode == 2) {
+        GVS_CUDA(c, ensure(c, t->cm32lo, nnodes * sizeof(float4)));
+        GVS_CUDA(c, ensure(c, t->pos32lo, n * sizeof(float4)));
+    }
+    if (t->precision != mode + 1) {
         k_pack_nodes<<<nblk(nnodes), 256, 0, st>>>(nnodes, as<uint8_t>(t->level), as<uint32_t>(t->first),
                                                     as<uint32_t>(t->cnt), as<uint32_t>(t->skip), as<double>(t->mass),
                                                     as<double>(t->comx), as<double>(t->comy), as<double>(t->comz),
-                                                    f64 ? nullptr : as<float4>(t->cm32),
-                                                    f64 ? as<double4>(t->cm64) : nullptr, as<int4>(t->meta));
-        if (!f64)
+                                                    mode != 0 ? as<float4>(t->cm32) : nullptr,
+                                                    mode != 1 ? as<double4>(t->cm64) : nullptr, as<int4>(t->meta),
+                                                    mode == 2 ? as<float4>(t->cm32lo) : nullptr);
+        if (mode != 0)
             k_pack_particles<<<nblk(n), 256, 0, st>>>(n, as<double>(t->sx), as<double>(t->sy), as<double>(t->sz),
-                                                      as<double>(t->sm), as<float4>(t->pos32));
-        c->prof.launches += f64 ? 1 : 2;
-        t->precision = f64 ? 1 : 0;
+                                                      as<double>(t->sm), as<float4>(t->pos32),
+                                                      mode == 2 ? as<float4>(t->pos32lo) : nullptr);
+        c->prof.launches += mode != 0 ? 2 : 1;
+        t->precision = mode + 1;
     }
+    // the mixed walk's certified margin: X bounds every coordinate (the root cell);
+    // f32 rounding moves the hi-word distance by at most ~1.3 E, E = 2^-21 X
+    const double X = std::max(std::fabs(t->root[0]), std::max(std::fabs(t->root[1]), std::fabs(t->root[2]))) +
+                     t->root[3];
+    const double E = std::ldexp(X, -21);
     S2Table tab;
     for (int L = 0; L <= MAXL; ++L) {
         const double hw = ldexp(t->root[3], -L);  // exact: child half width = parent * 0.5
         const double s = hw * 2.0;
         tab.s2[L] = s * s;
         tab.s2f[L] = (float)(s * s);
+        const double rc = theta > 0.0 ? s / theta : INFINITY;  // accept iff d > s / theta
+        const double lo = rc - 3.0 * E, hi = rc + 3.0 * E;
+        tab.lo2[L] = lo > 0.0 ? (float)(lo * lo * (1.0 - 0x1p-19)) : -1.0f;
+        tab.hi2[L] = (float)(hi * hi * (1.0 + 0x1p-19));
     }
     GVS_CUDA(c, ensure(c, t->acc, 3 * n * sizeof(double)));
     if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], st));
-    if (f64)
-        k_walk<true><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, as<int4>(t->meta), nullptr, as<double4>(t->cm64),
-                                                   nullptr, as<double>(t->sx), as<double>(t->sy), as<double>(t->sz),
-                                                   as<double>(t->sm), tab, theta * theta, eps * eps,
-                                                   as<double>(t->acc));
+    if (mode == 0)
+        k_walk<0><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, as<int4>(t->meta), nullptr, as<double4>(t->cm64),
+                                                nullptr, as<double>(t->sx), as<double>(t->sy), as<double>(t->sz),
+                                                as<double>(t->sm), tab, theta * theta, eps * eps,
+                                                as<double>(t->acc), nullptr, nullptr);
+    else if (mode == 1)
+        k_walk<1><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, as<int4>(t->meta), as<float4>(t->cm32), nullptr,
+                                                as<float4>(t->pos32), as<double>(t->sx), as<double>(t->sy),
+                                                as<double>(t->sz), as<double>(t->sm), tab, theta * theta, eps * eps,
+                                                as<double>(t->acc), nullptr, nullptr);
     else
-        k_walk<false><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, as<int4>(t->meta), as<float4>(t->cm32), nullptr,
-                                                    as<float4>(t->pos32), as<double>(t->sx), as<double>(t->sy),
-                                                    as<double>(t->sz), as<double>(t->sm), tab, theta * theta,
-                                                    eps * eps, as<double>(t->acc));
+        k_walk<2><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, as<int4>(t->meta), as<float4>(t->cm32),
+                                                as<double4>(t->cm64), as<float4>(t->pos32), as<double>(t->sx),
+                                                as<double>(t->sy), as<double>(t->sz), as<double>(t->sm), tab,
+                                                theta * theta, eps * eps, as<double>(t->acc),
+                                                as<float4>(t->cm32lo), as<float4>(t->pos32lo));
     c->prof.launches += 1;
     GVS_TRY(check_launch(c, "tree walk"));
     if (c->prof.on) {

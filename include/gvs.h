@@ -135,8 +135,11 @@ gvs_status gvs_gravity_direct(gvs_ctx *ctx, size_t n, const double *x, const dou
 
 /* BarnesHut::compute_accelerations (crates/sim-core/src/barnes_hut.rs:139-192): octree
  * of the given positions, opening test s^2 < theta^2 d^2, monopoles.  precision
- * GVS_PREC_FP64 / FP64_EXACT walks in f64 (the reference's arithmetic per term),
- * GVS_PREC_FP32 / MIXED walks on f32 positions and f32 moments.  Accumulates. */
+ * GVS_PREC_FP64 / FP64_EXACT walks in f64 (the reference's arithmetic per term);
+ * GVS_PREC_MIXED takes the reference's opening decisions (an f32 test with a
+ * certified margin, the f64 test near the boundary) and sums f32 terms on
+ * float-float separations with compensated sums (within 1e-6 of f64);
+ * GVS_PREC_FP32 walks on plain f32 positions and moments (fastest).  Accumulates. */
 gvs_status gvs_gravity_bh(gvs_ctx *ctx, size_t n, const double *x, const double *y, const double *z,
                           const double *mass, double softening, double theta, int precision, double *ax, double *ay,
                           double *az);

@@ -6,7 +6,9 @@ reference tree's (Octree::rebuild, crates/sim-core/src/octree.rs:156-239).
 Forces: the f64 walk makes the reference's accept decisions on a bottom-up
 centre of mass (a few ulps from the reference's incremental one) and sums
 children 0..7 instead of 7..0, so it agrees with the oracle's BarnesHut to
-<= 1e-12 relative RMS; the f32 walk within 1e-4 of the f64 walk.
+<= 1e-12 relative RMS; the f32 walk within 1e-4 of the f64 walk; the mixed walk
+(f32 terms on float-float separations, the reference's opening decisions)
+within 1e-6 of the oracle's BarnesHut and of the f64 walk.
 """
 import numpy as np
 import pytest
@@ -144,6 +146,38 @@ def test_bh_f32_walk(ctx, theta):
     # f32 absolute positions at |x| ~ 10 resolve separations to ~1e-6; the bound
     # sits two orders of magnitude below the BH approximation error (~5e-3).
     assert err <= 1e-4
+
+
+@pytest.mark.parametrize("theta", [0.3, 0.5, 0.7])
+@pytest.mark.parametrize("name", ["plummer1000", "collision4096", "lattice8"])
+def test_bh_mixed_vs_oracle(ctx, name, theta):
+    """Mixed walk: same accepted nodes as the reference (f64 rechecks near the
+    opening boundary), f32 terms on float-float separations: within 1e-6."""
+    p = cases()[name]
+    eps = 0.05
+    q = p.copy()
+    q.clear_accelerations()
+    G.BarnesHut(eps, theta, G.PREC_MIXED, ctx).compute_accelerations(q)
+    r = to_oracle(p)
+    O.bh(r, eps, theta)
+    err = rel_rms(q.acc(), r.acc())
+    print(f"{name} theta={theta} mixed walk vs oracle BH rel RMS {err:.2e}")
+    assert err <= 1e-6, err
+
+
+@pytest.mark.parametrize("theta", [0.5, 0.7])
+def test_bh_mixed_walk_large(ctx, theta):
+    """At 2^16 (two Plummer spheres 20 apart, eps 1e-3) the mixed walk stays within
+    1e-6 of the f64 walk, where the plain f32 walk is ~1e-5 away."""
+    p = G.collision(1 << 16, seed=7)
+    eps = 1e-3
+    a64 = p.copy()
+    G.BarnesHut(eps, theta, G.PREC_FP64, ctx).compute_accelerations(a64)
+    am = p.copy()
+    G.BarnesHut(eps, theta, G.PREC_MIXED, ctx).compute_accelerations(am)
+    err = rel_rms(am.acc(), a64.acc())
+    print(f"theta={theta} mixed walk vs f64 walk rel RMS {err:.2e}")
+    assert err <= 1e-6
 
 
 def test_bh_vs_direct_subset(ctx):
