@@ -749,18 +749,20 @@ __host__ __device__ constexpr int wtile_f4(int tj) { return 2 * tj; }
 // explicit u = m_k w_j - m_j w_k form is used, which is exactly zero for the
 // self pair (the split A/S form would leave the rounding of two large
 // self terms, m_k eps^-3 w_k, that should cancel).
-template <int TJ, int NP, int MASK, bool GUARD, bool OWN>
+template <int TJ, int NP, int MASK, bool GUARD, bool OWN, int NJ = TJ>
 __device__ __forceinline__ void tile_vjp(const float4 *__restrict__ tile, const float4 *__restrict__ wt,
                                          const f2 *nx, const f2 *ny, const f2 *nz, const f2 *nxl, const f2 *nyl,
                                          const f2 *nzl, const f2 *wkx, const f2 *wky, const f2 *wkz, const f2 *mk,
                                          f2 e2, f2 *ax, f2 *ay, f2 *az, f2 *S, f2 *Ax, f2 *Ay, f2 *Az, f2 *Bx,
-                                         f2 *By, f2 *Bz, f2 *Cx, f2 *Cy, f2 *Cz, f2 *Gx, f2 *Gy, f2 *Gz, f2 *gm) {
+                                         f2 *By, f2 *Bz, f2 *Cx, f2 *Cy, f2 *Cz, f2 *Gx, f2 *Gy, f2 *Gz, f2 *gm,
+                                         int j0 = 0) {
     const f2 mthree = pk(-3.f, -3.f);
-    const float4 *jd = tile + 2;
-    const float4 *jl = tile + 2 + 2 * TJ;
+    const float4 *jd = tile + 2 + 2 * j0;
+    const float4 *jl = tile + 2 + 2 * TJ + 2 * j0;
+    const float4 *jw = wt + 2 * j0;
 #pragma unroll 2
-    for (int j = 0; j < TJ; ++j) {
-        const float4 a = jd[2 * j], b = jd[2 * j + 1], wa = wt[2 * j], wb = wt[2 * j + 1];
+    for (int j = 0; j < NJ; ++j) {
+        const float4 a = jd[2 * j], b = jd[2 * j + 1], wa = jw[2 * j], wb = jw[2 * j + 1];
         const f2 xj = pk(a.x, a.y), yj = pk(a.z, a.w), zj = pk(b.x, b.y), mj = pk(b.z, b.w);
         const f2 wx = pk(wa.x, wa.y), wy = pk(wa.z, wa.w), wz = pk(wb.x, wb.y);
         f2 xl = 0ull, yl = 0ull, zl = 0ull;
@@ -836,8 +838,11 @@ __global__ void __launch_bounds__(NT) k_force_vjp32(const float4 *__restrict__ p
     float4 *sw = smem_v + NSTAGE * TF4;     // NSTAGE adjoint-vector tiles
     __shared__ __align__(8) uint64_t bar[NSTAGE];
     __shared__ float4 ci[IPT][2];
+    __shared__ float4 wbox[NT / 32][IPT];  // per warp: box of its targets in each target tile
+    constexpr int NCH = TJ / 32;
+    static_assert(NCH * NP <= 32, "one lane per (source chunk, target pair)");
 
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const size_t ibase = (size_t)blockIdx.x * NT * IPT;
     const int t0 = blockIdx.y * tiles_per_split;
     const int nt = max(0, min(ntiles, t0 + tiles_per_split) - t0);
@@ -850,6 +855,9 @@ __global__ void __launch_bounds__(NT) k_force_vjp32(const float4 *__restrict__ p
         ci[tid][0] = __ldg(tp);
         ci[tid][1] = __ldg(tp + 1);
     }
+    if (tid < (NT / 32) * IPT)
+        wbox[tid / IPT][tid % IPT] =
+            __ldg(pack + ((size_t)blockIdx.x * IPT + tid % IPT) * TF4 + chunk_box(TJ) + tid / IPT);
     __syncthreads();
     if (tid == 0)
         for (int s = 0; s < NSTAGE && s < nt; ++s) {
@@ -899,15 +907,28 @@ __global__ void __launch_bounds__(NT) k_force_vjp32(const float4 *__restrict__ p
         const float4 *tile = spos + s * TF4;
         const float4 jh = tile[0], jo = tile[1];
         f2 nx[NP], ny[NP], nz[NP], nxl[NP], nyl[NP], nzl[NP];
-        int mask = 0;
-#pragma unroll
-        for (int p = 0; p < NP; ++p) {
+        // near-field test as in direct_item: one lane per (source chunk, target pair)
+        bool near = false;
+        if (lane < NCH * NP) {
+            const int c = lane % NCH, p = lane / NCH;
+            const float4 sb = tile[chunk_box(TJ) + c];
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
-                const float4 h = ci[2 * p + q][0];
-                const float dist = fmaxf(fabsf(h.x - jh.x), fmaxf(fabsf(h.y - jh.y), fabsf(h.z - jh.z)));
-                if (dist < 0.5f * (h.w + jh.w)) mask |= 1 << p;
+                const float4 h = ci[2 * p + q][0], l = ci[2 * p + q][1], tb = wbox[warp][2 * p + q];
+                const float ddx = ((h.x - jh.x) + (l.x - jo.x)) + (tb.x - sb.x);
+                const float ddy = ((h.y - jh.y) + (l.y - jo.y)) + (tb.y - sb.y);
+                const float ddz = ((h.z - jh.z) + (l.z - jo.z)) + (tb.z - sb.z);
+                const float dist = fmaxf(fabsf(ddx), fmaxf(fabsf(ddy), fabsf(ddz)));
+                near = near || (dist < NEAR_KAPPA * (tb.w + sb.w));
             }
+        }
+        const unsigned cmask = __ballot_sync(0xFFFFFFFFu, near);
+        int mask = 0;  // pair p has some near chunk
+#pragma unroll
+        for (int p = 0; p < NP; ++p)
+            if ((cmask >> (p * NCH)) & ((1u << NCH) - 1u)) mask |= 1 << p;
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
             if ((mask >> p) & 1) {
                 float o[2][6], hh[2][3], ll[2][3];
                 upk(ox[p], o[0][0], o[1][0]); upk(oy[p], o[0][1], o[1][1]); upk(oz[p], o[0][2], o[1][2]);
@@ -960,8 +981,22 @@ __global__ void __launch_bounds__(NT) k_force_vjp32(const float4 *__restrict__ p
             tile_vjp<TJ, NP, 0, GUARD, false>(tile, wt, nx, ny, nz, nxl, nyl, nzl, wkx, wky, wkz, mk, e2, ax, ay, az,
                                               S, Ax, Ay, Az, Bx, By, Bz, Cx, Cy, Cz, Gx, Gy, Gz, gm);
         } else {
-            tile_vjp<TJ, NP, ALL, GUARD, false>(tile, wt, nx, ny, nz, nxl, nyl, nzl, wkx, wky, wkz, mk, e2, ax, ay,
-                                                az, S, Ax, Ay, Az, Bx, By, Bz, Cx, Cy, Cz, Gx, Gy, Gz, gm);
+            // chunk by chunk: a near chunk takes every pair on the float-float path
+            // (pairs without a near chunk have zero lo parts)
+#pragma unroll 1
+            for (int c = 0; c < NCH; ++c) {
+                unsigned any = 0;
+#pragma unroll
+                for (int p = 0; p < NP; ++p) any |= (cmask >> (p * NCH + c)) & 1u;
+                if (any)
+                    tile_vjp<TJ, NP, ALL, GUARD, false, 32>(tile, wt, nx, ny, nz, nxl, nyl, nzl, wkx, wky, wkz, mk,
+                                                            e2, ax, ay, az, S, Ax, Ay, Az, Bx, By, Bz, Cx, Cy, Cz,
+                                                            Gx, Gy, Gz, gm, 32 * c);
+                else
+                    tile_vjp<TJ, NP, 0, GUARD, false, 32>(tile, wt, nx, ny, nz, nxl, nyl, nzl, wkx, wky, wkz, mk, e2,
+                                                          ax, ay, az, S, Ax, Ay, Az, Bx, By, Bz, Cx, Cy, Cz, Gx, Gy,
+                                                          Gz, gm, 32 * c);
+            }
         }
         // g = m_k (A - 3 B) - w_k S + 3 C for this tile, then fold into (hi, lo)
 #pragma unroll
