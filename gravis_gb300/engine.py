@@ -498,6 +498,71 @@ def compute_diagnostics(p: Particles, softening: float, time: float = 0.0, step:
     return d
 
 
+# ---- snapshots ----------------------------------------------------------------------
+_MAGIC = {b"NBODY001": 1, b"NBODY002": 2, b"NBODY003": 3}
+
+
+@dataclass
+class Snapshot:
+    """snapshot.rs:1-170: the NBODY003 binary format (little-endian): magic, time, step,
+    softening, dt, count, x y z vx vy vz mass (f64), particle_type (u8), then
+    internal_energy, smoothing_length, density (f64).  NBODY001/002 are read too.
+    Accelerations are not stored: initialize() recomputes them."""
+    time: float
+    step: int
+    softening: float
+    dt: float
+    particles: Particles
+
+    @classmethod
+    def capture(cls, p: Particles, time: float, step: int, softening: float, dt: float) -> "Snapshot":
+        return cls(time, step, softening, dt, p.copy())
+
+    def write_to(self, fh):
+        p = self.particles
+        fh.write(b"NBODY003")
+        fh.write(np.array([self.time], "<f8").tobytes() + np.array([self.step], "<u8").tobytes())
+        fh.write(np.array([self.softening, self.dt], "<f8").tobytes() + np.array([p.count], "<u8").tobytes())
+        for f in ("x", "y", "z", "vx", "vy", "vz", "mass"):
+            fh.write(np.asarray(getattr(p, f), "<f8").tobytes())
+        fh.write(np.asarray(p.particle_type, np.uint8).tobytes())
+        for f in ("internal_energy", "smoothing_length", "density"):
+            fh.write(np.asarray(getattr(p, f), "<f8").tobytes())
+
+    @classmethod
+    def read_from(cls, fh) -> "Snapshot":
+        magic = fh.read(8)
+        if magic not in _MAGIC:
+            raise ValueError("Invalid snapshot magic bytes")
+        ver = _MAGIC[magic]
+        time, = np.frombuffer(fh.read(8), "<f8")
+        step, = np.frombuffer(fh.read(8), "<u8")
+        softening, dt = np.frombuffer(fh.read(16), "<f8")
+        n, = np.frombuffer(fh.read(8), "<u8")
+        n = int(n)
+        p = Particles(n)
+
+        def vec(dtype, size):
+            b = fh.read(size * np.dtype(dtype).itemsize)
+            if len(b) != size * np.dtype(dtype).itemsize:
+                raise ValueError("snapshot: truncated")
+            return np.frombuffer(b, dtype).copy()
+
+        for f in ("x", "y", "z", "vx", "vy", "vz", "mass"):
+            setattr(p, f, vec("<f8", n))
+        if ver >= 2:
+            p.particle_type = vec(np.uint8, n)
+        if ver >= 3:
+            for f in ("internal_energy", "smoothing_length", "density"):
+                setattr(p, f, vec("<f8", n))
+        return cls(float(time), int(step), float(softening), float(dt), p)
+
+    def initialize(self, gravity: "GravitySolver"):
+        """Snapshot::initialize (snapshot.rs:152-158): recompute a before stepping."""
+        self.particles.clear_accelerations()
+        gravity.compute_accelerations(self.particles)
+
+
 # ---- scenarios ----------------------------------------------------------------------
 class PlummerSphere:
     """scenarios/plummer_sphere.rs:79-153."""

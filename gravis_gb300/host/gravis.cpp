@@ -5,6 +5,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
+#include <istream>
+#include <ostream>
 
 namespace gravis {
 
@@ -224,6 +227,86 @@ Diagnostics compute_diagnostics(const Context &c, double softening, double time,
     gvs_diag d;
     c.check(gvs_diagnostics(c.get(), softening, with_potential ? 1 : 0, &d));
     return from_c(d, time, step);
+}
+
+// ---- snapshots (NBODY001..003) -------------------------------------------------------
+namespace {
+static_assert(sizeof(double) == 8 && sizeof(uint64_t) == 8, "64-bit fields");
+bool little_endian() {
+    const uint16_t one = 1;
+    uint8_t b;
+    std::memcpy(&b, &one, 1);
+    return b == 1;
+}
+template <class T> void put(std::ostream &w, T v) { w.write(reinterpret_cast<const char *>(&v), sizeof v); }
+template <class T> T get(std::istream &r) {
+    T v;
+    if (!r.read(reinterpret_cast<char *>(&v), sizeof v)) throw Error(GVS_ERR_INVALID_ARG, "snapshot: truncated");
+    return v;
+}
+void put_vec(std::ostream &w, const std::vector<double> &v) {
+    w.write(reinterpret_cast<const char *>(v.data()), (std::streamsize)(v.size() * 8));
+}
+void get_vec(std::istream &r, std::vector<double> &v, size_t n) {
+    v.assign(n, 0.0);
+    if (n && !r.read(reinterpret_cast<char *>(v.data()), (std::streamsize)(n * 8)))
+        throw Error(GVS_ERR_INVALID_ARG, "snapshot: truncated");
+}
+}  // namespace
+
+Snapshot Snapshot::capture(const Particles &p, double time, uint64_t step, double softening, double dt) {
+    Snapshot s;
+    s.time = time;
+    s.step = step;
+    s.softening = softening;
+    s.dt = dt;
+    s.particles = p;
+    return s;
+}
+
+void Snapshot::write_to(std::ostream &w) const {
+    if (!little_endian()) throw Error(GVS_ERR_INVALID_ARG, "snapshot: big-endian hosts are not supported");
+    const Particles &p = particles;
+    w.write("NBODY003", 8);
+    put(w, time);
+    put(w, step);
+    put(w, softening);
+    put(w, dt);
+    put(w, (uint64_t)p.count);
+    for (const auto *v : {&p.x, &p.y, &p.z, &p.vx, &p.vy, &p.vz, &p.mass}) put_vec(w, *v);
+    w.write(reinterpret_cast<const char *>(p.particle_type.data()), (std::streamsize)p.count);
+    for (const auto *v : {&p.internal_energy, &p.smoothing_length, &p.density}) put_vec(w, *v);
+    if (!w) throw Error(GVS_ERR_INVALID_ARG, "snapshot: write failed");
+}
+
+Snapshot Snapshot::read_from(std::istream &r) {
+    if (!little_endian()) throw Error(GVS_ERR_INVALID_ARG, "snapshot: big-endian hosts are not supported");
+    char magic[8];
+    if (!r.read(magic, 8)) throw Error(GVS_ERR_INVALID_ARG, "snapshot: truncated");
+    int version = 0;
+    if (std::memcmp(magic, "NBODY003", 8) == 0) version = 3;
+    else if (std::memcmp(magic, "NBODY002", 8) == 0) version = 2;
+    else if (std::memcmp(magic, "NBODY001", 8) == 0) version = 1;
+    else throw Error(GVS_ERR_INVALID_ARG, "Invalid snapshot magic bytes");
+    Snapshot s;
+    s.time = get<double>(r);
+    s.step = get<uint64_t>(r);
+    s.softening = get<double>(r);
+    s.dt = get<double>(r);
+    const size_t n = (size_t)get<uint64_t>(r);
+    Particles &p = s.particles;
+    p.resize(n);  // accelerations and the computed gas fields stay zero
+    for (auto *v : {&p.x, &p.y, &p.z, &p.vx, &p.vy, &p.vz, &p.mass}) get_vec(r, *v, n);
+    if (version >= 2 && n && !r.read(reinterpret_cast<char *>(p.particle_type.data()), (std::streamsize)n))
+        throw Error(GVS_ERR_INVALID_ARG, "snapshot: truncated");
+    if (version >= 3)
+        for (auto *v : {&p.internal_energy, &p.smoothing_length, &p.density}) get_vec(r, *v, n);
+    return s;
+}
+
+void Snapshot::initialize(const GravitySolver &gravity) {
+    particles.clear_accelerations();
+    gravity.compute_accelerations(particles);
 }
 
 // ---- scenarios -----------------------------------------------------------------------

@@ -19,6 +19,7 @@
 
 #include <array>
 #include <cstdint>
+#include <iosfwd>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -205,6 +206,22 @@ struct EvrardCollapse {  // evrard_collapse.rs:15-71
     Particles generate() const;
     double suggested_dt() const;
     double suggested_softening() const;
+};
+
+// Snapshot (crates/sim-core/src/snapshot.rs:1-170): the NBODY003 binary format --
+// magic, time, step, softening, dt, count, then x y z vx vy vz mass (f64 each),
+// particle_type (u8), internal_energy, smoothing_length, density (f64), all
+// little-endian.  read_from also accepts NBODY001/002.  Accelerations are not
+// stored: initialize() recomputes them before stepping, as the reference requires.
+struct Snapshot {
+    double time = 0.0;
+    uint64_t step = 0;
+    double softening = 0.0, dt = 0.0;
+    Particles particles;
+    static Snapshot capture(const Particles &p, double time, uint64_t step, double softening, double dt);
+    void write_to(std::ostream &w) const;
+    static Snapshot read_from(std::istream &r);
+    void initialize(const GravitySolver &gravity);
 };
 
 // Rust's `{:.Ne}` formatting of an f64 (exponent without sign padding or '+').

@@ -5,13 +5,16 @@
 // which are themselves computed on the GPU).
 //
 // Extra flags (no reference counterpart): --precision fp64-exact|fp64|fp32|mixed
-// for the force paths, and --device N.  Scenarios: plummer, two-body (kepler),
+// for the force paths, --device N, and --restart SNAPSHOT (continue from an
+// NBODY snapshot: its time, step, softening and dt; accelerations recomputed,
+// as Snapshot::initialize does).  Scenarios: plummer, two-body (kepler),
 // evrard-collapse; the others are outside the engine's scope.
 #include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <filesystem>
 #include <fstream>
 #include <memory>
 #include <string>
@@ -35,6 +38,9 @@ struct Cli {
     double theta = 0.5;
     std::string precision = "fp64-exact";
     int device = 0;
+    unsigned long long snapshot_interval = 0;
+    std::string snapshot_dir = "artifacts/snapshots";
+    std::string restart;
 };
 
 [[noreturn]] void die(const std::string &msg) {
@@ -57,7 +63,10 @@ void usage() {
         "      --algorithm NAME       brute-force | barnes-hut (default brute-force)\n"
         "      --theta T              Barnes-Hut opening angle (default 0.5)\n"
         "      --precision P          fp64-exact | fp64 | fp32 | mixed (default fp64-exact)\n"
-        "      --device N             CUDA device (default 0)\n");
+        "      --device N             CUDA device (default 0)\n"
+        "      --snapshot-interval N  write an NBODY003 snapshot every N steps, 0 = off (default 0)\n"
+        "      --snapshot-dir DIR     snapshot directory (default artifacts/snapshots)\n"
+        "      --restart PATH         continue from a snapshot (its time, step, softening, dt)\n");
 }
 
 Cli parse(int argc, char **argv) {
@@ -82,6 +91,9 @@ Cli parse(int argc, char **argv) {
         else if (a == "--theta") c.theta = std::atof(val().c_str());
         else if (a == "--precision") c.precision = val();
         else if (a == "--device") c.device = std::atoi(val().c_str());
+        else if (a == "--snapshot-interval") c.snapshot_interval = std::strtoull(val().c_str(), nullptr, 10);
+        else if (a == "--snapshot-dir") c.snapshot_dir = val();
+        else if (a == "--restart") c.restart = val();
         else die("unknown argument " + a);
     }
     // the reference's input checks (main.rs:66-95)
@@ -135,12 +147,36 @@ Built build(const Cli &c) {
     return b;
 }
 
+void write_snapshot(const Context &ctx, Particles &p, const std::string &dir, double time, unsigned long long step,
+                    double softening, double dt) {
+    download(ctx, p);
+    char name[64];
+    std::snprintf(name, sizeof name, "/snap_%08llu.bin", step);
+    std::ofstream f(dir + name, std::ios::binary);
+    if (!f) die("Failed to create snapshot " + dir + name);
+    Snapshot::capture(p, time, step, softening, dt).write_to(f);
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
     const Cli cli = parse(argc, argv);
     try {
-        Built built = build(cli);
+        Built built;
+        double t_start = 0.0;
+        unsigned long long step0 = 0;
+        if (!cli.restart.empty()) {
+            std::ifstream f(cli.restart, std::ios::binary);
+            if (!f) die("Failed to open snapshot " + cli.restart);
+            Snapshot snap = Snapshot::read_from(f);
+            built = {snap.particles, snap.dt, snap.softening, "restart of " + cli.restart};
+            t_start = snap.time;
+            step0 = snap.step;
+            if (cli.dt > 0.0) built.dt = cli.dt;
+            if (cli.softening >= 0.0) built.softening = cli.softening;
+        } else {
+            built = build(cli);
+        }
         Particles &p = built.particles;
         const double softening = built.softening;
         const int prec = precision_of(cli.precision);
@@ -162,20 +198,22 @@ int main(int argc, char **argv) {
             *csv << Diagnostics::csv_header() << "\n";
         }
 
+        if (cli.snapshot_interval > 0) std::filesystem::create_directories(cli.snapshot_dir);
         // initial accelerations (main.rs:150-155): clear, gravity, SPH
         upload(ctx, p, false);
         ctx.check(gvs_compute_forces(ctx.get(), algo, prec, softening, cli.theta));
         if (use_sph) ctx.check(gvs_sph_compute(ctx.get(), &sph.params, nullptr, nullptr, nullptr, nullptr));
 
         const bool full = cli.diag_interval > 0 || csv;
-        const Diagnostics d0 = compute_diagnostics(ctx, softening, 0.0, 0, full);
+        const Diagnostics d0 = compute_diagnostics(ctx, softening, t_start, step0, full);
         std::fprintf(stderr, "Initial:    E=%.10e  2K/|U|=%.4f\n", d0.total_energy, d0.virial_ratio);
         if (csv) *csv << d0.to_csv_row() << "\n";
 
         const auto t0 = std::chrono::steady_clock::now();
-        double sim_time = 0.0, current_dt = built.dt;
-        unsigned long long step = 0;
-        while (step < cli.steps) {
+        double sim_time = t_start, current_dt = built.dt;
+        unsigned long long step = step0;
+        const unsigned long long last = step0 + cli.steps;
+        while (step < last) {
             if (use_sph) {
                 // step_with_sph, dt_next capped at 1.5x (main.rs:181-187)
                 double dt_next = 0.0;
@@ -186,8 +224,10 @@ int main(int argc, char **argv) {
                 ++step;
             } else {
                 // a fixed dt: run up to the next diagnostics step in one device-resident call
-                unsigned long long k = cli.steps - step;
+                unsigned long long k = last - step;
                 if (cli.diag_interval > 0) k = std::min(k, cli.diag_interval - step % cli.diag_interval);
+                if (cli.snapshot_interval > 0)
+                    k = std::min(k, cli.snapshot_interval - step % cli.snapshot_interval);
                 ctx.check(gvs_kdk_steps(ctx.get(), algo, prec, softening, cli.theta, current_dt, (long long)k));
                 for (unsigned long long s = 0; s < k; ++s) sim_time += current_dt;  // same sum as step by step
                 step += k;
@@ -199,18 +239,20 @@ int main(int argc, char **argv) {
                              d.total_energy, de, d.virial_ratio);
                 if (csv) *csv << d.to_csv_row() << "\n";
             }
+            if (cli.snapshot_interval > 0 && step % cli.snapshot_interval == 0)
+                write_snapshot(ctx, p, cli.snapshot_dir, sim_time, step, softening, current_dt);
         }
         ctx.check(gvs_sync(ctx.get()));
         const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 
-        const Diagnostics fd = compute_diagnostics(ctx, softening, sim_time, cli.steps, full);
+        const Diagnostics fd = compute_diagnostics(ctx, softening, sim_time, last, full);
         const double de = (fd.total_energy - d0.total_energy) / std::fabs(d0.total_energy);
         std::fprintf(stderr, "\n=== Final ===\nSim time:   %.6e\nWall time:  %.3fs\nSteps/sec:  %.0f\n", sim_time, wall,
                      (double)cli.steps / wall);
         std::fprintf(stderr, "Energy:     %.10e  (dE/E = %+.6e)\nMomentum:   %.6e\nAng. Mom:   %.6e\n",
                      fd.total_energy, de, fd.momentum_magnitude(), fd.angular_momentum_magnitude());
         std::fprintf(stderr, "COM drift:  %.6e\nVirial:     %.4f\n", fd.com_drift(), fd.virial_ratio);
-        const bool already = cli.diag_interval > 0 && cli.steps % cli.diag_interval == 0;
+        const bool already = cli.diag_interval > 0 && last % cli.diag_interval == 0;
         if (csv && !already) *csv << fd.to_csv_row() << "\n";
         std::printf("{\"steps\": %llu, \"wall_s\": %.6f, \"particle_steps_per_s\": %.6e, \"dE_over_E\": %.6e}\n",
                     cli.steps, wall, (double)p.count * (double)cli.steps / wall, de);

@@ -101,3 +101,54 @@ def test_drop_in_classes_match_resident_path(built):
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     assert r.stdout.count("ok  ") == 5
+
+
+# ---- snapshots (snapshot.rs: NBODY001..003) --------------------------------------------
+def test_snapshot_round_trip_and_old_versions(tmp_path):
+    """snapshot.rs:187-258 on the Python mirror: NBODY003 round trip; NBODY001/002
+    files read with zero types / gas fields."""
+    import io
+    import numpy as np
+    import gravis_gb300 as G
+    p = G.Particles(5)
+    rng = np.random.default_rng(3)
+    for f in ("x", "y", "z", "vx", "vy", "vz", "mass", "internal_energy", "smoothing_length", "density"):
+        getattr(p, f)[:] = rng.random(5)
+    p.particle_type[:] = [0, 4, 4, 1, 0]
+    buf = io.BytesIO()
+    G.Snapshot.capture(p, 1.25, 77, 0.01, 1e-3).write_to(buf)
+    raw = buf.getvalue()
+    assert raw[:8] == b"NBODY003" and len(raw) == 8 + 5 * 8 + 7 * 5 * 8 + 5 + 3 * 5 * 8
+    s = G.Snapshot.read_from(io.BytesIO(raw))
+    assert (s.time, s.step, s.softening, s.dt) == (1.25, 77, 0.01, 1e-3)
+    for f in ("x", "vz", "mass", "internal_energy", "density"):
+        assert np.array_equal(getattr(s.particles, f), getattr(p, f))
+    assert np.array_equal(s.particles.particle_type, p.particle_type)
+    assert np.all(s.particles.ax == 0.0)
+    v1 = b"NBODY001" + raw[8:8 + 40 + 7 * 40]
+    s1 = G.Snapshot.read_from(io.BytesIO(v1))
+    assert np.all(s1.particles.particle_type == 0) and np.all(s1.particles.internal_energy == 0.0)
+    assert np.array_equal(s1.particles.y, p.y)
+    with pytest.raises(ValueError):
+        G.Snapshot.read_from(io.BytesIO(b"NBODY999" + raw[8:]))
+
+
+@pytest.mark.gpu
+def test_headless_snapshot_restart_is_seamless(built, tmp_path):
+    """Run 200 steps writing snapshots every 100; restart from step 100 and run 100
+    more: the step-200 snapshots are identical (FP64_EXACT, accelerations recomputed
+    on restart as Snapshot::initialize does), and Python reads the C++ files."""
+    import numpy as np
+    import gravis_gb300 as G
+    a, b = tmp_path / "a", tmp_path / "b"
+    r = run("--scenario", "plummer", "-n", "2000", "--steps", "200", "--diag-interval", "0",
+            "--snapshot-interval", "100", "--snapshot-dir", str(a))
+    assert r.returncode == 0, r.stderr
+    r = run("--restart", str(a / "snap_00000100.bin"), "--steps", "100", "--diag-interval", "0",
+            "--snapshot-interval", "100", "--snapshot-dir", str(b))
+    assert r.returncode == 0, r.stderr
+    with open(a / "snap_00000200.bin", "rb") as fa, open(b / "snap_00000200.bin", "rb") as fb:
+        sa, sb = G.Snapshot.read_from(fa), G.Snapshot.read_from(fb)
+    assert sa.step == sb.step == 200 and sa.time == sb.time
+    for f in ("x", "y", "z", "vx", "vy", "vz", "mass"):
+        assert np.array_equal(getattr(sa.particles, f), getattr(sb.particles, f)), f
