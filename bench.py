@@ -471,13 +471,29 @@ def run_workload(a, d):
                     ms.append(ctx.elapsed(0, 1))
             return sum(ms), clk.summary()
 
-        qe, qm = sph_only(G.PREC_FP64_EXACT), sph_only(G.PREC_MIXED)
+        qe = sph_only(G.PREC_FP64_EXACT)
+        ctx.profile(True)
+        qm = sph_only(G.PREC_MIXED)
+        redo = ctx.profile_read()["sph_f64_redo"]
+        ctx.profile(False)
 
         def rel(f):
             x, y = getattr(qm, f), getattr(qe, f)
             return float(np.sqrt(((x - y) ** 2).sum() / max((y ** 2).sum(), 1e-300)))
 
         errs = {f: rel(f) for f in ("density", "smoothing_length", "ax", "ay", "az", "du_dt")}
+        # where the relative RMS comes from: particles whose h differs by more than 1e-5 are
+        # those whose h-iteration stopping decision (|dh|/h < 1e-3) fell the other way
+        dh = np.abs(qm.smoothing_length - qe.smoothing_length) / np.maximum(qe.smoothing_length, 1e-300)
+        am, ae = np.stack([qm.ax, qm.ay, qm.az], 1), np.stack([qe.ax, qe.ay, qe.az], 1)
+        scale = np.sqrt((ae ** 2).sum(1).mean())
+        ea = np.sqrt(((am - ae) ** 2).sum(1)) / scale
+        errs["h_iteration_outliers"] = int((dh > 1e-5).sum())
+        errs["particles_rerun_in_f64"] = int(redo)
+        errs["per_particle_a_err_over_rms_a"] = {"p50": float(np.percentile(ea, 50)),
+                                                 "p99": float(np.percentile(ea, 99)),
+                                                 "p99.9": float(np.percentile(ea, 99.9)),
+                                                 "max": float(ea.max())}
         t_ex, _ = timed(G.PREC_FP64_EXACT)
         t, clk = timed(G.PREC_MIXED)
         res.update({"value": n * a.steps / (t * 1e-3), "ms_per_step": t / a.steps,

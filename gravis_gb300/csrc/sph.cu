@@ -44,6 +44,7 @@ struct SphState {
     DevBuf dtpart;
     DevBuf pos4, node4;  // f32 copies for the neighbour-search prefilter
     DevBuf a4, b4, c4, d4, e4, f4;  // mixed precision: packed sources (see k_sph_src_*)
+    DevBuf redo_idx, redo_count;    // mixed precision: particles whose h iteration runs again in f64
     bool have_intermediates = false;
 };
 
@@ -321,16 +322,13 @@ __device__ __forceinline__ void density_sums_f64(const TreeView &tv, const doubl
 }
 
 // compute_density (density.rs:42-125) for one target per thread, then the EOS.
-__global__ void k_density(const TreeView tv, const float4 *__restrict__ pos4, const float4 *__restrict__ node4,
-                          const uint8_t *__restrict__ gas, const double *__restrict__ sm,
-                          const double *__restrict__ su, double *__restrict__ sh, uint32_t *__restrict__ list,
-                          uint32_t *__restrict__ cnt, int kmax, double gamma, double eta, double h_max,
-                          double *__restrict__ rho_out, double *__restrict__ omega_out, double *__restrict__ pres,
-                          double *__restrict__ cs, unsigned *__restrict__ err) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= tv.n) return;
-    omega_out[i] = 1.0;
-    if (!gas[i]) return;
+__device__ void density_particle_f64(const TreeView &tv, const float4 *__restrict__ pos4,
+                                     const float4 *__restrict__ node4, const double *__restrict__ sm,
+                                     const double *__restrict__ su, double *__restrict__ sh,
+                                     uint32_t *__restrict__ list, uint32_t *__restrict__ cnt, int kmax, double gamma,
+                                     double eta, double h_max, double *__restrict__ rho_out,
+                                     double *__restrict__ omega_out, double *__restrict__ pres,
+                                     double *__restrict__ cs, unsigned *__restrict__ err, size_t i) {
     const double search_padding = 1.1;
     const double xi = tv.sx[i], yi = tv.sy[i], zi = tv.sz[i];
     const double m_i = sm[i];
@@ -368,6 +366,20 @@ __global__ void k_density(const TreeView tv, const float4 *__restrict__ pos4, co
     const double u = su[i];
     pres[i] = (gamma - 1.0) * rho_last * u;
     cs[i] = sqrt(gamma * (gamma - 1.0) * fmax(u, 0.0));
+}
+
+__global__ void k_density(const TreeView tv, const float4 *__restrict__ pos4, const float4 *__restrict__ node4,
+                          const uint8_t *__restrict__ gas, const double *__restrict__ sm,
+                          const double *__restrict__ su, double *__restrict__ sh, uint32_t *__restrict__ list,
+                          uint32_t *__restrict__ cnt, int kmax, double gamma, double eta, double h_max,
+                          double *__restrict__ rho_out, double *__restrict__ omega_out, double *__restrict__ pres,
+                          double *__restrict__ cs, unsigned *__restrict__ err) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= tv.n) return;
+    omega_out[i] = 1.0;
+    if (!gas[i]) return;
+    density_particle_f64(tv, pos4, node4, sm, su, sh, list, cnt, kmax, gamma, eta, h_max, rho_out, omega_out, pres,
+                         cs, err, i);
 }
 
 // compute_forces (forces.rs:69-232), one target per thread.
@@ -494,14 +506,14 @@ __global__ void k_sph_src_pos(const TreeView tv, const double *__restrict__ sm, 
 
 // sources for the mixed forces (after the density pass):
 //   c = (vx hi, vy hi, vz hi, 1/h)  d = (vx lo, vy lo, vz lo, -5 norm / h^5)
-//   e = (h, max(rho, floor), P / (Omega rho^2), c)  f = (alpha, P, u, 0)
+//   e = (h, max(rho, floor), P / (Omega rho^2), c)  f = (alpha, P, u, m P / (Omega rho^2) K(h))
 __global__ void k_sph_src_hydro(size_t n, const double *__restrict__ svx, const double *__restrict__ svy,
                                 const double *__restrict__ svz, const double *__restrict__ sh,
                                 const double *__restrict__ srho, const double *__restrict__ spres,
                                 const double *__restrict__ scs, const double *__restrict__ salpha,
                                 const double *__restrict__ somega, const double *__restrict__ su,
-                                float4 *__restrict__ c4, float4 *__restrict__ d4, float4 *__restrict__ e4,
-                                float4 *__restrict__ f4) {
+                                const double *__restrict__ sm, float4 *__restrict__ c4, float4 *__restrict__ d4,
+                                float4 *__restrict__ e4, float4 *__restrict__ f4) {
     const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     float vxh, vxl, vyh, vyl, vzh, vzl;
@@ -513,10 +525,11 @@ __global__ void k_sph_src_hydro(size_t n, const double *__restrict__ svx, const 
     const double p = spres[j];
     const double por2 = rho > 0.0 ? p / (somega[j] * rho * rho) : 0.0;
     const double h2 = h * h;
+    const double K = -5.0 * norm3d() / (h2 * h2 * h);
     c4[j] = make_float4(vxh, vyh, vzh, (float)(1.0 / h));
-    d4[j] = make_float4(vxl, vyl, vzl, (float)(-5.0 * norm3d() / (h2 * h2 * h)));
+    d4[j] = make_float4(vxl, vyl, vzl, (float)K);
     e4[j] = make_float4((float)h, (float)rho, (float)por2, (float)scs[j]);
-    f4[j] = make_float4((float)salpha[j], (float)p, (float)su[j], 0.f);
+    f4[j] = make_float4((float)salpha[j], (float)p, (float)su[j], (float)(sm[j] * por2 * K));
 }
 
 // Mixed sums of one density iteration: S1 = sum m f(q), S2 = sum m (5 q^2 s^3 - 3 f(q))
@@ -532,7 +545,7 @@ __device__ __forceinline__ void density_sums_mixed(const float4 *__restrict__ a4
         const float dy = __fadd_rn(__fsub_rn(pa.y, a.y), __fsub_rn(pb.y, b.y));
         const float dz = __fadd_rn(__fsub_rn(pa.z, a.z), __fsub_rn(pb.z, b.z));
         const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-        const float r = d2 > 0.f ? __fmul_rn(d2, rsqrt_approx(d2)) : 0.f;
+        const float r = __fsqrt_rn(d2);  // correctly rounded: the net SPH force is a small remainder of the pair terms
         const float q = __fmul_rn(r, ih);
         if (q < 2.0f) {
             const float sq = __fmaf_rn(-0.5f, q, 1.0f);
@@ -547,10 +560,12 @@ __device__ __forceinline__ void density_sums_mixed(const float4 *__restrict__ a4
     s2 = (double)h2 + (double)l2;
 }
 
-// compute_density with mixed sums.  A decision of the h iteration that lies
-// within 1e-6 of its threshold (convergence at 1e-3, re-query at a ratio of
-// 1.1) is taken again on the f64 sums of that iteration, so the iteration
-// path is the f64 one.
+// compute_density with mixed sums.  The mixed h sequence drifts from the f64
+// one by ~1e-7 relative, so a stopping or re-query decision that comes within
+// 1e-4 of its threshold (convergence at 1e-3, re-query at a ratio of 1.1) could
+// go the other way.  Such a particle is listed for k_density_redo, which runs
+// its whole iteration again on the f64 path from the initial h: every
+// particle's iteration path is then the f64 one.
 __global__ void k_density_mixed(const TreeView tv, const float4 *__restrict__ pos4, const float4 *__restrict__ node4,
                                 const float4 *__restrict__ a4, const float4 *__restrict__ b4,
                                 const uint8_t *__restrict__ gas, const double *__restrict__ sm,
@@ -558,7 +573,7 @@ __global__ void k_density_mixed(const TreeView tv, const float4 *__restrict__ po
                                 uint32_t *__restrict__ cnt, int kmax, double gamma, double eta, double h_max,
                                 double *__restrict__ rho_out, double *__restrict__ omega_out,
                                 double *__restrict__ pres, double *__restrict__ cs, unsigned *__restrict__ err,
-                                unsigned *__restrict__ f64_redo) {
+                                uint32_t *__restrict__ redo_idx, unsigned *__restrict__ redo_count) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= tv.n) return;
     omega_out[i] = 1.0;
@@ -571,19 +586,15 @@ __global__ void k_density_mixed(const TreeView tv, const float4 *__restrict__ po
     uint32_t *row = list + i * (size_t)kmax;
     int count = (int)cnt[i];
     double rho_last = rho_out[i];
-    unsigned redo = 0;
+    bool close = false;
     for (int it = 0; it < 5; ++it) {
         double s1, s2;
         density_sums_mixed(a4, b4, row, count, pa, pb, (float)(1.0 / h), s1, s2);
         const double nh3 = norm3d() / (h * h * h);
-        double rho = nh3 * s1, dws = nh3 / h * s2;
-        double h_new = rho > 0.0 ? fmin(eta * cbrt(m_i / rho), h_max) : fmin(h, h_max);
+        const double rho = nh3 * s1, dws = nh3 / h * s2;
+        const double h_new = rho > 0.0 ? fmin(eta * cbrt(m_i / rho), h_max) : fmin(h, h_max);
         const double ratio = fabs(h_new - h) / fmax(h, 1e-30);
-        if (fabs(ratio - 1e-3) < 1e-6 || fabs(h_new / h - search_padding) < 1e-6) {
-            density_sums_f64(tv, sm, row, count, xi, yi, zi, h, rho, dws);
-            h_new = rho > 0.0 ? fmin(eta * cbrt(m_i / rho), h_max) : fmin(h, h_max);
-            ++redo;
-        }
+        close = close || fabs(ratio - 1e-3) < 1e-4 || fabs(h_new / h - search_padding) < 1e-4;
         if (rho > 0.0) {
             const double dh_drho = -h_new / (3.0 * rho);
             double om = 1.0 - dh_drho * dws;
@@ -605,22 +616,59 @@ __global__ void k_density_mixed(const TreeView tv, const float4 *__restrict__ po
         }
         h = h_new;
     }
-    if (redo) atomicAdd(f64_redo, redo);
+    if (close) redo_idx[atomicAdd(redo_count, 1u)] = (uint32_t)i;
     rho_out[i] = rho_last;
     const double u = su[i];
     pres[i] = (gamma - 1.0) * rho_last * u;
     cs[i] = sqrt(gamma * (gamma - 1.0) * fmax(u, 0.0));
 }
 
+// The listed particles' h iteration again, on the f64 path from the initial h
+// h0 and the original neighbour list (re-queried at radius 2 h0 1.1, as
+// build_neighbor_lists made it).  Grid-stride over the list, whose length is on
+// the device.
+__global__ void k_density_redo(const TreeView tv, const float4 *__restrict__ pos4, const float4 *__restrict__ node4,
+                               const double *__restrict__ sm, const double *__restrict__ su,
+                               const double *__restrict__ h0, double *__restrict__ sh, uint32_t *__restrict__ list,
+                               uint32_t *__restrict__ cnt, int kmax, double gamma, double eta, double h_max,
+                               double *__restrict__ rho_out, double *__restrict__ omega_out,
+                               double *__restrict__ pres, double *__restrict__ cs, unsigned *__restrict__ err,
+                               const uint32_t *__restrict__ redo_idx, const unsigned *__restrict__ redo_count,
+                               unsigned *__restrict__ redo_total) {
+    const unsigned m = *redo_count;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && m) atomicAdd(redo_total, m);
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+        const size_t i = redo_idx[k];
+        const double hh = h0[i];
+        sh[i] = hh;
+        omega_out[i] = 1.0;
+        int count = ball_query_thread(tv, pos4, node4, prefilter_scale(tv), tv.sx[i], tv.sy[i], tv.sz[i],
+                                      2.0 * hh * 1.1, list + i * (size_t)kmax, kmax);
+        if (count > kmax) {
+            atomicOr(err, (unsigned)DERR_NEIGH_OVERFLOW);
+            count = kmax;
+        }
+        cnt[i] = (uint32_t)count;
+        density_particle_f64(tv, pos4, node4, sm, su, sh, list, cnt, kmax, gamma, eta, h_max, rho_out, omega_out,
+                             pres, cs, err, i);
+    }
+}
+
 // compute_forces (forces.rs:69-232) with f32 pair terms.  With q/r = 1/h the
 // kernel gradient is dx * K(h) s^3, K(h) = -5 norm / h^5, and |grad W| =
-// -K(h) s^3 r.
+// -K(h) s^3 r.  The net pressure force is a small remainder of its pair terms,
+// so the per-target factors are kept out of the sums and applied in f64:
+//   a   = -(P_i/(Omega_i rho_i^2) K_i) sum m_j s_i^3 dx - sum (m P/(Omega rho^2) K)_j s_j^3 dx
+//         - sum m_j Pi_ij K_avg s_avg^3 dx
+//   du  =  (P_i/(Omega_i rho_i^2) K_i) sum m_j s_i^3 (v.dx) + 1/2 sum m_j Pi_ij K_avg s_avg^3 (v.dx) + cond.
+//   div v = -(K_i / rho_i) sum m_j s_i^3 (v.dx)
 __global__ void __launch_bounds__(128) k_forces_mixed(
     size_t n, const uint8_t *__restrict__ gas, const uint32_t *__restrict__ list, const uint32_t *__restrict__ cnt,
     int kmax, const float4 *__restrict__ a4, const float4 *__restrict__ b4, const float4 *__restrict__ c4,
     const float4 *__restrict__ d4, const float4 *__restrict__ e4, const float4 *__restrict__ f4,
     const double *__restrict__ sh, const double *__restrict__ srho, const double *__restrict__ scs,
-    const double *__restrict__ salpha, gvs_sph_params prm, double *__restrict__ sax, double *__restrict__ say,
+    const double *__restrict__ salpha, const double *__restrict__ spres, const double *__restrict__ somega,
+    gvs_sph_params prm, double *__restrict__ sax, double *__restrict__ say,
     double *__restrict__ saz, double *__restrict__ sdu, double *__restrict__ sdivv, double *__restrict__ smaxmu,
     double *__restrict__ sdalpha) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -631,12 +679,16 @@ __global__ void __launch_bounds__(128) k_forces_mixed(
     sax[i] = say[i] = saz[i] = sdu[i] = 0.0;
     if (!gas[i]) return;
     const float4 pa = a4[i], pb = b4[i], pc = c4[i], pd = d4[i], pe = e4[i], pf = f4[i];
-    const float hi_f = pe.x, ih_i = pc.w, K_i = pd.w, rho_i = pe.y, por2_i = pe.z, c_i = pe.w;
+    const float hi_f = pe.x, ih_i = pc.w, rho_i = pe.y, c_i = pe.w;
     const float alpha_i = pf.x, p_i = pf.y, u_i = pf.z;
     const float beta = (float)prm.beta_visc, acond = (float)prm.alpha_cond;
     const float cnorm5 = (float)(-5.0 * norm3d() * 32.0);  // K(h_avg) = cnorm5 / (hi + hj)^5
-    float axh = 0.f, axl = 0.f, ayh = 0.f, ayl = 0.f, azh = 0.f, azl = 0.f, duh = 0.f, dul = 0.f, dvh = 0.f,
-          dvl = 0.f, mmu = 0.f;
+    // (hi, lo) sums: A = m s_i^3 dx, B = c_j s_j^3 dx, C = m Pi K_avg s_avg^3 dx (3 components each),
+    // D1 = m s_i^3 v.dx, D2 = m Pi K_avg s_avg^3 v.dx, E = conduction
+    float sum[12][2];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) sum[k][0] = sum[k][1] = 0.f;
+    float mmu = 0.f;
     const uint32_t *row = list + i * (size_t)kmax;
     const int count = (int)cnt[i];
     for (int k = 0; k < count; ++k) {
@@ -647,7 +699,7 @@ __global__ void __launch_bounds__(128) k_forces_mixed(
         const float dy = __fadd_rn(__fsub_rn(pa.y, a.y), __fsub_rn(pb.y, b.y));
         const float dz = __fadd_rn(__fsub_rn(pa.z, a.z), __fsub_rn(pb.z, b.z));
         const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-        const float r = d2 > 0.f ? __fmul_rn(d2, rsqrt_approx(d2)) : 0.f;
+        const float r = __fsqrt_rn(d2);  // correctly rounded: the net SPH force is a small remainder of the pair terms
         const float4 e = e4[j];
         const float hj = e.x;
         if (r >= 2.0f * hi_f && r >= 2.0f * hj) continue;
@@ -658,13 +710,13 @@ __global__ void __launch_bounds__(128) k_forces_mixed(
         const float dvz = __fadd_rn(__fsub_rn(pc.z, c.z), __fsub_rn(pd.z, d.z));
         const float vr = __fmaf_rn(dvz, dz, __fmaf_rn(dvy, dy, __fmul_rn(dvx, dx)));
         // kernel-gradient scalars (gradient = scalar * (dx, dy, dz)); zero at r = 0 or q >= 2
-        float fi = 0.f, fj = 0.f, fa = 0.f, sa3 = 0.f, Ka = 0.f;
+        float si3 = 0.f, sj3 = 0.f, fa = 0.f, sa3 = 0.f, Ka = 0.f;
         const float hsum = __fadd_rn(hi_f, hj);
         const float h_avg = 0.5f * hsum;
         if (r >= 1e-30f) {
             const float qi = __fmul_rn(r, ih_i), qj = __fmul_rn(r, c.w);
-            if (qi < 2.0f) { const float s = __fmaf_rn(-0.5f, qi, 1.0f); fi = __fmul_rn(K_i, __fmul_rn(__fmul_rn(s, s), s)); }
-            if (qj < 2.0f) { const float s = __fmaf_rn(-0.5f, qj, 1.0f); fj = __fmul_rn(d.w, __fmul_rn(__fmul_rn(s, s), s)); }
+            if (qi < 2.0f) { const float s = __fmaf_rn(-0.5f, qi, 1.0f); si3 = __fmul_rn(__fmul_rn(s, s), s); }
+            if (qj < 2.0f) { const float s = __fmaf_rn(-0.5f, qj, 1.0f); sj3 = __fmul_rn(__fmul_rn(s, s), s); }
             const float iha = __frcp_rn(h_avg);
             const float qa = __fmul_rn(r, iha);
             if (qa < 2.0f) {
@@ -675,7 +727,7 @@ __global__ void __launch_bounds__(128) k_forces_mixed(
                 fa = __fmul_rn(Ka, sa3);
             }
         }
-        const float rho_j = e.y, por2_j = e.z, c_j = e.w, alpha_j = f.x, p_j = f.y, u_j = f.z;
+        const float rho_j = e.y, c_j = e.w, alpha_j = f.x, p_j = f.y, u_j = f.z, cw_j = f.w;
         float pi_ij = 0.f;
         if (vr < 0.f) {
             const float alpha_avg = 0.5f * __fadd_rn(alpha_i, alpha_j);
@@ -687,29 +739,45 @@ __global__ void __launch_bounds__(128) k_forces_mixed(
             if (rho_avg > 0.f)
                 pi_ij = __fdiv_rn(__fmaf_rn(beta * mu, mu, -__fmul_rn(__fmul_rn(alpha_avg, c_avg), mu)), rho_avg);
         }
-        const float t = __fmul_rn(mj, __fmaf_rn(pi_ij, fa, __fmaf_rn(por2_j, fj, __fmul_rn(por2_i, fi))));
-        tsum(axh, axl, -__fmul_rn(t, dx));
-        tsum(ayh, ayl, -__fmul_rn(t, dy));
-        tsum(azh, azl, -__fmul_rn(t, dz));
-        const float vgi = __fmul_rn(fi, vr), vga = __fmul_rn(fa, vr);
-        float du = __fmul_rn(mj, __fmaf_rn(0.5f * pi_ij, vga, __fmul_rn(por2_i, vgi)));
+        const float ma = __fmul_rn(mj, si3), mb = __fmul_rn(cw_j, sj3);
+        tsum(sum[0][0], sum[0][1], __fmul_rn(ma, dx));
+        tsum(sum[1][0], sum[1][1], __fmul_rn(ma, dy));
+        tsum(sum[2][0], sum[2][1], __fmul_rn(ma, dz));
+        tsum(sum[3][0], sum[3][1], __fmul_rn(mb, dx));
+        tsum(sum[4][0], sum[4][1], __fmul_rn(mb, dy));
+        tsum(sum[5][0], sum[5][1], __fmul_rn(mb, dz));
+        tsum(sum[9][0], sum[9][1], __fmul_rn(ma, vr));
+        if (pi_ij != 0.f) {
+            const float mc = __fmul_rn(__fmul_rn(mj, pi_ij), fa);
+            tsum(sum[6][0], sum[6][1], __fmul_rn(mc, dx));
+            tsum(sum[7][0], sum[7][1], __fmul_rn(mc, dy));
+            tsum(sum[8][0], sum[8][1], __fmul_rn(mc, dz));
+            tsum(sum[10][0], sum[10][1], __fmul_rn(mc, vr));
+        }
         if (acond > 0.f) {
             const float rho_sum = __fadd_rn(rho_i, rho_j);
             if (rho_sum > 0.f) {
                 const float v_sig = sqrtf(__fdiv_rn(fabsf(__fsub_rn(p_i, p_j)), 0.5f * rho_sum));
                 const float abs_gw = -__fmul_rn(__fmul_rn(Ka, sa3), r);
-                du = __fmaf_rn(__fmul_rn(mj, acond), __fmul_rn(__fdiv_rn(__fmul_rn(v_sig, __fsub_rn(u_i, u_j)), rho_sum), abs_gw), du);
+                tsum(sum[11][0], sum[11][1],
+                     __fmul_rn(__fmul_rn(mj, acond),
+                               __fmul_rn(__fdiv_rn(__fmul_rn(v_sig, __fsub_rn(u_i, u_j)), rho_sum), abs_gw)));
             }
         }
-        tsum(duh, dul, du);
-        tsum(dvh, dvl, -__fmul_rn(mj, vgi));
     }
-    sax[i] = (double)axh + (double)axl;
-    say[i] = (double)ayh + (double)ayl;
-    saz[i] = (double)azh + (double)azl;
-    sdu[i] = (double)duh + (double)dul;
+    double S[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) S[k] = (double)sum[k][0] + (double)sum[k][1];
     const double rho_i64 = fmax(srho[i], 1e-10);
-    const double dva = (double)dvh + (double)dvl;
+    const double hh = sh[i], hh2 = hh * hh;
+    const double K_i64 = -5.0 * norm3d() / (hh2 * hh2 * hh);
+    const double por2_i64 = rho_i64 > 0.0 ? spres[i] / (somega[i] * rho_i64 * rho_i64) : 0.0;
+    const double pk = por2_i64 * K_i64;
+    sax[i] = -(pk * S[0] + S[3] + S[6]);
+    say[i] = -(pk * S[1] + S[4] + S[7]);
+    saz[i] = -(pk * S[2] + S[5] + S[8]);
+    sdu[i] = pk * S[9] + 0.5 * S[10] + S[11];
+    const double dva = -K_i64 * S[9];
     double dv = 0.0;
     if (rho_i64 > 0.0) dv = dva / rho_i64;
     sdivv[i] = dv;
@@ -831,7 +899,7 @@ void sph_free(Ctx *c) {
     DevBuf *all[] = {&s->list, &s->cnt, &s->gas, &s->sx, &s->sy, &s->sz, &s->svx, &s->svy, &s->svz, &s->sm,
                      &s->sh, &s->su, &s->salpha, &s->srho, &s->spres, &s->scs, &s->somega, &s->sdivv, &s->smaxmu,
                      &s->sdalpha, &s->sax, &s->say, &s->saz, &s->sdu, &s->dtpart, &s->pos4, &s->node4,
-                     &s->a4, &s->b4, &s->c4, &s->d4, &s->e4, &s->f4};
+                     &s->a4, &s->b4, &s->c4, &s->d4, &s->e4, &s->f4, &s->redo_idx, &s->redo_count};
     for (DevBuf *b : all)
         if (b->ptr) cudaFree(b->ptr);
     delete s;
@@ -860,6 +928,8 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
     if (mixed) {
         DevBuf *f4s[] = {&S->a4, &S->b4, &S->c4, &S->d4, &S->e4, &S->f4};
         for (DevBuf *d : f4s) GVS_CUDA(c, ensure(c, *d, n * 16));
+        GVS_CUDA(c, ensure(c, S->redo_idx, n * 4));
+        GVS_CUDA(c, ensure(c, S->redo_count, 4));
     }
     k_gather_sph<<<nb(n), 256, 0, st>>>(n, tv.perm, as<uint8_t>(c->ptype), as<double>(c->vx), as<double>(c->vy),
                                         as<double>(c->vz), as<double>(c->m), as<double>(c->h), as<double>(c->u),
@@ -884,13 +954,22 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
         k_neighbors<<<nb(n, 128), 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4), as<uint8_t>(S->gas),
                                                 as<double>(S->sh), 1.1, S->kmax,
                                                 as<uint32_t>(S->list), as<uint32_t>(S->cnt), err_ptr(c));
-        if (mixed)
+        if (mixed) {
+            GVS_CUDA(c, cudaMemsetAsync(S->redo_count.ptr, 0, 4, st));
             k_density_mixed<<<nb(n, 128), 128, 0, st>>>(
                 tv, as<float4>(S->pos4), as<float4>(S->node4), as<float4>(S->a4), as<float4>(S->b4),
                 as<uint8_t>(S->gas), as<double>(S->sm), as<double>(S->su), as<double>(S->sh), as<uint32_t>(S->list),
                 as<uint32_t>(S->cnt), S->kmax, prm->gamma, prm->eta, prm->h_max, as<double>(S->srho),
-                as<double>(S->somega), as<double>(S->spres), as<double>(S->scs), err_ptr(c), err_ptr(c) + 10);
-        else
+                as<double>(S->somega), as<double>(S->spres), as<double>(S->scs), err_ptr(c),
+                as<uint32_t>(S->redo_idx), as<unsigned>(S->redo_count));
+            k_density_redo<<<std::max(1, c->num_sms * 2), 128, 0, st>>>(
+                tv, as<float4>(S->pos4), as<float4>(S->node4), as<double>(S->sm), as<double>(S->su),
+                as<double>(c->scratch_b), as<double>(S->sh), as<uint32_t>(S->list), as<uint32_t>(S->cnt), S->kmax,
+                prm->gamma, prm->eta, prm->h_max, as<double>(S->srho), as<double>(S->somega), as<double>(S->spres),
+                as<double>(S->scs), err_ptr(c), as<uint32_t>(S->redo_idx), as<unsigned>(S->redo_count),
+                err_ptr(c) + 10);
+            c->prof.launches += 1;
+        } else
             k_density<<<nb(n, 128), 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4), as<uint8_t>(S->gas),
                                                   as<double>(S->sm), as<double>(S->su),
                                                   as<double>(S->sh), as<uint32_t>(S->list), as<uint32_t>(S->cnt),
@@ -914,12 +993,13 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
         k_sph_src_hydro<<<nb(n), 256, 0, st>>>(n, as<double>(S->svx), as<double>(S->svy), as<double>(S->svz),
                                                as<double>(S->sh), as<double>(S->srho), as<double>(S->spres),
                                                as<double>(S->scs), as<double>(S->salpha), as<double>(S->somega),
-                                               as<double>(S->su), as<float4>(S->c4), as<float4>(S->d4),
+                                               as<double>(S->su), as<double>(S->sm), as<float4>(S->c4), as<float4>(S->d4),
                                                as<float4>(S->e4), as<float4>(S->f4));
         k_forces_mixed<<<nb(n, 128), 128, 0, st>>>(
             n, as<uint8_t>(S->gas), as<uint32_t>(S->list), as<uint32_t>(S->cnt), S->kmax, as<float4>(S->a4),
             as<float4>(S->b4), as<float4>(S->c4), as<float4>(S->d4), as<float4>(S->e4), as<float4>(S->f4),
-            as<double>(S->sh), as<double>(S->srho), as<double>(S->scs), as<double>(S->salpha), *prm,
+            as<double>(S->sh), as<double>(S->srho), as<double>(S->scs), as<double>(S->salpha), as<double>(S->spres),
+            as<double>(S->somega), *prm,
             as<double>(S->sax), as<double>(S->say), as<double>(S->saz), as<double>(S->sdu), as<double>(S->sdivv),
             as<double>(S->smaxmu), as<double>(S->sdalpha));
         c->prof.launches += 1;

@@ -89,7 +89,8 @@ typedef struct gvs_profile {
     double near_tile_visits;  /* of which took the float-float near-field path */
     double vjp_ms;            /* device time of the fused force + VJP kernels (adjoint) */
     long long vjp_launches;
-    long long sph_f64_redo;   /* mixed SPH: h-iteration steps redone on f64 sums (borderline) */
+    long long sph_f64_redo;   /* mixed SPH: particles whose h iteration was rerun on the f64 path
+                                 (a stopping or re-query decision within 1e-4 of its threshold) */
 } gvs_profile;
 
 /* ---- library / context ---------------------------------------------------- */

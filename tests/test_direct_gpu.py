@@ -271,3 +271,24 @@ def test_graph_replayed_steps_equal_eager_steps(ctx, prec):
     ctx.kdk_steps(G.ALGO_DIRECT, prec, eps, 0.0, dt, 3)
     ctx.kdk_steps(G.ALGO_DIRECT, prec, eps, 0.0, 0.5 * dt, 3)
     ctx.sync()
+
+
+def test_mixed_at_full_size(ctx):
+    """N = 2^20 (the headline workload): mixed forces on 2048 random targets within
+    1e-6 relative RMS of the exact f64 sum, and the size-independent momentum
+    check: sum m a = 0 up to the f32 rounding of the pair terms."""
+    n = 1 << 20
+    p = G.PlummerSphere(n, seed=1).generate()
+    eps = 0.04 / n ** (1.0 / 3.0)
+    ctx.set_state(p)
+    ctx.compute_forces(G.ALGO_DIRECT, G.PREC_MIXED, eps)
+    q = G.Particles(n)
+    ctx.get_state(q)
+    idx = np.sort(np.random.default_rng(4).choice(n, 2048, replace=False))
+    ref = ctx.direct_subset(idx, eps)
+    err = rel_rms(q.acc()[idx], ref)
+    print(f"N=2^20 mixed vs exact on 2048 targets: rel RMS {err:.2e}")
+    assert err <= 1e-6
+    ma = (q.acc() * q.mass[:, None]).sum(0)
+    scale = (np.abs(q.acc()) * q.mass[:, None]).sum(0)
+    assert np.all(np.abs(ma) <= 1e-6 * scale), (ma, scale)
