@@ -80,13 +80,34 @@ __global__ void k_bbox_part(const double *__restrict__ x, const double *__restri
     }
 }
 
-__global__ void k_bbox_final(double *part, int nparts) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    for (int b = 1; b < nparts; ++b)
+// One block of 256 threads folds the per-block parts into part[0..5].
+__global__ void __launch_bounds__(256) k_bbox_final(double *part, int nparts) {
+    double v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x)
+#pragma unroll
         for (int d = 0; d < 3; ++d) {
-            part[d] = fmin(part[d], part[b * 6 + d]);
-            part[3 + d] = fmax(part[3 + d], part[b * 6 + 3 + d]);
+            v[d] = fmin(v[d], part[b * 6 + d]);
+            v[3 + d] = fmax(v[3 + d], part[b * 6 + 3 + d]);
         }
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        for (int o = 16; o > 0; o >>= 1) {
+            v[d] = fmin(v[d], __shfl_xor_sync(0xFFFFFFFFu, v[d], o));
+            v[3 + d] = fmax(v[3 + d], __shfl_xor_sync(0xFFFFFFFFu, v[3 + d], o));
+        }
+    __shared__ double s[8][6];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 6; ++k) s[w][k] = v[k];
+    __syncthreads();  // every thread has read its parts before part[0..5] is written
+    if (threadIdx.x == 0) {
+        for (int ww = 1; ww < (int)(blockDim.x >> 5); ++ww)
+            for (int d = 0; d < 3; ++d) {
+                s[0][d] = fmin(s[0][d], s[ww][d]);
+                s[0][3 + d] = fmax(s[0][3 + d], s[ww][3 + d]);
+            }
+        for (int k = 0; k < 6; ++k) part[k] = s[0][k];
+    }
 }
 
 __global__ void k_hilbert(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
@@ -1194,7 +1215,7 @@ gvs_status bbox_minmax(Ctx *c, double *dev_out6, DevBuf &part_buf) {
     GVS_CUDA(c, ensure(c, part_buf, (size_t)nb * 6 * sizeof(double)));
     double *bb = as<double>(part_buf);
     k_bbox_part<<<nb, 256, 0, c->stream>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z), n, bb);
-    k_bbox_final<<<1, 32, 0, c->stream>>>(bb, nb);
+    k_bbox_final<<<1, 256, 0, c->stream>>>(bb, nb);
     c->prof.launches += 2;
     GVS_CUDA(c, cudaMemcpyAsync(dev_out6, bb, 6 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     return check_launch(c, "bounding box");
@@ -1211,7 +1232,7 @@ gvs_status spatial_order(Ctx *c) {
     GVS_CUDA(c, ensure(c, c->perm_alt, n * 4));
     double *bb = as<double>(c->bbox_part);
     k_bbox_part<<<nb, 256, 0, c->stream>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z), n, bb);
-    k_bbox_final<<<1, 32, 0, c->stream>>>(bb, nb);
+    k_bbox_final<<<1, 256, 0, c->stream>>>(bb, nb);
     k_hilbert<<<ceil_div((long long)n, 256), 256, 0, c->stream>>>(as<double>(c->x), as<double>(c->y),
                                                                   as<double>(c->z), n, bb, as<uint64_t>(c->keys),
                                                                   as<uint32_t>(c->perm));

@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(SCAN_NT) k_scan_apply(const uint32_t *in, size
 // then the block-local scans plus their offsets.  In place is safe: every thread
 // reads its own elements before writing them.
 void scan_counts_inplace(Ctx *c, uint32_t *a, size_t m, uint32_t *bsum) {
-    if (m <= 16 * 1024) {  // small tables: one launch of one block beats three launches
+    if (m <= 4 * 1024) {  // small tables: one launch of one block beats three launches
         k_scan1<<<1, 1024, 0, c->stream>>>(a, (int)m);
         c->prof.launches += 1;
         return;

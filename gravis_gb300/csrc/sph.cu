@@ -42,7 +42,7 @@ struct SphState {
     DevBuf sx, sy, sz, svx, svy, svz, sm, sh, su, salpha;  // sorted inputs
     DevBuf srho, spres, scs, somega, sdivv, smaxmu, sdalpha, sax, say, saz, sdu;  // sorted outputs
     DevBuf dtpart;
-    DevBuf pos4, node4;  // f32 copies for the neighbour-search prefilter
+    DevBuf pos4, node4, meta4;  // neighbour search: f32 positions, node records (see k_sph_f32copies)
     DevBuf a4, b4, c4, d4, e4, f4;  // mixed precision: packed sources (see k_sph_src_*)
     DevBuf redo_idx, redo_count;    // mixed precision: particles whose h iteration runs again in f64
     bool have_intermediates = false;
@@ -177,12 +177,67 @@ __device__ __forceinline__ int pref_box(const Prefilter &f, float4 b) {
     return d2 < f.rin2 ? 1 : (d2 > f.rout2 ? 0 : -1);
 }
 
-__global__ void k_sph_f32copies(const TreeView tv, float4 *__restrict__ pos4, float4 *__restrict__ node4) {
+// Node records of the walk: meta4 = (skip, first, count, depth); node4 = the cell
+// box (centre, half width) in f32, except for a one-particle leaf, where it is
+// that particle's f32 position: the particle test then decides (a particle
+// certainly inside the sphere lies in a box that certainly meets it, and one
+// certainly outside adds nothing either way), and only an undecided one runs
+// both of the reference's f64 tests, box then particle.
+__global__ void k_sph_f32copies(const TreeView tv, float4 *__restrict__ pos4, float4 *__restrict__ node4,
+                                int4 *__restrict__ meta4) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < tv.n) pos4[i] = make_float4((float)tv.sx[i], (float)tv.sy[i], (float)tv.sz[i], 0.f);
-    if (i < tv.nnodes)
-        node4[i] = make_float4((float)tv.bx[i], (float)tv.by[i], (float)tv.bz[i],
-                               (float)ldexp(tv.root_hw, -(int)tv.level[i]));
+    if (i < tv.nnodes) {
+        const uint32_t c = tv.cnt[i], f = tv.first[i];
+        meta4[i] = make_int4((int)tv.skip[i], (int)f, (int)c, (int)tv.level[i]);
+        node4[i] = c == 1 ? make_float4((float)tv.sx[f], (float)tv.sy[f], (float)tv.sz[f], 0.f)
+                          : make_float4((float)tv.bx[i], (float)tv.by[i], (float)tv.bz[i],
+                                        (float)ldexp(tv.root_hw, -(int)tv.level[i]));
+    }
+}
+
+// One node of the ball query: appends its hits to row in depth-first order and
+// returns the next node.  See k_sph_f32copies for the record layout.
+__device__ __forceinline__ uint32_t ball_visit(const TreeView &tv, const float4 *__restrict__ pos4, int4 mt,
+                                               float4 nd, uint32_t k, const Prefilter &pf, double px, double py,
+                                               double pz, double radius, uint32_t *row, int kmax, int &count) {
+    const double r2 = radius * radius;
+    if (mt.z == 1) {  // one-particle leaf
+        const uint32_t j = (uint32_t)mt.y;
+        int in = pref_point(pf, nd);
+        if (in < 0) {
+            const double hw = ldexp(tv.root_hw, -mt.w);
+            in = sphere_hits_box(px, py, pz, radius, tv.bx[k], tv.by[k], tv.bz[k], hw);
+            if (in) {
+                const double dx = tv.sx[j] - px, dy = tv.sy[j] - py, dz = tv.sz[j] - pz;
+                in = dx * dx + dy * dy + dz * dz <= r2;
+            }
+        }
+        if (in) {
+            if (count < kmax) row[count] = j;
+            ++count;
+        }
+        return (uint32_t)mt.x;
+    }
+    int hit = pref_box(pf, nd);
+    if (hit < 0) {
+        const double hw = ldexp(tv.root_hw, -mt.w);
+        hit = sphere_hits_box(px, py, pz, radius, tv.bx[k], tv.by[k], tv.bz[k], hw);
+    }
+    if (!hit) return (uint32_t)mt.x;
+    if (mt.z == 0) return k + 1;  // internal: descend
+    for (uint32_t j = (uint32_t)mt.y; j < (uint32_t)(mt.y + mt.z); ++j) {  // bucket leaf
+        int in = pref_point(pf, pos4[j]);
+        if (in < 0) {
+            const double dx = tv.sx[j] - px, dy = tv.sy[j] - py, dz = tv.sz[j] - pz;
+            in = dx * dx + dy * dy + dz * dz <= r2;
+        }
+        if (in) {
+            if (count < kmax) row[count] = j;
+            ++count;
+        }
+    }
+    return (uint32_t)mt.x;
 }
 
 __global__ void k_gather_sph(size_t n, const uint32_t *__restrict__ perm, const uint8_t *__restrict__ ptype,
@@ -208,51 +263,22 @@ __global__ void k_gather_sph(size_t n, const uint32_t *__restrict__ perm, const 
 // Ball query of one target (per-thread walk), used for the re-queries of the
 // density iteration.  Returns the number found (writes at most kmax).
 __device__ int ball_query_thread(const TreeView &tv, const float4 *__restrict__ pos4,
-                                 const float4 *__restrict__ node4, float E, double px, double py, double pz,
-                                 double radius, uint32_t *row, int kmax) {
-    const double r2 = radius * radius;
+                                 const float4 *__restrict__ node4, const int4 *__restrict__ meta4, float E, double px,
+                                 double py, double pz, double radius, uint32_t *row, int kmax) {
     const Prefilter pf = prefilter(px, py, pz, radius, E);
     int count = 0;
     uint32_t k = 0;
-    while ((size_t)k < tv.nnodes) {
-        int hit = pref_box(pf, node4[k]);
-        if (hit < 0) {
-            const double hw = ldexp(tv.root_hw, -(int)tv.level[k]);
-            hit = sphere_hits_box(px, py, pz, radius, tv.bx[k], tv.by[k], tv.bz[k], hw);
-        }
-        if (!hit) {
-            k = tv.skip[k];
-            continue;
-        }
-        const uint32_t nc = tv.cnt[k];
-        if (nc > 0) {
-            const uint32_t f = tv.first[k];
-            for (uint32_t j = f; j < f + nc; ++j) {
-                int in = pref_point(pf, pos4[j]);
-                if (in < 0) {
-                    const double dx = tv.sx[j] - px, dy = tv.sy[j] - py, dz = tv.sz[j] - pz;
-                    in = dx * dx + dy * dy + dz * dz <= r2;
-                }
-                if (in) {
-                    if (count < kmax) row[count] = j;
-                    ++count;
-                }
-            }
-            k = tv.skip[k];
-        } else {
-            k = k + 1;
-        }
-    }
+    while ((size_t)k < tv.nnodes) k = ball_visit(tv, pos4, meta4[k], node4[k], k, pf, px, py, pz, radius, row, kmax, count);
     return count;
 }
 
 // Neighbour lists of all gas particles (build_neighbor_lists with factor):
 // warp-synchronous walk, each lane with its own next-node pointer.
 __global__ void __launch_bounds__(128) k_neighbors(const TreeView tv, const float4 *__restrict__ pos4,
-                                                   const float4 *__restrict__ node4, const uint8_t *__restrict__ gas,
-                                                   const double *__restrict__ sh, double factor, int kmax,
-                                                   uint32_t *__restrict__ list, uint32_t *__restrict__ cnt,
-                                                   unsigned *__restrict__ err) {
+                                                   const float4 *__restrict__ node4, const int4 *__restrict__ meta4,
+                                                   const uint8_t *__restrict__ gas, const double *__restrict__ sh,
+                                                   double factor, int kmax, uint32_t *__restrict__ list,
+                                                   uint32_t *__restrict__ cnt, unsigned *__restrict__ err) {
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = t < tv.n && gas[t];
     double px = 0, py = 0, pz = 0, radius = 0;
@@ -260,7 +286,6 @@ __global__ void __launch_bounds__(128) k_neighbors(const TreeView tv, const floa
         px = tv.sx[t]; py = tv.sy[t]; pz = tv.sz[t];
         radius = 2.0 * sh[t] * factor;
     }
-    const double r2 = radius * radius;
     const Prefilter pf = prefilter(px, py, pz, radius, prefilter_scale(tv));
     uint32_t *row = list + t * (size_t)kmax;
     int count = 0;
@@ -269,33 +294,7 @@ __global__ void __launch_bounds__(128) k_neighbors(const TreeView tv, const floa
         const uint32_t k = __reduce_min_sync(0xFFFFFFFFu, next);
         if ((size_t)k >= tv.nnodes) break;
         if (next != k) continue;
-        int hit = pref_box(pf, node4[k]);
-        if (hit < 0) {
-            const double hw = ldexp(tv.root_hw, -(int)tv.level[k]);
-            hit = sphere_hits_box(px, py, pz, radius, tv.bx[k], tv.by[k], tv.bz[k], hw);
-        }
-        if (!hit) {
-            next = tv.skip[k];
-            continue;
-        }
-        const uint32_t nc = tv.cnt[k];
-        if (nc > 0) {
-            const uint32_t f = tv.first[k];
-            for (uint32_t j = f; j < f + nc; ++j) {
-                int in = pref_point(pf, pos4[j]);
-                if (in < 0) {
-                    const double dx = tv.sx[j] - px, dy = tv.sy[j] - py, dz = tv.sz[j] - pz;
-                    in = dx * dx + dy * dy + dz * dz <= r2;
-                }
-                if (in) {
-                    if (count < kmax) row[count] = j;
-                    ++count;
-                }
-            }
-            next = tv.skip[k];
-        } else {
-            next = k + 1;
-        }
+        next = ball_visit(tv, pos4, meta4[k], node4[k], k, pf, px, py, pz, radius, row, kmax, count);
     }
     if (t < tv.n) {
         cnt[t] = active ? (uint32_t)count : 0u;
@@ -323,7 +322,8 @@ __device__ __forceinline__ void density_sums_f64(const TreeView &tv, const doubl
 
 // compute_density (density.rs:42-125) for one target per thread, then the EOS.
 __device__ void density_particle_f64(const TreeView &tv, const float4 *__restrict__ pos4,
-                                     const float4 *__restrict__ node4, const double *__restrict__ sm,
+                                     const float4 *__restrict__ node4, const int4 *__restrict__ meta4,
+                                     const double *__restrict__ sm,
                                      const double *__restrict__ su, double *__restrict__ sh,
                                      uint32_t *__restrict__ list, uint32_t *__restrict__ cnt, int kmax, double gamma,
                                      double eta, double h_max, double *__restrict__ rho_out,
@@ -352,7 +352,7 @@ __device__ void density_particle_f64(const TreeView &tv, const float4 *__restric
         const double search_radius = 2.0 * h * search_padding;
         if (2.0 * h_new > search_radius) {
             const double new_radius = 2.0 * h_new * search_padding;
-            count = ball_query_thread(tv, pos4, node4, prefilter_scale(tv), xi, yi, zi, new_radius, row, kmax);
+            count = ball_query_thread(tv, pos4, node4, meta4, prefilter_scale(tv), xi, yi, zi, new_radius, row, kmax);
             if (count > kmax) {
                 atomicOr(err, (unsigned)DERR_NEIGH_OVERFLOW);
                 count = kmax;
@@ -369,7 +369,7 @@ __device__ void density_particle_f64(const TreeView &tv, const float4 *__restric
 }
 
 __global__ void k_density(const TreeView tv, const float4 *__restrict__ pos4, const float4 *__restrict__ node4,
-                          const uint8_t *__restrict__ gas, const double *__restrict__ sm,
+                          const int4 *__restrict__ meta4, const uint8_t *__restrict__ gas, const double *__restrict__ sm,
                           const double *__restrict__ su, double *__restrict__ sh, uint32_t *__restrict__ list,
                           uint32_t *__restrict__ cnt, int kmax, double gamma, double eta, double h_max,
                           double *__restrict__ rho_out, double *__restrict__ omega_out, double *__restrict__ pres,
@@ -378,8 +378,8 @@ __global__ void k_density(const TreeView tv, const float4 *__restrict__ pos4, co
     if (i >= tv.n) return;
     omega_out[i] = 1.0;
     if (!gas[i]) return;
-    density_particle_f64(tv, pos4, node4, sm, su, sh, list, cnt, kmax, gamma, eta, h_max, rho_out, omega_out, pres,
-                         cs, err, i);
+    density_particle_f64(tv, pos4, node4, meta4, sm, su, sh, list, cnt, kmax, gamma, eta, h_max, rho_out, omega_out,
+                         pres, cs, err, i);
 }
 
 // compute_forces (forces.rs:69-232), one target per thread.
@@ -561,12 +561,13 @@ __device__ __forceinline__ void density_sums_mixed(const float4 *__restrict__ a4
 }
 
 // compute_density with mixed sums.  The mixed h sequence drifts from the f64
-// one by ~1e-7 relative, so a stopping or re-query decision that comes within
-// 1e-4 of its threshold (convergence at 1e-3, re-query at a ratio of 1.1) could
+// one by ~3e-8 relative, so a stopping or re-query decision that comes within
+// 1e-5 of its threshold (convergence at 1e-3, re-query at a ratio of 1.1) could
 // go the other way.  Such a particle is listed for k_density_redo, which runs
 // its whole iteration again on the f64 path from the initial h: every
 // particle's iteration path is then the f64 one.
 __global__ void k_density_mixed(const TreeView tv, const float4 *__restrict__ pos4, const float4 *__restrict__ node4,
+                                const int4 *__restrict__ meta4,
                                 const float4 *__restrict__ a4, const float4 *__restrict__ b4,
                                 const uint8_t *__restrict__ gas, const double *__restrict__ sm,
                                 const double *__restrict__ su, double *__restrict__ sh, uint32_t *__restrict__ list,
@@ -586,7 +587,7 @@ __global__ void k_density_mixed(const TreeView tv, const float4 *__restrict__ po
     uint32_t *row = list + i * (size_t)kmax;
     int count = (int)cnt[i];
     double rho_last = rho_out[i];
-    bool close = false;
+    bool close = false, requeried = false;
     for (int it = 0; it < 5; ++it) {
         double s1, s2;
         density_sums_mixed(a4, b4, row, count, pa, pb, (float)(1.0 / h), s1, s2);
@@ -594,7 +595,7 @@ __global__ void k_density_mixed(const TreeView tv, const float4 *__restrict__ po
         const double rho = nh3 * s1, dws = nh3 / h * s2;
         const double h_new = rho > 0.0 ? fmin(eta * cbrt(m_i / rho), h_max) : fmin(h, h_max);
         const double ratio = fabs(h_new - h) / fmax(h, 1e-30);
-        close = close || fabs(ratio - 1e-3) < 1e-4 || fabs(h_new / h - search_padding) < 1e-4;
+        close = close || fabs(ratio - 1e-3) < 1e-5 || fabs(h_new / h - search_padding) < 1e-5;
         if (rho > 0.0) {
             const double dh_drho = -h_new / (3.0 * rho);
             double om = 1.0 - dh_drho * dws;
@@ -607,7 +608,8 @@ __global__ void k_density_mixed(const TreeView tv, const float4 *__restrict__ po
         const double search_radius = 2.0 * h * search_padding;
         if (2.0 * h_new > search_radius) {
             const double new_radius = 2.0 * h_new * search_padding;
-            count = ball_query_thread(tv, pos4, node4, prefilter_scale(tv), xi, yi, zi, new_radius, row, kmax);
+            count = ball_query_thread(tv, pos4, node4, meta4, prefilter_scale(tv), xi, yi, zi, new_radius, row, kmax);
+            requeried = true;
             if (count > kmax) {
                 atomicOr(err, (unsigned)DERR_NEIGH_OVERFLOW);
                 count = kmax;
@@ -616,41 +618,101 @@ __global__ void k_density_mixed(const TreeView tv, const float4 *__restrict__ po
         }
         h = h_new;
     }
-    if (close) redo_idx[atomicAdd(redo_count, 1u)] = (uint32_t)i;
+    // the top bit marks a row that no longer holds the original list
+    if (close) redo_idx[atomicAdd(redo_count, 1u)] = (uint32_t)i | (requeried ? 0x80000000u : 0u);
     rho_out[i] = rho_last;
     const double u = su[i];
     pres[i] = (gamma - 1.0) * rho_last * u;
     cs[i] = sqrt(gamma * (gamma - 1.0) * fmax(u, 0.0));
 }
 
-// The listed particles' h iteration again, on the f64 path from the initial h
-// h0 and the original neighbour list (re-queried at radius 2 h0 1.1, as
-// build_neighbor_lists made it).  Grid-stride over the list, whose length is on
-// the device.
-__global__ void k_density_redo(const TreeView tv, const float4 *__restrict__ pos4, const float4 *__restrict__ node4,
-                               const double *__restrict__ sm, const double *__restrict__ su,
-                               const double *__restrict__ h0, double *__restrict__ sh, uint32_t *__restrict__ list,
-                               uint32_t *__restrict__ cnt, int kmax, double gamma, double eta, double h_max,
-                               double *__restrict__ rho_out, double *__restrict__ omega_out,
-                               double *__restrict__ pres, double *__restrict__ cs, unsigned *__restrict__ err,
-                               const uint32_t *__restrict__ redo_idx, const unsigned *__restrict__ redo_count,
-                               unsigned *__restrict__ redo_total) {
+// The listed particles' h iteration again, from the initial h h0 and the
+// original neighbour list (re-queried at radius 2 h0 1.1 when the mixed pass
+// had replaced it), with f64 sums.  One warp per particle: the lanes stride the
+// list and the partial sums meet in a fixed shuffle tree, so the sums differ
+// from the sequential f64 ones only in rounding (~1e-16), far below the 1e-5
+// band that sent the particle here; the decisions are the f64 path's.
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(128) k_density_redo(
+    const TreeView tv, const float4 *__restrict__ pos4, const float4 *__restrict__ node4,
+    const int4 *__restrict__ meta4, const double *__restrict__ sm, const double *__restrict__ su,
+    const double *__restrict__ h0, double *__restrict__ sh, uint32_t *__restrict__ list,
+    uint32_t *__restrict__ cnt, int kmax, double gamma, double eta, double h_max, double *__restrict__ rho_out,
+    double *__restrict__ omega_out, double *__restrict__ pres, double *__restrict__ cs, unsigned *__restrict__ err,
+    const uint32_t *__restrict__ redo_idx, const unsigned *__restrict__ redo_count, unsigned *__restrict__ redo_total) {
     const unsigned m = *redo_count;
     if (blockIdx.x == 0 && threadIdx.x == 0 && m) atomicAdd(redo_total, m);
-    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
-        const size_t i = redo_idx[k];
-        const double hh = h0[i];
-        sh[i] = hh;
-        omega_out[i] = 1.0;
-        int count = ball_query_thread(tv, pos4, node4, prefilter_scale(tv), tv.sx[i], tv.sy[i], tv.sz[i],
-                                      2.0 * hh * 1.1, list + i * (size_t)kmax, kmax);
-        if (count > kmax) {
-            atomicOr(err, (unsigned)DERR_NEIGH_OVERFLOW);
-            count = kmax;
+    const int lane = threadIdx.x & 31;
+    const unsigned wpb = blockDim.x >> 5;
+    for (unsigned k = blockIdx.x * wpb + (threadIdx.x >> 5); k < m; k += gridDim.x * wpb) {
+        const uint32_t code = redo_idx[k];
+        const size_t i = code & 0x7FFFFFFFu;
+        const double xi = tv.sx[i], yi = tv.sy[i], zi = tv.sz[i], m_i = sm[i];
+        uint32_t *row = list + i * (size_t)kmax;
+        double h = h0[i];
+        int count = (int)cnt[i];
+        if (code & 0x80000000u) {  // restore the original list
+            if (lane == 0) {
+                count = ball_query_thread(tv, pos4, node4, meta4, prefilter_scale(tv), xi, yi, zi, 2.0 * h * 1.1,
+                                          row, kmax);
+                if (count > kmax) {
+                    atomicOr(err, (unsigned)DERR_NEIGH_OVERFLOW);
+                    count = kmax;
+                }
+                cnt[i] = (uint32_t)count;
+            }
+            count = __shfl_sync(0xFFFFFFFFu, count, 0);
+            __syncwarp();
         }
-        cnt[i] = (uint32_t)count;
-        density_particle_f64(tv, pos4, node4, sm, su, sh, list, cnt, kmax, gamma, eta, h_max, rho_out, omega_out,
-                             pres, cs, err, i);
+        double rho_last = rho_out[i], om_last = 1.0;
+        for (int it = 0; it < 5; ++it) {
+            double rho = 0.0, dws = 0.0;
+            for (int q = lane; q < count; q += 32) {
+                const uint32_t j = row[q];
+                const double dx = xi - tv.sx[j], dy = yi - tv.sy[j], dz = zi - tv.sz[j];
+                const double r = sqrt(dx * dx + dy * dy + dz * dz);
+                if (r < 2.0 * h) {
+                    rho += sm[j] * kw(r, h);
+                    dws += sm[j] * kdwdh(r, h);
+                }
+            }
+            rho = warp_sum(rho);
+            dws = warp_sum(dws);
+            const double h_new = rho > 0.0 ? fmin(eta * cbrt(m_i / rho), h_max) : fmin(h, h_max);
+            if (rho > 0.0) {
+                const double dh_drho = -h_new / (3.0 * rho);
+                om_last = fmax(1.0 - dh_drho * dws, 0.1);
+            }
+            rho_last = rho;
+            const bool done = fabs(h_new - h) / fmax(h, 1e-30) < 1e-3;
+            if (!done && 2.0 * h_new > 2.0 * h * 1.1) {  // re-query at the new radius
+                if (lane == 0) {
+                    count = ball_query_thread(tv, pos4, node4, meta4, prefilter_scale(tv), xi, yi, zi,
+                                              2.0 * h_new * 1.1, row, kmax);
+                    if (count > kmax) {
+                        atomicOr(err, (unsigned)DERR_NEIGH_OVERFLOW);
+                        count = kmax;
+                    }
+                    cnt[i] = (uint32_t)count;
+                }
+                count = __shfl_sync(0xFFFFFFFFu, count, 0);
+                __syncwarp();
+            }
+            h = h_new;
+            if (done) break;
+        }
+        if (lane == 0) {
+            sh[i] = h;
+            omega_out[i] = om_last;
+            rho_out[i] = rho_last;
+            const double u = su[i];
+            pres[i] = (gamma - 1.0) * rho_last * u;
+            cs[i] = sqrt(gamma * (gamma - 1.0) * fmax(u, 0.0));
+        }
     }
 }
 
@@ -898,7 +960,7 @@ void sph_free(Ctx *c) {
     if (!s) return;
     DevBuf *all[] = {&s->list, &s->cnt, &s->gas, &s->sx, &s->sy, &s->sz, &s->svx, &s->svy, &s->svz, &s->sm,
                      &s->sh, &s->su, &s->salpha, &s->srho, &s->spres, &s->scs, &s->somega, &s->sdivv, &s->smaxmu,
-                     &s->sdalpha, &s->sax, &s->say, &s->saz, &s->sdu, &s->dtpart, &s->pos4, &s->node4,
+                     &s->sdalpha, &s->sax, &s->say, &s->saz, &s->sdu, &s->dtpart, &s->pos4, &s->node4, &s->meta4,
                      &s->a4, &s->b4, &s->c4, &s->d4, &s->e4, &s->f4, &s->redo_idx, &s->redo_count};
     for (DevBuf *b : all)
         if (b->ptr) cudaFree(b->ptr);
@@ -923,7 +985,9 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
     GVS_CUDA(c, ensure(c, S->cnt, n * 4));
     GVS_CUDA(c, ensure(c, S->pos4, n * 16));
     GVS_CUDA(c, ensure(c, S->node4, tv.nnodes * 16));
-    k_sph_f32copies<<<nb(std::max(n, tv.nnodes)), 256, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4));
+    GVS_CUDA(c, ensure(c, S->meta4, tv.nnodes * 16));
+    k_sph_f32copies<<<nb(std::max(n, tv.nnodes)), 256, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4),
+                                                                as<int4>(S->meta4));
     const bool mixed = prm->precision == GVS_PREC_MIXED;
     if (mixed) {
         DevBuf *f4s[] = {&S->a4, &S->b4, &S->c4, &S->d4, &S->e4, &S->f4};
@@ -951,26 +1015,26 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
     for (int attempt = 0; attempt < 4; ++attempt) {
         GVS_CUDA(c, ensure(c, S->list, n * (size_t)S->kmax * 4));
         GVS_CUDA(c, cudaMemcpyAsync(S->sh.ptr, c->scratch_b.ptr, b8, cudaMemcpyDeviceToDevice, st));
-        k_neighbors<<<nb(n, 128), 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4), as<uint8_t>(S->gas),
+        k_neighbors<<<nb(n, 128), 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4), as<int4>(S->meta4), as<uint8_t>(S->gas),
                                                 as<double>(S->sh), 1.1, S->kmax,
                                                 as<uint32_t>(S->list), as<uint32_t>(S->cnt), err_ptr(c));
         if (mixed) {
             GVS_CUDA(c, cudaMemsetAsync(S->redo_count.ptr, 0, 4, st));
             k_density_mixed<<<nb(n, 128), 128, 0, st>>>(
-                tv, as<float4>(S->pos4), as<float4>(S->node4), as<float4>(S->a4), as<float4>(S->b4),
+                tv, as<float4>(S->pos4), as<float4>(S->node4), as<int4>(S->meta4), as<float4>(S->a4), as<float4>(S->b4),
                 as<uint8_t>(S->gas), as<double>(S->sm), as<double>(S->su), as<double>(S->sh), as<uint32_t>(S->list),
                 as<uint32_t>(S->cnt), S->kmax, prm->gamma, prm->eta, prm->h_max, as<double>(S->srho),
                 as<double>(S->somega), as<double>(S->spres), as<double>(S->scs), err_ptr(c),
                 as<uint32_t>(S->redo_idx), as<unsigned>(S->redo_count));
             k_density_redo<<<std::max(1, c->num_sms * 2), 128, 0, st>>>(
-                tv, as<float4>(S->pos4), as<float4>(S->node4), as<double>(S->sm), as<double>(S->su),
+                tv, as<float4>(S->pos4), as<float4>(S->node4), as<int4>(S->meta4), as<double>(S->sm), as<double>(S->su),
                 as<double>(c->scratch_b), as<double>(S->sh), as<uint32_t>(S->list), as<uint32_t>(S->cnt), S->kmax,
                 prm->gamma, prm->eta, prm->h_max, as<double>(S->srho), as<double>(S->somega), as<double>(S->spres),
                 as<double>(S->scs), err_ptr(c), as<uint32_t>(S->redo_idx), as<unsigned>(S->redo_count),
                 err_ptr(c) + 10);
             c->prof.launches += 1;
         } else
-            k_density<<<nb(n, 128), 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4), as<uint8_t>(S->gas),
+            k_density<<<nb(n, 128), 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4), as<int4>(S->meta4), as<uint8_t>(S->gas),
                                                   as<double>(S->sm), as<double>(S->su),
                                                   as<double>(S->sh), as<uint32_t>(S->list), as<uint32_t>(S->cnt),
                                                   S->kmax, prm->gamma, prm->eta, prm->h_max, as<double>(S->srho),

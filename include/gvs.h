@@ -90,7 +90,7 @@ typedef struct gvs_profile {
     double vjp_ms;            /* device time of the fused force + VJP kernels (adjoint) */
     long long vjp_launches;
     long long sph_f64_redo;   /* mixed SPH: particles whose h iteration was rerun on the f64 path
-                                 (a stopping or re-query decision within 1e-4 of its threshold) */
+                                 (a stopping or re-query decision within 1e-5 of its threshold) */
 } gvs_profile;
 
 /* ---- library / context ---------------------------------------------------- */
