@@ -161,6 +161,44 @@ def cpu_sample(n, seed, eps, targets, rng_seed=0):
     return n / step_s, cores, dt, f"{len(idx)} of {n} targets x {n} sources (one force evaluation), extrapolated"
 
 
+def to_oracle(p):
+    """The oracle's Particles with the same arrays (gas fields included)."""
+    import oracle as O
+    q = O.Particles(p.count)
+    for a, b in (("x", "x"), ("y", "y"), ("z", "z"), ("vx", "vx"), ("vy", "vy"), ("vz", "vz"), ("mass", "mass"),
+                 ("density", "density"), ("pressure", "pressure"), ("internal_energy", "u"),
+                 ("smoothing_length", "h"), ("sound_speed", "cs"), ("alpha_visc", "alpha"),
+                 ("particle_type", "ptype")):
+        getattr(q, b)[:] = getattr(p, a)
+    return q
+
+
+def cpu_bh_sample(G, theta, eps, n=1 << 20):
+    """The oracle's BarnesHut (serial build, threaded walk) for one force evaluation
+    of the same two-sphere system at a bounded N."""
+    import oracle as O
+    q = to_oracle(G.collision(n, seed=7))
+    t0 = time.perf_counter()
+    O.bh(q, eps, theta)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": UNIT, "cores": O.lib().orc_max_threads(), "kind": "port",
+            "sample": f"one BarnesHut force evaluation (tree build + walk) of the same collision ICs at N={n}, "
+                      f"theta={theta}; the step's KDK update is not included"}
+
+
+def cpu_sph_sample(G, n=1 << 16):
+    """The oracle's SphSolver::compute (neighbours, density, forces) once on the same
+    gas sphere at a bounded N."""
+    import oracle as O
+    q = to_oracle(G.gas_sphere_1r(n))
+    s = O.Sph()
+    t0 = time.perf_counter()
+    s.compute(q)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": UNIT, "cores": O.lib().orc_max_threads(), "kind": "port",
+            "sample": f"one SphSolver::compute of the rho~1/r sphere at N={n} (no gravity, no KDK update)"}
+
+
 def run_reference(a, d: Dist):
     if d.rank != 0:
         return
@@ -421,6 +459,8 @@ def run_workload(a, d):
                     "accuracy": {"per_particle_rms_rel_err_vs_exact_f64_direct": float(rel),
                                  "subset": "4096 random particles"},
                     "clocks": clk.summary()})
+        if d.rank == 0 and not a.no_extras:
+            res["cpu_baseline"] = cpu_bh_sample(G, theta, eps)
     elif a.workload == "sph":
         n = a.n
         p = G.gas_sphere_1r(n)
@@ -505,6 +545,8 @@ def run_workload(a, d):
                                   "what": "the same steps with the reference's f64 SPH arithmetic"},
                     "mixed_over_f64": t_ex / t,
                     "mixed_vs_f64_rel_rms": errs, "clocks": clk})
+        if d.rank == 0 and not a.no_extras:
+            res["cpu_baseline"] = cpu_sph_sample(G)
     elif a.workload == "ensemble":
         from gravis_gb300.engine import plummer_ensemble
         sizes = G.ensemble_sizes(a.nsys, seed=2024)
