@@ -99,6 +99,7 @@ SIGNATURES = {
     "gvs_event_record": (_ST, [_P, _i]),
     "gvs_event_elapsed": (_ST, [_P, _i, _i, C.POINTER(C.c_float)]),
     "gvs_l2_flush": (_ST, [_P]),
+    "gvs_check_bounded_wait": (_ST, [_P, C.c_uint]),
     "gvs_measure_fp32_peak": (_ST, [_P, C.POINTER(C.c_double)]),
     "gvs_fp32_peak_variants": (_ST, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 }

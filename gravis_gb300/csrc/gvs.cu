@@ -791,6 +791,26 @@ __global__ void k_fp32_peak_mixed(float *out, float a, float b) {
 }
 }  // namespace
 
+// Self-test of the bounded-wait path: one thread waits on an mbarrier that
+// nothing arrives at, for `cap` polls, then sets the timeout flag and returns.
+__global__ void k_wait_probe(unsigned *err, unsigned cap) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x != 0) return;
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    mbar_wait_bounded(&bar, 0u, err, cap);
+}
+
+extern "C" gvs_status gvs_check_bounded_wait(gvs_ctx *c, unsigned polls) {
+    GVS_TRY(check_ctx(c));
+    if (polls == 0 || polls > (1u << 20)) return fail(c, GVS_ERR_INVALID_ARG, "polls must be in [1, 2^20]");
+    cudaSetDevice(c->device);
+    k_wait_probe<<<1, 32, 0, c->stream>>>(err_ptr(c), polls);
+    c->prof.launches += 1;
+    GVS_TRY(check_launch(c, "bounded-wait probe"));
+    return read_device_errors(c);  // GVS_ERR_TIMEOUT expected; the word is cleared
+}
+
 extern "C" gvs_status gvs_measure_fp32_peak(gvs_ctx *c, double *tflops) {
     GVS_TRY(check_ctx(c));
     if (!tflops) return fail(c, GVS_ERR_INVALID_ARG, "tflops is NULL");

@@ -300,6 +300,11 @@ gvs_status gvs_event_record(gvs_ctx *ctx, int slot);
 gvs_status gvs_event_elapsed(gvs_ctx *ctx, int slot_a, int slot_b, float *ms);
 /* Writes a buffer larger than L2 on the context stream (cold-cache timing). */
 gvs_status gvs_l2_flush(gvs_ctx *ctx);
+/* Self-test of failure detection (no reference counterpart): a kernel waits on an
+ * mbarrier that nothing completes, gives up after `polls` polls (1 .. 2^20), sets the
+ * timeout bit of the device error word and exits.  Returns GVS_ERR_TIMEOUT when the
+ * bounded-wait path works; the error word is cleared and the context stays usable. */
+gvs_status gvs_check_bounded_wait(gvs_ctx *ctx, unsigned polls);
 /* Measured FP32 FMA throughput of this GPU (TFLOP/s, 2 flop per FMA). */
 gvs_status gvs_measure_fp32_peak(gvs_ctx *ctx, double *tflops);
 /* The three probe forms of the last gvs_measure_fp32_peak: scalar FMA, packed f32x2 FMA,

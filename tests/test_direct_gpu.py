@@ -292,3 +292,19 @@ def test_mixed_at_full_size(ctx):
     ma = (q.acc() * q.mass[:, None]).sum(0)
     scale = (np.abs(q.acc()) * q.mass[:, None]).sum(0)
     assert np.all(np.abs(ma) <= 1e-6 * scale), (ma, scale)
+
+
+def test_bounded_wait_reports_timeout_and_context_survives(ctx):
+    """A device wait that runs out returns GVS_ERR_TIMEOUT through the error word
+    (no trap, no hang), and the same context computes forces right after."""
+    from gravis_gb300 import _lib as L
+    st = ctx._lib.gvs_check_bounded_wait(ctx.h, 1000)
+    assert st == L.ERR_TIMEOUT
+    assert ctx._lib.gvs_check_bounded_wait(ctx.h, 0) == L.ERR_INVALID_ARG
+    p = G.PlummerSphere(500, seed=2).generate()
+    a = gpu_acc(ctx, p, 0.01, G.PREC_FP64_EXACT)
+    q = O.plummer(500, 2)
+    q.clear_accelerations()
+    O.bf_gather(q, 0.01)
+    assert np.array_equal(a, q.acc())
+
