@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--workload", default="direct", choices=["direct", "plummer1k", "bh", "sph", "ensemble", "adjoint"],
                     help="direct (default headline); the others print their own line")
     ap.add_argument("--theta", type=float, default=0.5)
+    ap.add_argument("--sph-precision", default="both", choices=["both", "mixed", "f64"],
+                    help="SPH workload: time both pair-arithmetic forms (and compare them), or one only")
     ap.add_argument("--nsys", type=int, default=512, help="systems in the ensemble workload")
     ap.add_argument("--adjoint-steps", type=int, default=200, help="steps of the adjoint side measurement")
     return ap.parse_args()
@@ -511,6 +513,18 @@ def run_workload(a, d):
                     ms.append(ctx.elapsed(0, 1))
             return sum(ms), clk.summary()
 
+        if a.sph_precision != "both":  # one form only (profiling runs): no comparison
+            prec = G.PREC_MIXED if a.sph_precision == "mixed" else G.PREC_FP64_EXACT
+            t, clk = timed(prec)
+            res.update({"value": n * a.steps / (t * 1e-3), "ms_per_step": t / a.steps,
+                        "dtype": "f32 SPH pair terms (mixed)" if prec == G.PREC_MIXED else "f64 SPH",
+                        "config": {"workload": f"grad-h SPH + BH gravity, rho~1/r gas sphere N={n}, "
+                                               f"{a.sph_precision} pair arithmetic only", "n": n},
+                        "clocks": clk})
+            ctx.close()
+            if d.rank == 0:
+                print(json.dumps(res), flush=True)
+            return
         qe = sph_only(G.PREC_FP64_EXACT)
         ctx.profile(True)
         qm = sph_only(G.PREC_MIXED)
