@@ -438,8 +438,12 @@ def run_workload(a, d):
         ctx.get_state(q)
         rel = np.sqrt((((q.acc()[idx] - ref) ** 2).sum(1) / (ref ** 2).sum(1)).mean())
         # the walk forms side by side on the final state: time and distance to the f64 walk
+        # (fp32: the group walk, the FP32 default; fp32_per_particle: the reference's
+        # per-particle test on f32 positions)
         walks = {}
-        for wname, wp in (("fp64", G.PREC_FP64), ("mixed", G.PREC_MIXED), ("fp32", G.PREC_FP32)):
+        for wname, wp, grp in (("fp64", G.PREC_FP64, 64), ("mixed", G.PREC_MIXED, 64), ("fp32", G.PREC_FP32, 64),
+                               ("fp32_per_particle", G.PREC_FP32, 0)):
+            ctx.set_bh_walk(grp)
             ctx.compute_forces(G.ALGO_BH, wp, eps, theta)  # builds the packed node arrays
             ctx.profile(True)
             ctx.compute_forces(G.ALGO_BH, wp, eps, theta)
@@ -448,10 +452,17 @@ def run_workload(a, d):
             qw = G.Particles(n)
             ctx.get_state(qw)
             walks[wname] = {"walk_ms": pw["force_ms"], "acc": qw.acc()}
-        a64 = walks["fp64"].pop("acc")
-        for wname in ("mixed", "fp32"):
+            if pw["bh_groups"]:
+                walks[wname].update({"groups": pw["bh_groups"], "groups_walked_per_particle": pw["bh_group_fallbacks"],
+                                     "group_iterations": pw["bh_group_iterations"]})
+        ctx.set_bh_walk(64)
+        a64 = walks["fp64"]["acc"]
+        for wname in walks:
             aw = walks[wname].pop("acc")
-            walks[wname]["rel_rms_vs_fp64_walk"] = float(np.sqrt(((aw - a64) ** 2).sum() / (a64 ** 2).sum()))
+            if wname != "fp64":
+                walks[wname]["rel_rms_vs_fp64_walk"] = float(np.sqrt(((aw - a64) ** 2).sum() / (a64 ** 2).sum()))
+            walks[wname]["per_particle_rms_rel_err_vs_exact_f64_direct"] = float(
+                np.sqrt((((aw[idx] - ref) ** 2).sum(1) / (ref ** 2).sum(1)).mean()))
         res.update({"value": n * a.steps / (t * 1e-3), "ms_per_step": t / a.steps, "dtype": "f32 walk / f64 state",
                     "walk_forms": walks,
                     "config": {"workload": f"Barnes-Hut KDK, two Plummer spheres N={n} seed 7, theta={theta}, "

@@ -44,7 +44,8 @@ class Profile(C.Structure):
     _fields_ = [("force_ms", C.c_double), ("force_launches", C.c_longlong), ("launches", C.c_longlong),
                 ("force_flops", C.c_double), ("force_bytes", C.c_double), ("tile_visits", C.c_double),
                 ("near_tile_visits", C.c_double), ("vjp_ms", C.c_double), ("vjp_launches", C.c_longlong),
-                ("sph_f64_redo", C.c_longlong)]
+                ("sph_f64_redo", C.c_longlong), ("bh_groups", C.c_longlong),
+                ("bh_group_fallbacks", C.c_longlong), ("bh_group_iterations", C.c_longlong)]
 
 
 _P = C.c_void_p  # every array argument is passed as a raw address
@@ -92,6 +93,7 @@ SIGNATURES = {
     "gvs_ic_ensemble_sizes": (_ST, [_sz, _u64, _d, _d, _P]),
     "gvs_autotune_direct": (_ST, [_P, _i, _d, C.POINTER(_i), C.POINTER(_i), C.POINTER(_d)]),
     "gvs_set_direct_shape": (_ST, [_P, _i, _i, _i, _i]),
+    "gvs_set_bh_walk": (_ST, [_P, _i, _i]),
     "gvs_autotune_report": (_ST, [_P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                   C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "gvs_profile_enable": (_ST, [_P, _i]),

@@ -57,6 +57,11 @@ struct Tree {
     DevBuf sx, sy, sz, sm;           // sorted particle positions / masses (f64)
     DevBuf pos32, cm32, cm64, meta, acc;
     DevBuf pos32lo, cm32lo;  // mixed walk: f32 lo words of positions and COMs
+    // group walk (f32): child-slot records, groups of <= 32*NPL particles, work counter
+    DevBuf nk, koff, krec, groups, gcount;
+    unsigned long long grp_version = ~0ull;
+    int grp_size = 0;
+    int walk_blocks = 0;  // resident blocks of the group walk (per GPU)
 };
 
 namespace {
@@ -439,6 +444,416 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
     acc[2 * n + t] = az;
 }
 
+// ---- group walk (FP32) ---------------------------------------------------------
+// A faster f32 form of the walk for GVS_PREC_FP32.  One warp serves a group of
+// up to 32*NPL particles that share a tree cell: the cells with at most that
+// many particles whose parent has more (siblings merged while they fit).  The
+// warp opens nodes 32 at a time with a group test -- accept if
+// s^2 < theta^2 d^2 with d the distance from the node's COM to the box of the
+// group's particles -- and collects accepted nodes and leaves in a shared
+// interaction list that every lane then evaluates for its own particles.
+// d <= |com - p| for every particle p of the group, so each particle accepts
+// only nodes its own walk (the reference's test) would accept: its force is a
+// refinement of the per-particle Barnes-Hut sum (more nodes opened, never
+// fewer).  Node records are stored by child slot (the children of a node are
+// contiguous) so that opening a node pushes one (slot, count) range.
+//
+// Stack bound: an iteration pops whole ranges (at most 32 nodes) from the top
+// and pushes at most 32 ranges, the children of the nodes it popped.  Grouping
+// the stack into the batches that iterations pushed, the least node depth of
+// each batch increases strictly from bottom to top (a batch's nodes are one
+// level below the shallowest node popped to make it, and that node's batch is
+// the one it lands on or lies above it).  Depths run 0..42, so the stack never
+// holds more than 43 batches of 32 ranges.
+constexpr int GW_WARPS = 4;
+constexpr int GW_SCAP = (MAXL + 1) * 32;
+constexpr int GW_ICAP = 128;
+
+struct GroupSmem {
+    uint32_t stack[GW_SCAP];  // (first child slot << 3) | (children - 1)
+    float4 il[2 * GW_ICAP];   // interaction list: (x, x, y, y), (z, z, m, m)
+};
+
+__device__ __forceinline__ uint32_t sub_count(uint32_t k, size_t nnodes, size_t n, const uint32_t *__restrict__ first,
+                                              const uint32_t *__restrict__ skip) {
+    const uint32_t e = skip[k];
+    return (uint32_t)((e < nnodes ? (size_t)first[e] : n) - first[k]);
+}
+
+__global__ void k_nkids(size_t nnodes, const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ skip,
+                        uint32_t *__restrict__ nk) {
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nnodes) return;
+    uint32_t c = 0;
+    if (cnt[k] == 0) {
+        const uint32_t end = skip[k];
+        for (uint32_t ch = (uint32_t)k + 1; ch < end; ch = skip[ch]) ++c;
+    }
+    nk[k] = c;
+}
+
+struct S2f {
+    float s2[MAXL + 1];
+};
+
+// Record of node x: (com, mass) and (first child slot, children, 0, s^2) for an
+// internal node, (-1, particle, 1, 0) for a one-particle leaf, (-2, first, count, 0)
+// for a bucket leaf.
+__device__ __forceinline__ void write_rec(float4 *__restrict__ krec, uint32_t slot, uint32_t x,
+                                          const uint8_t *__restrict__ level, const uint32_t *__restrict__ first,
+                                          const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ nk,
+                                          const uint32_t *__restrict__ koff, const double *__restrict__ mass,
+                                          const double *__restrict__ cx, const double *__restrict__ cy,
+                                          const double *__restrict__ cz, const S2f &tab) {
+    krec[2 * (size_t)slot] = make_float4((float)cx[x], (float)cy[x], (float)cz[x], (float)mass[x]);
+    const uint32_t c = cnt[x];
+    int4 b;
+    if (c == 0) b = make_int4((int)(1u + koff[x]), (int)nk[x], 0, __float_as_int(tab.s2[level[x]]));
+    else if (c == 1) b = make_int4(-1, (int)first[x], 1, 0);
+    else b = make_int4(-2, (int)first[x], (int)c, 0);
+    reinterpret_cast<int4 *>(krec)[2 * (size_t)slot + 1] = b;
+}
+
+// Each internal node writes its children's records at slots 1 + koff[k] + c;
+// node 0 also writes the root's record at slot 0.
+__global__ void k_krec(size_t nnodes, const uint8_t *__restrict__ level, const uint32_t *__restrict__ first,
+                       const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ skip,
+                       const uint32_t *__restrict__ nk, const uint32_t *__restrict__ koff,
+                       const double *__restrict__ mass, const double *__restrict__ cx, const double *__restrict__ cy,
+                       const double *__restrict__ cz, const S2f tab, float4 *__restrict__ krec) {
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nnodes) return;
+    if (k == 0) write_rec(krec, 0, 0, level, first, cnt, nk, koff, mass, cx, cy, cz, tab);
+    if (cnt[k] != 0) return;
+    const uint32_t end = skip[k];
+    uint32_t slot = 1u + koff[k];
+    for (uint32_t ch = (uint32_t)k + 1; ch < end; ch = skip[ch], ++slot)
+        write_rec(krec, slot, ch, level, first, cnt, nk, koff, mass, cx, cy, cz, tab);
+}
+
+// Groups: a node with more than G particles emits its children's particle
+// ranges, merging children of an aligned block of octants (an x pair, an xy quad)
+// while all of them and their sum stay within G: the union of such octants is a
+// box that holds no other child's particles, so a merged group never spans a
+// denser sibling.  A bucket leaf with more than G particles is cut into runs of
+// G; a root with at most G particles is one group.  Runs are contiguous in
+// sorted particle order.
+__global__ void k_groups(size_t nnodes, size_t n, uint32_t G, const uint8_t *__restrict__ level,
+                         const uint32_t *__restrict__ first, const uint32_t *__restrict__ cnt,
+                         const uint32_t *__restrict__ skip, const uint64_t *__restrict__ khi,
+                         const uint64_t *__restrict__ klo, int2 *__restrict__ groups,
+                         uint32_t *__restrict__ ngroups) {
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nnodes) return;
+    const uint32_t ck = sub_count((uint32_t)k, nnodes, n, first, skip);
+    if (ck <= G) {
+        if (k == 0) groups[atomicAdd(ngroups, 1u)] = make_int2((int)first[0], (int)ck);
+        return;
+    }
+    if (cnt[k] != 0) {
+        for (uint32_t j = 0; j < ck; j += G)
+            groups[atomicAdd(ngroups, 1u)] = make_int2((int)(first[k] + j), (int)min(G, ck - j));
+        return;
+    }
+    uint32_t c8[8], f8[8];
+    for (int o = 0; o < 8; ++o) c8[o] = 0u, f8[o] = 0u;
+    const int L = level[k] + 1;
+    const uint32_t end = skip[k];
+    for (uint32_t ch = (uint32_t)k + 1; ch < end; ch = skip[ch]) {
+        const uint32_t f = first[ch];
+        const int o = octant_at(khi[f], klo[f], L);
+        c8[o] = sub_count(ch, nnodes, n, first, skip);
+        f8[o] = f;
+    }
+    for (int a = 0; a < 8;) {
+        int size = 4;
+        for (;; size >>= 1) {
+            if (a % size) continue;
+            uint32_t tot = 0;
+            bool ok = true;
+            for (int o = a; o < a + size; ++o) {
+                ok = ok && c8[o] <= G;
+                tot += c8[o];
+            }
+            if ((ok && tot <= G) || size == 1) break;
+        }
+        uint32_t tot = 0, f0 = 0;
+        bool ok = true;
+        for (int o = a + size - 1; o >= a; --o) {
+            ok = ok && c8[o] <= G;
+            tot += c8[o];
+            if (c8[o]) f0 = f8[o];
+        }
+        if (ok && tot > 0u) groups[atomicAdd(ngroups, 1u)] = make_int2((int)f0, (int)tot);
+        a += size;
+    }
+}
+
+__device__ __forceinline__ float warp_min(float v) {
+    for (int o = 16; o; o >>= 1) v = fminf(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+    for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    return v;
+}
+
+// Every lane adds the list's monopole terms to its NPL particles: packed f32x2
+// over a particle pair (NPL 2), scalar f32 for one particle.  GUARD (unsoftened
+// runs) keeps r^2 > 0, so a particle's own leaf adds exactly zero.
+template <int NPL, bool GUARD>
+__device__ __forceinline__ void group_eval(const float4 *__restrict__ il, int cnt, f2 nx, f2 ny, f2 nz, float eps2,
+                                           f2 &ax, f2 &ay, f2 &az) {
+    if constexpr (NPL == 2) {
+        const f2 e2 = pk(eps2, eps2);
+#pragma unroll 4
+        for (int k = 0; k < cnt; ++k) {
+            const float4 a = il[2 * k], b = il[2 * k + 1];
+            const f2 dx = add2(pk(a.x, a.y), nx), dy = add2(pk(a.z, a.w), ny), dz = add2(pk(b.x, b.y), nz);
+            f2 r2 = fma2(dx, dx, e2);
+            r2 = fma2(dy, dy, r2);
+            r2 = fma2(dz, dz, r2);
+            float ra, rb;
+            upk(r2, ra, rb);
+            if (GUARD) { ra = fmaxf(ra, 1e-24f); rb = fmaxf(rb, 1e-24f); }
+            const f2 ri = pk(rsqrt_approx(ra), rsqrt_approx(rb));
+            const f2 sm = mul2(mul2(pk(b.z, b.w), ri), mul2(ri, ri));
+            ax = fma2(sm, dx, ax);
+            ay = fma2(sm, dy, ay);
+            az = fma2(sm, dz, az);
+        }
+    } else {
+        float x0, x1, y0, y1, z0, z1, fx, fy, fz, u;
+        upk(nx, x0, x1); upk(ny, y0, y1); upk(nz, z0, z1);
+        upk(ax, fx, u); upk(ay, fy, u); upk(az, fz, u);
+#pragma unroll 4
+        for (int k = 0; k < cnt; ++k) {
+            const float4 a = il[2 * k], b = il[2 * k + 1];
+            const float dx = a.x + x0, dy = a.z + y0, dz = b.x + z0;
+            float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+            if (GUARD) r2 = fmaxf(r2, 1e-24f);
+            const float ri = rsqrt_approx(r2);
+            const float sm = b.z * ri * (ri * ri);
+            fx = fmaf(sm, dx, fx);
+            fy = fmaf(sm, dy, fy);
+            fz = fmaf(sm, dz, fz);
+        }
+        ax = pk(fx, 0.f); ay = pk(fy, 0.f); az = pk(fz, 0.f);
+    }
+}
+
+// The per-particle f32 walk (k_walk<1>'s loop) of one particle per lane: the
+// group walk's fallback for groups whose box lies close to much denser matter.
+__device__ __forceinline__ void walk_lanes_f32(size_t t, bool active, size_t nnodes, const int4 *__restrict__ meta,
+                                               const float4 *__restrict__ cm32, const float4 *__restrict__ p32,
+                                               const float *s2f, float theta2f, float eps2f, float &fx, float &fy,
+                                               float &fz) {
+    float qx = 0.f, qy = 0.f, qz = 0.f;
+    if (active) {
+        const float4 q = p32[t];
+        qx = q.x; qy = q.y; qz = q.z;
+    }
+    uint32_t next = active ? 0u : 0xFFFFFFFFu;
+    for (;;) {
+        const uint32_t m = __reduce_min_sync(0xFFFFFFFFu, next);
+        if ((size_t)m >= nnodes) break;
+        if (next != m) continue;
+        const int4 mt = meta[m];
+        if (mt.z > 0) {
+            for (int j = mt.y; j < mt.y + mt.z; ++j) {
+                if ((size_t)j == t) continue;
+                const float4 q = p32[j];
+                if (q.w != 0.f) add_force32(qx, qy, qz, q.x, q.y, q.z, q.w, eps2f, fx, fy, fz);
+            }
+            next = (uint32_t)mt.x;
+        } else {
+            const float4 c = cm32[m];
+            if (c.w == 0.f) {
+                next = (uint32_t)mt.x;
+            } else {
+                const float dx = c.x - qx, dy = c.y - qy, dz = c.z - qz;
+                const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                if (s2f[mt.w] < theta2f * d2) {
+                    add_force32(qx, qy, qz, c.x, c.y, c.z, c.w, eps2f, fx, fy, fz);
+                    next = (uint32_t)mt.x;
+                } else {
+                    next = m + 1;
+                }
+            }
+        }
+    }
+}
+
+template <int NPL, bool GUARD>
+__global__ void __launch_bounds__(GW_WARPS * 32) k_walk_group(const int2 *__restrict__ groups,
+                                                             uint32_t *__restrict__ gcount,
+                                                             const float4 *__restrict__ krec,
+                                                             const float4 *__restrict__ p32, float theta2f,
+                                                             float eps2f, size_t n, size_t nnodes,
+                                                             const int4 *__restrict__ meta,
+                                                             const float4 *__restrict__ cm32, const S2Table tab,
+                                                             int budget, double *__restrict__ acc,
+                                                             unsigned *__restrict__ err) {
+    constexpr unsigned FULL = 0xFFFFFFFFu;
+    __shared__ GroupSmem smem[GW_WARPS];
+    const int lane = threadIdx.x & 31;
+    uint32_t *stack = smem[threadIdx.x >> 5].stack;
+    float4 *il = smem[threadIdx.x >> 5].il;
+    const unsigned lt = (1u << lane) - 1u;
+    const uint32_t ngroups = gcount[0];
+    for (;;) {
+        uint32_t g = 0;
+        if (lane == 0) g = atomicAdd(gcount + 1, 1u);
+        g = __shfl_sync(FULL, g, 0);
+        if (g >= ngroups) break;
+        const int2 gr = groups[g];
+        float px[2], py[2], pz[2];
+        float lox = INFINITY, loy = INFINITY, loz = INFINITY, hix = -INFINITY, hiy = -INFINITY, hiz = -INFINITY;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int k = q * 32 + lane;
+            const float4 p = p32[gr.x + (q < NPL && k < gr.y ? k : 0)];
+            px[q] = p.x; py[q] = p.y; pz[q] = p.z;
+            lox = fminf(lox, p.x); loy = fminf(loy, p.y); loz = fminf(loz, p.z);
+            hix = fmaxf(hix, p.x); hiy = fmaxf(hiy, p.y); hiz = fmaxf(hiz, p.z);
+        }
+        lox = warp_min(lox); loy = warp_min(loy); loz = warp_min(loz);
+        hix = warp_max(hix); hiy = warp_max(hiy); hiz = warp_max(hiz);
+        const f2 nx = pk(-px[0], -px[1]), ny = pk(-py[0], -py[1]), nz = pk(-pz[0], -pz[1]);
+        f2 ax = 0ull, ay = 0ull, az = 0ull;
+        int top = 1, nil = 0;
+        if (lane == 0) stack[0] = 0u;  // the root: slot 0, one node
+        __syncwarp();
+        // a group that needs more than `budget` iterations (its box lies close to much
+        // denser matter, which it would open down to the particles) is walked per particle
+        int iters = 0;
+        bool fallback = false;
+        while (top > 0) {
+            if (++iters > budget) {
+                fallback = true;
+                break;
+            }
+            // pop whole ranges from the top, at most 32 nodes
+            const uint32_t e = lane < top ? stack[top - 1 - lane] : 0u;
+            const int nkl = lane < top ? (int)(e & 7u) + 1 : 0;
+            int cum = nkl;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(FULL, cum, o);
+                if (lane >= o) cum += v;
+            }
+            const bool take = lane < top && cum <= 32;
+            const int kr = __popc(__ballot_sync(FULL, take));
+            const int total = __shfl_sync(FULL, cum, kr - 1);
+            const unsigned starts = __reduce_or_sync(FULL, take ? (1u << (cum - nkl)) : 0u);
+            top -= kr;
+            __syncwarp();
+            const bool has = lane < total;
+            const unsigned upto = lane == 31 ? FULL : ((2u << lane) - 1u);
+            const int r = max(__popc(starts & upto) - 1, 0);
+            const uint32_t er = __shfl_sync(FULL, e, r);
+            const int sr = __shfl_sync(FULL, cum - nkl, r);
+            float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
+            int4 B = make_int4(0, 0, 0, 0);
+            if (has) {
+                const size_t slot = (size_t)(er >> 3) + (size_t)(lane - sr);
+                A = krec[2 * slot];
+                B = reinterpret_cast<const int4 *>(krec)[2 * slot + 1];
+            }
+            bool accept = false, open = false, bucket = false;
+            if (has && A.w != 0.f) {
+                if (B.x == -1) {
+                    accept = true;
+                } else if (B.x == -2) {
+                    bucket = true;
+                } else {
+                    const float dx = fmaxf(fmaxf(lox - A.x, A.x - hix), 0.f);
+                    const float dy = fmaxf(fmaxf(loy - A.y, A.y - hiy), 0.f);
+                    const float dz = fmaxf(fmaxf(loz - A.z, A.z - hiz), 0.f);
+                    const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                    if (__int_as_float(B.w) < theta2f * d2) accept = true;
+                    else open = true;
+                }
+            }
+            const unsigned om = __ballot_sync(FULL, open);
+            if (top + __popc(om) > GW_SCAP) {  // unreachable by the bound above; flagged, never written
+                if (lane == 0) atomicOr(err, DERR_STACK_OVERFLOW);
+            } else {
+                if (open) stack[top + __popc(om & lt)] = ((uint32_t)B.x << 3) | (uint32_t)(B.y - 1);
+                top += __popc(om);
+            }
+            const unsigned am = __ballot_sync(FULL, accept);
+            if (accept) {
+                float4 *s = il + 2 * (nil + __popc(am & lt));
+                s[0] = make_float4(A.x, A.x, A.y, A.y);
+                s[1] = make_float4(A.z, A.z, A.w, A.w);
+            }
+            nil += __popc(am);
+            unsigned bm = __ballot_sync(FULL, bucket);
+            while (bm) {  // leaves of coincident-key particles (rare): members one by one
+                const int b = __ffs(bm) - 1;
+                bm &= bm - 1;
+                const int bf = __shfl_sync(FULL, B.y, b), bc = __shfl_sync(FULL, B.z, b);
+                for (int j0 = 0; j0 < bc; j0 += 32) {
+                    if (nil > GW_ICAP - 32) {
+                        __syncwarp();
+                        group_eval<NPL, GUARD>(il, nil, nx, ny, nz, eps2f, ax, ay, az);
+                        nil = 0;
+                        __syncwarp();
+                    }
+                    const int j = j0 + lane;
+                    const float4 q = j < bc ? p32[bf + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    const bool ok = j < bc && q.w != 0.f;
+                    const unsigned qm = __ballot_sync(FULL, ok);
+                    if (ok) {
+                        float4 *s = il + 2 * (nil + __popc(qm & lt));
+                        s[0] = make_float4(q.x, q.x, q.y, q.y);
+                        s[1] = make_float4(q.z, q.z, q.w, q.w);
+                    }
+                    nil += __popc(qm);
+                }
+            }
+            __syncwarp();
+            if (nil > GW_ICAP - 32) {
+                group_eval<NPL, GUARD>(il, nil, nx, ny, nz, eps2f, ax, ay, az);
+                nil = 0;
+                __syncwarp();
+            }
+        }
+        float fx[2], fy[2], fz[2];
+        if (lane == 0) {
+            atomicAdd(reinterpret_cast<unsigned long long *>(err + 12), (unsigned long long)iters);
+            atomicAdd(err + 14, 1u);
+            if (fallback) atomicAdd(err + 15, 1u);
+        }
+        if (fallback) {
+#pragma unroll
+            for (int q = 0; q < NPL; ++q) {
+                const int k = q * 32 + lane;
+                fx[q] = fy[q] = fz[q] = 0.f;
+                walk_lanes_f32((size_t)gr.x + k, k < gr.y, nnodes, meta, cm32, p32, tab.s2f, theta2f, eps2f, fx[q],
+                               fy[q], fz[q]);
+            }
+        } else {
+            if (nil) group_eval<NPL, GUARD>(il, nil, nx, ny, nz, eps2f, ax, ay, az);
+            upk(ax, fx[0], fx[1]);
+            upk(ay, fy[0], fy[1]);
+            upk(az, fz[0], fz[1]);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < NPL; ++q) {
+            const int k = q * 32 + lane;
+            if (k < gr.y) {
+                const size_t i = (size_t)gr.x + k;
+                acc[i] = fx[q];
+                acc[n + i] = fy[q];
+                acc[2 * n + i] = fz[q];
+            }
+        }
+    }
+}
+
 __global__ void k_scatter_acc(size_t n, const double *__restrict__ acc, const uint32_t *__restrict__ perm,
                               double *__restrict__ AX, double *__restrict__ AY, double *__restrict__ AZ,
                               int accumulate) {
@@ -467,7 +882,8 @@ void tree_free(Ctx *c) {
     DevBuf *all[] = {&t->bb, &t->bbpart, &t->khi, &t->klo, &t->khi2, &t->klo2, &t->perm, &t->perm2, &t->iota,
                      &t->iota2, &t->delta, &t->nown, &t->off, &t->total, &t->level, &t->first, &t->cnt, &t->skip,
                      &t->mass, &t->comx, &t->comy, &t->comz, &t->boxx, &t->boxy, &t->boxz, &t->sx, &t->sy,
-                     &t->sz, &t->sm, &t->pos32, &t->cm32, &t->cm64, &t->meta, &t->acc, &t->pos32lo, &t->cm32lo};
+                     &t->sz, &t->sm, &t->pos32, &t->cm32, &t->cm64, &t->meta, &t->acc, &t->pos32lo, &t->cm32lo, &t->nk, &t->koff, &t->krec,
+                     &t->groups, &t->gcount};
     for (DevBuf *b : all)
         if (b->ptr) cudaFree(b->ptr);
     delete t;
@@ -569,6 +985,39 @@ gvs_status tree_build(Ctx *c) {
     return GVS_OK;
 }
 
+// Child-slot records and particle groups of the current tree for the group walk.
+static gvs_status group_prepare(Ctx *c, Tree *t, int gsize) {
+    if (t->grp_version == t->version && t->grp_size == gsize) return GVS_OK;
+    const size_t nn = t->nnodes, n = t->n;
+    cudaStream_t st = c->stream;
+    GVS_CUDA(c, ensure(c, t->nk, nn * 4));
+    GVS_CUDA(c, ensure(c, t->koff, nn * 4));
+    GVS_CUDA(c, ensure(c, t->krec, nn * 2 * sizeof(float4)));
+    GVS_CUDA(c, ensure(c, t->groups, n * sizeof(int2)));
+    GVS_CUDA(c, ensure(c, t->gcount, 16));
+    k_nkids<<<nblk(nn), 256, 0, st>>>(nn, as<uint32_t>(t->cnt), as<uint32_t>(t->skip), as<uint32_t>(t->nk));
+    c->prof.launches += 1;
+    GVS_TRY(exclusive_scan_u32(c, as<uint32_t>(t->nk), as<uint32_t>(t->koff), nn, nullptr));
+    S2f tab;
+    for (int L = 0; L <= MAXL; ++L) {
+        const double s = 2.0 * std::ldexp(t->root[3], -L);
+        tab.s2[L] = (float)(s * s);
+    }
+    k_krec<<<nblk(nn), 256, 0, st>>>(nn, as<uint8_t>(t->level), as<uint32_t>(t->first), as<uint32_t>(t->cnt),
+                                     as<uint32_t>(t->skip), as<uint32_t>(t->nk), as<uint32_t>(t->koff),
+                                     as<double>(t->mass), as<double>(t->comx), as<double>(t->comy),
+                                     as<double>(t->comz), tab, as<float4>(t->krec));
+    GVS_CUDA(c, cudaMemsetAsync(t->gcount.ptr, 0, 8, st));
+    k_groups<<<nblk(nn), 256, 0, st>>>(nn, n, (uint32_t)gsize, as<uint8_t>(t->level), as<uint32_t>(t->first),
+                                       as<uint32_t>(t->cnt), as<uint32_t>(t->skip), as<uint64_t>(t->khi),
+                                       as<uint64_t>(t->klo), as<int2>(t->groups), as<uint32_t>(t->gcount));
+    c->prof.launches += 2;
+    GVS_TRY(check_launch(c, "group walk setup"));
+    t->grp_version = t->version;
+    t->grp_size = gsize;
+    return GVS_OK;
+}
+
 gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accumulate) {
     const size_t n = c->n;
     if (n == 0) return GVS_OK;
@@ -620,8 +1069,26 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
         tab.hi2[L] = (float)(hi * hi * (1.0 + 0x1p-19));
     }
     GVS_CUDA(c, ensure(c, t->acc, 3 * n * sizeof(double)));
+    // FP32 with a group size set: the group walk (slot records fit 29 bits)
+    const bool group = mode == 1 && c->bh_group > 0 && nnodes < (size_t(1) << 29);
+    if (group) GVS_TRY(group_prepare(c, t, c->bh_group));
     if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], st));
-    if (mode == 0)
+    if (group) {
+        GVS_CUDA(c, cudaMemsetAsync(as<uint32_t>(t->gcount) + 1, 0, 4, st));
+        const bool guard = eps == 0.0;
+        const float th2 = (float)(theta * theta), e2 = (float)(eps * eps);
+        auto launch = [&](auto kern) -> gvs_status {
+            int per_sm = 0;
+            GVS_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, GW_WARPS * 32, 0));
+            kern<<<std::max(1, per_sm) * c->num_sms, GW_WARPS * 32, 0, st>>>(
+                as<int2>(t->groups), as<uint32_t>(t->gcount), as<float4>(t->krec), as<float4>(t->pos32), th2, e2,
+                n, nnodes, as<int4>(t->meta), as<float4>(t->cm32), tab, c->bh_budget, as<double>(t->acc), err_ptr(c));
+            return GVS_OK;
+        };
+        if (c->bh_group == 64) GVS_TRY(guard ? launch(k_walk_group<2, true>) : launch(k_walk_group<2, false>));
+        else GVS_TRY(guard ? launch(k_walk_group<1, true>) : launch(k_walk_group<1, false>));
+        c->prof.launches += 2;
+    } else if (mode == 0)
         k_walk<0><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, as<int4>(t->meta), nullptr, as<double4>(t->cm64),
                                                 nullptr, as<double>(t->sx), as<double>(t->sy), as<double>(t->sz),
                                                 as<double>(t->sm), tab, theta * theta, eps * eps,

@@ -279,49 +279,6 @@ __global__ void k_pack64(const double *__restrict__ X, const double *__restrict_
     pack[s] = make_double4(X[o], Y[o], Z[o], valid ? M[o] : 0.0);
 }
 
-// ---------------------------------------------------------------------------
-// f32x2 helpers (packed two-lane f32 arithmetic, sm_100+)
-// ---------------------------------------------------------------------------
-typedef unsigned long long f2;  // two f32 lanes in one 64-bit register pair
-
-__device__ __forceinline__ f2 pk(float a, float b) {
-    f2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ void upk(f2 v, float &a, float &b) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-}
-__device__ __forceinline__ f2 add2(f2 a, f2 b) {
-    f2 r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
-    f2 r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
-    f2 r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
-    f2 r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-
-// (hi, lo) += v, lane-wise, with Knuth's two-sum (error-free for hi + v).
-__device__ __forceinline__ void two_sum2(f2 &hi, f2 &lo, f2 v) {
-    const f2 s = add2(hi, v);
-    const f2 bp = sub2(s, hi);
-    const f2 e = add2(sub2(hi, sub2(s, bp)), sub2(v, bp));
-    lo = add2(lo, e);
-    hi = s;
-}
-
 // Sources [j0, j0 + NJ) of a tile against NP target pairs.  nx.. hold
 // -(x_i - c_J) per pair.  Pairs whose bit is set in MASK also add the f32 lo
 // parts of both sides (float-float separations): sources close to the

@@ -555,6 +555,17 @@ gvs_status gvs_set_direct_shape(gvs_ctx *c, int nthreads, int ipt, int min_block
     return GVS_OK;
 }
 
+gvs_status gvs_set_bh_walk(gvs_ctx *c, int group_size, int budget) {
+    GVS_TRY(check_ctx(c));
+    if (group_size != 0 && group_size != 32 && group_size != 64)
+        return fail(c, GVS_ERR_INVALID_ARG, "BH walk group size must be 0 (per-particle), 32 or 64, got %d",
+                    group_size);
+    if (budget < 0) return fail(c, GVS_ERR_INVALID_ARG, "BH group-walk budget must be >= 0, got %d", budget);
+    c->bh_group = group_size;
+    c->bh_budget = budget > 0 ? budget : 1024;
+    return GVS_OK;
+}
+
 gvs_status gvs_autotune_report(gvs_ctx *c, int cap, int *count, int *nthreads, int *ipt, int *min_blocks,
                                int *unroll, double *ms) {
     GVS_TRY(check_ctx(c));
@@ -656,7 +667,7 @@ gvs_status gvs_profile_enable(gvs_ctx *c, int on) {
     c->prof.tile_visits = 0.0;
     c->prof.vjp_ms = 0.0;
     c->prof.vjp_launches = 0;
-    GVS_CUDA(c, cudaMemsetAsync(err_ptr(c) + 8, 0, sizeof(unsigned long long) + sizeof(unsigned), c->stream));
+    GVS_CUDA(c, cudaMemsetAsync(err_ptr(c) + 8, 0, 8 * sizeof(unsigned), c->stream));
     return GVS_OK;
 }
 
@@ -678,6 +689,11 @@ gvs_status gvs_profile_read(gvs_ctx *c, gvs_profile *out) {
     unsigned redo = 0;
     GVS_CUDA(c, cudaMemcpy(&redo, err_ptr(c) + 10, sizeof redo, cudaMemcpyDeviceToHost));
     out->sph_f64_redo = redo;
+    unsigned words[4] = {0, 0, 0, 0};  // group walk: iterations (u64), groups, fallbacks
+    GVS_CUDA(c, cudaMemcpy(words, err_ptr(c) + 12, sizeof words, cudaMemcpyDeviceToHost));
+    out->bh_group_iterations = (long long)((unsigned long long)words[0] | ((unsigned long long)words[1] << 32));
+    out->bh_groups = words[2];
+    out->bh_group_fallbacks = words[3];
     return GVS_OK;
 }
 

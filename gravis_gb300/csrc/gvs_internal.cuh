@@ -97,6 +97,8 @@ struct Ctx {
 
     Prof prof;
     Tune tune;
+    int bh_group = 64;    // FP32 Barnes-Hut: particles per walk group (32, 64), 0 = per-particle walk
+    int bh_budget = 1024; // group-walk iterations before a group is walked per particle
     unsigned long long alloc_gen = 0;  // bumped whenever ensure() (re)allocates a buffer
 
     // One direct-sum KDK step captured as a CUDA graph, replayed by gvs_kdk_steps.
@@ -204,6 +206,47 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     s = __fadd_rn(a, b);
     float bp = __fsub_rn(s, a);
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+
+// f32x2 helpers (packed two-lane f32 arithmetic, sm_100+)
+typedef unsigned long long f2;  // two f32 lanes in one 64-bit register pair
+
+__device__ __forceinline__ f2 pk(float a, float b) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void upk(f2 v, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+// (hi, lo) += v, lane-wise, with Knuth's two-sum (error-free for hi + v).
+__device__ __forceinline__ void two_sum2(f2 &hi, f2 &lo, f2 v) {
+    const f2 s = add2(hi, v);
+    const f2 bp = sub2(s, hi);
+    const f2 e = add2(sub2(hi, sub2(s, bp)), sub2(v, bp));
+    lo = add2(lo, e);
+    hi = s;
 }
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }

@@ -135,12 +135,17 @@ def test_bh_accuracy_table(ctx, golden):
 
 @pytest.mark.parametrize("theta", [0.5, 0.7])
 def test_bh_f32_walk(ctx, theta):
+    """The per-particle f32 walk (the reference's test on f32 positions)."""
     p = G.collision(1 << 16, seed=7)
     eps = 1e-3
     a64 = p.copy()
     G.BarnesHut(eps, theta, G.PREC_FP64, ctx).compute_accelerations(a64)
     a32 = p.copy()
-    G.BarnesHut(eps, theta, G.PREC_FP32, ctx).compute_accelerations(a32)
+    ctx.set_bh_walk(0)
+    try:
+        G.BarnesHut(eps, theta, G.PREC_FP32, ctx).compute_accelerations(a32)
+    finally:
+        ctx.set_bh_walk(64)
     err = rel_rms(a32.acc(), a64.acc())
     print(f"theta={theta} f32 walk vs f64 walk rel RMS {err:.2e}")
     # f32 absolute positions at |x| ~ 10 resolve separations to ~1e-6; the bound
@@ -194,6 +199,103 @@ def test_bh_vs_direct_subset(ctx):
         rel = np.sqrt((((q.acc()[idx] - ref) ** 2).sum(1) / (ref ** 2).sum(1)).mean())
         print(f"theta={theta} BH f32 vs direct f64 per-particle RMS {rel:.3e}")
         assert rel < bound
+
+
+def with_duplicates(p, k, at=0):
+    """p plus k particles at exactly the position of particle `at` (a bucket leaf of k + 1)."""
+    q = G.Particles(p.count + k)
+    for f in ("x", "y", "z", "vx", "vy", "vz", "mass"):
+        getattr(q, f)[:p.count] = getattr(p, f)
+        getattr(q, f)[p.count:] = getattr(p, f)[at]
+    return q
+
+
+@pytest.mark.parametrize("gsize", [32, 64])
+@pytest.mark.parametrize("case", ["plummer", "buckets"])
+def test_bh_group_walk_theta_zero_is_direct(ctx, gsize, case):
+    """theta = 0 opens every node, so the group walk is the f32 all-pairs sum,
+    including the members of bucket leaves (100 coincident particles: a bucket
+    larger than a group, cut into several groups)."""
+    p = G.PlummerSphere(3000, seed=5).generate()
+    if case == "buckets":
+        p = with_duplicates(p, 99, at=17)
+    eps = 0.01
+    ref = p.copy()
+    G.BruteForce(eps, G.PREC_FP64_EXACT, ctx).compute_accelerations(ref)
+    ctx.set_bh_walk(gsize)
+    try:
+        q = p.copy()
+        G.BarnesHut(eps, 0.0, G.PREC_FP32, ctx).compute_accelerations(q)
+    finally:
+        ctx.set_bh_walk(64)
+    err = rel_rms(q.acc(), ref.acc())
+    print(f"group {gsize} {case}: theta=0 vs f64 direct rel RMS {err:.2e}")
+    # f32 terms on absolute f32 positions summed over ~3000 sources
+    assert err <= 5e-6
+
+
+@pytest.mark.parametrize("theta", [0.5, 0.7])
+def test_bh_group_walk_refines_per_particle(ctx, theta):
+    """The group test accepts only nodes every particle of the group would accept,
+    so the group walk is at least as close to the exact f64 direct sum as the
+    per-particle walk."""
+    n = 1 << 17
+    p = G.collision(n, seed=7)
+    eps = 1e-3
+    ctx.set_state(p)
+    idx = np.sort(np.random.default_rng(1).choice(n, 2048, replace=False))
+    ref = ctx.direct_subset(idx, eps)
+    errs = {}
+    try:
+        for g in (0, 32, 64):
+            ctx.set_bh_walk(g)
+            q = p.copy()
+            G.BarnesHut(eps, theta, G.PREC_FP32, ctx).compute_accelerations(q)
+            errs[g] = float(np.sqrt((((q.acc()[idx] - ref) ** 2).sum(1) / (ref ** 2).sum(1)).mean()))
+    finally:
+        ctx.set_bh_walk(64)
+    print(f"theta={theta} per-particle RMS vs f64 direct: " + ", ".join(f"{k}: {v:.3e}" for k, v in errs.items()))
+    assert errs[32] <= errs[0] and errs[64] <= errs[0]
+
+
+def test_bh_group_walk_unsoftened(ctx):
+    """eps = 0: a particle's own leaf adds exactly zero (no 0/0), forces stay finite
+    and agree with the f64 walk to f32 accuracy at theta = 0."""
+    p = G.PlummerSphere(2000, seed=13).generate()
+    ref = p.copy()
+    G.BruteForce(0.0, G.PREC_FP64_EXACT, ctx).compute_accelerations(ref)
+    q = p.copy()
+    G.BarnesHut(0.0, 0.0, G.PREC_FP32, ctx).compute_accelerations(q)
+    assert np.isfinite(q.acc()).all()
+    assert rel_rms(q.acc(), ref.acc()) <= 1e-4
+
+
+def test_bh_group_walk_fallback_is_per_particle_walk(ctx):
+    """With a budget of one iteration every group falls back to the per-particle walk,
+    which must reproduce the per-particle kernel bit for bit."""
+    p = G.collision(1 << 15, seed=7)
+    eps, theta = 1e-3, 0.5
+    ctx.set_bh_walk(0)
+    try:
+        a = p.copy()
+        G.BarnesHut(eps, theta, G.PREC_FP32, ctx).compute_accelerations(a)
+        ctx.set_bh_walk(64, 1)
+        ctx.profile(True)
+        b = p.copy()
+        G.BarnesHut(eps, theta, G.PREC_FP32, ctx).compute_accelerations(b)
+        pr = ctx.profile_read()
+        ctx.profile(False)
+    finally:
+        ctx.set_bh_walk(64)
+    assert pr["bh_groups"] > 0 and pr["bh_group_fallbacks"] == pr["bh_groups"]
+    assert np.array_equal(a.acc(), b.acc())
+
+
+def test_bh_group_walk_rejects_bad_size(ctx):
+    with pytest.raises(G.GvsError):
+        ctx.set_bh_walk(48)
+    with pytest.raises(G.GvsError):
+        ctx.set_bh_walk(64, -1)
 
 
 def test_bh_deterministic_and_resident_steps(ctx):
