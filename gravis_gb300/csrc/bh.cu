@@ -12,8 +12,10 @@
 //  1. Key: each particle replays the reference's f64 halving arithmetic for
 //     42 levels (centre +- hw/2, same rounding), recording 3 octant bits per
 //     level: a 126-bit octant-path key (two u64 words, 21 levels each).
-//  2. Sort: stable radix sort by (high word, low word).  Sorted order = the
-//     depth-first order of the reference tree with children 0..7.
+//  2. Sort: by (high word, low word), ties in index order.  Sorted order = the
+//     depth-first order of the reference tree with children 0..7.  The low
+//     word is computed only for particles whose high word a neighbour shares:
+//     everyone else's cell ends above depth 22.
 //  3. Nodes: with d_i = common prefix depth of sorted keys i-1 and i, particle
 //     i starts exactly the nodes at depths d_i+1 .. max(d_i, d_{i+1})+1 (the
 //     last is its leaf).  A prefix sum of those counts gives every node an
@@ -21,8 +23,10 @@
 //     subtree covers node indices [idx, off[e]) -- the skip pointer.
 //     Particles that share all 42 levels (closer than 2^-42 of the box) form
 //     one bucket leaf; the reference would keep splitting down to depth 64.
-//  4. Moments: mass and centre of mass in f64, bottom-up one level at a time
-//     (a node sums its children in child order, so results are deterministic).
+//  4. Moments: mass and centre of mass in f64, bottom-up in one pass (the
+//     last child to finish sums its parent's children in child order, so
+//     results are deterministic); the centre is the mass-weighted sum times
+//     the f64 reciprocal of the mass.
 //     The reference updates the COM incrementally in insertion order; the
 //     two agree to a few ulps.
 //  5. Walk: the reference's per-particle stack walk (barnes_hut.rs:44-108):
@@ -59,6 +63,7 @@ struct Tree {
     DevBuf pos32lo, cm32lo;  // mixed walk: f32 lo words of positions and COMs
     // group walk (f32): child-slot records, groups of <= 32*NPL particles, work counter
     DevBuf nk, koff, krec, groups, gcount;
+    DevBuf parent, arrive;  // per node: parent index, children that finished their moments
     unsigned long long grp_version = ~0ull;
     int grp_size = 0;
     int walk_blocks = 0;  // resident blocks of the group walk (per GPU)
@@ -95,28 +100,116 @@ __global__ void k_root(double *bb) {
     bb[6] = c[0]; bb[7] = c[1]; bb[8] = c[2]; bb[9] = hw;
 }
 
-// Octant-path key (octant, child_bounds: octree.rs:52-79), 42 levels.
+// hw * 0.5 for the cell half widths: exact for normal hw (a root half width is
+// >= 1e-10, so 42 halvings stay far above the subnormal range); an exponent
+// decrement instead of an f64 multiply (GB300 runs f64 at 1/64 of the f32 rate).
+__device__ __forceinline__ double half_of(double hw, bool finite) {
+    return finite ? __longlong_as_double(__double_as_longlong(hw) - (1ll << 52)) : __dmul_rn(hw, 0.5);
+}
+
+// Order-preserving map of f64 to u64: a >= b <=> ord64(a) >= ord64(b) for non-NaN
+// a, b, with -0 mapped like +0 -- so the octant tests x >= centre run on the
+// integer pipe with the f64 compare's result.
+__device__ __forceinline__ unsigned long long ord64(double v) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    if (b == 0x8000000000000000ull) b = 0ull;
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ bool nan64(double v) {
+    return ((unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull;
+}
+
+// Octant path of one point (octant, child_bounds: octree.rs:52-79): the
+// reference's f64 centre updates (round to nearest, no contraction) and its
+// x >= centre tests (false when either side is NaN), levels 1..LMAX; levels
+// 1..21 go to hi, 22..42 to lo.
+template <int LMAX>
+__device__ __forceinline__ void octant_path(double x, double y, double z, const double *__restrict__ bb, uint64_t &hi,
+                                            uint64_t &lo) {
+    const unsigned long long ox = ord64(x), oy = ord64(y), oz = ord64(z);
+    const bool nx = nan64(x), ny = nan64(y), nz = nan64(z);
+    double cx = bb[6], cy = bb[7], cz = bb[8], hw = bb[9];
+    const bool fin = isfinite(hw);
+    hi = 0;
+    lo = 0;
+    for (int L = 1; L <= LMAX; ++L) {
+        const bool gx = !nx && !nan64(cx) && ox >= ord64(cx);
+        const bool gy = !ny && !nan64(cy) && oy >= ord64(cy);
+        const bool gz = !nz && !nan64(cz) && oz >= ord64(cz);
+        const int oct = (gx ? 1 : 0) | (gy ? 2 : 0) | (gz ? 4 : 0);
+        if (L <= 21) hi = (hi << 3) | (uint64_t)oct;
+        else lo = (lo << 3) | (uint64_t)oct;
+        if (L == LMAX) break;
+        const double q = half_of(hw, fin);
+        cx = __dadd_rn(cx, gx ? q : -q);
+        cy = __dadd_rn(cy, gy ? q : -q);
+        cz = __dadd_rn(cz, gz ? q : -q);
+        hw = q;
+    }
+}
+
+// Keys, levels 1..LMAX (42: both words; 21: the high word, lo = 0).
+template <int LMAX>
 __global__ void k_keys(const double *__restrict__ X, const double *__restrict__ Y, const double *__restrict__ Z,
                        size_t n, const double *__restrict__ bb, uint64_t *__restrict__ khi,
                        uint64_t *__restrict__ klo, uint32_t *__restrict__ perm) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double x = X[i], y = Y[i], z = Z[i];
-    double cx = bb[6], cy = bb[7], cz = bb[8], hw = bb[9];
-    uint64_t hi = 0, lo = 0;
-    for (int L = 1; L <= MAXL; ++L) {
-        const int oct = (x >= cx ? 1 : 0) | (y >= cy ? 2 : 0) | (z >= cz ? 4 : 0);
-        const double q = __dmul_rn(hw, 0.5);
-        cx = __dadd_rn(cx, (oct & 1) ? q : -q);
-        cy = __dadd_rn(cy, (oct & 2) ? q : -q);
-        cz = __dadd_rn(cz, (oct & 4) ? q : -q);
-        hw = q;
-        if (L <= 21) hi = (hi << 3) | (uint64_t)oct;
-        else lo = (lo << 3) | (uint64_t)oct;
-    }
+    uint64_t hi, lo;
+    octant_path<LMAX>(X[i], Y[i], Z[i], bb, hi, lo);
     khi[i] = hi;
-    klo[i] = lo;
+    if (klo) klo[i] = lo;
     perm[i] = (uint32_t)i;
+}
+
+// After the sort by the high word: particles whose high word equals a
+// neighbour's (runs of points closer than 2^-21 of the root box) get their low
+// word; everyone else's stays 0 (their cells end above depth 22, where the low
+// word is never consulted).  stat[0] counts them; stat[1] is set if a run is
+// longer than RUN_MAX.
+constexpr int RUN_MAX = 64;
+__global__ void k_keys_lo(const uint64_t *__restrict__ khi, const uint32_t *__restrict__ perm,
+                          const double *__restrict__ X, const double *__restrict__ Y, const double *__restrict__ Z,
+                          size_t n, const double *__restrict__ bb, uint64_t *__restrict__ klo,
+                          uint32_t *__restrict__ stat) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t h = khi[i];
+    const bool prev = i > 0 && khi[i - 1] == h, next = i + 1 < n && khi[i + 1] == h;
+    uint64_t lo = 0;
+    if (prev || next) {
+        const uint32_t o = perm[i];
+        uint64_t hh;
+        octant_path<MAXL>(X[o], Y[o], Z[o], bb, hh, lo);
+        atomicAdd(stat, 1u);
+        if (!prev && i + RUN_MAX < n && khi[i + RUN_MAX] == h) atomicOr(stat + 1, 1u);
+    }
+    klo[i] = lo;
+}
+
+// Sorts each run of equal high words by (low word, original index) -- the
+// order a stable sort by (high, low) gives -- one thread per run start,
+// insertion sort (runs hold at most RUN_MAX particles).
+__global__ void k_sort_runs(const uint64_t *__restrict__ khi, size_t n, uint64_t *__restrict__ klo,
+                            uint32_t *__restrict__ perm) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i + 1 >= n) return;
+    const uint64_t h = khi[i];
+    if ((i > 0 && khi[i - 1] == h) || khi[i + 1] != h) return;
+    size_t e = i + 1;
+    while (e < n && khi[e] == h) ++e;
+    for (size_t a = i + 1; a < e; ++a) {
+        const uint64_t kl = klo[a];
+        const uint32_t kp = perm[a];
+        size_t b = a;
+        while (b > i && (klo[b - 1] > kl || (klo[b - 1] == kl && perm[b - 1] > kp))) {
+            klo[b] = klo[b - 1];
+            perm[b] = perm[b - 1];
+            --b;
+        }
+        klo[b] = kl;
+        perm[b] = kp;
+    }
 }
 
 __global__ void k_iota(uint32_t *a, size_t n) {
@@ -161,9 +254,10 @@ __global__ void k_nodes(const uint64_t *__restrict__ khi, const uint64_t *__rest
     if (b < a) return;
     const uint64_t hi = khi[i], lo = klo[i];
     double cx = bb[6], cy = bb[7], cz = bb[8], hw = bb[9];
+    const bool fin = isfinite(hw);
     for (int L = 1; L < a; ++L) {  // descend to depth a
         const int oct = octant_at(hi, lo, L);
-        const double q = __dmul_rn(hw, 0.5);
+        const double q = half_of(hw, fin);
         cx = __dadd_rn(cx, (oct & 1) ? q : -q);
         cy = __dadd_rn(cy, (oct & 2) ? q : -q);
         cz = __dadd_rn(cz, (oct & 4) ? q : -q);
@@ -173,7 +267,7 @@ __global__ void k_nodes(const uint64_t *__restrict__ khi, const uint64_t *__rest
     for (int L = a; L <= b; ++L) {
         if (L >= 1) {
             const int oct = octant_at(hi, lo, L);
-            const double q = __dmul_rn(hw, 0.5);
+            const double q = half_of(hw, fin);
             cx = __dadd_rn(cx, (oct & 1) ? q : -q);
             cy = __dadd_rn(cy, (oct & 2) ? q : -q);
             cz = __dadd_rn(cz, (oct & 4) ? q : -q);
@@ -202,38 +296,75 @@ __global__ void k_nodes(const uint64_t *__restrict__ khi, const uint64_t *__rest
     }
 }
 
-// Bottom-up moments for the nodes of depth L.
-__global__ void k_moments(int L, size_t nnodes, const uint8_t *__restrict__ level, const uint32_t *__restrict__ first,
-                          const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ skip,
-                          const double *__restrict__ sx, const double *__restrict__ sy, const double *__restrict__ sz,
-                          const double *__restrict__ sm, double *__restrict__ mass, double *__restrict__ cx,
-                          double *__restrict__ cy, double *__restrict__ cz) {
+// Parent links and child counts: each internal node walks its children (the
+// skip chain k+1, skip[k+1], ... up to skip[k]).
+__global__ void k_links(size_t nnodes, const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ skip,
+                        uint32_t *__restrict__ parent, uint32_t *__restrict__ nk) {
     const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nnodes || level[k] != L) return;
-    const uint32_t c0 = cnt[k];
+    if (k >= nnodes) return;
+    if (k == 0) parent[0] = 0xFFFFFFFFu;
+    uint32_t c = 0;
+    if (cnt[k] == 0) {
+        const uint32_t end = skip[k];
+        for (uint32_t ch = (uint32_t)k + 1; ch < end; ch = skip[ch], ++c) parent[ch] = (uint32_t)k;
+    }
+    nk[k] = c;
+}
+
+// Mass and centre of mass in f64, bottom-up in one pass.  Each leaf sums its
+// members in order; then the thread whose child finishes a parent last (an
+// arrival counter per node) sums that parent's children in child order 0..7 and
+// moves up.  Every node's sum has a fixed order, so the result does not depend
+// on which thread computes it.  Writes are fenced before the arrival count;
+// the last arriver fences after it and reads the children through L2.
+__global__ void k_moments_up(size_t nnodes, const uint32_t *__restrict__ first, const uint32_t *__restrict__ cnt,
+                             const uint32_t *__restrict__ skip, const uint32_t *__restrict__ parent,
+                             const uint32_t *__restrict__ nk, uint32_t *__restrict__ arrive,
+                             const double *__restrict__ sx, const double *__restrict__ sy,
+                             const double *__restrict__ sz, const double *__restrict__ sm, double *mass, double *cx,
+                             double *cy, double *cz) {
+    const size_t k0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k0 >= nnodes) return;
+    const uint32_t c0 = cnt[k0];
+    if (c0 == 0) return;
+    uint32_t k = (uint32_t)k0;
     if (c0 == 1) {
         const uint32_t p = first[k];
         mass[k] = sm[p]; cx[k] = sx[p]; cy[k] = sy[p]; cz[k] = sz[p];
-        return;
-    }
-    double M = 0.0, X = 0.0, Yv = 0.0, Zv = 0.0;
-    if (c0 > 1) {  // bucket leaf: members in order
+    } else {  // bucket leaf: members in order
+        double M = 0.0, X = 0.0, Yv = 0.0, Zv = 0.0;
         for (uint32_t p = first[k]; p < first[k] + c0; ++p) {
             const double m = sm[p];
             M += m; X += m * sx[p]; Yv += m * sy[p]; Zv += m * sz[p];
         }
-    } else {  // internal: children in order 0..7
-        const uint32_t end = skip[k];
-        for (uint32_t ch = (uint32_t)k + 1; ch < end; ch = skip[ch]) {
-            const double m = mass[ch];
-            M += m; X += m * cx[ch]; Yv += m * cy[ch]; Zv += m * cz[ch];
+        mass[k] = M;
+        if (M > 0.0) {
+            const double r = 1.0 / M;  // one f64 division per node, not three
+            cx[k] = X * r; cy[k] = Yv * r; cz[k] = Zv * r;
+        } else {
+            cx[k] = cy[k] = cz[k] = 0.0;
         }
     }
-    mass[k] = M;
-    if (M > 0.0) {
-        cx[k] = X / M; cy[k] = Yv / M; cz[k] = Zv / M;
-    } else {
-        cx[k] = cy[k] = cz[k] = 0.0;
+    for (;;) {
+        const uint32_t up = parent[k];
+        if (up == 0xFFFFFFFFu) return;
+        __threadfence();
+        if (atomicAdd(arrive + up, 1u) != nk[up] - 1u) return;
+        __threadfence();
+        k = up;
+        double M = 0.0, X = 0.0, Yv = 0.0, Zv = 0.0;
+        const uint32_t end = skip[k];
+        for (uint32_t ch = k + 1; ch < end; ch = skip[ch]) {
+            const double m = __ldcg(mass + ch);
+            M += m; X += m * __ldcg(cx + ch); Yv += m * __ldcg(cy + ch); Zv += m * __ldcg(cz + ch);
+        }
+        mass[k] = M;
+        if (M > 0.0) {
+            const double r = 1.0 / M;  // one f64 division per node, not three
+            cx[k] = X * r; cy[k] = Yv * r; cz[k] = Zv * r;
+        } else {
+            cx[k] = cy[k] = cz[k] = 0.0;
+        }
     }
 }
 
@@ -478,18 +609,6 @@ __device__ __forceinline__ uint32_t sub_count(uint32_t k, size_t nnodes, size_t 
                                               const uint32_t *__restrict__ skip) {
     const uint32_t e = skip[k];
     return (uint32_t)((e < nnodes ? (size_t)first[e] : n) - first[k]);
-}
-
-__global__ void k_nkids(size_t nnodes, const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ skip,
-                        uint32_t *__restrict__ nk) {
-    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nnodes) return;
-    uint32_t c = 0;
-    if (cnt[k] == 0) {
-        const uint32_t end = skip[k];
-        for (uint32_t ch = (uint32_t)k + 1; ch < end; ch = skip[ch]) ++c;
-    }
-    nk[k] = c;
 }
 
 struct S2f {
@@ -883,7 +1002,7 @@ void tree_free(Ctx *c) {
                      &t->iota2, &t->delta, &t->nown, &t->off, &t->total, &t->level, &t->first, &t->cnt, &t->skip,
                      &t->mass, &t->comx, &t->comy, &t->comz, &t->boxx, &t->boxy, &t->boxz, &t->sx, &t->sy,
                      &t->sz, &t->sm, &t->pos32, &t->cm32, &t->cm64, &t->meta, &t->acc, &t->pos32lo, &t->cm32lo, &t->nk, &t->koff, &t->krec,
-                     &t->groups, &t->gcount};
+                     &t->groups, &t->gcount, &t->parent, &t->arrive};
     for (DevBuf *b : all)
         if (b->ptr) cudaFree(b->ptr);
     delete t;
@@ -900,46 +1019,70 @@ gvs_status tree_build(Ctx *c) {
     GVS_CUDA(c, ensure(c, t->bb, 16 * sizeof(double)));
     GVS_TRY(bbox_minmax(c, as<double>(t->bb), t->bbpart));
     k_root<<<1, 1, 0, st>>>(as<double>(t->bb));
-    // keys, sorted by (hi, lo): lo first, then a stable sort by hi
     const size_t b8 = n * 8, b4 = n * 4;
     GVS_CUDA(c, ensure(c, t->khi, b8)); GVS_CUDA(c, ensure(c, t->klo, b8));
     GVS_CUDA(c, ensure(c, t->khi2, b8)); GVS_CUDA(c, ensure(c, t->klo2, b8));
     GVS_CUDA(c, ensure(c, t->perm, b4)); GVS_CUDA(c, ensure(c, t->perm2, b4));
     GVS_CUDA(c, ensure(c, t->iota, b4)); GVS_CUDA(c, ensure(c, t->iota2, b4));
-    k_keys<<<nblk(n), 256, 0, st>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z), n, as<double>(t->bb),
-                                    as<uint64_t>(t->khi), as<uint64_t>(t->klo), as<uint32_t>(t->perm));
+    // keys: the high word (levels 1..21) for everyone, sorted; the low word only
+    // for runs of equal high words, which are then sorted by it.  A run longer
+    // than RUN_MAX (hundreds of near-coincident points) takes the full path: both
+    // words for everyone, sorted by low then (stably) by high.
+    GVS_CUDA(c, ensure(c, t->total, 16));
+    k_keys<21><<<nblk(n), 256, 0, st>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z), n, as<double>(t->bb),
+                                        as<uint64_t>(t->khi), nullptr, as<uint32_t>(t->perm));
     c->prof.launches += 2;
     GVS_TRY(check_launch(c, "tree keys"));
-    uint64_t *klo_s;
-    uint32_t *perm1;
-    GVS_TRY(radix_sort_u64(c, as<uint64_t>(t->klo), as<uint32_t>(t->perm), as<uint64_t>(t->klo2),
-                           as<uint32_t>(t->perm2), n, 0, 64, &klo_s, &perm1));
-    // khi in lo-sorted order, then the stable sort by hi carrying lo-order slots
-    uint64_t *khi_g = as<uint64_t>(t->khi2);
-    k_gather<uint64_t><<<nblk(n), 256, 0, st>>>(as<uint64_t>(t->khi), perm1, khi_g, n);
-    k_iota<<<nblk(n), 256, 0, st>>>(as<uint32_t>(t->iota), n);
-    c->prof.launches += 2;
     uint64_t *khi_s;
-    uint32_t *slot;
-    GVS_TRY(radix_sort_u64(c, khi_g, as<uint32_t>(t->iota), as<uint64_t>(t->khi), as<uint32_t>(t->iota2), n, 0, 64,
-                           &khi_s, &slot));
-    // khi_s lives in khi2 (even number of passes); final perm and lo keys
-    uint32_t *perm_final = (perm1 == as<uint32_t>(t->perm)) ? as<uint32_t>(t->perm2) : as<uint32_t>(t->perm);
-    uint64_t *klo_final = (klo_s == as<uint64_t>(t->klo)) ? as<uint64_t>(t->klo2) : as<uint64_t>(t->klo);
-    k_gather<uint32_t><<<nblk(n), 256, 0, st>>>(perm1, slot, perm_final, n);
-    k_gather<uint64_t><<<nblk(n), 256, 0, st>>>(klo_s, slot, klo_final, n);
-    c->prof.launches += 2;
-    // make the canonical buffers hold the final arrays
-    if (perm_final != as<uint32_t>(t->perm)) std::swap(t->perm, t->perm2);
-    if (klo_final != as<uint64_t>(t->klo)) std::swap(t->klo, t->klo2);
+    uint32_t *perm_s;
+    GVS_TRY(radix_sort_u64(c, as<uint64_t>(t->khi), as<uint32_t>(t->perm), as<uint64_t>(t->khi2),
+                           as<uint32_t>(t->perm2), n, 0, 64, &khi_s, &perm_s));
     if (khi_s != as<uint64_t>(t->khi)) std::swap(t->khi, t->khi2);
+    if (perm_s != as<uint32_t>(t->perm)) std::swap(t->perm, t->perm2);
+    uint32_t stat[2] = {0, 0};
+    GVS_CUDA(c, cudaMemsetAsync(t->total.ptr, 0, 16, st));
+    k_keys_lo<<<nblk(n), 256, 0, st>>>(as<uint64_t>(t->khi), as<uint32_t>(t->perm), as<double>(c->x),
+                                       as<double>(c->y), as<double>(c->z), n, as<double>(t->bb),
+                                       as<uint64_t>(t->klo), as<uint32_t>(t->total) + 2);
+    GVS_CUDA(c, cudaMemcpyAsync(stat, as<uint32_t>(t->total) + 2, 8, cudaMemcpyDeviceToHost, st));
+    GVS_CUDA(c, cudaStreamSynchronize(st));
+    c->prof.launches += 1;
+    if (stat[1]) {
+        k_keys<MAXL><<<nblk(n), 256, 0, st>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z), n,
+                                              as<double>(t->bb), as<uint64_t>(t->khi), as<uint64_t>(t->klo),
+                                              as<uint32_t>(t->perm));
+        c->prof.launches += 1;
+        uint64_t *klo_s;
+        uint32_t *perm1;
+        GVS_TRY(radix_sort_u64(c, as<uint64_t>(t->klo), as<uint32_t>(t->perm), as<uint64_t>(t->klo2),
+                               as<uint32_t>(t->perm2), n, 0, 64, &klo_s, &perm1));
+        // khi in lo-sorted order, then the stable sort by hi carrying lo-order slots
+        uint64_t *khi_g = as<uint64_t>(t->khi2);
+        k_gather<uint64_t><<<nblk(n), 256, 0, st>>>(as<uint64_t>(t->khi), perm1, khi_g, n);
+        k_iota<<<nblk(n), 256, 0, st>>>(as<uint32_t>(t->iota), n);
+        c->prof.launches += 2;
+        uint32_t *slot;
+        GVS_TRY(radix_sort_u64(c, khi_g, as<uint32_t>(t->iota), as<uint64_t>(t->khi), as<uint32_t>(t->iota2), n, 0,
+                               64, &khi_s, &slot));
+        uint32_t *perm_final = (perm1 == as<uint32_t>(t->perm)) ? as<uint32_t>(t->perm2) : as<uint32_t>(t->perm);
+        uint64_t *klo_final = (klo_s == as<uint64_t>(t->klo)) ? as<uint64_t>(t->klo2) : as<uint64_t>(t->klo);
+        k_gather<uint32_t><<<nblk(n), 256, 0, st>>>(perm1, slot, perm_final, n);
+        k_gather<uint64_t><<<nblk(n), 256, 0, st>>>(klo_s, slot, klo_final, n);
+        c->prof.launches += 2;
+        if (perm_final != as<uint32_t>(t->perm)) std::swap(t->perm, t->perm2);
+        if (klo_final != as<uint64_t>(t->klo)) std::swap(t->klo, t->klo2);
+        if (khi_s != as<uint64_t>(t->khi)) std::swap(t->khi, t->khi2);
+    } else if (stat[0]) {
+        k_sort_runs<<<nblk(n), 256, 0, st>>>(as<uint64_t>(t->khi), n, as<uint64_t>(t->klo), as<uint32_t>(t->perm));
+        c->prof.launches += 1;
+    }
+    GVS_TRY(check_launch(c, "tree key runs"));
     uint64_t *KH = as<uint64_t>(t->khi), *KL = as<uint64_t>(t->klo);
     uint32_t *P = as<uint32_t>(t->perm);
     // node enumeration
     GVS_CUDA(c, ensure(c, t->delta, (n + 1) * 4));
     GVS_CUDA(c, ensure(c, t->nown, (n + 1) * 4));
     GVS_CUDA(c, ensure(c, t->off, (n + 1) * 4));
-    GVS_CUDA(c, ensure(c, t->total, 16));
     k_delta<<<nblk(n + 1), 256, 0, st>>>(KH, KL, n, as<int>(t->delta));
     k_nown<<<nblk(n + 1), 256, 0, st>>>(as<int>(t->delta), n, as<uint32_t>(t->nown));
     c->prof.launches += 2;
@@ -970,14 +1113,18 @@ gvs_status tree_build(Ctx *c) {
     k_gather<double><<<nblk(n), 256, 0, st>>>(as<double>(c->m), P, as<double>(t->sm), n);
     c->prof.launches += 5;
     GVS_TRY(check_launch(c, "tree nodes"));
-    for (int L = MAXL; L >= 0; --L) {
-        k_moments<<<nblk(nnodes), 256, 0, st>>>(L, nnodes, as<uint8_t>(t->level), as<uint32_t>(t->first),
-                                                 as<uint32_t>(t->cnt), as<uint32_t>(t->skip), as<double>(t->sx),
-                                                 as<double>(t->sy), as<double>(t->sz), as<double>(t->sm),
-                                                 as<double>(t->mass), as<double>(t->comx), as<double>(t->comy),
-                                                 as<double>(t->comz));
-    }
-    c->prof.launches += MAXL + 1;
+    GVS_CUDA(c, ensure(c, t->parent, nnodes * 4));
+    GVS_CUDA(c, ensure(c, t->nk, nnodes * 4));
+    GVS_CUDA(c, ensure(c, t->arrive, nnodes * 4));
+    k_links<<<nblk(nnodes), 256, 0, st>>>(nnodes, as<uint32_t>(t->cnt), as<uint32_t>(t->skip),
+                                          as<uint32_t>(t->parent), as<uint32_t>(t->nk));
+    GVS_CUDA(c, cudaMemsetAsync(t->arrive.ptr, 0, nnodes * 4, st));
+    k_moments_up<<<nblk(nnodes), 256, 0, st>>>(nnodes, as<uint32_t>(t->first), as<uint32_t>(t->cnt),
+                                               as<uint32_t>(t->skip), as<uint32_t>(t->parent), as<uint32_t>(t->nk),
+                                               as<uint32_t>(t->arrive), as<double>(t->sx), as<double>(t->sy),
+                                               as<double>(t->sz), as<double>(t->sm), as<double>(t->mass),
+                                               as<double>(t->comx), as<double>(t->comy), as<double>(t->comz));
+    c->prof.launches += 2;
     GVS_TRY(check_launch(c, "tree moments"));
     t->n = n;
     t->version = c->pos_version;
@@ -990,13 +1137,10 @@ static gvs_status group_prepare(Ctx *c, Tree *t, int gsize) {
     if (t->grp_version == t->version && t->grp_size == gsize) return GVS_OK;
     const size_t nn = t->nnodes, n = t->n;
     cudaStream_t st = c->stream;
-    GVS_CUDA(c, ensure(c, t->nk, nn * 4));
     GVS_CUDA(c, ensure(c, t->koff, nn * 4));
     GVS_CUDA(c, ensure(c, t->krec, nn * 2 * sizeof(float4)));
     GVS_CUDA(c, ensure(c, t->groups, n * sizeof(int2)));
     GVS_CUDA(c, ensure(c, t->gcount, 16));
-    k_nkids<<<nblk(nn), 256, 0, st>>>(nn, as<uint32_t>(t->cnt), as<uint32_t>(t->skip), as<uint32_t>(t->nk));
-    c->prof.launches += 1;
     GVS_TRY(exclusive_scan_u32(c, as<uint32_t>(t->nk), as<uint32_t>(t->koff), nn, nullptr));
     S2f tab;
     for (int L = 0; L <= MAXL; ++L) {

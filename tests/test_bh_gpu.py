@@ -48,8 +48,21 @@ def lattice(n_side, spacing):
     return p
 
 
+def close_pairs(n=2000, k=40, sep=1e-9):
+    """n Plummer particles plus k copies of the first k moved by sep*(1..k) in x: pairs
+    that share all 21 high key levels and split between depths 22 and 42."""
+    p = G.PlummerSphere(n, seed=4).generate()
+    q = G.Particles(n + k)
+    for f in ("x", "y", "z", "vx", "vy", "vz", "mass"):
+        getattr(q, f)[:n] = getattr(p, f)
+        getattr(q, f)[n:] = getattr(p, f)[:k]
+    q.x[n:] += sep * np.arange(1, k + 1)
+    return q
+
+
 def cases():
     return {
+        "close_pairs": close_pairs(),
         "plummer1000": G.PlummerSphere(1000, seed=42).generate(),
         "plummer20000": G.PlummerSphere(20000, seed=3).generate(),
         "collision4096": G.collision(4096, seed=7),
@@ -211,27 +224,37 @@ def with_duplicates(p, k, at=0):
 
 
 @pytest.mark.parametrize("gsize", [32, 64])
-@pytest.mark.parametrize("case", ["plummer", "buckets"])
+@pytest.mark.parametrize("case", ["plummer", "buckets", "bucket10", "close_pairs"])
 def test_bh_group_walk_theta_zero_is_direct(ctx, gsize, case):
     """theta = 0 opens every node, so the group walk is the f32 all-pairs sum,
-    including the members of bucket leaves (100 coincident particles: a bucket
-    larger than a group, cut into several groups)."""
+    including the members of bucket leaves: 100 coincident particles (a bucket
+    larger than a group, cut into several groups; a run of equal high key words
+    too long for the run sort, built on the full-key path), 10 coincident ones
+    (sorted by the run sort), and pairs split below depth 21."""
     p = G.PlummerSphere(3000, seed=5).generate()
     if case == "buckets":
         p = with_duplicates(p, 99, at=17)
+    elif case == "bucket10":
+        p = with_duplicates(p, 9, at=17)
+    elif case == "close_pairs":
+        p = close_pairs(3000, 40)
     eps = 0.01
     ref = p.copy()
     G.BruteForce(eps, G.PREC_FP64_EXACT, ctx).compute_accelerations(ref)
-    ctx.set_bh_walk(gsize)
     try:
+        ctx.set_bh_walk(0)
+        pp = p.copy()
+        G.BarnesHut(eps, 0.0, G.PREC_FP32, ctx).compute_accelerations(pp)
+        ctx.set_bh_walk(gsize)
         q = p.copy()
         G.BarnesHut(eps, 0.0, G.PREC_FP32, ctx).compute_accelerations(q)
     finally:
         ctx.set_bh_walk(64)
-    err = rel_rms(q.acc(), ref.acc())
-    print(f"group {gsize} {case}: theta=0 vs f64 direct rel RMS {err:.2e}")
-    # f32 terms on absolute f32 positions summed over ~3000 sources
-    assert err <= 5e-6
+    err, err_pp = rel_rms(q.acc(), ref.acc()), rel_rms(pp.acc(), ref.acc())
+    print(f"group {gsize} {case}: theta=0 vs f64 direct rel RMS {err:.2e} (per-particle f32 walk {err_pp:.2e})")
+    # the same f32 terms on absolute f32 positions as the per-particle walk, summed
+    # in another order: the same accuracy
+    assert err <= max(5e-6, 1.5 * err_pp)
 
 
 @pytest.mark.parametrize("theta", [0.5, 0.7])
