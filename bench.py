@@ -438,11 +438,13 @@ def run_workload(a, d):
         ctx.get_state(q)
         rel = np.sqrt((((q.acc()[idx] - ref) ** 2).sum(1) / (ref ** 2).sum(1)).mean())
         # the walk forms side by side on the final state: time and distance to the f64 walk
-        # (fp32: the group walk, the FP32 default; fp32_per_particle: the reference's
+        # (fp32: the group walk at its automatic group size, the FP32 default;
+        # fp32_groupG: G-particle groups; fp32_per_particle: the reference's
         # per-particle test on f32 positions)
         walks = {}
-        for wname, wp, grp in (("fp64", G.PREC_FP64, 64), ("mixed", G.PREC_MIXED, 64), ("fp32", G.PREC_FP32, 64),
-                               ("fp32_per_particle", G.PREC_FP32, 0)):
+        for wname, wp, grp in (("fp64", G.PREC_FP64, -1), ("mixed", G.PREC_MIXED, -1), ("fp32", G.PREC_FP32, -1),
+                               ("fp32_group32", G.PREC_FP32, 32), ("fp32_group64", G.PREC_FP32, 64),
+                               ("fp32_group128", G.PREC_FP32, 128), ("fp32_per_particle", G.PREC_FP32, 0)):
             ctx.set_bh_walk(grp)
             ctx.compute_forces(G.ALGO_BH, wp, eps, theta)  # builds the packed node arrays
             ctx.profile(True)
@@ -454,8 +456,10 @@ def run_workload(a, d):
             walks[wname] = {"walk_ms": pw["force_ms"], "acc": qw.acc()}
             if pw["bh_groups"]:
                 walks[wname].update({"groups": pw["bh_groups"], "groups_walked_per_particle": pw["bh_group_fallbacks"],
-                                     "group_iterations": pw["bh_group_iterations"]})
-        ctx.set_bh_walk(64)
+                                     "group_iterations": pw["bh_group_iterations"],
+                                     "interactions_per_particle": pw["bh_group_interactions"] / n,
+                                     "interactions_per_s": pw["bh_group_interactions"] / (pw["force_ms"] * 1e-3)})
+        ctx.set_bh_walk(-1)
         a64 = walks["fp64"]["acc"]
         for wname in walks:
             aw = walks[wname].pop("acc")

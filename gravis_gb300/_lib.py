@@ -45,7 +45,8 @@ class Profile(C.Structure):
                 ("force_flops", C.c_double), ("force_bytes", C.c_double), ("tile_visits", C.c_double),
                 ("near_tile_visits", C.c_double), ("vjp_ms", C.c_double), ("vjp_launches", C.c_longlong),
                 ("sph_f64_redo", C.c_longlong), ("bh_groups", C.c_longlong),
-                ("bh_group_fallbacks", C.c_longlong), ("bh_group_iterations", C.c_longlong)]
+                ("bh_group_fallbacks", C.c_longlong), ("bh_group_iterations", C.c_longlong),
+                ("bh_group_interactions", C.c_longlong)]
 
 
 _P = C.c_void_p  # every array argument is passed as a raw address

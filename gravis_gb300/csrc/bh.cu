@@ -59,7 +59,7 @@ struct Tree {
     DevBuf mass, comx, comy, comz;   // per node (f64)
     DevBuf boxx, boxy, boxz;         // per node cell centre (f64)
     DevBuf sx, sy, sz, sm;           // sorted particle positions / masses (f64)
-    DevBuf pos32, cm32, cm64, meta, acc;
+    DevBuf pos32, cm32, cm64, meta;
     DevBuf pos32lo, cm32lo;  // mixed walk: f32 lo words of positions and COMs
     // group walk (f32): child-slot records, groups of <= 32*NPL particles, work counter
     DevBuf nk, koff, krec, groups, gcount;
@@ -404,6 +404,23 @@ struct S2Table {
     float lo2[MAXL + 1], hi2[MAXL + 1];
 };
 
+// Where a walk leaves its sums: caller-order acceleration arrays, written (or
+// added to) at perm[i] for sorted particle i.
+struct AccOut {
+    const uint32_t *perm;
+    double *ax, *ay, *az;
+    int accumulate;
+};
+
+__device__ __forceinline__ void store_acc(const AccOut &o, size_t i, double fx, double fy, double fz) {
+    const uint32_t k = o.perm[i];
+    if (o.accumulate) {
+        o.ax[k] += fx; o.ay[k] += fy; o.az[k] += fz;
+    } else {
+        o.ax[k] = fx; o.ay[k] = fy; o.az[k] = fz;
+    }
+}
+
 // BarnesHut::add_force (barnes_hut.rs:114-135), IEEE f64 with no contraction.
 __device__ __forceinline__ void add_force64(double px, double py, double pz, double sx, double sy, double sz,
                                             double m, double eps2, double &ax, double &ay, double &az) {
@@ -457,7 +474,7 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
                                               const float4 *__restrict__ p32, const double *__restrict__ sx,
                                               const double *__restrict__ sy, const double *__restrict__ sz,
                                               const double *__restrict__ sm, const S2Table tab, double theta2,
-                                              double eps2, double *__restrict__ acc, const float4 *__restrict__ cm32lo,
+                                              double eps2, const AccOut out, const float4 *__restrict__ cm32lo,
                                               const float4 *__restrict__ p32lo) {
     constexpr bool F64 = MODE == 0;
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -570,9 +587,7 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
         ay = (double)fa[1] + (double)fa[4];
         az = (double)fa[2] + (double)fa[5];
     }
-    acc[t] = ax;
-    acc[n + t] = ay;
-    acc[2 * n + t] = az;
+    store_acc(out, t, ax, ay, az);
 }
 
 // ---- group walk (FP32) ---------------------------------------------------------
@@ -721,30 +736,35 @@ __device__ __forceinline__ float warp_max(float v) {
 // over a particle pair (NPL 2), scalar f32 for one particle.  GUARD (unsoftened
 // runs) keeps r^2 > 0, so a particle's own leaf adds exactly zero.
 template <int NPL, bool GUARD>
-__device__ __forceinline__ void group_eval(const float4 *__restrict__ il, int cnt, f2 nx, f2 ny, f2 nz, float eps2,
-                                           f2 &ax, f2 &ay, f2 &az) {
-    if constexpr (NPL == 2) {
+__device__ __forceinline__ void group_eval(const float4 *__restrict__ il, int cnt, const f2 *nx, const f2 *ny,
+                                           const f2 *nz, float eps2, f2 *ax, f2 *ay, f2 *az) {
+    if constexpr (NPL >= 2) {
+        constexpr int NP = NPL / 2;  // particle pairs per lane
         const f2 e2 = pk(eps2, eps2);
-#pragma unroll 4
+#pragma unroll (NP == 1 ? 4 : 2)
         for (int k = 0; k < cnt; ++k) {
             const float4 a = il[2 * k], b = il[2 * k + 1];
-            const f2 dx = add2(pk(a.x, a.y), nx), dy = add2(pk(a.z, a.w), ny), dz = add2(pk(b.x, b.y), nz);
-            f2 r2 = fma2(dx, dx, e2);
-            r2 = fma2(dy, dy, r2);
-            r2 = fma2(dz, dz, r2);
-            float ra, rb;
-            upk(r2, ra, rb);
-            if (GUARD) { ra = fmaxf(ra, 1e-24f); rb = fmaxf(rb, 1e-24f); }
-            const f2 ri = pk(rsqrt_approx(ra), rsqrt_approx(rb));
-            const f2 sm = mul2(mul2(pk(b.z, b.w), ri), mul2(ri, ri));
-            ax = fma2(sm, dx, ax);
-            ay = fma2(sm, dy, ay);
-            az = fma2(sm, dz, az);
+            const f2 sx = pk(a.x, a.y), sy = pk(a.z, a.w), sz = pk(b.x, b.y), sm = pk(b.z, b.w);
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                const f2 dx = add2(sx, nx[p]), dy = add2(sy, ny[p]), dz = add2(sz, nz[p]);
+                f2 r2 = fma2(dx, dx, e2);
+                r2 = fma2(dy, dy, r2);
+                r2 = fma2(dz, dz, r2);
+                float ra, rb;
+                upk(r2, ra, rb);
+                if (GUARD) { ra = fmaxf(ra, 1e-24f); rb = fmaxf(rb, 1e-24f); }
+                const f2 ri = pk(rsqrt_approx(ra), rsqrt_approx(rb));
+                const f2 f = mul2(mul2(sm, ri), mul2(ri, ri));
+                ax[p] = fma2(f, dx, ax[p]);
+                ay[p] = fma2(f, dy, ay[p]);
+                az[p] = fma2(f, dz, az[p]);
+            }
         }
     } else {
         float x0, x1, y0, y1, z0, z1, fx, fy, fz, u;
-        upk(nx, x0, x1); upk(ny, y0, y1); upk(nz, z0, z1);
-        upk(ax, fx, u); upk(ay, fy, u); upk(az, fz, u);
+        upk(nx[0], x0, x1); upk(ny[0], y0, y1); upk(nz[0], z0, z1);
+        upk(ax[0], fx, u); upk(ay[0], fy, u); upk(az[0], fz, u);
 #pragma unroll 4
         for (int k = 0; k < cnt; ++k) {
             const float4 a = il[2 * k], b = il[2 * k + 1];
@@ -757,7 +777,7 @@ __device__ __forceinline__ void group_eval(const float4 *__restrict__ il, int cn
             fy = fmaf(sm, dy, fy);
             fz = fmaf(sm, dz, fz);
         }
-        ax = pk(fx, 0.f); ay = pk(fy, 0.f); az = pk(fz, 0.f);
+        ax[0] = pk(fx, 0.f); ay[0] = pk(fy, 0.f); az[0] = pk(fz, 0.f);
     }
 }
 
@@ -811,7 +831,7 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_walk_group(const int2 *__rest
                                                              float eps2f, size_t n, size_t nnodes,
                                                              const int4 *__restrict__ meta,
                                                              const float4 *__restrict__ cm32, const S2Table tab,
-                                                             int budget, double *__restrict__ acc,
+                                                             int budget, const AccOut out,
                                                              unsigned *__restrict__ err) {
     constexpr unsigned FULL = 0xFFFFFFFFu;
     __shared__ GroupSmem smem[GW_WARPS];
@@ -826,10 +846,12 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_walk_group(const int2 *__rest
         g = __shfl_sync(FULL, g, 0);
         if (g >= ngroups) break;
         const int2 gr = groups[g];
-        float px[2], py[2], pz[2];
+        constexpr int NQ = NPL < 2 ? 2 : NPL;  // particle slots per lane (the scalar form pads to a pair)
+        constexpr int NP = NQ / 2;
+        float px[NQ], py[NQ], pz[NQ];
         float lox = INFINITY, loy = INFINITY, loz = INFINITY, hix = -INFINITY, hiy = -INFINITY, hiz = -INFINITY;
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
+        for (int q = 0; q < NQ; ++q) {
             const int k = q * 32 + lane;
             const float4 p = p32[gr.x + (q < NPL && k < gr.y ? k : 0)];
             px[q] = p.x; py[q] = p.y; pz[q] = p.z;
@@ -838,14 +860,21 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_walk_group(const int2 *__rest
         }
         lox = warp_min(lox); loy = warp_min(loy); loz = warp_min(loz);
         hix = warp_max(hix); hiy = warp_max(hiy); hiz = warp_max(hiz);
-        const f2 nx = pk(-px[0], -px[1]), ny = pk(-py[0], -py[1]), nz = pk(-pz[0], -pz[1]);
-        f2 ax = 0ull, ay = 0ull, az = 0ull;
+        f2 nx[NP], ny[NP], nz[NP], ax[NP], ay[NP], az[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            nx[p] = pk(-px[2 * p], -px[2 * p + 1]);
+            ny[p] = pk(-py[2 * p], -py[2 * p + 1]);
+            nz[p] = pk(-pz[2 * p], -pz[2 * p + 1]);
+            ax[p] = ay[p] = az[p] = 0ull;
+        }
         int top = 1, nil = 0;
         if (lane == 0) stack[0] = 0u;  // the root: slot 0, one node
         __syncwarp();
         // a group that needs more than `budget` iterations (its box lies close to much
         // denser matter, which it would open down to the particles) is walked per particle
         int iters = 0;
+        long long terms = 0;  // list entries evaluated (each against every particle of the group)
         bool fallback = false;
         while (top > 0) {
             if (++iters > budget) {
@@ -916,6 +945,7 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_walk_group(const int2 *__rest
                 for (int j0 = 0; j0 < bc; j0 += 32) {
                     if (nil > GW_ICAP - 32) {
                         __syncwarp();
+                        terms += nil;
                         group_eval<NPL, GUARD>(il, nil, nx, ny, nz, eps2f, ax, ay, az);
                         nil = 0;
                         __syncwarp();
@@ -934,16 +964,19 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_walk_group(const int2 *__rest
             }
             __syncwarp();
             if (nil > GW_ICAP - 32) {
+                terms += nil;
                 group_eval<NPL, GUARD>(il, nil, nx, ny, nz, eps2f, ax, ay, az);
                 nil = 0;
                 __syncwarp();
             }
         }
-        float fx[2], fy[2], fz[2];
+        float fx[NQ], fy[NQ], fz[NQ];
         if (lane == 0) {
             atomicAdd(reinterpret_cast<unsigned long long *>(err + 12), (unsigned long long)iters);
             atomicAdd(err + 14, 1u);
             if (fallback) atomicAdd(err + 15, 1u);
+            else atomicAdd(reinterpret_cast<unsigned long long *>(err + 16),
+                           (unsigned long long)(terms + nil) * (unsigned long long)gr.y);
         }
         if (fallback) {
 #pragma unroll
@@ -955,34 +988,19 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_walk_group(const int2 *__rest
             }
         } else {
             if (nil) group_eval<NPL, GUARD>(il, nil, nx, ny, nz, eps2f, ax, ay, az);
-            upk(ax, fx[0], fx[1]);
-            upk(ay, fy[0], fy[1]);
-            upk(az, fz[0], fz[1]);
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                upk(ax[p], fx[2 * p], fx[2 * p + 1]);
+                upk(ay[p], fy[2 * p], fy[2 * p + 1]);
+                upk(az[p], fz[2 * p], fz[2 * p + 1]);
+            }
         }
         __syncwarp();
 #pragma unroll
         for (int q = 0; q < NPL; ++q) {
             const int k = q * 32 + lane;
-            if (k < gr.y) {
-                const size_t i = (size_t)gr.x + k;
-                acc[i] = fx[q];
-                acc[n + i] = fy[q];
-                acc[2 * n + i] = fz[q];
-            }
+            if (k < gr.y) store_acc(out, (size_t)gr.x + k, fx[q], fy[q], fz[q]);
         }
-    }
-}
-
-__global__ void k_scatter_acc(size_t n, const double *__restrict__ acc, const uint32_t *__restrict__ perm,
-                              double *__restrict__ AX, double *__restrict__ AY, double *__restrict__ AZ,
-                              int accumulate) {
-    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    const uint32_t o = perm[s];
-    if (accumulate) {
-        AX[o] += acc[s]; AY[o] += acc[n + s]; AZ[o] += acc[2 * n + s];
-    } else {
-        AX[o] = acc[s]; AY[o] = acc[n + s]; AZ[o] = acc[2 * n + s];
     }
 }
 
@@ -1001,7 +1019,7 @@ void tree_free(Ctx *c) {
     DevBuf *all[] = {&t->bb, &t->bbpart, &t->khi, &t->klo, &t->khi2, &t->klo2, &t->perm, &t->perm2, &t->iota,
                      &t->iota2, &t->delta, &t->nown, &t->off, &t->total, &t->level, &t->first, &t->cnt, &t->skip,
                      &t->mass, &t->comx, &t->comy, &t->comz, &t->boxx, &t->boxy, &t->boxz, &t->sx, &t->sy,
-                     &t->sz, &t->sm, &t->pos32, &t->cm32, &t->cm64, &t->meta, &t->acc, &t->pos32lo, &t->cm32lo, &t->nk, &t->koff, &t->krec,
+                     &t->sz, &t->sm, &t->pos32, &t->cm32, &t->cm64, &t->meta, &t->pos32lo, &t->cm32lo, &t->nk, &t->koff, &t->krec,
                      &t->groups, &t->gcount, &t->parent, &t->arrive};
     for (DevBuf *b : all)
         if (b->ptr) cudaFree(b->ptr);
@@ -1212,10 +1230,14 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
         tab.lo2[L] = lo > 0.0 ? (float)(lo * lo * (1.0 - 0x1p-19)) : -1.0f;
         tab.hi2[L] = (float)(hi * hi * (1.0 + 0x1p-19));
     }
-    GVS_CUDA(c, ensure(c, t->acc, 3 * n * sizeof(double)));
+    const AccOut out{as<uint32_t>(t->perm), as<double>(c->ax), as<double>(c->ay), as<double>(c->az),
+                     accumulate ? 1 : 0};
     // FP32 with a group size set: the group walk (slot records fit 29 bits)
-    const bool group = mode == 1 && c->bh_group > 0 && nnodes < (size_t(1) << 29);
-    if (group) GVS_TRY(group_prepare(c, t, c->bh_group));
+    // (128-particle groups amortise the walk over more particles; below 2^21 particles
+    // they would leave too few groups to fill the GPU)
+    const int gsize = c->bh_group >= 0 ? c->bh_group : (n >= (size_t(1) << 21) ? 128 : 64);
+    const bool group = mode == 1 && gsize > 0 && nnodes < (size_t(1) << 29);
+    if (group) GVS_TRY(group_prepare(c, t, gsize));
     if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], st));
     if (group) {
         GVS_CUDA(c, cudaMemsetAsync(as<uint32_t>(t->gcount) + 1, 0, 4, st));
@@ -1226,27 +1248,28 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
             GVS_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, GW_WARPS * 32, 0));
             kern<<<std::max(1, per_sm) * c->num_sms, GW_WARPS * 32, 0, st>>>(
                 as<int2>(t->groups), as<uint32_t>(t->gcount), as<float4>(t->krec), as<float4>(t->pos32), th2, e2,
-                n, nnodes, as<int4>(t->meta), as<float4>(t->cm32), tab, c->bh_budget, as<double>(t->acc), err_ptr(c));
+                n, nnodes, as<int4>(t->meta), as<float4>(t->cm32), tab, c->bh_budget, out, err_ptr(c));
             return GVS_OK;
         };
-        if (c->bh_group == 64) GVS_TRY(guard ? launch(k_walk_group<2, true>) : launch(k_walk_group<2, false>));
+        if (gsize == 128) GVS_TRY(guard ? launch(k_walk_group<4, true>) : launch(k_walk_group<4, false>));
+        else if (gsize == 64) GVS_TRY(guard ? launch(k_walk_group<2, true>) : launch(k_walk_group<2, false>));
         else GVS_TRY(guard ? launch(k_walk_group<1, true>) : launch(k_walk_group<1, false>));
         c->prof.launches += 2;
     } else if (mode == 0)
         k_walk<0><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, as<int4>(t->meta), nullptr, as<double4>(t->cm64),
                                                 nullptr, as<double>(t->sx), as<double>(t->sy), as<double>(t->sz),
                                                 as<double>(t->sm), tab, theta * theta, eps * eps,
-                                                as<double>(t->acc), nullptr, nullptr);
+                                                out, nullptr, nullptr);
     else if (mode == 1)
         k_walk<1><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, as<int4>(t->meta), as<float4>(t->cm32), nullptr,
                                                 as<float4>(t->pos32), as<double>(t->sx), as<double>(t->sy),
                                                 as<double>(t->sz), as<double>(t->sm), tab, theta * theta, eps * eps,
-                                                as<double>(t->acc), nullptr, nullptr);
+                                                out, nullptr, nullptr);
     else
         k_walk<2><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, as<int4>(t->meta), as<float4>(t->cm32),
                                                 as<double4>(t->cm64), as<float4>(t->pos32), as<double>(t->sx),
                                                 as<double>(t->sy), as<double>(t->sz), as<double>(t->sm), tab,
-                                                theta * theta, eps * eps, as<double>(t->acc),
+                                                theta * theta, eps * eps, out,
                                                 as<float4>(t->cm32lo), as<float4>(t->pos32lo));
     c->prof.launches += 1;
     GVS_TRY(check_launch(c, "tree walk"));
@@ -1258,10 +1281,7 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
         c->prof.force_ms += ms;
         c->prof.force_launches += 1;
     }
-    k_scatter_acc<<<nblk(n), 256, 0, st>>>(n, as<double>(t->acc), as<uint32_t>(t->perm), as<double>(c->ax),
-                                           as<double>(c->ay), as<double>(c->az), accumulate ? 1 : 0);
-    c->prof.launches += 1;
-    return check_launch(c, "tree scatter");
+    return GVS_OK;
 }
 
 // ---- accessors used by the SPH neighbour search and the tests ------------------

@@ -557,8 +557,9 @@ gvs_status gvs_set_direct_shape(gvs_ctx *c, int nthreads, int ipt, int min_block
 
 gvs_status gvs_set_bh_walk(gvs_ctx *c, int group_size, int budget) {
     GVS_TRY(check_ctx(c));
-    if (group_size != 0 && group_size != 32 && group_size != 64)
-        return fail(c, GVS_ERR_INVALID_ARG, "BH walk group size must be 0 (per-particle), 32 or 64, got %d",
+    if (group_size != -1 && group_size != 0 && group_size != 32 && group_size != 64 && group_size != 128)
+        return fail(c, GVS_ERR_INVALID_ARG,
+                    "BH walk group size must be -1 (automatic), 0 (per-particle), 32, 64 or 128, got %d",
                     group_size);
     if (budget < 0) return fail(c, GVS_ERR_INVALID_ARG, "BH group-walk budget must be >= 0, got %d", budget);
     c->bh_group = group_size;
@@ -667,7 +668,7 @@ gvs_status gvs_profile_enable(gvs_ctx *c, int on) {
     c->prof.tile_visits = 0.0;
     c->prof.vjp_ms = 0.0;
     c->prof.vjp_launches = 0;
-    GVS_CUDA(c, cudaMemsetAsync(err_ptr(c) + 8, 0, 8 * sizeof(unsigned), c->stream));
+    GVS_CUDA(c, cudaMemsetAsync(err_ptr(c) + 8, 0, 10 * sizeof(unsigned), c->stream));
     return GVS_OK;
 }
 
@@ -694,6 +695,9 @@ gvs_status gvs_profile_read(gvs_ctx *c, gvs_profile *out) {
     out->bh_group_iterations = (long long)((unsigned long long)words[0] | ((unsigned long long)words[1] << 32));
     out->bh_groups = words[2];
     out->bh_group_fallbacks = words[3];
+    unsigned long long pairs = 0;
+    GVS_CUDA(c, cudaMemcpy(&pairs, err_ptr(c) + 16, sizeof pairs, cudaMemcpyDeviceToHost));
+    out->bh_group_interactions = (long long)pairs;
     return GVS_OK;
 }
 

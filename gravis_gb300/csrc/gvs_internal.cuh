@@ -97,7 +97,8 @@ struct Ctx {
 
     Prof prof;
     Tune tune;
-    int bh_group = 64;    // FP32 Barnes-Hut: particles per walk group (32, 64), 0 = per-particle walk
+    int bh_group = -1;    // FP32 Barnes-Hut: particles per walk group (32, 64, 128), 0 = per-particle
+                          // walk, -1 = 128 from 2^21 particles, else 64
     int bh_budget = 1024; // group-walk iterations before a group is walked per particle
     unsigned long long alloc_gen = 0;  // bumped whenever ensure() (re)allocates a buffer
 

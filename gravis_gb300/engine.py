@@ -232,9 +232,10 @@ class Context:
         self._ck(self._lib.gvs_set_direct_shape(self.h, nthreads, ipt, min_blocks, unroll))
 
     def set_bh_walk(self, group_size: int, budget: int = 0):
-        """FP32 Barnes-Hut walk: 64 or 32 particles per warp group (a refinement of each
-        particle's Barnes-Hut sum), or 0 for the per-particle walk.  Groups whose walk
-        exceeds `budget` iterations (0: 1024) are walked per particle."""
+        """FP32 Barnes-Hut walk: 32, 64 or 128 particles per warp group (a refinement of
+        each particle's Barnes-Hut sum), -1 for the automatic size (128 from 2^21
+        particles, else 64), or 0 for the per-particle walk.  Groups whose walk exceeds
+        `budget` iterations (0: 1024) are walked per particle."""
         self._ck(self._lib.gvs_set_bh_walk(self.h, group_size, budget))
 
     def autotune_report(self) -> list:
@@ -271,7 +272,8 @@ class Context:
                 "force_flops": pr.force_flops, "force_bytes": pr.force_bytes, "tile_visits": pr.tile_visits,
                 "near_tile_visits": pr.near_tile_visits, "vjp_ms": pr.vjp_ms, "vjp_launches": pr.vjp_launches,
                 "sph_f64_redo": pr.sph_f64_redo, "bh_groups": pr.bh_groups,
-                "bh_group_fallbacks": pr.bh_group_fallbacks, "bh_group_iterations": pr.bh_group_iterations}
+                "bh_group_fallbacks": pr.bh_group_fallbacks, "bh_group_iterations": pr.bh_group_iterations,
+                "bh_group_interactions": pr.bh_group_interactions}
 
     def event(self, slot: int):
         self._ck(self._lib.gvs_event_record(self.h, slot))

@@ -94,6 +94,8 @@ typedef struct gvs_profile {
     long long bh_groups;           /* FP32 Barnes-Hut group walk: groups walked */
     long long bh_group_fallbacks;  /* of which were walked per particle (over the iteration budget) */
     long long bh_group_iterations; /* group-walk iterations (32 nodes each) */
+    long long bh_group_interactions; /* particle-node (or particle-particle) terms the group walk
+                                        evaluated for real particles (fallback groups excluded) */
 } gvs_profile;
 
 /* ---- library / context ---------------------------------------------------- */
@@ -264,15 +266,16 @@ gvs_status gvs_autotune_direct(gvs_ctx *ctx, int precision, double softening, in
  * needs tiles that are small against the system); the autotuner skips such shapes. */
 gvs_status gvs_set_direct_shape(gvs_ctx *ctx, int nthreads, int ipt, int min_blocks, int unroll);
 /* Walk of the FP32 Barnes-Hut (gvs_gravity_bh / ALGO_BH with GVS_PREC_FP32).
- * group_size 64 (default) or 32: one warp walks the tree for a group of up to that
- * many particles sharing a tree cell, opening a node unless s^2 < theta^2 d^2 with d
- * the distance from its COM to the group's bounding box.  Every particle then sums a
+ * group_size 32, 64 or 128: one warp walks the tree for a group of up to that many
+ * particles sharing a tree cell, opening a node unless s^2 < theta^2 d^2 with d the
+ * distance from its COM to the group's bounding box.  Every particle then sums a
  * refinement of its own Barnes-Hut node set (the reference's test accepts every node
- * the group accepts).  0: the per-particle walk with the reference's test on f32
- * positions.  FP64 and MIXED walks are always per-particle.  A group whose walk takes
- * more than `budget` iterations (32 nodes each; 0 = the default 1024) is walked per
- * particle instead: its box lies close to much denser matter, which the group test
- * would open down to single particles. */
+ * the group accepts).  -1 (default): 128 from 2^21 particles, else 64.  0: the
+ * per-particle walk with the reference's test on f32 positions.  FP64 and MIXED walks
+ * are always per-particle.  A group whose walk takes more than `budget` iterations
+ * (32 nodes each; 0 = the default 1024) is walked per particle instead: its box lies
+ * close to much denser matter, which the group test would open down to single
+ * particles. */
 gvs_status gvs_set_bh_walk(gvs_ctx *ctx, int group_size, int budget);
 /* Every candidate of the last gvs_autotune_direct with its kernel time (ms per force
  * evaluation).  Always sets *count; fills the arrays (any may be NULL) if cap >= *count.

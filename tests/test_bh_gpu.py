@@ -158,7 +158,7 @@ def test_bh_f32_walk(ctx, theta):
     try:
         G.BarnesHut(eps, theta, G.PREC_FP32, ctx).compute_accelerations(a32)
     finally:
-        ctx.set_bh_walk(64)
+        ctx.set_bh_walk(-1)
     err = rel_rms(a32.acc(), a64.acc())
     print(f"theta={theta} f32 walk vs f64 walk rel RMS {err:.2e}")
     # f32 absolute positions at |x| ~ 10 resolve separations to ~1e-6; the bound
@@ -223,7 +223,7 @@ def with_duplicates(p, k, at=0):
     return q
 
 
-@pytest.mark.parametrize("gsize", [32, 64])
+@pytest.mark.parametrize("gsize", [32, 64, 128])
 @pytest.mark.parametrize("case", ["plummer", "buckets", "bucket10", "close_pairs"])
 def test_bh_group_walk_theta_zero_is_direct(ctx, gsize, case):
     """theta = 0 opens every node, so the group walk is the f32 all-pairs sum,
@@ -249,7 +249,7 @@ def test_bh_group_walk_theta_zero_is_direct(ctx, gsize, case):
         q = p.copy()
         G.BarnesHut(eps, 0.0, G.PREC_FP32, ctx).compute_accelerations(q)
     finally:
-        ctx.set_bh_walk(64)
+        ctx.set_bh_walk(-1)
     err, err_pp = rel_rms(q.acc(), ref.acc()), rel_rms(pp.acc(), ref.acc())
     print(f"group {gsize} {case}: theta=0 vs f64 direct rel RMS {err:.2e} (per-particle f32 walk {err_pp:.2e})")
     # the same f32 terms on absolute f32 positions as the per-particle walk, summed
@@ -270,15 +270,15 @@ def test_bh_group_walk_refines_per_particle(ctx, theta):
     ref = ctx.direct_subset(idx, eps)
     errs = {}
     try:
-        for g in (0, 32, 64):
+        for g in (0, 32, 64, 128):
             ctx.set_bh_walk(g)
             q = p.copy()
             G.BarnesHut(eps, theta, G.PREC_FP32, ctx).compute_accelerations(q)
             errs[g] = float(np.sqrt((((q.acc()[idx] - ref) ** 2).sum(1) / (ref ** 2).sum(1)).mean()))
     finally:
-        ctx.set_bh_walk(64)
+        ctx.set_bh_walk(-1)
     print(f"theta={theta} per-particle RMS vs f64 direct: " + ", ".join(f"{k}: {v:.3e}" for k, v in errs.items()))
-    assert errs[32] <= errs[0] and errs[64] <= errs[0]
+    assert errs[32] <= errs[0] and errs[64] <= errs[0] and errs[128] <= errs[0]
 
 
 def test_bh_group_walk_unsoftened(ctx):
@@ -309,7 +309,7 @@ def test_bh_group_walk_fallback_is_per_particle_walk(ctx):
         pr = ctx.profile_read()
         ctx.profile(False)
     finally:
-        ctx.set_bh_walk(64)
+        ctx.set_bh_walk(-1)
     assert pr["bh_groups"] > 0 and pr["bh_group_fallbacks"] == pr["bh_groups"]
     assert np.array_equal(a.acc(), b.acc())
 
