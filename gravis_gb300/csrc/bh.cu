@@ -65,6 +65,7 @@ struct Tree {
     DevBuf nk, koff, krec, groups, gcount;
     DevBuf parent, arrive;  // per node: parent index, children that finished their moments
     unsigned long long grp_version = ~0ull;
+    unsigned long long centres_version = ~0ull;  // tree version the cell centres were built for
     int grp_size = 0;
     int walk_blocks = 0;  // resident blocks of the group walk (per GPU)
 };
@@ -241,38 +242,19 @@ __global__ void k_nown(const int *__restrict__ delta, size_t n, uint32_t *__rest
     nown[i] = b >= a ? (uint32_t)(b - a + 1) : 0u;
 }
 
-// One thread per particle: writes the nodes it starts.
+// One thread per particle: writes the nodes it starts (integer work only).
 __global__ void k_nodes(const uint64_t *__restrict__ khi, const uint64_t *__restrict__ klo,
                         const int *__restrict__ delta, const uint32_t *__restrict__ off, size_t n,
-                        const double *__restrict__ bb, uint8_t *__restrict__ level, uint32_t *__restrict__ first,
-                        uint32_t *__restrict__ cnt, uint32_t *__restrict__ skip, double *__restrict__ bx,
-                        double *__restrict__ by, double *__restrict__ bz) {
+                        uint8_t *__restrict__ level, uint32_t *__restrict__ first, uint32_t *__restrict__ cnt,
+                        uint32_t *__restrict__ skip) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int a = delta[i] + 1;
     const int b = min(max(delta[i], delta[i + 1]) + 1, MAXL);
     if (b < a) return;
     const uint64_t hi = khi[i], lo = klo[i];
-    double cx = bb[6], cy = bb[7], cz = bb[8], hw = bb[9];
-    const bool fin = isfinite(hw);
-    for (int L = 1; L < a; ++L) {  // descend to depth a
-        const int oct = octant_at(hi, lo, L);
-        const double q = half_of(hw, fin);
-        cx = __dadd_rn(cx, (oct & 1) ? q : -q);
-        cy = __dadd_rn(cy, (oct & 2) ? q : -q);
-        cz = __dadd_rn(cz, (oct & 4) ? q : -q);
-        hw = q;
-    }
     const uint32_t base = off[i];
     for (int L = a; L <= b; ++L) {
-        if (L >= 1) {
-            const int oct = octant_at(hi, lo, L);
-            const double q = half_of(hw, fin);
-            cx = __dadd_rn(cx, (oct & 1) ? q : -q);
-            cy = __dadd_rn(cy, (oct & 2) ? q : -q);
-            cz = __dadd_rn(cz, (oct & 4) ? q : -q);
-            hw = q;
-        }
         // end of the depth-L cell of particle i
         size_t e;
         if (delta[i + 1] < L) {
@@ -292,7 +274,39 @@ __global__ void k_nodes(const uint64_t *__restrict__ khi, const uint64_t *__rest
         first[idx] = (uint32_t)i;
         cnt[idx] = leaf ? (uint32_t)(e - i) : 0u;
         skip[idx] = off[e];
-        bx[idx] = cx; by[idx] = cy; bz[idx] = cz;
+    }
+}
+
+// Cell centres of the nodes particle i starts (child_bounds, octree.rs:52-64):
+// the reference's f64 halving replayed down the particle's key.  Only the SPH
+// neighbour search reads them, so they are built on its first request.
+__global__ void k_centres(const uint64_t *__restrict__ khi, const uint64_t *__restrict__ klo,
+                          const int *__restrict__ delta, const uint32_t *__restrict__ off, size_t n,
+                          const double *__restrict__ bb, double *__restrict__ bx, double *__restrict__ by,
+                          double *__restrict__ bz) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int a = delta[i] + 1;
+    const int b = min(max(delta[i], delta[i + 1]) + 1, MAXL);
+    if (b < a) return;
+    const uint64_t hi = khi[i], lo = klo[i];
+    double cx = bb[6], cy = bb[7], cz = bb[8], hw = bb[9];
+    const bool fin = isfinite(hw);
+    const uint32_t base = off[i];
+    for (int L = 1; L <= b; ++L) {
+        const int oct = octant_at(hi, lo, L);
+        const double q = half_of(hw, fin);
+        cx = __dadd_rn(cx, (oct & 1) ? q : -q);
+        cy = __dadd_rn(cy, (oct & 2) ? q : -q);
+        cz = __dadd_rn(cz, (oct & 4) ? q : -q);
+        hw = q;
+        if (L >= a) {
+            const uint32_t idx = base + (uint32_t)(L - a);
+            bx[idx] = cx; by[idx] = cy; bz[idx] = cz;
+        }
+    }
+    if (a == 0) {  // the root
+        bx[base] = bb[6]; by[base] = bb[7]; bz[base] = bb[8];
     }
 }
 
@@ -1116,12 +1130,8 @@ gvs_status tree_build(Ctx *c) {
     GVS_CUDA(c, ensure(c, t->skip, nnodes * 4));
     GVS_CUDA(c, ensure(c, t->mass, nnodes * 8)); GVS_CUDA(c, ensure(c, t->comx, nnodes * 8));
     GVS_CUDA(c, ensure(c, t->comy, nnodes * 8)); GVS_CUDA(c, ensure(c, t->comz, nnodes * 8));
-    GVS_CUDA(c, ensure(c, t->boxx, nnodes * 8)); GVS_CUDA(c, ensure(c, t->boxy, nnodes * 8));
-    GVS_CUDA(c, ensure(c, t->boxz, nnodes * 8));
-    k_nodes<<<nblk(n), 256, 0, st>>>(KH, KL, as<int>(t->delta), as<uint32_t>(t->off), n, as<double>(t->bb),
-                                     as<uint8_t>(t->level), as<uint32_t>(t->first), as<uint32_t>(t->cnt),
-                                     as<uint32_t>(t->skip), as<double>(t->boxx), as<double>(t->boxy),
-                                     as<double>(t->boxz));
+    k_nodes<<<nblk(n), 256, 0, st>>>(KH, KL, as<int>(t->delta), as<uint32_t>(t->off), n, as<uint8_t>(t->level),
+                                     as<uint32_t>(t->first), as<uint32_t>(t->cnt), as<uint32_t>(t->skip));
     // sorted particle data
     GVS_CUDA(c, ensure(c, t->sx, b8)); GVS_CUDA(c, ensure(c, t->sy, b8));
     GVS_CUDA(c, ensure(c, t->sz, b8)); GVS_CUDA(c, ensure(c, t->sm, b8));
@@ -1295,6 +1305,18 @@ gvs_status tree_view(Ctx *c, TreeView *v) {
     v->cnt = as<uint32_t>(t->cnt);
     v->skip = as<uint32_t>(t->skip);
     v->perm = as<uint32_t>(t->perm);
+    if (t->centres_version != t->version) {
+        const size_t nn = t->nnodes, n = t->n;
+        GVS_CUDA(c, ensure(c, t->boxx, nn * 8));
+        GVS_CUDA(c, ensure(c, t->boxy, nn * 8));
+        GVS_CUDA(c, ensure(c, t->boxz, nn * 8));
+        k_centres<<<nblk(n), 256, 0, c->stream>>>(as<uint64_t>(t->khi), as<uint64_t>(t->klo), as<int>(t->delta),
+                                                  as<uint32_t>(t->off), n, as<double>(t->bb), as<double>(t->boxx),
+                                                  as<double>(t->boxy), as<double>(t->boxz));
+        c->prof.launches += 1;
+        GVS_TRY(check_launch(c, "cell centres"));
+        t->centres_version = t->version;
+    }
     v->bx = as<double>(t->boxx);
     v->by = as<double>(t->boxy);
     v->bz = as<double>(t->boxz);
