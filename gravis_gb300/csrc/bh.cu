@@ -92,6 +92,7 @@ __device__ __forceinline__ int octant_at(uint64_t hi, uint64_t lo, int L) {  // 
 }
 
 // Root cube: BoundingBox::containing (octree.rs:29-43), f64 without contraction.
+// bb[10], bb[11]: the fixed-point frame of the keys' fast path (see k_keys).
 __global__ void k_root(double *bb) {
     if (threadIdx.x || blockIdx.x) return;
     double c[3];
@@ -99,6 +100,16 @@ __global__ void k_root(double *bb) {
     double e = fmax(fmax(__dsub_rn(bb[3], bb[0]), __dsub_rn(bb[4], bb[1])), __dsub_rn(bb[5], bb[2]));
     double hw = __dadd_rn(__dmul_rn(__dmul_rn(0.5, e), 1.001), 1e-10);
     bb[6] = c[0]; bb[7] = c[1]; bb[8] = c[2]; bb[9] = hw;
+    // V = (x - c)/(2 hw) + 1/2 in [0, 1): its binary digits are the octant tests
+    // against the exact cell planes.  margin (units of 2^-62 of V) bounds the
+    // f64 error of V (~2^-51) plus the drift of the reference's rounded centres
+    // from the exact planes (<= 21 half-ulps of X = max|c| + hw), doubled; 0
+    // disables the fast path.
+    const double X = fmax(fabs(c[0]), fmax(fabs(c[1]), fabs(c[2]))) + hw;
+    const double ratio = X / hw;
+    const bool ok = isfinite(hw) && hw > 0.0 && isfinite(X) && ratio < 1e6;
+    bb[10] = ok ? 1.0 / (2.0 * hw) : 0.0;
+    bb[11] = ok ? 8192.0 + 65536.0 * ceil(ratio) : 0.0;
 }
 
 // hw * 0.5 for the cell half widths: exact for normal hw (a root half width is
@@ -149,6 +160,49 @@ __device__ __forceinline__ void octant_path(double x, double y, double z, const 
     }
 }
 
+// The high key word on the integer pipe.  The reference's centres c~_L are f64
+// sums that drift from the exact planes c_L = c + hw * sum(+-2^-k) by at most 21
+// half-ulps of X; a coordinate farther than that from every plane it is tested
+// against gets the same octant from the exact plane, which is one bit of its
+// fixed-point position V.  Returns false (the caller replays the f64 path) if
+// any tested plane lies within the certified margin, or for NaN / out-of-box
+// input.
+__device__ __forceinline__ bool fast_hi(double x, double y, double z, const double *__restrict__ bb,
+                                        uint64_t &hi) {
+    const double inv = bb[10];
+    if (inv == 0.0) return false;
+    const unsigned long long margin = (unsigned long long)bb[11];
+    const double p[3] = {x, y, z}, c[3] = {bb[6], bb[7], bb[8]};
+    unsigned long long W[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double v = __dadd_rn(__dmul_rn(__dsub_rn(p[d], c[d]), inv), 0.5);
+        // v in (0, 1) and W = floor(v 2^62), from the bit pattern (NaN and v <= 0 fail)
+        const long long b = __double_as_longlong(v);
+        if (!(b > 0 && b < 0x3FF0000000000000ll)) return false;
+        const int sh = (int)((b >> 52) & 0x7FF) - 1023 + 10;  // exponent e in [-1022, -1]: v 2^62 = m 2^(e + 10)
+        const unsigned long long m = ((unsigned long long)b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+        W[d] = sh >= 0 ? m << sh : (sh > -64 ? m >> -sh : 0ull);
+    }
+    uint64_t h = 0;
+    bool ok = true;
+#pragma unroll
+    for (int L = 1; L <= 21; ++L) {
+        const unsigned long long half = 1ull << (62 - L), mask = (half << 1) - 1ull;
+        int oct = 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const unsigned long long r = W[d] & mask;
+            const unsigned long long dist = r >= half ? r - half : half - r;
+            ok = ok && dist > margin;
+            oct |= (int)((W[d] >> (62 - L)) & 1ull) << d;
+        }
+        h = (h << 3) | (uint64_t)oct;
+    }
+    hi = h;
+    return ok;
+}
+
 // Keys, levels 1..LMAX (42: both words; 21: the high word, lo = 0).
 template <int LMAX>
 __global__ void k_keys(const double *__restrict__ X, const double *__restrict__ Y, const double *__restrict__ Z,
@@ -156,8 +210,8 @@ __global__ void k_keys(const double *__restrict__ X, const double *__restrict__ 
                        uint64_t *__restrict__ klo, uint32_t *__restrict__ perm) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    uint64_t hi, lo;
-    octant_path<LMAX>(X[i], Y[i], Z[i], bb, hi, lo);
+    uint64_t hi, lo = 0;
+    if (LMAX != 21 || !fast_hi(X[i], Y[i], Z[i], bb, hi)) octant_path<LMAX>(X[i], Y[i], Z[i], bb, hi, lo);
     khi[i] = hi;
     if (klo) klo[i] = lo;
     perm[i] = (uint32_t)i;
