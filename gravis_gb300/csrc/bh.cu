@@ -26,7 +26,9 @@
 //  4. Moments: mass and centre of mass in f64, bottom-up in one pass (the
 //     last child to finish sums its parent's children in child order, so
 //     results are deterministic); the centre is the mass-weighted sum times
-//     the f64 reciprocal of the mass.
+//     the f64 reciprocal of the mass.  Built when the f64 or mixed walk (or
+//     the export) first needs them; the FP32 walk sums f32 moments instead,
+//     as offsets from each node's first particle.
 //     The reference updates the COM incrementally in insertion order; the
 //     two agree to a few ulps.
 //  5. Walk: the reference's per-particle stack walk (barnes_hut.rs:44-108):
@@ -66,6 +68,8 @@ struct Tree {
     DevBuf parent, arrive;  // per node: parent index, children that finished their moments
     unsigned long long grp_version = ~0ull;
     unsigned long long centres_version = ~0ull;  // tree version the cell centres were built for
+    unsigned long long m64_version = ~0ull;      // ... the f64 moments were built for
+    DevBuf mo32;                                  // FP32 walk: per node (offset from first particle, mass)
     int grp_size = 0;
     int walk_blocks = 0;  // resident blocks of the group walk (per GPU)
 };
@@ -436,6 +440,56 @@ __global__ void k_moments_up(size_t nnodes, const uint32_t *__restrict__ first, 
     }
 }
 
+// FP32-walk moments: mass and centre of mass in f32 on the FMA pipe, bottom-up
+// like k_moments_up.  Each node's centre is kept as an offset from its first
+// particle (f32), so the sums see differences of the size of the cell, not of the
+// coordinates: mo[k] = (offset, mass), cm32[k] = (first particle + offset, mass).
+// A one-particle leaf's record is that particle's f32 position and mass exactly.
+__global__ void k_moments32_up(size_t nnodes, const uint32_t *__restrict__ first, const uint32_t *__restrict__ cnt,
+                               const uint32_t *__restrict__ skip, const uint32_t *__restrict__ parent,
+                               const uint32_t *__restrict__ nk, uint32_t *__restrict__ arrive,
+                               const float4 *__restrict__ p32, float4 *mo, float4 *__restrict__ cm32) {
+    const size_t k0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k0 >= nnodes) return;
+    const uint32_t c0 = cnt[k0];
+    if (c0 == 0) return;
+    uint32_t k = (uint32_t)k0;
+    float4 r = p32[first[k]];
+    float M = 0.f, X = 0.f, Yv = 0.f, Zv = 0.f;
+    if (c0 == 1) {
+        M = r.w;
+    } else {  // bucket leaf: members in order
+        for (uint32_t p = first[k]; p < first[k] + c0; ++p) {
+            const float4 q = p32[p];
+            M += q.w;
+            X = fmaf(q.w, q.x - r.x, X); Yv = fmaf(q.w, q.y - r.y, Yv); Zv = fmaf(q.w, q.z - r.z, Zv);
+        }
+    }
+    for (;;) {
+        const float inv = M > 0.f ? 1.0f / M : 0.f;
+        const float ox = X * inv, oy = Yv * inv, oz = Zv * inv;
+        mo[k] = make_float4(ox, oy, oz, M);
+        cm32[k] = make_float4(r.x + ox, r.y + oy, r.z + oz, M);
+        const uint32_t up = parent[k];
+        if (up == 0xFFFFFFFFu) return;
+        __threadfence();
+        if (atomicAdd(arrive + up, 1u) != nk[up] - 1u) return;
+        __threadfence();
+        k = up;
+        r = p32[first[k]];
+        M = 0.f; X = 0.f; Yv = 0.f; Zv = 0.f;
+        const uint32_t end = skip[k];
+        for (uint32_t ch = k + 1; ch < end; ch = skip[ch]) {
+            const float4 q = __ldcg(mo + ch);
+            const float4 rc = p32[first[ch]];
+            M += q.w;
+            X = fmaf(q.w, (rc.x - r.x) + q.x, X);
+            Yv = fmaf(q.w, (rc.y - r.y) + q.y, Yv);
+            Zv = fmaf(q.w, (rc.z - r.z) + q.z, Zv);
+        }
+    }
+}
+
 __global__ void k_pack_nodes(size_t nnodes, const uint8_t *__restrict__ level, const uint32_t *__restrict__ first,
                              const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ skip,
                              const double *__restrict__ mass, const double *__restrict__ cx,
@@ -704,10 +758,9 @@ struct S2f {
 __device__ __forceinline__ void write_rec(float4 *__restrict__ krec, uint32_t slot, uint32_t x,
                                           const uint8_t *__restrict__ level, const uint32_t *__restrict__ first,
                                           const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ nk,
-                                          const uint32_t *__restrict__ koff, const double *__restrict__ mass,
-                                          const double *__restrict__ cx, const double *__restrict__ cy,
-                                          const double *__restrict__ cz, const S2f &tab) {
-    krec[2 * (size_t)slot] = make_float4((float)cx[x], (float)cy[x], (float)cz[x], (float)mass[x]);
+                                          const uint32_t *__restrict__ koff, const float4 *__restrict__ cm32,
+                                          const S2f &tab) {
+    krec[2 * (size_t)slot] = cm32[x];
     const uint32_t c = cnt[x];
     int4 b;
     if (c == 0) b = make_int4((int)(1u + koff[x]), (int)nk[x], 0, __float_as_int(tab.s2[level[x]]));
@@ -721,16 +774,15 @@ __device__ __forceinline__ void write_rec(float4 *__restrict__ krec, uint32_t sl
 __global__ void k_krec(size_t nnodes, const uint8_t *__restrict__ level, const uint32_t *__restrict__ first,
                        const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ skip,
                        const uint32_t *__restrict__ nk, const uint32_t *__restrict__ koff,
-                       const double *__restrict__ mass, const double *__restrict__ cx, const double *__restrict__ cy,
-                       const double *__restrict__ cz, const S2f tab, float4 *__restrict__ krec) {
+                       const float4 *__restrict__ cm32, const S2f tab, float4 *__restrict__ krec) {
     const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nnodes) return;
-    if (k == 0) write_rec(krec, 0, 0, level, first, cnt, nk, koff, mass, cx, cy, cz, tab);
+    if (k == 0) write_rec(krec, 0, 0, level, first, cnt, nk, koff, cm32, tab);
     if (cnt[k] != 0) return;
     const uint32_t end = skip[k];
     uint32_t slot = 1u + koff[k];
     for (uint32_t ch = (uint32_t)k + 1; ch < end; ch = skip[ch], ++slot)
-        write_rec(krec, slot, ch, level, first, cnt, nk, koff, mass, cx, cy, cz, tab);
+        write_rec(krec, slot, ch, level, first, cnt, nk, koff, cm32, tab);
 }
 
 // Groups: a node with more than G particles emits its children's particle
@@ -1088,7 +1140,7 @@ void tree_free(Ctx *c) {
                      &t->iota2, &t->delta, &t->nown, &t->off, &t->total, &t->level, &t->first, &t->cnt, &t->skip,
                      &t->mass, &t->comx, &t->comy, &t->comz, &t->boxx, &t->boxy, &t->boxz, &t->sx, &t->sy,
                      &t->sz, &t->sm, &t->pos32, &t->cm32, &t->cm64, &t->meta, &t->pos32lo, &t->cm32lo, &t->nk, &t->koff, &t->krec,
-                     &t->groups, &t->gcount, &t->parent, &t->arrive};
+                     &t->groups, &t->gcount, &t->parent, &t->arrive, &t->mo32};
     for (DevBuf *b : all)
         if (b->ptr) cudaFree(b->ptr);
     delete t;
@@ -1182,8 +1234,6 @@ gvs_status tree_build(Ctx *c) {
     GVS_CUDA(c, ensure(c, t->level, nnodes));
     GVS_CUDA(c, ensure(c, t->first, nnodes * 4)); GVS_CUDA(c, ensure(c, t->cnt, nnodes * 4));
     GVS_CUDA(c, ensure(c, t->skip, nnodes * 4));
-    GVS_CUDA(c, ensure(c, t->mass, nnodes * 8)); GVS_CUDA(c, ensure(c, t->comx, nnodes * 8));
-    GVS_CUDA(c, ensure(c, t->comy, nnodes * 8)); GVS_CUDA(c, ensure(c, t->comz, nnodes * 8));
     k_nodes<<<nblk(n), 256, 0, st>>>(KH, KL, as<int>(t->delta), as<uint32_t>(t->off), n, as<uint8_t>(t->level),
                                      as<uint32_t>(t->first), as<uint32_t>(t->cnt), as<uint32_t>(t->skip));
     // sorted particle data
@@ -1200,17 +1250,31 @@ gvs_status tree_build(Ctx *c) {
     GVS_CUDA(c, ensure(c, t->arrive, nnodes * 4));
     k_links<<<nblk(nnodes), 256, 0, st>>>(nnodes, as<uint32_t>(t->cnt), as<uint32_t>(t->skip),
                                           as<uint32_t>(t->parent), as<uint32_t>(t->nk));
+    c->prof.launches += 1;
+    GVS_TRY(check_launch(c, "tree links"));
+    t->n = n;
+    t->version = c->pos_version;
+    t->precision = -1;
+    return GVS_OK;
+}
+
+// The f64 moments (mass, centre of mass) of the current tree, on first request:
+// the f64 and mixed walks and the tree export read them; the FP32 walk has its own.
+static gvs_status tree_moments64(Ctx *c, Tree *t) {
+    if (t->m64_version == t->version) return GVS_OK;
+    const size_t nnodes = t->nnodes;
+    cudaStream_t st = c->stream;
+    GVS_CUDA(c, ensure(c, t->mass, nnodes * 8)); GVS_CUDA(c, ensure(c, t->comx, nnodes * 8));
+    GVS_CUDA(c, ensure(c, t->comy, nnodes * 8)); GVS_CUDA(c, ensure(c, t->comz, nnodes * 8));
     GVS_CUDA(c, cudaMemsetAsync(t->arrive.ptr, 0, nnodes * 4, st));
     k_moments_up<<<nblk(nnodes), 256, 0, st>>>(nnodes, as<uint32_t>(t->first), as<uint32_t>(t->cnt),
                                                as<uint32_t>(t->skip), as<uint32_t>(t->parent), as<uint32_t>(t->nk),
                                                as<uint32_t>(t->arrive), as<double>(t->sx), as<double>(t->sy),
                                                as<double>(t->sz), as<double>(t->sm), as<double>(t->mass),
                                                as<double>(t->comx), as<double>(t->comy), as<double>(t->comz));
-    c->prof.launches += 2;
+    c->prof.launches += 1;
     GVS_TRY(check_launch(c, "tree moments"));
-    t->n = n;
-    t->version = c->pos_version;
-    t->precision = -1;
+    t->m64_version = t->version;
     return GVS_OK;
 }
 
@@ -1231,8 +1295,7 @@ static gvs_status group_prepare(Ctx *c, Tree *t, int gsize) {
     }
     k_krec<<<nblk(nn), 256, 0, st>>>(nn, as<uint8_t>(t->level), as<uint32_t>(t->first), as<uint32_t>(t->cnt),
                                      as<uint32_t>(t->skip), as<uint32_t>(t->nk), as<uint32_t>(t->koff),
-                                     as<double>(t->mass), as<double>(t->comx), as<double>(t->comy),
-                                     as<double>(t->comz), tab, as<float4>(t->krec));
+                                     as<float4>(t->cm32), tab, as<float4>(t->krec));
     GVS_CUDA(c, cudaMemsetAsync(t->gcount.ptr, 0, 8, st));
     k_groups<<<nblk(nn), 256, 0, st>>>(nn, n, (uint32_t)gsize, as<uint8_t>(t->level), as<uint32_t>(t->first),
                                        as<uint32_t>(t->cnt), as<uint32_t>(t->skip), as<uint64_t>(t->khi),
@@ -1265,10 +1328,11 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
         GVS_CUDA(c, ensure(c, t->pos32lo, n * sizeof(float4)));
     }
     if (t->precision != mode + 1) {
+        if (mode != 1) GVS_TRY(tree_moments64(c, t));
         k_pack_nodes<<<nblk(nnodes), 256, 0, st>>>(nnodes, as<uint8_t>(t->level), as<uint32_t>(t->first),
                                                     as<uint32_t>(t->cnt), as<uint32_t>(t->skip), as<double>(t->mass),
                                                     as<double>(t->comx), as<double>(t->comy), as<double>(t->comz),
-                                                    mode != 0 ? as<float4>(t->cm32) : nullptr,
+                                                    mode == 2 ? as<float4>(t->cm32) : nullptr,
                                                     mode != 1 ? as<double4>(t->cm64) : nullptr, as<int4>(t->meta),
                                                     mode == 2 ? as<float4>(t->cm32lo) : nullptr);
         if (mode != 0)
@@ -1276,6 +1340,17 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
                                                       as<double>(t->sm), as<float4>(t->pos32),
                                                       mode == 2 ? as<float4>(t->pos32lo) : nullptr);
         c->prof.launches += mode != 0 ? 2 : 1;
+        if (mode == 1) {  // f32 moments from the f32 particles
+            GVS_CUDA(c, ensure(c, t->mo32, nnodes * sizeof(float4)));
+            GVS_CUDA(c, cudaMemsetAsync(t->arrive.ptr, 0, nnodes * 4, st));
+            k_moments32_up<<<nblk(nnodes), 256, 0, st>>>(nnodes, as<uint32_t>(t->first), as<uint32_t>(t->cnt),
+                                                         as<uint32_t>(t->skip), as<uint32_t>(t->parent),
+                                                         as<uint32_t>(t->nk), as<uint32_t>(t->arrive),
+                                                         as<float4>(t->pos32), as<float4>(t->mo32),
+                                                         as<float4>(t->cm32));
+            c->prof.launches += 1;
+        }
+        GVS_TRY(check_launch(c, "walk packing"));
         t->precision = mode + 1;
     }
     // the mixed walk's certified margin: X bounds every coordinate (the root cell);
@@ -1386,6 +1461,7 @@ gvs_status tree_export(Ctx *c, size_t cap, uint8_t *level, uint32_t *first, uint
                        double *mass, double *com, uint32_t *perm, uint64_t *keys, size_t *nnodes) {
     GVS_TRY(tree_build(c));
     Tree *t = tree_of(c);
+    GVS_TRY(tree_moments64(c, t));
     *nnodes = t->nnodes;
     if (cap < t->nnodes) return GVS_OK;
     cudaStream_t st = c->stream;
