@@ -855,11 +855,10 @@ __device__ __forceinline__ float warp_max(float v) {
 // Every lane adds the list's monopole terms to its NPL particles: packed f32x2
 // over a particle pair (NPL 2), scalar f32 for one particle.  GUARD (unsoftened
 // runs) keeps r^2 > 0, so a particle's own leaf adds exactly zero.
-template <int NPL, bool GUARD>
+template <int NPL, bool GUARD, int NP = (NPL >= 2 ? NPL / 2 : 1)>
 __device__ __forceinline__ void group_eval(const float4 *__restrict__ il, int cnt, const f2 *nx, const f2 *ny,
                                            const f2 *nz, float eps2, f2 *ax, f2 *ay, f2 *az) {
-    if constexpr (NPL >= 2) {
-        constexpr int NP = NPL / 2;  // particle pairs per lane
+    if constexpr (NPL >= 2) {  // NP particle pairs per lane (fewer than NPL/2 when the group leaves slots empty)
         const f2 e2 = pk(eps2, eps2);
 #pragma unroll (NP == 1 ? 4 : 2)
         for (int k = 0; k < cnt; ++k) {
@@ -981,6 +980,12 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_walk_group(const int2 *__rest
         lox = warp_min(lox); loy = warp_min(loy); loz = warp_min(loz);
         hix = warp_max(hix); hiy = warp_max(hiy); hiz = warp_max(hiz);
         f2 nx[NP], ny[NP], nz[NP], ax[NP], ay[NP], az[NP];
+        // a 128-slot group with at most 64 particles uses only the first slot pair of each lane
+        const bool half = NPL == 4 && gr.y <= 64;
+        auto eval = [&](const float4 *list, int count) {
+            if (half) group_eval<NPL, GUARD, 1>(list, count, nx, ny, nz, eps2f, ax, ay, az);
+            else group_eval<NPL, GUARD>(list, count, nx, ny, nz, eps2f, ax, ay, az);
+        };
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
             nx[p] = pk(-px[2 * p], -px[2 * p + 1]);
@@ -1066,7 +1071,7 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_walk_group(const int2 *__rest
                     if (nil > GW_ICAP - 32) {
                         __syncwarp();
                         terms += nil;
-                        group_eval<NPL, GUARD>(il, nil, nx, ny, nz, eps2f, ax, ay, az);
+                        eval(il, nil);
                         nil = 0;
                         __syncwarp();
                     }
@@ -1085,7 +1090,7 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_walk_group(const int2 *__rest
             __syncwarp();
             if (nil > GW_ICAP - 32) {
                 terms += nil;
-                group_eval<NPL, GUARD>(il, nil, nx, ny, nz, eps2f, ax, ay, az);
+                eval(il, nil);
                 nil = 0;
                 __syncwarp();
             }
@@ -1107,7 +1112,7 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_walk_group(const int2 *__rest
                                fy[q], fz[q]);
             }
         } else {
-            if (nil) group_eval<NPL, GUARD>(il, nil, nx, ny, nz, eps2f, ax, ay, az);
+            if (nil) eval(il, nil);
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
                 upk(ax[p], fx[2 * p], fx[2 * p + 1]);
