@@ -274,31 +274,42 @@ __device__ int ball_query_thread(const TreeView &tv, const float4 *__restrict__ 
 
 // Neighbour lists of all gas particles (build_neighbor_lists with factor):
 // warp-synchronous walk, each lane with its own next-node pointer.
+// One particle per lane; warps take chunks of 32 sorted particles from a counter
+// (work[0]), so uneven walks balance across the GPU and no partial wave is left.
 __global__ void __launch_bounds__(128) k_neighbors(const TreeView tv, const float4 *__restrict__ pos4,
                                                    const float4 *__restrict__ node4, const int4 *__restrict__ meta4,
                                                    const uint8_t *__restrict__ gas, const double *__restrict__ sh,
                                                    double factor, int kmax, uint32_t *__restrict__ list,
-                                                   uint32_t *__restrict__ cnt, unsigned *__restrict__ err) {
-    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = t < tv.n && gas[t];
-    double px = 0, py = 0, pz = 0, radius = 0;
-    if (active) {
-        px = tv.sx[t]; py = tv.sy[t]; pz = tv.sz[t];
-        radius = 2.0 * sh[t] * factor;
-    }
-    const Prefilter pf = prefilter(px, py, pz, radius, prefilter_scale(tv));
-    uint32_t *row = list + t * (size_t)kmax;
-    int count = 0;
-    uint32_t next = active ? 0u : 0xFFFFFFFFu;
+                                                   uint32_t *__restrict__ cnt, unsigned *__restrict__ err,
+                                                   unsigned *__restrict__ work) {
+    const int lane = threadIdx.x & 31;
+    const float E = prefilter_scale(tv);
     for (;;) {
-        const uint32_t k = __reduce_min_sync(0xFFFFFFFFu, next);
-        if ((size_t)k >= tv.nnodes) break;
-        if (next != k) continue;
-        next = ball_visit(tv, pos4, meta4[k], node4[k], k, pf, px, py, pz, radius, row, kmax, count);
-    }
-    if (t < tv.n) {
-        cnt[t] = active ? (uint32_t)count : 0u;
-        if (count > kmax) atomicOr(err, (unsigned)DERR_NEIGH_OVERFLOW);
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(work, 32u);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if ((size_t)base >= tv.n) break;
+        const size_t t = (size_t)base + lane;
+        const bool active = t < tv.n && gas[t];
+        double px = 0, py = 0, pz = 0, radius = 0;
+        if (active) {
+            px = tv.sx[t]; py = tv.sy[t]; pz = tv.sz[t];
+            radius = 2.0 * sh[t] * factor;
+        }
+        const Prefilter pf = prefilter(px, py, pz, radius, E);
+        uint32_t *row = list + t * (size_t)kmax;
+        int count = 0;
+        uint32_t next = active ? 0u : 0xFFFFFFFFu;
+        for (;;) {
+            const uint32_t k = __reduce_min_sync(0xFFFFFFFFu, next);
+            if ((size_t)k >= tv.nnodes) break;
+            if (next != k) continue;
+            next = ball_visit(tv, pos4, meta4[k], node4[k], k, pf, px, py, pz, radius, row, kmax, count);
+        }
+        if (t < tv.n) {
+            cnt[t] = active ? (uint32_t)count : 0u;
+            if (count > kmax) atomicOr(err, (unsigned)DERR_NEIGH_OVERFLOW);
+        }
     }
 }
 
@@ -1015,9 +1026,16 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
     for (int attempt = 0; attempt < 4; ++attempt) {
         GVS_CUDA(c, ensure(c, S->list, n * (size_t)S->kmax * 4));
         GVS_CUDA(c, cudaMemcpyAsync(S->sh.ptr, c->scratch_b.ptr, b8, cudaMemcpyDeviceToDevice, st));
-        k_neighbors<<<nb(n, 128), 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4), as<int4>(S->meta4), as<uint8_t>(S->gas),
-                                                as<double>(S->sh), 1.1, S->kmax,
-                                                as<uint32_t>(S->list), as<uint32_t>(S->cnt), err_ptr(c));
+        {
+            int per_sm = 0;
+            GVS_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_neighbors, 128, 0));
+            const int blocks = (int)std::min<size_t>(nb(n, 128), (size_t)std::max(1, per_sm) * c->num_sms);
+            GVS_CUDA(c, cudaMemsetAsync(err_ptr(c) + 20, 0, 4, st));
+            k_neighbors<<<blocks, 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4), as<int4>(S->meta4),
+                                                as<uint8_t>(S->gas), as<double>(S->sh), 1.1, S->kmax,
+                                                as<uint32_t>(S->list), as<uint32_t>(S->cnt), err_ptr(c),
+                                                err_ptr(c) + 20);
+        }
         if (mixed) {
             GVS_CUDA(c, cudaMemsetAsync(S->redo_count.ptr, 0, 4, st));
             k_density_mixed<<<nb(n, 128), 128, 0, st>>>(
