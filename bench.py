@@ -403,6 +403,16 @@ def adjoint_ratio(ctx, G, n=16384, steps=200, every=100, seed=42, eps=0.01, dt=1
     return out
 
 
+def hbm_peak_gbs():
+    """HBM copy bandwidth measured on this machine (MEASURED_PEAKS.json beside this file), else
+    the fallback figure of one earlier GB300 measurement; returns (GB/s, source)."""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback 6.8 TB/s"
+
+
 def run_workload(a, d):
     """Secondary workloads (one JSON line each; the default run is the direct sum)."""
     import gravis_gb300 as G
@@ -467,6 +477,17 @@ def run_workload(a, d):
                 walks[wname]["rel_rms_vs_fp64_walk"] = float(np.sqrt(((aw - a64) ** 2).sum() / (a64 ** 2).sum()))
             walks[wname]["per_particle_rms_rel_err_vs_exact_f64_direct"] = float(
                 np.sqrt((((aw[idx] - ref) ** 2).sum(1) / (ref ** 2).sum(1)).mean()))
+        # roofline of the walk: counted node/particle terms x 20 flop against the FP32 peak
+        walk_s = prof["force_ms"] * 1e-3
+        terms_s = prof["bh_group_interactions"] / walk_s if walk_s > 0 else 0.0
+        peak32 = ctx.fp32_peak_tflops()
+        res["roofline"] = {"bound": "fp32", "achieved": terms_s * 20 / 1e12, "peak": peak32, "unit": "TFLOP/s",
+                           "frac": terms_s * 20 / 1e12 / peak32 if peak32 else None, "traffic": None,
+                           "kernel": "k_walk_group (FP32 group walk)",
+                           "terms_per_s": terms_s, "terms_per_particle": prof["bh_group_interactions"] / (n * a.steps),
+                           "peak_source": "measured FP32 FMA probe (gvs_measure_fp32_peak)",
+                           "work_unit": "20 flop per node or particle term evaluated for a real particle; "
+                                        "DRAM traffic of the walk is in profiles/ (ncu)"}
         res.update({"value": n * a.steps / (t * 1e-3), "ms_per_step": t / a.steps, "dtype": "f32 walk / f64 state",
                     "walk_forms": walks,
                     "config": {"workload": f"Barnes-Hut KDK, two Plummer spheres N={n} seed 7, theta={theta}, "
@@ -574,6 +595,14 @@ def run_workload(a, d):
                                   "what": "the same steps with the reference's f64 SPH arithmetic"},
                     "mixed_over_f64": t_ex / t,
                     "mixed_vs_f64_rel_rms": errs, "clocks": clk})
+        # roofline per the algorithmic bytes of one SPH step (density 120 B, forces 160 B,
+        # neighbour rows 840 B, KDK 120 B per particle)
+        hbm, hbm_src = hbm_peak_gbs()
+        gbs = n * 1240.0 / (t / a.steps * 1e-3) / 1e9
+        res["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                           "traffic": None, "bytes_per_particle_step": 1240, "peak_source": hbm_src,
+                           "note": "the SPH kernels are issue- and latency-bound well below this roofline "
+                                   "(neighbour walk, f32 pair gathers); their ncu figures are in profiles/"}
         if d.rank == 0 and not a.no_extras:
             res["cpu_baseline"] = cpu_sph_sample(G)
     elif a.workload == "ensemble":

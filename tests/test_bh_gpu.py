@@ -281,6 +281,23 @@ def test_bh_group_walk_refines_per_particle(ctx, theta):
     assert errs[32] <= errs[0] and errs[64] <= errs[0] and errs[128] <= errs[0]
 
 
+@pytest.mark.parametrize("n", [1, 2, 3, 33, 200])
+@pytest.mark.parametrize("eps", [0.0, 0.01])
+def test_bh_group_walk_tiny(ctx, n, eps):
+    """Tiny systems (a root that is a leaf, one partial group) through the FP32 group walk
+    at theta = 0: the f32 all-pairs sum; a lone particle feels nothing."""
+    p = G.PlummerSphere(n, seed=21).generate()
+    ref = p.copy()
+    G.BruteForce(eps, G.PREC_FP64_EXACT, ctx).compute_accelerations(ref)
+    q = p.copy()
+    G.BarnesHut(eps, 0.0, G.PREC_FP32, ctx).compute_accelerations(q)
+    assert np.isfinite(q.acc()).all()
+    if n == 1:
+        assert not q.acc().any()
+    else:
+        assert rel_rms(q.acc(), ref.acc()) <= 1e-5
+
+
 def test_bh_group_walk_unsoftened(ctx):
     """eps = 0: a particle's own leaf adds exactly zero (no 0/0), forces stay finite
     and agree with the f64 walk to f32 accuracy at theta = 0."""
