@@ -1097,10 +1097,10 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_walk_group(const int2 *__rest
         }
         float fx[NQ], fy[NQ], fz[NQ];
         if (lane == 0) {
-            atomicAdd(reinterpret_cast<unsigned long long *>(err + 12), (unsigned long long)iters);
-            atomicAdd(err + 14, 1u);
-            if (fallback) atomicAdd(err + 15, 1u);
-            else atomicAdd(reinterpret_cast<unsigned long long *>(err + 16),
+            atomicAdd(reinterpret_cast<unsigned long long *>(err + EW_BH_ITERS), (unsigned long long)iters);
+            atomicAdd(err + EW_BH_GROUPS, 1u);
+            if (fallback) atomicAdd(err + EW_BH_FALLBACKS, 1u);
+            else atomicAdd(reinterpret_cast<unsigned long long *>(err + EW_BH_TERMS),
                            (unsigned long long)(terms + nil) * (unsigned long long)gr.y);
         }
         if (fallback) {

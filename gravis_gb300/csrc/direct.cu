@@ -1259,7 +1259,7 @@ gvs_status launch32_t(Ctx *c, float eps2, int nsplit_req, double **partial_out, 
     GVS_CUDA(c, ensure(c, c->partial, (size_t)nsplit_eff * 3 * npad * sizeof(double)));
     dim3 grid(iblocks, nsplit_eff);
     if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], c->stream));
-    unsigned long long *nearc = reinterpret_cast<unsigned long long *>(err_ptr(c) + 8);
+    unsigned long long *nearc = reinterpret_cast<unsigned long long *>(err_ptr(c) + EW_NEAR_TILES);
     kern<<<grid, NT, smem, c->stream>>>(as<float4>(c->jpack32), ntiles, tps, eps2, as<double>(c->partial), npad,
                                         err_ptr(c), nearc);
     c->prof.launches += 1;
@@ -1508,7 +1508,7 @@ gvs_status ens_pairs(Ctx *c, const float4 *pack, const int4 *items, int nitems, 
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, ENS_TJ, smem);
     const int grid = std::max(1, std::min(nitems, c->num_sms * std::max(1, per_sm)));
     GVS_CUDA(c, cudaMemsetAsync(counter, 0, sizeof(unsigned), c->stream));
-    unsigned long long *nearc = reinterpret_cast<unsigned long long *>(err_ptr(c) + 8);
+    unsigned long long *nearc = reinterpret_cast<unsigned long long *>(err_ptr(c) + EW_NEAR_TILES);
     kern<<<grid, ENS_TJ, smem, c->stream>>>(pack, items, nitems, counter, eps2, partial, npad, err_ptr(c), nearc);
     c->prof.launches += 1;
     return check_launch(c, "ensemble pair kernel");

@@ -668,7 +668,8 @@ gvs_status gvs_profile_enable(gvs_ctx *c, int on) {
     c->prof.tile_visits = 0.0;
     c->prof.vjp_ms = 0.0;
     c->prof.vjp_launches = 0;
-    GVS_CUDA(c, cudaMemsetAsync(err_ptr(c) + 8, 0, 10 * sizeof(unsigned), c->stream));
+    GVS_CUDA(c, cudaMemsetAsync(err_ptr(c) + EW_NEAR_TILES, 0, (EW_PROFILE_END - EW_NEAR_TILES) * sizeof(unsigned),
+                                c->stream));
     return GVS_OK;
 }
 
@@ -684,19 +685,19 @@ gvs_status gvs_profile_read(gvs_ctx *c, gvs_profile *out) {
     out->vjp_ms = c->prof.vjp_ms;
     out->vjp_launches = c->prof.vjp_launches;
     unsigned long long nearc = 0;
-    GVS_CUDA(c, cudaMemcpy(&nearc, err_ptr(c) + 8, sizeof nearc, cudaMemcpyDeviceToHost));
+    GVS_CUDA(c, cudaMemcpy(&nearc, err_ptr(c) + EW_NEAR_TILES, sizeof nearc, cudaMemcpyDeviceToHost));
     out->near_tile_visits = (double)nearc;
     out->tile_visits = c->prof.tile_visits;
     unsigned redo = 0;
-    GVS_CUDA(c, cudaMemcpy(&redo, err_ptr(c) + 10, sizeof redo, cudaMemcpyDeviceToHost));
+    GVS_CUDA(c, cudaMemcpy(&redo, err_ptr(c) + EW_SPH_REDO, sizeof redo, cudaMemcpyDeviceToHost));
     out->sph_f64_redo = redo;
     unsigned words[4] = {0, 0, 0, 0};  // group walk: iterations (u64), groups, fallbacks
-    GVS_CUDA(c, cudaMemcpy(words, err_ptr(c) + 12, sizeof words, cudaMemcpyDeviceToHost));
+    GVS_CUDA(c, cudaMemcpy(words, err_ptr(c) + EW_BH_ITERS, sizeof words, cudaMemcpyDeviceToHost));
     out->bh_group_iterations = (long long)((unsigned long long)words[0] | ((unsigned long long)words[1] << 32));
     out->bh_groups = words[2];
     out->bh_group_fallbacks = words[3];
     unsigned long long pairs = 0;
-    GVS_CUDA(c, cudaMemcpy(&pairs, err_ptr(c) + 16, sizeof pairs, cudaMemcpyDeviceToHost));
+    GVS_CUDA(c, cudaMemcpy(&pairs, err_ptr(c) + EW_BH_TERMS, sizeof pairs, cudaMemcpyDeviceToHost));
     out->bh_group_interactions = (long long)pairs;
     return GVS_OK;
 }

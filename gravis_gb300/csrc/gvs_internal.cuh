@@ -33,6 +33,21 @@ enum DeviceError : unsigned {
     DERR_SPIN_TIMEOUT = 1u << 6,   // persistent-kernel queue wait hit its cap
 };
 
+// Layout of the context's device word area (err_word, 64 u32): word 0 holds the
+// DeviceError flags; the rest are counters that kernels add to and the profile
+// reads (u64 counters take two aligned words).
+enum ErrWordSlot : int {
+    EW_FLAGS = 0,
+    EW_NEAR_TILES = 8,      // u64: float-float near-field blocks of the f32 pair kernel
+    EW_SPH_REDO = 10,       // mixed SPH particles rerun on the f64 path
+    EW_BH_ITERS = 12,       // u64: BH group-walk iterations
+    EW_BH_GROUPS = 14,      // BH groups walked
+    EW_BH_FALLBACKS = 15,   // ... of which walked per particle
+    EW_BH_TERMS = 16,       // u64: BH group-walk terms evaluated for real particles
+    EW_PROFILE_END = 18,    // profile counters: [EW_NEAR_TILES, EW_PROFILE_END)
+    EW_NEIGH_WORK = 20,     // work counter of the SPH neighbour search
+};
+
 // ---------------------------------------------------------------------------
 // a growable device buffer owned by the context
 // ---------------------------------------------------------------------------

@@ -1030,11 +1030,11 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
             int per_sm = 0;
             GVS_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_neighbors, 128, 0));
             const int blocks = (int)std::min<size_t>(nb(n, 128), (size_t)std::max(1, per_sm) * c->num_sms);
-            GVS_CUDA(c, cudaMemsetAsync(err_ptr(c) + 20, 0, 4, st));
+            GVS_CUDA(c, cudaMemsetAsync(err_ptr(c) + EW_NEIGH_WORK, 0, 4, st));
             k_neighbors<<<blocks, 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4), as<int4>(S->meta4),
                                                 as<uint8_t>(S->gas), as<double>(S->sh), 1.1, S->kmax,
                                                 as<uint32_t>(S->list), as<uint32_t>(S->cnt), err_ptr(c),
-                                                err_ptr(c) + 20);
+                                                err_ptr(c) + EW_NEIGH_WORK);
         }
         if (mixed) {
             GVS_CUDA(c, cudaMemsetAsync(S->redo_count.ptr, 0, 4, st));
@@ -1049,7 +1049,7 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
                 as<double>(c->scratch_b), as<double>(S->sh), as<uint32_t>(S->list), as<uint32_t>(S->cnt), S->kmax,
                 prm->gamma, prm->eta, prm->h_max, as<double>(S->srho), as<double>(S->somega), as<double>(S->spres),
                 as<double>(S->scs), err_ptr(c), as<uint32_t>(S->redo_idx), as<unsigned>(S->redo_count),
-                err_ptr(c) + 10);
+                err_ptr(c) + EW_SPH_REDO);
             c->prof.launches += 1;
         } else
             k_density<<<nb(n, 128), 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4), as<int4>(S->meta4), as<uint8_t>(S->gas),
