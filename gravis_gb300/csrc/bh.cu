@@ -66,6 +66,7 @@ struct Tree {
     // group walk (f32): child-slot records, groups of <= 32*NPL particles, work counter
     DevBuf nk, koff, krec, groups, gcount;
     DevBuf parent, arrive;  // per node: parent index, children that finished their moments
+    DevBuf leaf_of;         // per sorted particle: the leaf that holds it
     unsigned long long grp_version = ~0ull;
     unsigned long long centres_version = ~0ull;  // tree version the cell centres were built for
     unsigned long long m64_version = ~0ull;      // ... the f64 moments were built for
@@ -369,14 +370,18 @@ __global__ void k_centres(const uint64_t *__restrict__ khi, const uint64_t *__re
 }
 
 // Parent links and child counts: each internal node walks its children (the
-// skip chain k+1, skip[k+1], ... up to skip[k]).
-__global__ void k_links(size_t nnodes, const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ skip,
-                        uint32_t *__restrict__ parent, uint32_t *__restrict__ nk) {
+// skip chain k+1, skip[k+1], ... up to skip[k]); each leaf records itself as
+// the leaf of its particles.
+__global__ void k_links(size_t nnodes, const uint32_t *__restrict__ first, const uint32_t *__restrict__ cnt,
+                        const uint32_t *__restrict__ skip, uint32_t *__restrict__ parent, uint32_t *__restrict__ nk,
+                        uint32_t *__restrict__ leaf_of) {
     const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nnodes) return;
     if (k == 0) parent[0] = 0xFFFFFFFFu;
     uint32_t c = 0;
-    if (cnt[k] == 0) {
+    const uint32_t lc = cnt[k];
+    for (uint32_t j = first[k]; j < first[k] + lc; ++j) leaf_of[j] = (uint32_t)k;
+    if (lc == 0) {
         const uint32_t end = skip[k];
         for (uint32_t ch = (uint32_t)k + 1; ch < end; ch = skip[ch], ++c) parent[ch] = (uint32_t)k;
     }
@@ -1145,7 +1150,7 @@ void tree_free(Ctx *c) {
                      &t->iota2, &t->delta, &t->nown, &t->off, &t->total, &t->level, &t->first, &t->cnt, &t->skip,
                      &t->mass, &t->comx, &t->comy, &t->comz, &t->boxx, &t->boxy, &t->boxz, &t->sx, &t->sy,
                      &t->sz, &t->sm, &t->pos32, &t->cm32, &t->cm64, &t->meta, &t->pos32lo, &t->cm32lo, &t->nk, &t->koff, &t->krec,
-                     &t->groups, &t->gcount, &t->parent, &t->arrive, &t->mo32};
+                     &t->groups, &t->gcount, &t->parent, &t->arrive, &t->mo32, &t->leaf_of};
     for (DevBuf *b : all)
         if (b->ptr) cudaFree(b->ptr);
     delete t;
@@ -1253,8 +1258,9 @@ gvs_status tree_build(Ctx *c) {
     GVS_CUDA(c, ensure(c, t->parent, nnodes * 4));
     GVS_CUDA(c, ensure(c, t->nk, nnodes * 4));
     GVS_CUDA(c, ensure(c, t->arrive, nnodes * 4));
-    k_links<<<nblk(nnodes), 256, 0, st>>>(nnodes, as<uint32_t>(t->cnt), as<uint32_t>(t->skip),
-                                          as<uint32_t>(t->parent), as<uint32_t>(t->nk));
+    GVS_CUDA(c, ensure(c, t->leaf_of, n * 4));
+    k_links<<<nblk(nnodes), 256, 0, st>>>(nnodes, as<uint32_t>(t->first), as<uint32_t>(t->cnt), as<uint32_t>(t->skip),
+                                          as<uint32_t>(t->parent), as<uint32_t>(t->nk), as<uint32_t>(t->leaf_of));
     c->prof.launches += 1;
     GVS_TRY(check_launch(c, "tree links"));
     t->n = n;
@@ -1439,6 +1445,8 @@ gvs_status tree_view(Ctx *c, TreeView *v) {
     v->cnt = as<uint32_t>(t->cnt);
     v->skip = as<uint32_t>(t->skip);
     v->perm = as<uint32_t>(t->perm);
+    v->parent = as<uint32_t>(t->parent);
+    v->leaf_of = as<uint32_t>(t->leaf_of);
     if (t->centres_version != t->version) {
         const size_t nn = t->nnodes, n = t->n;
         GVS_CUDA(c, ensure(c, t->boxx, nn * 8));

@@ -341,7 +341,7 @@ void tree_free(Ctx *c);
 struct TreeView {
     size_t n, nnodes;
     const uint8_t *level;
-    const uint32_t *first, *cnt, *skip, *perm;
+    const uint32_t *first, *cnt, *skip, *perm, *parent, *leaf_of;  // leaf_of[j]: the leaf holding particle j
     const double *bx, *by, *bz, *sx, *sy, *sz;  // cell centres; sorted positions
     double root_hw;                              // half width at depth 0 (depth L: root_hw * 2^-L)
 };

@@ -183,18 +183,42 @@ __device__ __forceinline__ int pref_box(const Prefilter &f, float4 b) {
 // certainly inside the sphere lies in a box that certainly meets it, and one
 // certainly outside adds nothing either way), and only an undecided one runs
 // both of the reference's f64 tests, box then particle.
+//
+// meta4 = (skip, first particle, count, depth): count > 0 for a leaf, minus the
+// subtree's particle count for an internal node.
 __global__ void k_sph_f32copies(const TreeView tv, float4 *__restrict__ pos4, float4 *__restrict__ node4,
                                 int4 *__restrict__ meta4) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < tv.n) pos4[i] = make_float4((float)tv.sx[i], (float)tv.sy[i], (float)tv.sz[i], 0.f);
     if (i < tv.nnodes) {
-        const uint32_t c = tv.cnt[i], f = tv.first[i];
-        meta4[i] = make_int4((int)tv.skip[i], (int)f, (int)c, (int)tv.level[i]);
+        const uint32_t c = tv.cnt[i], f = tv.first[i], sk = tv.skip[i];
+        const uint32_t sub = (uint32_t)((sk < tv.nnodes ? (size_t)tv.first[sk] : tv.n) - f);
+        meta4[i] = make_int4((int)sk, (int)f, c > 0 ? (int)c : -(int)sub, (int)tv.level[i]);
         node4[i] = c == 1 ? make_float4((float)tv.sx[f], (float)tv.sy[f], (float)tv.sz[f], 0.f)
                           : make_float4((float)tv.bx[i], (float)tv.by[i], (float)tv.bz[i],
                                         (float)ldexp(tv.root_hw, -(int)tv.level[i]));
     }
 }
+
+// The reference's query (octree.rs:245-308) for one sphere and particle j: every
+// cell on the path from the root to j's leaf passes sphere_intersects_aabb, then
+// the distance test.  For the prefilter's undecided cases.
+__device__ bool member_exact(const TreeView &tv, uint32_t leaf, uint32_t j, double px, double py, double pz,
+                             double radius) {
+    for (uint32_t a = leaf; a != 0xFFFFFFFFu; a = tv.parent[a]) {
+        const double hw = ldexp(tv.root_hw, -(int)tv.level[a]);
+        if (!sphere_hits_box(px, py, pz, radius, tv.bx[a], tv.by[a], tv.bz[a], hw)) return false;
+    }
+    const double dx = tv.sx[j] - px, dy = tv.sy[j] - py, dz = tv.sz[j] - pz;
+    return dx * dx + dy * dy + dz * dz <= radius * radius;
+}
+
+// Cells of at most RANGE_MAX particles are not descended: their particles (a
+// contiguous, depth-first-ordered range) are tested directly.  A particle
+// certainly inside the sphere lies in cells that all certainly meet it; one
+// certainly outside is dropped either way; an undecided one runs the reference's
+// tests on its whole path (member_exact), so the lists are the reference's.
+constexpr int RANGE_MAX = 32;
 
 // One node of the ball query: appends its hits to row in depth-first order and
 // returns the next node.  See k_sph_f32copies for the record layout.
@@ -225,12 +249,18 @@ __device__ __forceinline__ uint32_t ball_visit(const TreeView &tv, const float4 
         hit = sphere_hits_box(px, py, pz, radius, tv.bx[k], tv.by[k], tv.bz[k], hw);
     }
     if (!hit) return (uint32_t)mt.x;
-    if (mt.z == 0) return k + 1;  // internal: descend
-    for (uint32_t j = (uint32_t)mt.y; j < (uint32_t)(mt.y + mt.z); ++j) {  // bucket leaf
+    if (mt.z < -RANGE_MAX) return k + 1;  // internal: descend
+    const bool bucket = mt.z > 1;         // else a small internal cell, tested as a range
+    const uint32_t c = (uint32_t)(bucket ? mt.z : -mt.z);
+    for (uint32_t j = (uint32_t)mt.y; j < (uint32_t)mt.y + c; ++j) {
         int in = pref_point(pf, pos4[j]);
         if (in < 0) {
-            const double dx = tv.sx[j] - px, dy = tv.sy[j] - py, dz = tv.sz[j] - pz;
-            in = dx * dx + dy * dy + dz * dz <= r2;
+            if (bucket) {  // this leaf's box passed: the particle test decides
+                const double dx = tv.sx[j] - px, dy = tv.sy[j] - py, dz = tv.sz[j] - pz;
+                in = dx * dx + dy * dy + dz * dz <= r2;
+            } else {
+                in = member_exact(tv, tv.leaf_of[j], j, px, py, pz, radius) ? 1 : 0;
+            }
         }
         if (in) {
             if (count < kmax) row[count] = j;
