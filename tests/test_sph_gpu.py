@@ -69,6 +69,9 @@ def cases():
     g1r.vy[:] = -0.1 * g1r.y
     return {"lattice5_h0.8": lattice_gas(5, 0.5, 0.8), "lattice8_h1": lattice_gas(8, 0.5, 1.0),
             "lattice6_hbad": lattice_gas(6, 0.5, 2.0),  # density.rs h_convergence: re-queries
+            # 2 h 1.1 == 1.0 exactly in f64: neighbours two lattice steps away sit exactly on the
+            # search sphere (the prefilter's undecided case, settled by the reference's f64 tests)
+            "lattice8_tie": lattice_gas(8, 0.5, 1.0 / 2.2),
             "jittered": lattice_gas(10, 0.3, 0.45, jitter=0.05, vel=0.1), "evrard1000": ev, "sphere1r_4000": g1r}
 
 
