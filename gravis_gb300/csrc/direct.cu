@@ -129,6 +129,84 @@ __global__ void k_hilbert(const double *__restrict__ x, const double *__restrict
     idx[i] = (uint32_t)i;
 }
 
+// Small systems (n <= SMALL_ORDER_MAX): the whole Hilbert ordering in one block --
+// bounding box, keys (k_hilbert's formula), and a bitonic sort of (key, index)
+// pairs in shared memory.  (key, index) pairs are distinct, so the sorted order is
+// the stable radix sort's; the permutation is the one the multi-kernel path gives,
+// from one launch instead of ~27 (which dominate a step of a thousand particles).
+constexpr int SMALL_ORDER_MAX = 8192;
+
+__global__ void __launch_bounds__(1024) k_small_order(const double *__restrict__ x, const double *__restrict__ y,
+                                                      const double *__restrict__ z, int n, int P,
+                                                      uint32_t *__restrict__ perm) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint64_t *key = reinterpret_cast<uint64_t *>(smem_raw);
+    uint32_t *idx = reinterpret_cast<uint32_t *>(key + P);
+    __shared__ double red[32][6];
+    __shared__ double bb[6];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int i = tid; i < n; i += blockDim.x) {
+        const double v[3] = {x[i], y[i], z[i]};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            mn[d] = fmin(mn[d], v[d]);
+            mx[d] = fmax(mx[d], v[d]);
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        for (int o = 16; o > 0; o >>= 1) {
+            mn[d] = fmin(mn[d], __shfl_xor_sync(0xFFFFFFFFu, mn[d], o));
+            mx[d] = fmax(mx[d], __shfl_xor_sync(0xFFFFFFFFu, mx[d], o));
+        }
+    if (lane == 0)
+        for (int d = 0; d < 3; ++d) red[w][d] = mn[d], red[w][3 + d] = mx[d];
+    __syncthreads();
+    if (tid < 6) {
+        double v = red[0][tid];
+        for (int ww = 1; ww < (int)(blockDim.x >> 5); ++ww) v = tid < 3 ? fmin(v, red[ww][tid]) : fmax(v, red[ww][tid]);
+        bb[tid] = v;
+    }
+    __syncthreads();
+    const double ext = fmax(fmax(bb[3] - bb[0], bb[4] - bb[1]), bb[5] - bb[2]);
+    const double inv = ext > 0.0 ? 2097151.99 / ext : 0.0;
+    for (int i = tid; i < P; i += blockDim.x) {
+        uint64_t k = ~0ull;
+        if (i < n) {
+            uint32_t q[3];
+            const double v[3] = {x[i], y[i], z[i]};
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                double t = (v[d] - bb[d]) * inv;
+                t = fmin(fmax(t, 0.0), 2097151.0);
+                q[d] = (uint32_t)t;
+            }
+            k = hilbert_key(q[0], q[1], q[2]);
+        }
+        key[i] = k;
+        idx[i] = (uint32_t)i;
+    }
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < P; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const uint64_t ka = key[i], kb = key[l];
+                    const uint32_t ia = idx[i], ib = idx[l];
+                    const bool gt = ka > kb || (ka == kb && ia > ib);
+                    if (((i & k) == 0) == gt) {
+                        key[i] = kb; key[l] = ka;
+                        idx[i] = ib; idx[l] = ia;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = tid; i < n; i += blockDim.x) perm[i] = idx[i];
+}
+
 // ---------------------------------------------------------------------------
 // packing of source tiles
 // ---------------------------------------------------------------------------
@@ -1181,6 +1259,17 @@ gvs_status bbox_minmax(Ctx *c, double *dev_out6, DevBuf &part_buf) {
 // Hilbert order of the resident positions: c->perm[s] = caller index of sorted slot s.
 gvs_status spatial_order(Ctx *c) {
     const size_t n = c->n;
+    if (n <= (size_t)SMALL_ORDER_MAX) {
+        GVS_CUDA(c, ensure(c, c->perm, n * 4));
+        int P = 1;
+        while (P < (int)n) P <<= 1;
+        const int smem = P * (int)(sizeof(uint64_t) + sizeof(uint32_t));
+        set_smem(k_small_order, smem);
+        k_small_order<<<1, 1024, smem, c->stream>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z), (int)n, P,
+                                                    as<uint32_t>(c->perm));
+        c->prof.launches += 1;
+        return check_launch(c, "small-system order");
+    }
     const int nb = std::min(c->num_sms * 4, std::max(1, ceil_div((long long)n, 256)));
     GVS_CUDA(c, ensure(c, c->bbox_part, (size_t)nb * 6 * sizeof(double)));
     GVS_CUDA(c, ensure(c, c->keys, n * 8));
