@@ -1307,9 +1307,12 @@ struct Launch32 {
 int auto_split(Ctx *c, int iblocks, int ntiles, int blocks_per_sm) {
     const long long conc = (long long)c->num_sms * std::max(1, blocks_per_sm);
     const int lo = std::max(1, (int)((4 * conc + iblocks - 1) / iblocks));
-    int best = std::min(lo, std::max(1, ntiles / 4));
+    // splits of at least 4 source tiles amortise the partial sums; a system too small
+    // to fill one wave that way (a few thousand particles) splits down to single tiles
+    const int cap = (long long)iblocks * std::max(1, ntiles / 4) < conc ? ntiles : std::max(1, ntiles / 4);
+    int best = std::min(lo, cap);
     double best_eff = -1.0;
-    for (int ns = best; ns <= std::min(64, std::max(best, ntiles / 4)); ++ns) {
+    for (int ns = best; ns <= std::min(64, std::max(best, cap)); ++ns) {
         const int tps = ceil_div(ntiles, ns);
         const long long total = (long long)iblocks * ceil_div(ntiles, tps);
         const double waves = (double)total / conc;
