@@ -351,6 +351,29 @@ def test_bh_deterministic_and_resident_steps(ctx):
     assert np.array_equal(outs[0], outs[1])
 
 
+@pytest.mark.parametrize("gsize", [64, 128])
+def test_bh_group_walk_kdk_energy(ctx, gsize):
+    """The FP32 group walk over 500 KDK steps (Plummer N=2000, theta 0.5, dt 1e-3) conserves
+    energy at least as well as the reference's f64 walk on the same system."""
+    p = G.PlummerSphere(2000, seed=42).generate()
+    eps = 0.05
+    drift = {}
+    try:
+        for name, prec, g in (("f64", G.PREC_FP64, -1), ("group", G.PREC_FP32, gsize)):
+            ctx.set_bh_walk(g)
+            ctx.set_state(p)
+            ctx.compute_forces(G.ALGO_BH, prec, eps, 0.5)
+            e0 = ctx.diagnostics(eps).total_energy
+            ctx.kdk_steps(G.ALGO_BH, prec, eps, 0.5, 1e-3, 500)
+            e1 = ctx.diagnostics(eps).total_energy
+            drift[name] = abs(e1 - e0) / abs(e0)
+    finally:
+        ctx.set_bh_walk(-1)
+    print(f"group {gsize}: |dE/E| f64 walk {drift['f64']:.2e}, group walk {drift['group']:.2e}")
+    assert drift["group"] < 1e-3
+    assert drift["group"] <= 2.0 * drift["f64"] + 1e-6
+
+
 def test_bh_kdk_energy(ctx):
     """Plummer N=2000 with BH theta=0.5: 500 steps at dt=1e-3 keep |dE/E| small (tests/barnes_hut.rs)."""
     p = G.PlummerSphere(2000, seed=42).generate()
