@@ -726,9 +726,9 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
 // group's particles -- and collects accepted nodes and leaves in a shared
 // interaction list that every lane then evaluates for its own particles.
 // d <= |com - p| for every particle p of the group, so each particle accepts
-// only nodes its own walk (the reference's test) would accept: its force is a
-// refinement of the per-particle Barnes-Hut sum (more nodes opened, never
-// fewer).  Node records are stored by child slot (the children of a node are
+// only nodes its own walk (the reference's test) would accept -- up to the f32
+// rounding of the test at the opening boundary: its force is a refinement of the
+// per-particle Barnes-Hut sum (more nodes opened, never fewer).  Node records are stored by child slot (the children of a node are
 // contiguous) so that opening a node pushes one (slot, count) range.
 //
 // Stack bound: an iteration pops whole ranges (at most 32 nodes) from the top

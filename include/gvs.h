@@ -270,7 +270,7 @@ gvs_status gvs_set_direct_shape(gvs_ctx *ctx, int nthreads, int ipt, int min_blo
  * particles sharing a tree cell, opening a node unless s^2 < theta^2 d^2 with d the
  * distance from its COM to the group's bounding box.  Every particle then sums a
  * refinement of its own Barnes-Hut node set (the reference's test accepts every node
- * the group accepts).  -1 (default): 128 from 2^21 particles, else 64.  0: the
+ * the group accepts, up to the f32 rounding of the test at the opening boundary).  -1 (default): 128 from 2^21 particles, else 64.  0: the
  * per-particle walk with the reference's test on f32 positions.  FP64 and MIXED walks
  * are always per-particle.  A group whose walk takes more than `budget` iterations
  * (32 nodes each; 0 = the default 1024) is walked per particle instead: its box lies
