@@ -41,7 +41,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gvs", choices=["gvs", "reference"])
-    ap.add_argument("--n", type=int, default=1 << 20)
+    ap.add_argument("--n", type=int, default=None,
+                    help="particles: 2^20 (direct), 2^22 (bh), 2^18 (sph) unless given")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--dt", type=float, default=1e-4)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "fp64", "fp64_exact"])
@@ -55,8 +56,13 @@ def parse():
     ap.add_argument("--sph-precision", default="both", choices=["both", "mixed", "f64"],
                     help="SPH workload: time both pair-arithmetic forms (and compare them), or one only")
     ap.add_argument("--nsys", type=int, default=512, help="systems in the ensemble workload")
-    ap.add_argument("--adjoint-steps", type=int, default=200, help="steps of the adjoint side measurement")
-    return ap.parse_args()
+    ap.add_argument("--adjoint-steps", type=int, default=200,
+                    help="steps of the adjoint measurement (the adjoint workload's config is 1000)")
+    ap.add_argument("--adjoint-n", type=int, default=16384, help="particles of the adjoint measurement")
+    a = ap.parse_args()
+    if a.n is None:
+        a.n = {"bh": 1 << 22, "sph": 1 << 18}.get(a.workload, 1 << 20)
+    return a
 
 
 # ---- distributed plumbing (replicas only: no data-path collective) -------------------
@@ -347,7 +353,7 @@ def run_engine(a, d: Dist):
         got = full.acc()[idx]
         extras["force_rel_rms_mixed_vs_fp64"] = float(np.sqrt(((got - ref) ** 2).sum() / (ref ** 2).sum()))
         extras["force_rel_err_subset"] = "1024 random targets, exact f64 reference on the GPU"
-        extras["adjoint"] = adjoint_ratio(ctx, G, n=16384, steps=a.adjoint_steps, every=100)
+        extras["adjoint"] = adjoint_ratio(ctx, G, n=a.adjoint_n, steps=a.adjoint_steps, every=100)
         line["extras"] = extras
         try:
             v, cores, secs, sample = cpu_sample(a.n, a.seed, eps, a.cpu_targets)
@@ -710,7 +716,7 @@ def run_workload(a, d):
                     "cpu_baseline": {"value": n * ks / tc, "unit": UNIT, "cores": 1, "kind": "port",
                                      "sample": f"{ks} KDK steps of the same system, serial symmetric BruteForce"}})
     elif a.workload == "adjoint":
-        r = adjoint_ratio(ctx, G, n=a.n, steps=a.steps, every=100)
+        r = adjoint_ratio(ctx, G, n=a.adjoint_n, steps=a.adjoint_steps, every=100)
         res.update({"value": r["adjoint_over_forward"], "unit": "backward/forward", "higher_is_better": False,
                     "adjoint": r})
     ctx.close()
