@@ -1186,6 +1186,64 @@ __global__ void k_reduce_vjp(const double *__restrict__ partial, int nsplit, siz
 // ---------------------------------------------------------------------------
 // FP64_EXACT: the reference's arithmetic, one target per thread
 // ---------------------------------------------------------------------------
+// Small systems in FP64_EXACT: one thread per target leaves most of the GPU idle
+// (a thousand targets are 32 warps), and GB300 runs f64 at a small fraction of
+// f32.  The terms of the sum are independent; only their addition is ordered.  So
+// a source chunk's terms (the reference's operations for pair (i, j), unchanged)
+// are computed by N x C threads, and then every target adds its chunk of terms
+// in ascending j (skipping j = i) onto its running sum: the same operations in
+// the same order, bit for bit, with all SMs computing the terms.
+constexpr size_t EXACT_SPLIT_MAX = 40000;            // larger systems fill the GPU with targets alone
+constexpr size_t EXACT_TERMS_BYTES = size_t(192) << 20;  // term buffer per chunk
+
+__global__ void k_exact_terms(const double *__restrict__ X, const double *__restrict__ Y,
+                              const double *__restrict__ Z, const double *__restrict__ M, size_t n, size_t j0,
+                              double eps2, double *__restrict__ TX, double *__restrict__ TY,
+                              double *__restrict__ TZ) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t jj = blockIdx.y, j = j0 + jj, o = jj * n + i;
+    if (j == i) {  // never added (the sum skips j = i)
+        TX[o] = TY[o] = TZ[o] = 0.0;
+        return;
+    }
+    const double xi = X[i], yi = Y[i], zi = Z[i];
+    const double dx = __dsub_rn(X[j], xi), dy = __dsub_rn(Y[j], yi), dz = __dsub_rn(Z[j], zi);
+    const double r2 = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)), eps2);
+    const double inv_r3 = __ddiv_rn(1.0, __dmul_rn(r2, __dsqrt_rn(r2)));
+    const double f = __dmul_rn(M[j], inv_r3);
+    TX[o] = __dmul_rn(f, dx);
+    TY[o] = __dmul_rn(f, dy);
+    TZ[o] = __dmul_rn(f, dz);
+}
+
+// Adds a chunk's terms in ascending j onto each target's running sum.
+__global__ void k_exact_sum(size_t n, size_t j0, int C, const double *__restrict__ TX,
+                            const double *__restrict__ TY, const double *__restrict__ TZ, double *__restrict__ S) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double sx = S[i], sy = S[n + i], sz = S[2 * n + i];
+    for (int jj = 0; jj < C; ++jj) {
+        if (j0 + (size_t)jj == i) continue;
+        const size_t o = (size_t)jj * n + i;
+        sx = __dadd_rn(sx, TX[o]);
+        sy = __dadd_rn(sy, TY[o]);
+        sz = __dadd_rn(sz, TZ[o]);
+    }
+    S[i] = sx; S[n + i] = sy; S[2 * n + i] = sz;
+}
+
+__global__ void k_exact_store(size_t n, const double *__restrict__ S, double *__restrict__ AX,
+                              double *__restrict__ AY, double *__restrict__ AZ, int accumulate) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (accumulate) {
+        AX[i] = __dadd_rn(AX[i], S[i]); AY[i] = __dadd_rn(AY[i], S[n + i]); AZ[i] = __dadd_rn(AZ[i], S[2 * n + i]);
+    } else {
+        AX[i] = S[i]; AY[i] = S[n + i]; AZ[i] = S[2 * n + i];
+    }
+}
+
 constexpr int EX_NT = 128;
 
 __global__ void __launch_bounds__(EX_NT) k_direct_exact(const double *__restrict__ X, const double *__restrict__ Y,
@@ -1451,10 +1509,31 @@ gvs_status direct_forces(Ctx *c, int precision, double eps, bool accumulate) {
     const double eps2 = eps * eps;
     if (precision == GVS_PREC_FP64_EXACT) {
         if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], c->stream));
-        k_direct_exact<<<ceil_div((long long)n, EX_NT), EX_NT, 0, c->stream>>>(
-            as<double>(c->x), as<double>(c->y), as<double>(c->z), as<double>(c->m), n, eps2, as<double>(c->ax),
-            as<double>(c->ay), as<double>(c->az), accumulate ? 1 : 0, nullptr, 0);
-        c->prof.launches += 1;
+        if (n <= EXACT_SPLIT_MAX) {
+            const int C = (int)std::max<size_t>(1, std::min<size_t>(n, EXACT_TERMS_BYTES / (24 * n)));
+            GVS_CUDA(c, ensure(c, c->exact_terms, (size_t)C * n * 24));
+            GVS_CUDA(c, ensure(c, c->exact_sums, n * 24));
+            GVS_CUDA(c, cudaMemsetAsync(c->exact_sums.ptr, 0, n * 24, c->stream));
+            double *T = as<double>(c->exact_terms);
+            for (size_t j0 = 0; j0 < n; j0 += (size_t)C) {
+                const int cc = (int)std::min<size_t>((size_t)C, n - j0);
+                k_exact_terms<<<dim3(ceil_div((long long)n, 128), cc), 128, 0, c->stream>>>(
+                    as<double>(c->x), as<double>(c->y), as<double>(c->z), as<double>(c->m), n, j0, eps2, T,
+                    T + (size_t)cc * n, T + 2 * (size_t)cc * n);
+                k_exact_sum<<<ceil_div((long long)n, 32), 32, 0, c->stream>>>(
+                    n, j0, cc, T, T + (size_t)cc * n, T + 2 * (size_t)cc * n, as<double>(c->exact_sums));
+                c->prof.launches += 2;
+            }
+            k_exact_store<<<ceil_div((long long)n, 256), 256, 0, c->stream>>>(
+                n, as<double>(c->exact_sums), as<double>(c->ax), as<double>(c->ay), as<double>(c->az),
+                accumulate ? 1 : 0);
+            c->prof.launches += 1;
+        } else {
+            k_direct_exact<<<ceil_div((long long)n, EX_NT), EX_NT, 0, c->stream>>>(
+                as<double>(c->x), as<double>(c->y), as<double>(c->z), as<double>(c->m), n, eps2, as<double>(c->ax),
+                as<double>(c->ay), as<double>(c->az), accumulate ? 1 : 0, nullptr, 0);
+            c->prof.launches += 1;
+        }
         GVS_TRY(check_launch(c, "direct exact kernel"));
         if (c->prof.on) {
             GVS_CUDA(c, cudaEventRecord(c->prof.ev[1], c->stream));

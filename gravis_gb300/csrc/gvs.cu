@@ -250,6 +250,7 @@ gvs_status gvs_destroy(gvs_ctx *c) {
     DevBuf *all[] = {&c->x, &c->y, &c->z, &c->vx, &c->vy, &c->vz, &c->ax, &c->ay, &c->az, &c->m,
                      &c->ptype, &c->u, &c->h, &c->alpha, &c->rho, &c->pres, &c->cs, &c->du_dt, &c->omega,
                      &c->div_v, &c->max_mu, &c->dalpha_dt, &c->keys, &c->keys_alt, &c->perm, &c->perm_alt,
+                     &c->exact_terms, &c->exact_sums,
                      &c->sort_hist, &c->bbox_part, &c->jpack32, &c->jpack64, &c->partial, &c->scratch_a,
                      &c->scratch_b, &c->err_word, &c->red_part, &c->l2_flush};
     for (DevBuf *b : all)

@@ -97,6 +97,7 @@ struct Ctx {
     // direct-sum scratch
     DevBuf keys, keys_alt, perm, perm_alt, sort_hist, bbox_part;
     DevBuf jpack32, jpack64, partial;
+    DevBuf exact_terms, exact_sums;  // FP64_EXACT for small systems: a source chunk's terms, running sums
     // generic scratch
     DevBuf scratch_a, scratch_b, err_word, red_part, l2_flush;
 
