@@ -1217,7 +1217,8 @@ __global__ void k_exact_terms(const double *__restrict__ X, const double *__rest
     TZ[o] = __dmul_rn(f, dz);
 }
 
-// Adds a chunk's terms in ascending j onto each target's running sum.
+// Adds a chunk's terms in ascending j onto each target's running sum (launched as
+// 8-thread blocks: a thousand serial sums then spread over 125 SMs' f64 pipes).
 __global__ void k_exact_sum(size_t n, size_t j0, int C, const double *__restrict__ TX,
                             const double *__restrict__ TY, const double *__restrict__ TZ, double *__restrict__ S) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1520,7 +1521,7 @@ gvs_status direct_forces(Ctx *c, int precision, double eps, bool accumulate) {
                 k_exact_terms<<<dim3(ceil_div((long long)n, 128), cc), 128, 0, c->stream>>>(
                     as<double>(c->x), as<double>(c->y), as<double>(c->z), as<double>(c->m), n, j0, eps2, T,
                     T + (size_t)cc * n, T + 2 * (size_t)cc * n);
-                k_exact_sum<<<ceil_div((long long)n, 32), 32, 0, c->stream>>>(
+                k_exact_sum<<<ceil_div((long long)n, 8), 8, 0, c->stream>>>(
                     n, j0, cc, T, T + (size_t)cc * n, T + 2 * (size_t)cc * n, as<double>(c->exact_sums));
                 c->prof.launches += 2;
             }
