@@ -89,6 +89,7 @@ SIGNATURES = {
     "gvs_ic_plummer": (_ST, [_sz, _u64, _d, _d] + [_P] * 7),
     "gvs_ic_two_body": (_ST, [_d, _d, _d] + [_P] * 7),
     "gvs_ic_evrard": (_ST, [_sz, _u64, _d, _d, _d] + [_P] * 6),
+    "gvs_ic_cold_collapse": (_ST, [_sz, _u64, _d, _d, _i] + [_P] * 9),
     "gvs_ic_collision": (_ST, [_sz, _u64, _d] + [_P] * 7),
     "gvs_ic_gas_sphere_1r": (_ST, [_sz, _d, _d, _d, _d] + [_P] * 6),
     "gvs_ic_ensemble_sizes": (_ST, [_sz, _u64, _d, _d, _P]),

@@ -16,6 +16,7 @@
 //   Plummer        PlummerSphere::generate (scenarios/plummer_sphere.rs:106-133)
 //   two-body       TwoBody::generate (scenarios/two_body.rs:49-94)
 //   Evrard         EvrardCollapse::generate (scenarios/evrard_collapse.rs:45-57)
+//   cold collapse  ColdCollapse::generate (scenarios/cold_collapse.rs:60-101)
 //   collision      two Plummer spheres on a parabolic head-on orbit (composed from
 //                  sample_plummer_particle like galaxy_collision.rs:94-155)
 //   gas sphere 1/r a seedless stretched, perturbed lattice with rho ~ 1/r
@@ -198,6 +199,52 @@ gvs_status gvs_ic_evrard(size_t n, uint64_t seed, double total_mass, double radi
             ++count;
         }
     }
+    return GVS_OK;
+}
+
+// ColdCollapse::generate (scenarios/cold_collapse.rs:60-101): at rest, uniform in a
+// sphere of radius R.  Gravity-only: per particle, x, y, z ~ U[-1, 1) until inside
+// the unit sphere, scaled by R.  Gas: fill_uniform_gas_sphere (mod.rs:33-52) with
+// u = 0.05 and h = 1.5 x the mean spacing.  Then the COM frame.
+gvs_status gvs_ic_cold_collapse(size_t n, uint64_t seed, double radius, double total_mass, int sph, double *x,
+                                double *y, double *z, double *vx, double *vy, double *vz, double *mass, double *u,
+                                double *h) {
+    if (n == 0 || !x || !y || !z || !vx || !vy || !vz || !mass || !(radius > 0.0) || !(total_mass > 0.0) ||
+        (sph && (!u || !h)))
+        return GVS_ERR_INVALID_ARG;
+    ChaCha20Rng rng(seed);
+    const double m = total_mass / (double)n;
+    if (sph) {
+        const double vol = 4.0 / 3.0 * PI * (radius * radius * radius);
+        const double hh = 1.5 * cbrt(vol / (double)n);
+        size_t count = 0;
+        while (count < n) {
+            const double px = rng.uniform() * 2.0 * radius - radius;
+            const double py = rng.uniform() * 2.0 * radius - radius;
+            const double pz = rng.uniform() * 2.0 * radius - radius;
+            if (px * px + py * py + pz * pz <= radius * radius) {
+                x[count] = px; y[count] = py; z[count] = pz;
+                u[count] = 0.05; h[count] = hh;
+                ++count;
+            }
+        }
+    } else {
+        for (size_t i = 0; i < n; ++i) {
+            double px, py, pz;
+            for (;;) {
+                px = rng.range(-1.0, 1.0);
+                py = rng.range(-1.0, 1.0);
+                pz = rng.range(-1.0, 1.0);
+                if (px * px + py * py + pz * pz <= 1.0) break;
+            }
+            x[i] = px * radius; y[i] = py * radius; z[i] = pz * radius;
+        }
+    }
+    for (size_t i = 0; i < n; ++i) {
+        vx[i] = vy[i] = vz[i] = 0.0;
+        mass[i] = m;
+    }
+    com_frame(n, x, y, z, vx, vy, vz, mass);
     return GVS_OK;
 }
 

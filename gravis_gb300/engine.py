@@ -642,6 +642,37 @@ class EvrardCollapse:
         return math.pi / 2 * math.sqrt(self.radius ** 3 / (2.0 * self.total_mass)) / 500.0
 
 
+class ColdCollapse:
+    """scenarios/cold_collapse.rs:26-123: particles at rest, uniform in a sphere (gas if sph)."""
+
+    def __init__(self, n: int = 5000, radius: float = 1.0, total_mass: float = 1.0, seed: int = 42,
+                 sph: bool = False):
+        self.n, self.radius, self.total_mass, self.seed, self.sph = n, radius, total_mass, seed, sph
+
+    def name(self) -> str:
+        return "Cold Collapse (Gas)" if self.sph else "Cold Collapse"
+
+    def generate(self) -> Particles:
+        p = Particles(self.n)
+        check(L.load().gvs_ic_cold_collapse(self.n, self.seed, self.radius, self.total_mass, 1 if self.sph else 0,
+                                            _ptr(p.x), _ptr(p.y), _ptr(p.z), _ptr(p.vx), _ptr(p.vy), _ptr(p.vz),
+                                            _ptr(p.mass), _ptr(p.internal_energy), _ptr(p.smoothing_length)))
+        if self.sph:
+            p.particle_type[:] = GAS
+            p.alpha_visc[:] = 1.0
+        return p
+
+    def suggested_dt(self) -> float:
+        """Free-fall time pi/2 sqrt(R^3 / (2 G M)) over 200 (gas: 500)."""
+        t_ff = (math.pi / 2) * math.sqrt((self.radius * self.radius * self.radius) / (2.0 * 1.0 * self.total_mass))
+        return t_ff / 500.0 if self.sph else t_ff / 200.0
+
+    def suggested_softening(self) -> float:
+        """0.3 x the mean spacing (4/3 pi R^3 / n)^(1/3)."""
+        r3 = self.radius * self.radius * self.radius
+        return (4.0 / 3.0 * math.pi * r3 / self.n) ** (1.0 / 3.0) * 0.3
+
+
 def collision(n: int, seed: int = 7, separation: float = 20.0) -> Particles:
     """Two Plummer spheres on a parabolic head-on orbit (see gvs_ic_collision)."""
     p = Particles(n)

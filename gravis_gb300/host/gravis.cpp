@@ -352,4 +352,25 @@ double EvrardCollapse::suggested_softening() const {
     return 0.3 * std::cbrt(4.0 / 3.0 * M_PI * (radius * radius * radius) / (double)n_particles);
 }
 
+Particles ColdCollapse::generate() const {
+    Particles p(n);
+    ck(gvs_ic_cold_collapse(n, seed, radius, total_mass, sph ? 1 : 0, p.x.data(), p.y.data(), p.z.data(),
+                            p.vx.data(), p.vy.data(), p.vz.data(), p.mass.data(), p.internal_energy.data(),
+                            p.smoothing_length.data()),
+       nullptr);
+    if (sph) {
+        std::fill(p.particle_type.begin(), p.particle_type.end(), GAS);
+        std::fill(p.alpha_visc.begin(), p.alpha_visc.end(), 1.0);
+    }
+    return p;
+}
+// cold_collapse.rs:104-122: free-fall time over 200 (gas 500); 0.3 x (4/3 pi R^3 / n)^(1/3) by powf
+double ColdCollapse::suggested_dt() const {
+    const double t_ff = M_PI / 2.0 * std::sqrt(radius * radius * radius / (2.0 * 1.0 * total_mass));
+    return sph ? t_ff / 500.0 : t_ff / 200.0;
+}
+double ColdCollapse::suggested_softening() const {
+    return std::pow(4.0 / 3.0 * M_PI * (radius * radius * radius) / (double)n, 1.0 / 3.0) * 0.3;
+}
+
 }  // namespace gravis

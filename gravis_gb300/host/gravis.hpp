@@ -10,7 +10,7 @@
 //   step_with_sph                     crates/sim-core/src/sph/forces.rs:12-60
 //   Diagnostics, compute_diagnostics  crates/sim-core/src/diagnostics.rs:8-190
 //   PlummerSphere, TwoBody,           crates/sim-core/src/scenarios/{plummer_sphere,
-//   EvrardCollapse                      two_body,evrard_collapse}.rs
+//   EvrardCollapse, ColdCollapse        two_body,evrard_collapse,cold_collapse}.rs
 //
 // Names, argument meanings and the accumulate contract are sim-core's.  Every
 // numeric operation runs on the GPU through the C ABI; a failing call throws
@@ -203,6 +203,17 @@ struct EvrardCollapse {  // evrard_collapse.rs:15-71
     double total_mass = 1.0, radius = 1.0, u_0 = 0.05;
     uint64_t seed = 42;
     const char *name() const { return "Evrard Collapse"; }
+    Particles generate() const;
+    double suggested_dt() const;
+    double suggested_softening() const;
+};
+
+struct ColdCollapse {  // cold_collapse.rs:26-123
+    size_t n = 5000;
+    double radius = 1.0, total_mass = 1.0;
+    uint64_t seed = 42;
+    bool sph = false;
+    const char *name() const { return sph ? "Cold Collapse (Gas)" : "Cold Collapse"; }
     Particles generate() const;
     double suggested_dt() const;
     double suggested_softening() const;

@@ -297,6 +297,13 @@ gvs_status gvs_ic_two_body(double mass_ratio, double e, double a, double *x, dou
  * sphere by cube rejection; outputs positions, mass, u and h (velocities are zero). */
 gvs_status gvs_ic_evrard(size_t n, uint64_t seed, double total_mass, double radius, double u0, double *x, double *y,
                          double *z, double *mass, double *u, double *h);
+/* ColdCollapse::generate (scenarios/cold_collapse.rs:60-101): n particles at rest, uniform
+ * in a sphere of `radius`, COM frame.  sph != 0: gas particles (fill_uniform_gas_sphere,
+ * mod.rs:33-52; u = 0.05, h = 1.5 x mean spacing, written to u and h); else u and h may be
+ * NULL.  Outputs have length n. */
+gvs_status gvs_ic_cold_collapse(size_t n, uint64_t seed, double radius, double total_mass, int sph, double *x,
+                                double *y, double *z, double *vx, double *vy, double *vz, double *mass, double *u,
+                                double *h);
 /* Two Plummer spheres (n/2 each, total mass 1, scale radius 1) from one ChaCha20 stream,
  * `separation` apart on x, parabolic head-on approach, COM frame (composed from
  * sample_plummer_particle, plummer_sphere.rs:13-58, as galaxy_collision.rs:94-155 does). */

@@ -79,6 +79,9 @@ def lib():
             "orc_two_body_suggested_softening": (d, [d, d]),
             "orc_evrard_generate": (None, [P, i64, d, d, d, u64]),
             "orc_evrard_suggested_softening": (d, [i64, d]),
+            "orc_cold_collapse_generate": (None, [P, i64, d, d, u64, C.c_int]),
+            "orc_cold_collapse_suggested_dt": (d, [d, d, C.c_int]),
+            "orc_cold_collapse_suggested_softening": (d, [i64, d]),
             "orc_shift_to_com_frame": (None, [P]),
             "orc_bf_serial": (None, [P, d]),
             "orc_bf_gather": (None, [P, d, i32]),
@@ -186,6 +189,20 @@ def evrard(n: int, seed: int = 42, total_mass: float = 1.0, radius: float = 1.0,
     p = Particles(n)
     lib().orc_evrard_generate(p.c(), n, total_mass, radius, u0, seed)
     return p
+
+
+def cold_collapse(n: int, seed: int = 42, radius: float = 1.0, total_mass: float = 1.0, sph: bool = False) -> Particles:
+    p = Particles(n)
+    lib().orc_cold_collapse_generate(p.c(), n, radius, total_mass, seed, 1 if sph else 0)
+    return p
+
+
+def cold_collapse_suggested_dt(radius: float = 1.0, total_mass: float = 1.0, sph: bool = False) -> float:
+    return lib().orc_cold_collapse_suggested_dt(radius, total_mass, 1 if sph else 0)
+
+
+def cold_collapse_suggested_softening(n: int, radius: float = 1.0) -> float:
+    return lib().orc_cold_collapse_suggested_softening(n, radius)
 
 
 # ---- solvers -----------------------------------------------------------------

@@ -289,6 +289,56 @@ void orc_evrard_generate(orc_particles *p, int64_t n, double total_mass, double 
     }
 }
 
+/* ColdCollapse::generate (cold_collapse.rs:60-101): at rest, uniform in a sphere.
+ * Gravity-only: per particle, draw x, y, z ~ U[-1, 1) until inside the unit sphere,
+ * scale by R.  Gas (sph): fill_uniform_gas_sphere (mod.rs:33-52) with u = 0.05 and
+ * h from sphere_spacing.  Then shift_to_com_frame. */
+void orc_cold_collapse_generate(orc_particles *p, int64_t n, double radius, double total_mass, uint64_t seed,
+                                int sph) {
+    orc_rng r;
+    orc_rng_seed_u64(&r, seed);
+    p->n = n;
+    double m = total_mass / (double)n;
+    if (sph) {
+        double vol, sp, h;
+        sphere_spacing(radius, n, &vol, &sp, &h);
+        int64_t count = 0;
+        while (count < n) {
+            double x = orc_rng_f64(&r) * 2.0 * radius - radius;
+            double y = orc_rng_f64(&r) * 2.0 * radius - radius;
+            double z = orc_rng_f64(&r) * 2.0 * radius - radius;
+            if (x * x + y * y + z * z <= radius * radius) {
+                set_gas(p, count, x, y, z, m, 0.05, h);
+                count++;
+            }
+        }
+    } else {
+        for (int64_t i = 0; i < n; ++i) {
+            double x, y, z;
+            for (;;) {
+                x = orc_rng_range(&r, -1.0, 1.0);
+                y = orc_rng_range(&r, -1.0, 1.0);
+                z = orc_rng_range(&r, -1.0, 1.0);
+                if (x * x + y * y + z * z <= 1.0) break;
+            }
+            set_particle(p, i, x * radius, y * radius, z * radius, 0.0, 0.0, 0.0, m);
+        }
+    }
+    orc_shift_to_com_frame(p);
+}
+
+/* cold_collapse.rs:104-114: free-fall time / 200 (gravity) or / 500 (gas) */
+double orc_cold_collapse_suggested_dt(double radius, double total_mass, int sph) {
+    double t_ff = (ORC_PI / 2.0) * sqrt((radius * radius * radius) / (2.0 * 1.0 * total_mass));
+    return sph ? t_ff / 500.0 : t_ff / 200.0;
+}
+
+/* cold_collapse.rs:117-122: 0.3 x mean spacing, (4/3 pi R^3 / n)^(1/3) by powf */
+double orc_cold_collapse_suggested_softening(int64_t n, double radius) {
+    double s = pow(4.0 / 3.0 * ORC_PI * (radius * radius * radius) / (double)n, 1.0 / 3.0);
+    return s * 0.3;
+}
+
 /* evrard_collapse.rs:68-71 */
 double orc_evrard_suggested_softening(int64_t n, double radius) {
     double vol, sp, h;

@@ -60,6 +60,10 @@ double orc_two_body_period(double a);
 double orc_two_body_suggested_softening(double e, double a);
 void   orc_evrard_generate(orc_particles *p, int64_t n, double total_mass, double radius, double u0, uint64_t seed);
 double orc_evrard_suggested_softening(int64_t n, double radius);
+void   orc_cold_collapse_generate(orc_particles *p, int64_t n, double radius, double total_mass, uint64_t seed,
+                                  int sph);
+double orc_cold_collapse_suggested_dt(double radius, double total_mass, int sph);
+double orc_cold_collapse_suggested_softening(int64_t n, double radius);
 void   orc_shift_to_com_frame(orc_particles *p);
 
 /* ---- gravity ------------------------------------------------------------ */

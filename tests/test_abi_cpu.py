@@ -64,6 +64,34 @@ def test_two_body_and_evrard_ics_match_oracle(lib):
     assert np.array_equal(e.smoothing_length, f.h) and np.array_equal(e.internal_energy, f.u)
 
 
+@pytest.mark.parametrize("n,seed,sph", [(1, 5, False), (1000, 42, False), (777, 9, True), (5000, 42, True)])
+def test_cold_collapse_ics_match_oracle(lib, n, seed, sph):
+    """ColdCollapse (cold_collapse.rs:60-123): the library's arrays and suggested values equal
+    the oracle's restatement, for the gravity-only and the gas variant."""
+    s = G.ColdCollapse(n, radius=1.5, total_mass=2.0, seed=seed, sph=sph)
+    p = s.generate()
+    q = O.cold_collapse(n, seed, 1.5, 2.0, sph)
+    for f in ("x", "y", "z", "vx", "vy", "vz", "mass"):
+        assert np.array_equal(getattr(p, f), getattr(q, f)), f
+    if sph:
+        assert np.array_equal(p.smoothing_length, q.h) and np.array_equal(p.internal_energy, q.u)
+        assert (p.particle_type == G.engine.GAS).all()
+    assert not (p.vx.any() or p.vy.any() or p.vz.any())  # at rest; the COM velocity removed is zero
+    assert s.suggested_dt() == O.cold_collapse_suggested_dt(1.5, 2.0, sph)
+    assert s.suggested_softening() == O.cold_collapse_suggested_softening(n, 1.5)
+    # uniform sphere of radius 1.5 about the centre of mass
+    r = np.sqrt(p.x ** 2 + p.y ** 2 + p.z ** 2)
+    assert r.max() <= 2 * 1.5
+    assert s.name() == ("Cold Collapse (Gas)" if sph else "Cold Collapse")
+
+
+def test_cold_collapse_args_validated(lib):
+    x = np.zeros(4)
+    assert lib.gvs_ic_cold_collapse(4, 1, 1.0, 1.0, 1, *(x.ctypes.data,) * 7, None, None) == L.ERR_INVALID_ARG
+    assert lib.gvs_ic_cold_collapse(4, 1, -1.0, 1.0, 0, *(x.ctypes.data,) * 9) == L.ERR_INVALID_ARG
+    assert lib.gvs_ic_cold_collapse(4, 1, 1.0, 1.0, 0, *(x.ctypes.data,) * 7, None, None) == L.OK
+
+
 def test_collision_and_gas_sphere_ics(lib):
     p = G.collision(1000, seed=7)
     assert abs(p.total_mass() - 1.0) < 1e-12
