@@ -8,7 +8,8 @@
 // for the force paths, --device N, and --restart SNAPSHOT (continue from an
 // NBODY snapshot: its time, step, softening and dt; accelerations recomputed,
 // as Snapshot::initialize does).  Scenarios: plummer, two-body (kepler),
-// evrard-collapse; the others are outside the engine's scope.
+// cold-collapse, cold-collapse-gas, evrard-collapse; the others are outside the
+// engine's scope.
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -51,7 +52,8 @@ struct Cli {
 void usage() {
     std::printf(
         "gvs_headless: headless N-body runner on one GB300 (the counterpart of nbody-headless)\n"
-        "  -s, --scenario NAME        plummer | two-body | kepler | evrard-collapse (default plummer)\n"
+        "  -s, --scenario NAME        plummer | two-body | kepler | cold-collapse | cold-collapse-gas |\n"
+        "                             evrard-collapse (default plummer)\n"
         "  -n, --particles N          particle count (scenario default otherwise)\n"
         "      --steps N              timesteps (default 1000)\n"
         "      --dt DT                timestep (scenario suggestion otherwise)\n"
@@ -134,13 +136,20 @@ Built build(const Cli &c) {
         TwoBody s;
         s.eccentricity = c.eccentricity;
         b = {s.generate(), s.suggested_dt(), s.suggested_softening(), s.name()};
+    } else if (c.scenario == "cold-collapse" || c.scenario == "cold-collapse-gas") {
+        ColdCollapse s;
+        s.n = c.particles > 0 ? (size_t)c.particles : 5000;
+        s.sph = c.scenario == "cold-collapse-gas";
+        s.seed = c.seed;
+        b = {s.generate(), s.suggested_dt(), s.suggested_softening(), s.name()};
     } else if (c.scenario == "evrard-collapse") {
         EvrardCollapse s;
         s.n_particles = c.particles > 0 ? (size_t)c.particles : 5000;
         s.seed = c.seed;
         b = {s.generate(), s.suggested_dt(), s.suggested_softening(), s.name()};
     } else {
-        die("Unknown scenario: " + c.scenario + ". Available here: plummer, two-body, evrard-collapse");
+        die("Unknown scenario: " + c.scenario +
+            ". Available here: plummer, two-body, cold-collapse, cold-collapse-gas, evrard-collapse");
     }
     if (c.dt > 0.0) b.dt = c.dt;
     if (c.softening >= 0.0) b.softening = c.softening;

@@ -96,6 +96,24 @@ def test_headless_evrard_sph(built, tmp_path, precision):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("scenario,steps", [("cold-collapse", 100), ("cold-collapse-gas", 20)])
+def test_headless_cold_collapse(built, tmp_path, scenario, steps):
+    """scenario_builder's cold-collapse names run through the headless mirror: particles
+    start at rest (K = 0) and fall inward, conserving energy over the first steps."""
+    out = tmp_path / "cold.csv"
+    r = run("--scenario", scenario, "-n", "2000", "--steps", str(steps), "--diag-interval", str(steps // 2),
+            "--diag-csv", str(out))
+    assert r.returncode == 0, r.stderr
+    rows = read_csv(out)
+    assert [int(x["step"]) for x in rows] == [0, steps // 2, steps]
+    assert float(rows[0]["kinetic_energy"]) == 0.0
+    assert float(rows[-1]["kinetic_energy"]) > 0.0
+    e0, e1 = float(rows[0]["total_energy"]), float(rows[-1]["total_energy"])
+    assert abs((e1 - e0) / e0) < 1e-2
+    assert (float(rows[0]["thermal_energy"]) > 0.0) == (scenario == "cold-collapse-gas")
+
+
+@pytest.mark.gpu
 def test_drop_in_classes_match_resident_path(built):
     r = subprocess.run([CHECK], capture_output=True, text=True, timeout=600)
     print(r.stdout)
