@@ -1219,12 +1219,30 @@ __global__ void k_exact_terms(const double *__restrict__ X, const double *__rest
 
 // Adds a chunk's terms in ascending j onto each target's running sum (launched as
 // 8-thread blocks: a thousand serial sums then spread over 125 SMs' f64 pipes).
+// The sum is a serial chain, so its loads are issued 16 terms ahead of it.
 __global__ void k_exact_sum(size_t n, size_t j0, int C, const double *__restrict__ TX,
                             const double *__restrict__ TY, const double *__restrict__ TZ, double *__restrict__ S) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double sx = S[i], sy = S[n + i], sz = S[2 * n + i];
-    for (int jj = 0; jj < C; ++jj) {
+    constexpr int B = 16;  // terms loaded together, then added one by one in order
+    int jj = 0;
+    for (; jj + B <= C; jj += B) {
+        double tx[B], ty[B], tz[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const size_t o = (size_t)(jj + u) * n + i;
+            tx[u] = TX[o]; ty[u] = TY[o]; tz[u] = TZ[o];
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            if (j0 + (size_t)(jj + u) == i) continue;
+            sx = __dadd_rn(sx, tx[u]);
+            sy = __dadd_rn(sy, ty[u]);
+            sz = __dadd_rn(sz, tz[u]);
+        }
+    }
+    for (; jj < C; ++jj) {
         if (j0 + (size_t)jj == i) continue;
         const size_t o = (size_t)jj * n + i;
         sx = __dadd_rn(sx, TX[o]);
