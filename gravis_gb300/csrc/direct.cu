@@ -188,6 +188,37 @@ __global__ void __launch_bounds__(1024) k_small_order(const double *__restrict__
         idx[i] = (uint32_t)i;
     }
     __syncthreads();
+    if (P == (int)blockDim.x) {
+        // one element per thread: stages whose partner is in the same warp (j < 32)
+        // exchange through registers; the others through shared memory
+        uint64_t mk = key[tid];
+        uint32_t mi = idx[tid];
+        for (int k = 2; k <= P; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                uint64_t pk_;
+                uint32_t pi_;
+                if (j >= 32) {
+                    __syncthreads();
+                    key[tid] = mk;
+                    idx[tid] = mi;
+                    __syncthreads();
+                    pk_ = key[tid ^ j];
+                    pi_ = idx[tid ^ j];
+                } else {
+                    pk_ = __shfl_xor_sync(0xFFFFFFFFu, mk, j);
+                    pi_ = __shfl_xor_sync(0xFFFFFFFFu, mi, j);
+                }
+                const bool mine_gt = mk > pk_ || (mk == pk_ && mi > pi_);
+                const bool lower = (tid & j) == 0, asc = (tid & k) == 0;
+                // the lower slot keeps the smaller pair in an ascending run, the larger in a descending one
+                if ((lower == asc) == mine_gt) {
+                    mk = pk_;
+                    mi = pi_;
+                }
+            }
+        if (tid < n) perm[tid] = mi;
+        return;
+    }
     for (int k = 2; k <= P; k <<= 1)
         for (int j = k >> 1; j > 0; j >>= 1) {
             for (int i = tid; i < P; i += blockDim.x) {
@@ -1338,12 +1369,13 @@ gvs_status spatial_order(Ctx *c) {
     const size_t n = c->n;
     if (n <= (size_t)SMALL_ORDER_MAX) {
         GVS_CUDA(c, ensure(c, c->perm, n * 4));
-        int P = 1;
+        int P = 32;
         while (P < (int)n) P <<= 1;
         const int smem = P * (int)(sizeof(uint64_t) + sizeof(uint32_t));
         set_smem(k_small_order, smem);
-        k_small_order<<<1, 1024, smem, c->stream>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z), (int)n, P,
-                                                    as<uint32_t>(c->perm));
+        // up to 1024 particles: one thread per padded slot (register stages); beyond, 1024 threads
+        k_small_order<<<1, std::min(P, 1024), smem, c->stream>>>(as<double>(c->x), as<double>(c->y),
+                                                                 as<double>(c->z), (int)n, P, as<uint32_t>(c->perm));
         c->prof.launches += 1;
         return check_launch(c, "small-system order");
     }
