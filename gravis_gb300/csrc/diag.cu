@@ -6,7 +6,8 @@
 // so repeated calls agree bit for bit.  The O(N^2) softened potential
 // U = -sum_{i<j} m_i m_j / sqrt(r_ij^2 + eps^2) is an all-pairs f64 kernel:
 // each target i sums j > i in ascending j (the reference's inner loop), and
-// the per-target partial sums are added in a fixed tree order.
+// the per-target partial sums are added in a fixed tree order.  Up to 16384
+// particles the pairs run on a 2D grid of target blocks and source tiles.
 #include "gvs_internal.cuh"
 
 namespace gvs {
@@ -86,6 +87,49 @@ __global__ void __launch_bounds__(RNT) k_potential(size_t n, const double *__res
     if (threadIdx.x == 0) part[blockIdx.x] = s[0];
 }
 
+// Small systems: the same pair terms over a 2D grid of (64-target block, 64-source
+// tile) so that a thousand particles occupy a hundred SMs instead of four.  Tiles
+// wholly below the diagonal (every j <= i) add nothing; each block writes one
+// partial, summed on the host in a fixed order.
+constexpr int PNT = 64;
+constexpr size_t POT2D_MAX = 16384;
+
+__global__ void __launch_bounds__(PNT) k_potential2d(size_t n, const double *__restrict__ x,
+                                                     const double *__restrict__ y, const double *__restrict__ z,
+                                                     const double *__restrict__ m, double eps2,
+                                                     double *__restrict__ part) {
+    __shared__ double4 tile[PNT];
+    __shared__ double s[PNT];
+    const size_t bi = blockIdx.x, bj = blockIdx.y;
+    double acc = 0.0;
+    if (bj >= bi) {  // whole block takes the same branch
+        const size_t i = bi * PNT + threadIdx.x;
+        const bool active = i < n;
+        const double xi = active ? x[i] : 0.0, yi = active ? y[i] : 0.0, zi = active ? z[i] : 0.0;
+        const double mi = active ? m[i] : 0.0;
+        const size_t j0 = bj * PNT, jl = j0 + threadIdx.x;
+        tile[threadIdx.x] = jl < n ? make_double4(x[jl], y[jl], z[jl], m[jl]) : make_double4(0.0, 0.0, 0.0, 0.0);
+        __syncthreads();
+        const int jn = (int)min((size_t)PNT, n - j0);
+        for (int jj = 0; jj < jn; ++jj) {
+            const size_t j = j0 + jj;
+            if (j <= i) continue;
+            const double4 q = tile[jj];
+            const double dx = q.x - xi, dy = q.y - yi, dz = q.z - zi;
+            const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+            acc -= mi * q.w / sqrt(r2);
+        }
+        if (!active) acc = 0.0;
+    }
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = PNT / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[bi * gridDim.y + bj] = s[0];
+}
+
 }  // namespace
 
 gvs_status diagnostics(Ctx *c, double eps, int with_potential, gvs_diag *out) {
@@ -93,7 +137,9 @@ gvs_status diagnostics(Ctx *c, double eps, int with_potential, gvs_diag *out) {
     memset(out, 0, sizeof(*out));
     if (n == 0) return GVS_OK;
     const int nb = std::max(1, std::min(c->num_sms * 2, ceil_div((long long)n, RNT)));
-    const int npb = ceil_div((long long)n, RNT);
+    const bool pot2d = n <= POT2D_MAX;
+    const int nt2 = ceil_div((long long)n, PNT);
+    const int npb = pot2d ? nt2 * nt2 : ceil_div((long long)n, RNT);
     const size_t need = ((size_t)nb * NQ + (with_potential ? (size_t)npb : 0)) * sizeof(double);
     GVS_CUDA(c, ensure(c, c->red_part, need));
     double *part = as<double>(c->red_part);
@@ -103,8 +149,13 @@ gvs_status diagnostics(Ctx *c, double eps, int with_potential, gvs_diag *out) {
     c->prof.launches += 1;
     GVS_TRY(check_launch(c, "diagnostic sums"));
     if (with_potential) {
-        k_potential<<<npb, RNT, 0, c->stream>>>(n, as<double>(c->x), as<double>(c->y), as<double>(c->z),
-                                                as<double>(c->m), eps * eps, part + (size_t)nb * NQ);
+        if (pot2d)
+            k_potential2d<<<dim3(nt2, nt2), PNT, 0, c->stream>>>(n, as<double>(c->x), as<double>(c->y),
+                                                                 as<double>(c->z), as<double>(c->m), eps * eps,
+                                                                 part + (size_t)nb * NQ);
+        else
+            k_potential<<<npb, RNT, 0, c->stream>>>(n, as<double>(c->x), as<double>(c->y), as<double>(c->z),
+                                                    as<double>(c->m), eps * eps, part + (size_t)nb * NQ);
         c->prof.launches += 1;
         GVS_TRY(check_launch(c, "potential"));
     }
