@@ -37,6 +37,8 @@ def test_null_context_is_invalid_arg(lib):
     d = L.Diag()
     assert lib.gvs_diagnostics(None, 0.01, 1, C.byref(d)) == L.ERR_INVALID_ARG
     assert lib.gvs_create(None, 0) == L.ERR_INVALID_ARG
+    assert lib.gvs_set_bh_walk(None, 64, 0) == L.ERR_INVALID_ARG
+    assert lib.gvs_set_direct_shape(None, 256, 4, 2, 2) == L.ERR_INVALID_ARG
 
 
 def test_ic_args_validated(lib):
