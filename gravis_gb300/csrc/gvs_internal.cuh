@@ -308,8 +308,6 @@ __device__ __forceinline__ uint64_t hilbert_key(uint32_t x0, uint32_t x1, uint32
 // subsystem entry points (defined in the .cu files)
 // ---------------------------------------------------------------------------
 // sort.cu
-gvs_status radix_sort_u32(Ctx *c, uint32_t *keys, uint32_t *vals, uint32_t *keys_alt, uint32_t *vals_alt, size_t n,
-                          int begin_bit, int end_bit, uint32_t **keys_out, uint32_t **vals_out);
 gvs_status radix_sort_u64(Ctx *c, uint64_t *keys, uint32_t *vals, uint64_t *keys_alt, uint32_t *vals_alt, size_t n,
                           int begin_bit, int end_bit, uint64_t **keys_out, uint32_t **vals_out);
 gvs_status exclusive_scan_u32(Ctx *c, const uint32_t *in, uint32_t *out, size_t n, uint32_t *total_dev);
@@ -327,7 +325,6 @@ void set_direct_shape(Ctx *c, int nthreads, int ipt, int minb, int unroll);
 gvs_status autotune_direct(Ctx *c, int precision, double eps, int *best_nt, int *best_ipt, double *best_ms);
 // kdk.cu
 gvs_status kick(Ctx *c, double half_dt);
-gvs_status drift(Ctx *c, double dt);
 gvs_status kick_drift(Ctx *c, double half_dt, double dt);
 gvs_status clear_acc(Ctx *c);
 // diag.cu

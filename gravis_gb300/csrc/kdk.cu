@@ -21,16 +21,6 @@ __global__ void k_kick(size_t n, double h, const double *__restrict__ ax, const 
     }
 }
 
-__global__ void k_drift(size_t n, double dt, const double *__restrict__ vx, const double *__restrict__ vy,
-                        const double *__restrict__ vz, double *__restrict__ x, double *__restrict__ y,
-                        double *__restrict__ z) {
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        x[i] = __dadd_rn(x[i], __dmul_rn(vx[i], dt));
-        y[i] = __dadd_rn(y[i], __dmul_rn(vy[i], dt));
-        z[i] = __dadd_rn(z[i], __dmul_rn(vz[i], dt));
-    }
-}
-
 // v += a*h; x += v*dt; a = 0 (the clear_accelerations that precedes the force call).
 __global__ void k_kick_drift(size_t n, double h, double dt, double *__restrict__ ax, double *__restrict__ ay,
                              double *__restrict__ az, double *__restrict__ vx, double *__restrict__ vy,
@@ -63,16 +53,6 @@ gvs_status kick(Ctx *c, double half_dt) {
                                                      as<double>(c->vz));
     c->prof.launches += 1;
     return check_launch(c, "kick");
-}
-
-gvs_status drift(Ctx *c, double dt) {
-    if (c->n == 0) return GVS_OK;
-    c->pos_version++;
-    k_drift<<<grid_for(c, c->n), 256, 0, c->stream>>>(c->n, dt, as<double>(c->vx), as<double>(c->vy),
-                                                      as<double>(c->vz), as<double>(c->x), as<double>(c->y),
-                                                      as<double>(c->z));
-    c->prof.launches += 1;
-    return check_launch(c, "drift");
 }
 
 gvs_status kick_drift(Ctx *c, double half_dt, double dt) {

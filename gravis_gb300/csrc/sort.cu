@@ -138,11 +138,6 @@ gvs_status radix_sort_impl(Ctx *c, K *keys, uint32_t *vals, K *keys_alt, uint32_
 }
 }  // namespace
 
-gvs_status radix_sort_u32(Ctx *c, uint32_t *keys, uint32_t *vals, uint32_t *keys_alt, uint32_t *vals_alt, size_t n,
-                          int begin_bit, int end_bit, uint32_t **keys_out, uint32_t **vals_out) {
-    return radix_sort_impl<uint32_t>(c, keys, vals, keys_alt, vals_alt, n, begin_bit, end_bit, keys_out, vals_out);
-}
-
 gvs_status radix_sort_u64(Ctx *c, uint64_t *keys, uint32_t *vals, uint64_t *keys_alt, uint32_t *vals_alt, size_t n,
                           int begin_bit, int end_bit, uint64_t **keys_out, uint32_t **vals_out) {
     return radix_sort_impl<uint64_t>(c, keys, vals, keys_alt, vals_alt, n, begin_bit, end_bit, keys_out, vals_out);
