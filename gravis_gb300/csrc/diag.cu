@@ -10,6 +10,9 @@
 // particles the pairs run on a 2D grid of target blocks and source tiles.
 #include "gvs_internal.cuh"
 
+#include <atomic>
+#include <mutex>
+
 namespace gvs {
 namespace {
 
@@ -193,10 +196,9 @@ gvs_status diagnostics(Ctx *c, double eps, int with_potential, gvs_diag *out) {
 //
 // Some callers cannot allocate device memory: a host that owns every device
 // byte through its own allocator (a game or visualisation engine, an ML
-// framework's caching allocator, a Rust host with an arena), code that runs
-// while a CUDA graph is being captured (cudaMalloc is not allowed during
-// capture), or a real-time loop where an allocation's implicit device
-// synchronisation is not acceptable.  For them the reductions below use a
+// framework's caching allocator, a Rust host with an arena), or a real-time
+// loop where an allocation's implicit device synchronisation is not
+// acceptable.  For them the reductions below use a
 // fixed scratch array that lives in the library image: a file-scope
 // __device__ array that every GPU which loads the library holds until the
 // process exits.  The caller passes device pointers for the inputs; nothing
@@ -213,13 +215,30 @@ constexpr size_t NOALLOC_SCRATCH_DOUBLES =
 // Shared by every call on a device; holds the last call's partial sums.
 static __device__ __align__(256) double g_diag_scratch[NOALLOC_SCRATCH_DOUBLES];
 
-// Device address of g_diag_scratch per device, looked up once per device.
+// Device address of g_diag_scratch and SM count, per device, looked up once per
+// device.  The pointer is published (release) after the SM count is written, and
+// the look-up runs under a mutex, so host threads making their first call on the
+// same device at the same time see a complete set-up.
 constexpr int NOALLOC_MAX_DEVICES = 64;
-static double *g_diag_scratch_ptr[NOALLOC_MAX_DEVICES] = {nullptr};
+static std::atomic<double *> g_diag_scratch_ptr[NOALLOC_MAX_DEVICES];
 static int g_diag_sms[NOALLOC_MAX_DEVICES] = {0};
+static std::mutex g_diag_setup_mu;
 
-// Adds the partial sums in the same order as gvs_diagnostics does on the host
-// (blocks in order, then potential blocks in order), so both agree bit for bit.
+// Restores the calling thread's current device on every return path.
+struct DeviceGuard {
+    int saved = -1;
+    DeviceGuard() {
+        if (cudaGetDevice(&saved) != cudaSuccess) saved = -1;
+    }
+    ~DeviceGuard() {
+        if (saved >= 0) cudaSetDevice(saved);
+    }
+};
+
+// Adds the partial sums in a fixed order (blocks in order, then potential
+// blocks in order), so repeated calls agree bit for bit.  gvs_diagnostics sums
+// the potential of small systems over a different block layout, so the two
+// entry points agree within f64 rounding (1e-12 relative), not bit for bit.
 __global__ void k_sums_final(const double *__restrict__ part, int nb, int npb, double *__restrict__ out) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     for (int k = 0; k < NQ; ++k) {
@@ -251,19 +270,25 @@ extern "C" gvs_status gvs_diagnostics_noalloc(int device, void *stream, size_t n
         return fail(nullptr, GVS_ERR_INVALID_ARG, "gvs_diagnostics_noalloc: device %d out of range", device);
     memset(out, 0, sizeof(*out));
     if (n == 0) return GVS_OK;
+    DeviceGuard guard;  // the caller's current device is restored on return
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
-    if (!g_diag_scratch_ptr[device]) {  // one-time set-up on this device (run it before any stream capture)
-        double *p = nullptr;
-        e = cudaGetSymbolAddress((void **)&p, g_diag_scratch);
-        if (e != cudaSuccess || !p) return cuda_fail(nullptr, e, "cudaGetSymbolAddress(g_diag_scratch)");
-        int sms = 0;
-        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-        if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaDeviceGetAttribute");
-        g_diag_sms[device] = sms;
-        g_diag_scratch_ptr[device] = p;
+    double *part = g_diag_scratch_ptr[device].load(std::memory_order_acquire);
+    if (!part) {  // one-time set-up on this device (make this first call before any stream capture)
+        std::lock_guard<std::mutex> lock(g_diag_setup_mu);
+        part = g_diag_scratch_ptr[device].load(std::memory_order_relaxed);
+        if (!part) {
+            double *p = nullptr;
+            e = cudaGetSymbolAddress((void **)&p, g_diag_scratch);
+            if (e != cudaSuccess || !p) return cuda_fail(nullptr, e, "cudaGetSymbolAddress(g_diag_scratch)");
+            int sms = 0;
+            e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+            if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaDeviceGetAttribute");
+            g_diag_sms[device] = sms;
+            g_diag_scratch_ptr[device].store(p, std::memory_order_release);
+            part = p;
+        }
     }
-    double *part = g_diag_scratch_ptr[device];
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int nb = std::max(1, std::min(std::min(g_diag_sms[device] * 2, NOALLOC_MAX_SUM_BLOCKS),
                                         ceil_div((long long)n, RNT)));

@@ -230,18 +230,21 @@ gvs_status gvs_sph_neighbors(gvs_ctx *ctx, size_t cap, size_t *total, uint32_t *
 
 /* Diagnostics of caller-owned device arrays WITHOUT ANY ALLOCATION.  No counterpart in
  * the reference.  For callers that cannot allocate device memory: a host whose own
- * allocator owns every device byte, code running while a CUDA graph is captured
- * (cudaMalloc is not allowed then), or a real-time loop that cannot afford the device
- * synchronisation an allocation implies.  x..mass (and ptype/u, which may both be NULL
- * for a gas-free system) are DEVICE pointers of length n on `device`; work is queued on
- * `stream` (a cudaStream_t, NULL for the legacy default stream) and the call waits for
- * it.  Results equal gvs_diagnostics on the same state.
+ * allocator owns every device byte (an engine or framework with its own memory pool),
+ * or a real-time loop that cannot afford the device synchronisation an allocation
+ * implies.  x..mass (and ptype/u, which may both be NULL for a gas-free system) are
+ * DEVICE pointers of length n on `device`; work is queued on `stream` (a cudaStream_t,
+ * NULL for the legacy default stream) and the call waits for it.  The calling thread's
+ * current device is restored on return.  Results agree with gvs_diagnostics on the same
+ * state within f64 rounding (1e-12 relative; small systems sum the potential over a
+ * different block layout there).
  * Scratch is a fixed ~270 KB array inside the library image that every GPU loading the
  * library keeps until the process exits; n above 4,194,304 is rejected with
  * GVS_ERR_INVALID_ARG.  The first call on a device looks the array's address up
  * (cudaGetSymbolAddress), so make that first call before any stream capture.  All calls
- * share the array: calls on one device that overlap on the GPU (other streams or other
- * host threads) race and must be serialised by the caller. */
+ * share the array and each overwrites what it reads: calls on one device that overlap on
+ * the GPU (other streams or other host threads) race and must be serialised by the
+ * caller. */
 gvs_status gvs_diagnostics_noalloc(int device, void *stream, size_t n, const double *x, const double *y,
                                    const double *z, const double *vx, const double *vy, const double *vz,
                                    const double *mass, const uint8_t *ptype, const double *u, double softening,

@@ -87,6 +87,7 @@ def lib():
             "orc_bf_gather": (None, [P, d, i32]),
             "orc_bf_gather_subset": (None, [P, d, C.c_void_p, i64, C.c_void_p, C.c_void_p, C.c_void_p, i32]),
             "orc_bh": (None, [P, d, d, i32]),
+            "orc_bh_subset": (None, [P, d, d, C.c_void_p, i64, C.c_void_p, C.c_void_p, C.c_void_p, i32]),
             "orc_gravity_apply": (None, [G, P]),
             "orc_kdk_step": (None, [P, G, d]),
             "orc_kdk_steps": (None, [P, G, d, i64]),
@@ -230,6 +231,15 @@ def bf_subset(p: Particles, softening: float, idx, nthreads: int = 0) -> np.ndar
 
 def bh(p: Particles, softening: float, theta: float, nthreads: int = 0):
     lib().orc_bh(p.c(), softening, theta, nthreads)
+
+
+def bh_subset(p: Particles, softening: float, theta: float, idx, nthreads: int = 0) -> np.ndarray:
+    """BarnesHut accelerations of the targets idx (the reference tree of all of p)."""
+    idx = np.ascontiguousarray(idx, dtype=np.int64)
+    out = np.zeros((3, len(idx)), dtype=np.float64)
+    lib().orc_bh_subset(p.c(), softening, theta, idx.ctypes.data, len(idx), out[0].ctypes.data,
+                        out[1].ctypes.data, out[2].ctypes.data, nthreads)
+    return out.T.copy()
 
 
 def kdk_step(p: Particles, g: _CGravity, dt: float):

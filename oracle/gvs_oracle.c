@@ -726,6 +726,31 @@ void orc_bh(orc_particles *p, double softening, double theta, int nthreads) {
     orc_octree_free(&t);
 }
 
+/* BarnesHut::compute_accelerations restricted to the targets idx[0..nidx)
+ * (barnes_hut.rs:139-192): the reference's tree of ALL particles
+ * (Octree::rebuild, octree.rs:156-164), walked by tree_walk_accel
+ * (barnes_hut.rs:44-108) for the listed targets only.  Writes (does not
+ * accumulate) out_ax..out_az[k] for target idx[k]. */
+void orc_bh_subset(const orc_particles *p, double softening, double theta, const int64_t *idx, int64_t nidx,
+                   double *oax, double *oay, double *oaz, int nthreads) {
+    if (p->n == 0 || nidx == 0) return;
+    orc_octree t = {0};
+    orc_octree_rebuild(&t, p);
+    double eps2 = softening * softening;
+    double theta2 = theta * theta;
+    (void)nthreads;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads_or_max(nthreads))
+    for (int64_t k = 0; k < nidx; ++k) {
+        const int64_t i = idx[k];
+        double acc[3];
+        bh_walk(&t, p->x[i], p->y[i], p->z[i], (uint32_t)i, eps2, theta2, acc);
+        oax[k] = acc[0];
+        oay[k] = acc[1];
+        oaz[k] = acc[2];
+    }
+    orc_octree_free(&t);
+}
+
 void orc_gravity_apply(const orc_gravity *g, orc_particles *p) {
     switch (g->kind) {
     case ORC_GRAV_BF: orc_bf_serial(p, g->softening); break;

@@ -77,6 +77,9 @@ void orc_bf_gather_subset(const orc_particles *p, double softening, const int64_
 
 /* BarnesHut::compute_accelerations (barnes_hut.rs:139-192), octree rebuilt per call. */
 void orc_bh(orc_particles *p, double softening, double theta, int nthreads);
+/* The reference tree of all particles, walked for the targets idx[0..nidx) only. */
+void orc_bh_subset(const orc_particles *p, double softening, double theta, const int64_t *idx, int64_t nidx,
+                   double *out_ax, double *out_ay, double *out_az, int nthreads);
 
 enum { ORC_GRAV_NONE = 0, ORC_GRAV_BF = 1, ORC_GRAV_BF_GATHER = 2, ORC_GRAV_BH = 3 };
 typedef struct orc_gravity {

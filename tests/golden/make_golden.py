@@ -7,7 +7,7 @@ The reference publishes three numeric artefacts produced by its own CPU code:
 This script copies their rows verbatim (as strings and parsed floats) into a
 JSON fixture so the tests can run where the reference is not mounted.
 
-Usage: python tests/golden/make_golden.py [path-to-gravis-checkout]
+Usage: python tests/golden/make_golden.py <path-to-gravis-checkout>
 """
 import csv
 import json
@@ -34,4 +34,6 @@ def main(root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path-to-gravis-checkout>")
+    main(sys.argv[1])

@@ -1,13 +1,15 @@
 """gvs_diagnostics_noalloc: the diagnostics entry point that allocates nothing.
 
 It exists for callers that cannot allocate device memory themselves -- hosts
-whose allocator owns all device memory, code running under CUDA graph
-capture, real-time loops -- and therefore hand the library device arrays they
-already own.  Its scratch is a fixed array inside the library.  This test
-calls it through the C ABI on device arrays and checks it against the
-allocating gvs_diagnostics on the same state, twice in a row (the fixed
-scratch keeps the previous call's contents, which must not leak into the
-next result).  It lives in its own file, collected last.
+whose own allocator owns all device memory, real-time loops that cannot
+afford an allocation's device synchronisation -- and therefore hand the
+library device arrays they already own.  Its scratch is a fixed array inside
+the library.  This test calls it through the C ABI on device arrays and checks
+it against the allocating gvs_diagnostics on the same state, two calls in a
+row per state, first on a larger system and then on a smaller one (the fixed
+scratch keeps the previous call's contents, which must not leak into the next
+result), once without the potential and once on a non-default stream.  It
+lives in its own file, collected last.
 """
 import ctypes as C
 
@@ -30,12 +32,25 @@ def _close(a, b):
     return abs(a - b) <= TOL * max(abs(b), 1e-300)
 
 
-def _check(d, e):
-    for f in ("kinetic_energy", "potential_energy", "thermal_energy", "total_energy", "virial_ratio"):
+def _check(d, e, with_potential=True):
+    fields = ["kinetic_energy", "thermal_energy"]
+    if with_potential:
+        fields += ["potential_energy", "total_energy", "virial_ratio"]
+    for f in fields:
         assert _close(getattr(d, f), getattr(e, f)), (f, getattr(d, f), getattr(e, f))
     for f in ("momentum", "angular_momentum", "center_of_mass", "center_of_mass_velocity"):
         a, b = np.array(getattr(d, f)[:]), np.array(getattr(e, f)[:])
         assert np.allclose(a, b, rtol=TOL, atol=1e-18), (f, a, b)
+
+
+def _noalloc(lib, p, dev, gas, eps, with_potential, stream=None):
+    got = L.Diag()
+    st = lib.gvs_diagnostics_noalloc(
+        0, stream, p.count, _dev(dev["x"]), _dev(dev["y"]), _dev(dev["z"]), _dev(dev["vx"]),
+        _dev(dev["vy"]), _dev(dev["vz"]), _dev(dev["mass"]), _dev(dev["ptype"]) if gas else None,
+        _dev(dev["internal_energy"]) if gas else None, eps, with_potential, C.byref(got))
+    L.check(st)
+    return got
 
 
 def test_noalloc_matches_allocating_entry_point():
@@ -45,6 +60,7 @@ def test_noalloc_matches_allocating_entry_point():
     lib = L.load()
     ctx = G.Context(0)
     try:
+        # the larger system first, so the smaller one runs over its leftover partial sums
         for p, eps, gas in ((G.PlummerSphere(20000, seed=4).generate(), 0.01, False),
                             (G.EvrardCollapse(3000, seed=2).generate(), 0.02, True)):
             ctx.set_state(p)
@@ -52,18 +68,19 @@ def test_noalloc_matches_allocating_entry_point():
             L.check(lib.gvs_diagnostics(ctx.h, eps, 1, C.byref(want)), ctx.h)
             dev = {f: torch.from_numpy(getattr(p, f).copy()).cuda() for f in
                    ("x", "y", "z", "vx", "vy", "vz", "mass", "internal_energy")}
-            ptype = torch.from_numpy(p.particle_type.copy()).cuda() if gas else None
+            dev["ptype"] = torch.from_numpy(p.particle_type.copy()).cuda()
             torch.cuda.synchronize()
             for _ in range(2):  # two calls in a row share the fixed scratch
-                got = L.Diag()
-                st = lib.gvs_diagnostics_noalloc(
-                    0, None, p.count, _dev(dev["x"]), _dev(dev["y"]), _dev(dev["z"]), _dev(dev["vx"]),
-                    _dev(dev["vy"]), _dev(dev["vz"]), _dev(dev["mass"]), _dev(ptype) if gas else None,
-                    _dev(dev["internal_energy"]) if gas else None, eps, 1, C.byref(got))
-                L.check(st)
+                got = _noalloc(lib, p, dev, gas, eps, 1)
                 _check(got, want)
             if gas:
                 assert got.thermal_energy > 0.0
+            # without the potential, on a stream of the caller's own
+            s = torch.cuda.Stream()
+            got = _noalloc(lib, p, dev, gas, eps, 0, stream=C.c_void_p(s.cuda_stream))
+            assert got.potential_energy == 0.0
+            _check(got, want, with_potential=False)
+            assert _close(got.total_energy, want.kinetic_energy + want.thermal_energy)
     finally:
         ctx.close()
 
