@@ -451,6 +451,11 @@ gvs_status gvs_kdk_steps(gvs_ctx *c, int algo, int precision, double eps, double
     GVS_TRY(check_prec_algo(c, algo, precision, eps, theta));
     if (!(dt > 0.0) || nsteps < 0) return fail(c, GVS_ERR_INVALID_ARG, "dt must be > 0 and nsteps >= 0");
     cudaSetDevice(c->device);
+    // Systems of at most 32 particles with the exact f64 sum run whole
+    // trajectories in one launch (one warp); the result is the same bit for bit.
+    if (algo == GVS_ALGO_DIRECT && precision == GVS_PREC_FP64_EXACT && kdk_tiny_eligible(c) && !c->prof.on &&
+        c->fault_kind == 0 && nsteps >= 2)
+        return kdk_tiny_exact(c, eps, dt, nsteps);
     // Direct-sum steps replay one captured step: the step is a fixed chain of
     // kernels with no host synchronisation (unless kernel timing is on).
     const bool graph = algo == GVS_ALGO_DIRECT && !c->prof.on && c->fault_kind == 0 && !c->sgraph.disabled &&

@@ -327,6 +327,9 @@ gvs_status autotune_direct(Ctx *c, int precision, double eps, int *best_nt, int 
 gvs_status kick(Ctx *c, double half_dt);
 gvs_status kick_drift(Ctx *c, double half_dt, double dt);
 gvs_status clear_acc(Ctx *c);
+// n <= 32, FP64_EXACT direct sum: nsteps whole KDK steps in one launch (bit-identical)
+bool kdk_tiny_eligible(const Ctx *c);
+gvs_status kdk_tiny_exact(Ctx *c, double eps, double dt, long long nsteps);
 // diag.cu
 gvs_status diagnostics(Ctx *c, double eps, int with_potential, gvs_diag *out);
 // bh.cu
