@@ -46,7 +46,7 @@ class Profile(C.Structure):
                 ("near_tile_visits", C.c_double), ("vjp_ms", C.c_double), ("vjp_launches", C.c_longlong),
                 ("sph_f64_redo", C.c_longlong), ("bh_groups", C.c_longlong),
                 ("bh_group_fallbacks", C.c_longlong), ("bh_group_iterations", C.c_longlong),
-                ("bh_group_interactions", C.c_longlong)]
+                ("bh_group_interactions", C.c_longlong), ("bh_walk_terms", C.c_longlong)]
 
 
 _P = C.c_void_p  # every array argument is passed as a raw address
@@ -103,6 +103,7 @@ SIGNATURES = {
     "gvs_event_record": (_ST, [_P, _i]),
     "gvs_event_elapsed": (_ST, [_P, _i, _i, C.POINTER(C.c_float)]),
     "gvs_l2_flush": (_ST, [_P]),
+    "gvs_stream": (_ST, [_P, C.POINTER(C.c_void_p)]),
     "gvs_check_bounded_wait": (_ST, [_P, C.c_uint]),
     "gvs_measure_fp32_peak": (_ST, [_P, C.POINTER(C.c_double)]),
     "gvs_fp32_peak_variants": (_ST, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),

@@ -602,8 +602,9 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
                                               const double *__restrict__ sy, const double *__restrict__ sz,
                                               const double *__restrict__ sm, const S2Table tab, double theta2,
                                               double eps2, const AccOut out, const float4 *__restrict__ cm32lo,
-                                              const float4 *__restrict__ p32lo) {
+                                              const float4 *__restrict__ p32lo, unsigned *__restrict__ err) {
     constexpr bool F64 = MODE == 0;
+    unsigned nterm = 0;  // node and particle terms this particle summed (profile counter)
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = t < n;
     double px = 0, py = 0, pz = 0;
@@ -627,6 +628,7 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
         if (mt.z > 0) {  // leaf
             if (mt.z == 1) {
                 if ((size_t)mt.y != t) {
+                    ++nterm;
                     if (F64) {
                         const double4 c = cm64[m];
                         if (c.w != 0.0) add_force64(px, py, pz, c.x, c.y, c.z, c.w, eps2, ax, ay, az);
@@ -644,6 +646,7 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
             } else {  // bucket of coincident-key particles: direct terms
                 for (int j = mt.y; j < mt.y + mt.z; ++j) {
                     if ((size_t)j == t) continue;
+                    ++nterm;
                     if (F64) {
                         if (sm[j] != 0.0) add_force64(px, py, pz, sx[j], sy[j], sz[j], sm[j], eps2, ax, ay, az);
                     } else if (MODE == 1) {
@@ -668,6 +671,7 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
                 const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
                 if (tab.s2[mt.w] < __dmul_rn(theta2, d2)) {
                     add_force64(px, py, pz, c.x, c.y, c.z, c.w, eps2, ax, ay, az);
+                    ++nterm;
                     next = (uint32_t)mt.x;
                 } else {
                     next = m + 1;
@@ -694,6 +698,7 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
                     accept = tab.s2[mt.w] < __dmul_rn(theta2, e2);
                 }
                 if (accept) {
+                    ++nterm;
                     if (MODE == 1) {
                         add_force32(qx, qy, qz, c.x, c.y, c.z, c.w, eps2f, fx, fy, fz);
                     } else {
@@ -707,6 +712,9 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
             }
         }
     }
+    const unsigned wterms = __reduce_add_sync(0xFFFFFFFFu, active ? nterm : 0u);
+    if ((threadIdx.x & 31) == 0 && wterms)
+        atomicAdd(reinterpret_cast<unsigned long long *>(err + EW_WALK_TERMS), (unsigned long long)wterms);
     if (!active) return;
     if (MODE == 1) { ax = fx; ay = fy; az = fz; }
     if (MODE == 2) {
@@ -1409,18 +1417,18 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
         k_walk<0><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, as<int4>(t->meta), nullptr, as<double4>(t->cm64),
                                                 nullptr, as<double>(t->sx), as<double>(t->sy), as<double>(t->sz),
                                                 as<double>(t->sm), tab, theta * theta, eps * eps,
-                                                out, nullptr, nullptr);
+                                                out, nullptr, nullptr, err_ptr(c));
     else if (mode == 1)
         k_walk<1><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, as<int4>(t->meta), as<float4>(t->cm32), nullptr,
                                                 as<float4>(t->pos32), as<double>(t->sx), as<double>(t->sy),
                                                 as<double>(t->sz), as<double>(t->sm), tab, theta * theta, eps * eps,
-                                                out, nullptr, nullptr);
+                                                out, nullptr, nullptr, err_ptr(c));
     else
         k_walk<2><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, as<int4>(t->meta), as<float4>(t->cm32),
                                                 as<double4>(t->cm64), as<float4>(t->pos32), as<double>(t->sx),
                                                 as<double>(t->sy), as<double>(t->sz), as<double>(t->sm), tab,
                                                 theta * theta, eps * eps, out,
-                                                as<float4>(t->cm32lo), as<float4>(t->pos32lo));
+                                                as<float4>(t->cm32lo), as<float4>(t->pos32lo), err_ptr(c));
     c->prof.launches += 1;
     GVS_TRY(check_launch(c, "tree walk"));
     if (c->prof.on) {

@@ -41,6 +41,7 @@ struct EnsState {
     int ntiles = 0, nitems = 0, max_split = 1;
     size_t npad = 0;
     double eps = 0.0;
+    double pairs = 0.0;              // sum over systems of N_i^2 (pair terms of one evaluation)
     DevBuf sys_of, off_dev, nsplit_dev, bb, keys, keys2, perm, perm2, sk, sk2, slot_orig, pslot, items, counter,
         pack, partial;
     cudaGraph_t graph = nullptr;
@@ -159,6 +160,8 @@ gvs_status ens_setup(Ctx *c, int nsys, const int64_t *sizes, double eps) {
     E->nsys = nsys;
     E->n = c->n;
     E->eps = eps;
+    E->pairs = 0.0;
+    for (int k = 0; k < nsys; ++k) E->pairs += (double)sizes[k] * (double)sizes[k];
     E->off.assign(nsys + 1, 0);
     E->tile_off.assign(nsys + 1, 0);
     E->nsplit.assign(nsys, 1);
@@ -260,8 +263,18 @@ gvs_status ens_forces(Ctx *c) {
     c->prof.launches += 2;
     GVS_TRY(ens_pack(c, E->ntiles, as<uint32_t>(E->slot_orig), as<float4>(E->pack)));
     const float e2 = (float)(E->eps * E->eps);
+    if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], st));
     GVS_TRY(ens_pairs(c, as<float4>(E->pack), as<int4>(E->items), E->nitems, as<unsigned>(E->counter), e2,
                       as<double>(E->partial), E->npad));
+    if (c->prof.on) {  // kernel time of the batched pair kernel
+        GVS_CUDA(c, cudaEventRecord(c->prof.ev[1], st));
+        GVS_CUDA(c, cudaEventSynchronize(c->prof.ev[1]));
+        float ms = 0.f;
+        GVS_CUDA(c, cudaEventElapsedTime(&ms, c->prof.ev[0], c->prof.ev[1]));
+        c->prof.force_ms += ms;
+        c->prof.force_launches += 1;
+        c->prof.force_flops += 20.0 * E->pairs;
+    }
     k_ens_reduce<<<nb(n), 256, 0, st>>>(as<double>(E->partial), E->npad, n, final_perm, as<uint32_t>(E->pslot),
                                         as<uint32_t>(E->nsplit_dev), as<double>(c->ax), as<double>(c->ay),
                                         as<double>(c->az));

@@ -705,6 +705,16 @@ gvs_status gvs_profile_read(gvs_ctx *c, gvs_profile *out) {
     unsigned long long pairs = 0;
     GVS_CUDA(c, cudaMemcpy(&pairs, err_ptr(c) + EW_BH_TERMS, sizeof pairs, cudaMemcpyDeviceToHost));
     out->bh_group_interactions = (long long)pairs;
+    unsigned long long wt = 0;
+    GVS_CUDA(c, cudaMemcpy(&wt, err_ptr(c) + EW_WALK_TERMS, sizeof wt, cudaMemcpyDeviceToHost));
+    out->bh_walk_terms = (long long)wt;
+    return GVS_OK;
+}
+
+gvs_status gvs_stream(gvs_ctx *c, void **stream) {
+    GVS_TRY(check_ctx(c));
+    if (!stream) return fail(c, GVS_ERR_INVALID_ARG, "stream is NULL");
+    *stream = static_cast<void *>(c->stream);
     return GVS_OK;
 }
 

@@ -44,8 +44,9 @@ enum ErrWordSlot : int {
     EW_BH_GROUPS = 14,      // BH groups walked
     EW_BH_FALLBACKS = 15,   // ... of which walked per particle
     EW_BH_TERMS = 16,       // u64: BH group-walk terms evaluated for real particles
-    EW_PROFILE_END = 18,    // profile counters: [EW_NEAR_TILES, EW_PROFILE_END)
-    EW_NEIGH_WORK = 20,     // work counter of the SPH neighbour search
+    EW_WALK_TERMS = 18,     // u64: terms summed by the per-particle BH walks (f64, mixed, f32)
+    EW_PROFILE_END = 20,    // profile counters: [EW_NEAR_TILES, EW_PROFILE_END)
+    EW_NEIGH_WORK = 22,     // work counter of the SPH neighbour search
 };
 
 // ---------------------------------------------------------------------------

@@ -273,7 +273,7 @@ class Context:
                 "near_tile_visits": pr.near_tile_visits, "vjp_ms": pr.vjp_ms, "vjp_launches": pr.vjp_launches,
                 "sph_f64_redo": pr.sph_f64_redo, "bh_groups": pr.bh_groups,
                 "bh_group_fallbacks": pr.bh_group_fallbacks, "bh_group_iterations": pr.bh_group_iterations,
-                "bh_group_interactions": pr.bh_group_interactions}
+                "bh_group_interactions": pr.bh_group_interactions, "bh_walk_terms": pr.bh_walk_terms}
 
     def event(self, slot: int):
         self._ck(self._lib.gvs_event_record(self.h, slot))
@@ -285,6 +285,12 @@ class Context:
 
     def l2_flush(self):
         self._ck(self._lib.gvs_l2_flush(self.h))
+
+    def stream(self) -> int:
+        """The context's cudaStream_t (as an integer), for ordering other CUDA work against it."""
+        s = C.c_void_p()
+        self._ck(self._lib.gvs_stream(self.h, C.byref(s)))
+        return s.value or 0
 
     def fp32_peak_tflops(self) -> float:
         v = C.c_double()

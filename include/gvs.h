@@ -96,6 +96,8 @@ typedef struct gvs_profile {
     long long bh_group_iterations; /* group-walk iterations (32 nodes each) */
     long long bh_group_interactions; /* particle-node (or particle-particle) terms the group walk
                                         evaluated for real particles (fallback groups excluded) */
+    long long bh_walk_terms;         /* node and particle terms summed by the per-particle walks
+                                        (f64, mixed and per-particle f32 Barnes-Hut) */
 } gvs_profile;
 
 /* ---- library / context ---------------------------------------------------- */
@@ -325,6 +327,9 @@ gvs_status gvs_profile_read(gvs_ctx *ctx, gvs_profile *out);
 /* Records event `slot` (0..15) on the context stream; elapsed ms between two slots. */
 gvs_status gvs_event_record(gvs_ctx *ctx, int slot);
 gvs_status gvs_event_elapsed(gvs_ctx *ctx, int slot_a, int slot_b, float *ms);
+/* The context's CUDA stream (a cudaStream_t), so that a caller can order its own CUDA
+ * work against the context's (events, stream waits).  No reference counterpart. */
+gvs_status gvs_stream(gvs_ctx *ctx, void **stream);
 /* Writes a buffer larger than L2 on the context stream (cold-cache timing). */
 gvs_status gvs_l2_flush(gvs_ctx *ctx);
 /* Self-test of failure detection (no reference counterpart): a kernel waits on an
