@@ -11,6 +11,9 @@ import re
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libgvs.so")
+# The bounds-checked build (same ABI); a process that sets GVS_CHECKED=1 before the
+# first load uses it.
+CHECKED_LIB_PATH = os.path.join(HERE, "libgvs_checked.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "gvs.h")
 
 OK, ERR_INVALID_ARG, ERR_OOM, ERR_LAUNCH, ERR_DEVICE, ERR_TIMEOUT, ERR_INJECTED, ERR_NO_DEVICE, ERR_STATE = range(9)
@@ -124,7 +127,7 @@ def load(path: str | None = None):
     global _lib
     if _lib is not None:
         return _lib
-    p = path or LIB_PATH
+    p = path or (CHECKED_LIB_PATH if os.environ.get("GVS_CHECKED") == "1" else LIB_PATH)
     if not os.path.exists(p):
         raise ImportError(f"{p} not found: build it with `python -m gravis_gb300.build` "
                           "(the engine has no CPU fallback)")

@@ -2,8 +2,10 @@
 
 Every translation unit under gravis_gb300/csrc is compiled in parallel with
 `-gencode arch=compute_103a,code=sm_103a -lineinfo -O3`, then linked into
-gravis_gb300/libgvs.so (CUDA runtime linked statically).  Objects go to
-gravis_gb300/_build/ (git-ignored).  Rebuilds only what changed.
+gravis_gb300/libgvs.so (CUDA runtime linked statically), and again with
+-DGVS_CHECKED into gravis_gb300/libgvs_checked.so (the bounds-checked build).
+Objects go to gravis_gb300/_build/ and _build_checked/ (git-ignored).
+Rebuilds only what changed.
 """
 from __future__ import annotations
 
@@ -49,8 +51,8 @@ def _stale(obj: str, src: str) -> bool:
 FILE_FLAGS = {"sph.cu": ["--fmad=false"]}
 
 
-def _compile(nvcc: str, src: str, extra: list[str]) -> str:
-    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+def _compile(nvcc: str, src: str, extra: list[str], build_dir: str) -> str:
+    obj = os.path.join(build_dir, os.path.basename(src) + ".o")
     if _stale(obj, src):
         cmd = [nvcc] + ARCH + NVCC_FLAGS + FILE_FLAGS.get(os.path.basename(src), []) + extra + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -65,32 +67,51 @@ def verbose() -> bool:
     return os.environ.get("GVS_BUILD_VERBOSE", "") not in ("", "0")
 
 
-def build(force: bool = False, extra: list[str] | None = None) -> str:
-    """Compile all sources and link libgvs.so; returns the library path."""
-    os.makedirs(BUILD, exist_ok=True)
+# The checked build: the same sources with -DGVS_CHECKED (kernels test the indices
+# they compute and the tree build its invariants; see csrc/gvs_internal.cuh),
+# linked as libgvs_checked.so from objects in _build_checked/.
+CHECKED_LIB = os.path.join(HERE, "libgvs_checked.so")
+VARIANTS = {"normal": (BUILD, LIB, []), "checked": (os.path.join(HERE, "_build_checked"), CHECKED_LIB,
+                                                    ["-DGVS_CHECKED"])}
+
+
+def build(force: bool = False, extra: list[str] | None = None, checked: bool = True) -> str:
+    """Compile all sources and link libgvs.so (and, with checked, libgvs_checked.so:
+    both variants' translation units compile in one parallel pool); returns the path
+    of libgvs.so."""
     nvcc = _nvcc()
     extra = list(extra or [])
     if verbose():
         extra += ["-Xptxas", "-v"]
-    stamp = os.path.join(BUILD, "flags.txt")
-    flags = " ".join(ARCH + NVCC_FLAGS + extra) + repr(sorted(FILE_FLAGS.items()))
-    if not os.path.exists(stamp) or open(stamp).read() != flags:
-        force = True
-        with open(stamp, "w") as fh:
-            fh.write(flags)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
-    if force:
-        for o in glob.glob(os.path.join(BUILD, "*.o")):
-            os.remove(o)
-    with cf.ThreadPoolExecutor(max_workers=max(2, min(len(srcs), os.cpu_count() or 4))) as ex:
-        objs = list(ex.map(lambda s: _compile(nvcc, s, extra), srcs))
-    if force or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        tmp = LIB + ".tmp"
-        cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart_static", "-ldl", "-lrt", "-lpthread"]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-        os.replace(tmp, LIB)
+    variants = ["normal", "checked"] if checked else ["normal"]
+    jobs = []
+    for v in variants:
+        bdir, _, vflags = VARIANTS[v]
+        os.makedirs(bdir, exist_ok=True)
+        stamp = os.path.join(bdir, "flags.txt")
+        flags = " ".join(ARCH + NVCC_FLAGS + extra + vflags) + repr(sorted(FILE_FLAGS.items()))
+        vforce = force
+        if not os.path.exists(stamp) or open(stamp).read() != flags:
+            vforce = True
+            with open(stamp, "w") as fh:
+                fh.write(flags)
+        if vforce:
+            for o in glob.glob(os.path.join(bdir, "*.o")):
+                os.remove(o)
+        jobs += [(v, src, extra + vflags, bdir) for src in srcs]
+    with cf.ThreadPoolExecutor(max_workers=max(2, min(len(jobs), os.cpu_count() or 4))) as ex:
+        objs = list(ex.map(lambda j: (j[0], _compile(nvcc, j[1], j[2], j[3])), jobs))
+    for v in variants:
+        _, lib, _ = VARIANTS[v]
+        vobjs = [o for vv, o in objs if vv == v]
+        if not os.path.exists(lib) or any(os.path.getmtime(o) > os.path.getmtime(lib) for o in vobjs):
+            tmp = lib + ".tmp"
+            cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + vobjs + ["-lcudart_static", "-ldl", "-lrt", "-lpthread"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"link failed ({v}):\n{r.stdout}\n{r.stderr}")
+            os.replace(tmp, lib)
     build_host()
     return LIB
 

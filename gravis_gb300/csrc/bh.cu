@@ -65,6 +65,10 @@ struct Tree {
     DevBuf pos32lo, cm32lo;  // mixed walk: f32 lo words of positions and COMs
     // group walk (f32): child-slot records, groups of <= 32*NPL particles, work counter
     DevBuf nk, koff, krec, groups, gcount;
+    // parity group walk (mixed): child-slot records with f32 lo words and node ids,
+    // groups of <= 32 particles, work counter
+    DevBuf prec, pgroups, pgcount;
+    unsigned long long koff_version = ~0ull, pgrp_version = ~0ull;
     DevBuf parent, arrive;  // per node: parent index, children that finished their moments
     DevBuf leaf_of;         // per sorted particle: the leaf that holds it
     unsigned long long grp_version = ~0ull;
@@ -239,6 +243,10 @@ __global__ void k_keys_lo(const uint64_t *__restrict__ khi, const uint32_t *__re
     uint64_t lo = 0;
     if (prev || next) {
         const uint32_t o = perm[i];
+        if (!CHK_IDX(o, n)) {
+            klo[i] = 0;
+            return;
+        }
         uint64_t hh;
         octant_path<MAXL>(X[o], Y[o], Z[o], bb, hh, lo);
         atomicAdd(stat, 1u);
@@ -280,7 +288,10 @@ __global__ void k_iota(uint32_t *a, size_t n) {
 template <class T>
 __global__ void k_gather(const T *__restrict__ src, const uint32_t *__restrict__ idx, T *__restrict__ dst, size_t n) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) dst[i] = src[idx[i]];
+    if (i < n) {
+        const uint32_t j = idx[i];
+        if (CHK_IDX(j, n)) dst[i] = src[j];
+    }
 }
 
 // delta[i] = common depth of sorted keys i-1 and i (delta[0] = delta[n] = -1);
@@ -305,7 +316,7 @@ __global__ void k_nown(const int *__restrict__ delta, size_t n, uint32_t *__rest
 __global__ void k_nodes(const uint64_t *__restrict__ khi, const uint64_t *__restrict__ klo,
                         const int *__restrict__ delta, const uint32_t *__restrict__ off, size_t n,
                         uint8_t *__restrict__ level, uint32_t *__restrict__ first, uint32_t *__restrict__ cnt,
-                        uint32_t *__restrict__ skip) {
+                        uint32_t *__restrict__ skip, size_t nnodes) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int a = delta[i] + 1;
@@ -328,6 +339,7 @@ __global__ void k_nodes(const uint64_t *__restrict__ khi, const uint64_t *__rest
             e = lo_j;
         }
         const uint32_t idx = base + (uint32_t)(L - a);
+        if (!CHK_IDX(idx, nnodes)) return;
         const bool leaf = (e - i == 1) || L == MAXL;
         level[idx] = (uint8_t)L;
         first[idx] = (uint32_t)i;
@@ -374,16 +386,17 @@ __global__ void k_centres(const uint64_t *__restrict__ khi, const uint64_t *__re
 // the leaf of its particles.
 __global__ void k_links(size_t nnodes, const uint32_t *__restrict__ first, const uint32_t *__restrict__ cnt,
                         const uint32_t *__restrict__ skip, uint32_t *__restrict__ parent, uint32_t *__restrict__ nk,
-                        uint32_t *__restrict__ leaf_of) {
+                        uint32_t *__restrict__ leaf_of, size_t n) {
     const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nnodes) return;
     if (k == 0) parent[0] = 0xFFFFFFFFu;
     uint32_t c = 0;
     const uint32_t lc = cnt[k];
-    for (uint32_t j = first[k]; j < first[k] + lc; ++j) leaf_of[j] = (uint32_t)k;
+    for (uint32_t j = first[k]; j < first[k] + lc; ++j)
+        if (CHK_IDX(j, n)) leaf_of[j] = (uint32_t)k;
     if (lc == 0) {
         const uint32_t end = skip[k];
-        for (uint32_t ch = (uint32_t)k + 1; ch < end; ch = skip[ch], ++c) parent[ch] = (uint32_t)k;
+        for (uint32_t ch = (uint32_t)k + 1; ch < end && CHK_IDX(ch, nnodes); ch = skip[ch], ++c) parent[ch] = (uint32_t)k;
     }
     nk[k] = c;
 }
@@ -537,10 +550,12 @@ struct AccOut {
     const uint32_t *perm;
     double *ax, *ay, *az;
     int accumulate;
+    size_t n;  // length of perm's targets (the checked build tests every perm[i] against it)
 };
 
 __device__ __forceinline__ void store_acc(const AccOut &o, size_t i, double fx, double fy, double fz) {
     const uint32_t k = o.perm[i];
+    if (!CHK_IDX(k, o.n)) return;
     if (o.accumulate) {
         o.ax[k] += fx; o.ay[k] += fy; o.az[k] += fz;
     } else {
@@ -625,8 +640,14 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
         if ((size_t)m >= nnodes) break;
         if (next != m) continue;
         const int4 mt = meta[m];
+        if (!CHK((size_t)mt.x > m && (size_t)mt.x <= nnodes, DERR_TREE)) {  // a skip pointer must move forward
+            next = (uint32_t)nnodes;
+            continue;
+        }
         if (mt.z > 0) {  // leaf
-            if (mt.z == 1) {
+            if (!CHK(mt.y >= 0 && (size_t)mt.y + (size_t)mt.z <= n, DERR_BOUNDS)) {
+                next = (uint32_t)mt.x;
+            } else if (mt.z == 1) {
                 if ((size_t)mt.y != t) {
                     ++nterm;
                     if (F64) {
@@ -795,7 +816,7 @@ __global__ void k_krec(size_t nnodes, const uint8_t *__restrict__ level, const u
     const uint32_t end = skip[k];
     uint32_t slot = 1u + koff[k];
     for (uint32_t ch = (uint32_t)k + 1; ch < end; ch = skip[ch], ++slot)
-        write_rec(krec, slot, ch, level, first, cnt, nk, koff, cm32, tab);
+        if (CHK_IDX(slot, nnodes)) write_rec(krec, slot, ch, level, first, cnt, nk, koff, cm32, tab);
 }
 
 // Groups: a node with more than G particles emits its children's particle
@@ -805,6 +826,13 @@ __global__ void k_krec(size_t nnodes, const uint8_t *__restrict__ level, const u
 // denser sibling.  A bucket leaf with more than G particles is cut into runs of
 // G; a root with at most G particles is one group.  Runs are contiguous in
 // sorted particle order.
+// Appends a group (the list holds at most n groups: every group has a particle).
+__device__ __forceinline__ void push_group(int2 *__restrict__ groups, uint32_t *__restrict__ ngroups, size_t n,
+                                           int2 g) {
+    const uint32_t slot = atomicAdd(ngroups, 1u);
+    if (CHK_IDX(slot, n) && CHK(g.x >= 0 && g.y > 0 && (size_t)g.x + (size_t)g.y <= n, DERR_TREE)) groups[slot] = g;
+}
+
 __global__ void k_groups(size_t nnodes, size_t n, uint32_t G, const uint8_t *__restrict__ level,
                          const uint32_t *__restrict__ first, const uint32_t *__restrict__ cnt,
                          const uint32_t *__restrict__ skip, const uint64_t *__restrict__ khi,
@@ -814,12 +842,12 @@ __global__ void k_groups(size_t nnodes, size_t n, uint32_t G, const uint8_t *__r
     if (k >= nnodes) return;
     const uint32_t ck = sub_count((uint32_t)k, nnodes, n, first, skip);
     if (ck <= G) {
-        if (k == 0) groups[atomicAdd(ngroups, 1u)] = make_int2((int)first[0], (int)ck);
+        if (k == 0) push_group(groups, ngroups, n, make_int2((int)first[0], (int)ck));
         return;
     }
     if (cnt[k] != 0) {
         for (uint32_t j = 0; j < ck; j += G)
-            groups[atomicAdd(ngroups, 1u)] = make_int2((int)(first[k] + j), (int)min(G, ck - j));
+            push_group(groups, ngroups, n, make_int2((int)(first[k] + j), (int)min(G, ck - j)));
         return;
     }
     uint32_t c8[8], f8[8];
@@ -851,7 +879,7 @@ __global__ void k_groups(size_t nnodes, size_t n, uint32_t G, const uint8_t *__r
             tot += c8[o];
             if (c8[o]) f0 = f8[o];
         }
-        if (ok && tot > 0u) groups[atomicAdd(ngroups, 1u)] = make_int2((int)f0, (int)tot);
+        if (ok && tot > 0u) push_group(groups, ngroups, n, make_int2((int)f0, (int)tot));
         a += size;
     }
 }
@@ -978,6 +1006,8 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_walk_group(const int2 *__rest
         g = __shfl_sync(FULL, g, 0);
         if (g >= ngroups) break;
         const int2 gr = groups[g];
+        if (!CHK(gr.x >= 0 && gr.y > 0 && gr.y <= 32 * NPL && (size_t)gr.x + (size_t)gr.y <= n, DERR_BOUNDS))
+            continue;  // warp-uniform: every lane read the same group
         constexpr int NQ = NPL < 2 ? 2 : NPL;  // particle slots per lane (the scalar form pads to a pair)
         constexpr int NP = NQ / 2;
         float px[NQ], py[NQ], pz[NQ];
@@ -1043,8 +1073,10 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_walk_group(const int2 *__rest
             int4 B = make_int4(0, 0, 0, 0);
             if (has) {
                 const size_t slot = (size_t)(er >> 3) + (size_t)(lane - sr);
-                A = krec[2 * slot];
-                B = reinterpret_cast<const int4 *>(krec)[2 * slot + 1];
+                if (CHK_IDX(slot, nnodes)) {  // a bad slot reads as an empty node (A.w == 0)
+                    A = krec[2 * slot];
+                    B = reinterpret_cast<const int4 *>(krec)[2 * slot + 1];
+                }
             }
             bool accept = false, open = false, bucket = false;
             if (has && A.w != 0.f) {
@@ -1079,7 +1111,9 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_walk_group(const int2 *__rest
             while (bm) {  // leaves of coincident-key particles (rare): members one by one
                 const int b = __ffs(bm) - 1;
                 bm &= bm - 1;
-                const int bf = __shfl_sync(FULL, B.y, b), bc = __shfl_sync(FULL, B.z, b);
+                const int bf = __shfl_sync(FULL, B.y, b);
+                const int bc = CHK(bf >= 0 && (size_t)bf + (size_t)__shfl_sync(FULL, B.z, b) <= n, DERR_BOUNDS)
+                                   ? __shfl_sync(FULL, B.z, b) : 0;
                 for (int j0 = 0; j0 < bc; j0 += 32) {
                     if (nil > GW_ICAP - 32) {
                         __syncwarp();
@@ -1142,6 +1176,283 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_walk_group(const int2 *__rest
     }
 }
 
+// ---- parity group walk (MIXED) --------------------------------------------------
+// The mixed walk's decisions -- the reference's opening test for every particle --
+// made for a warp of up to 32 particles at once (one per lane, a tree cell of at
+// most 32 particles).  The warp pops up to 32 nodes per iteration; each stack entry
+// carries the lane mask of the particles whose walk reaches it.  Per node:
+//  - the box of the group's particles (f32 hi words) bounds every particle's f32
+//    distance to the COM from below (d2min) and above (d2max): rounding to nearest
+//    is monotone, so each particle's own f32 d^2, computed as k_walk<2> computes it,
+//    lies in [d2min, d2max].  d2min > hi2[L]: every particle in the mask accepts;
+//    d2max < lo2[L]: every one opens (the certified bands of the mixed walk);
+//  - otherwise each particle in the mask makes its own k_walk<2> decision (the f32
+//    test, the reference's f64 test inside the band), and the node is accepted for
+//    the particles that accept it and opened for the others.
+// So every particle sums exactly the terms of its own walk.  Accepted nodes and
+// leaves go to a shared list with their lane masks; each lane adds the entries of
+// its bit as f32 terms on float-float separations with compensated sums.
+constexpr int PW_ICAP = 128;
+constexpr int PW_WARPS = 3;  // 3 x 15 KB of stack and list: within the 48 KB of static shared memory
+
+struct PGroupSmem {
+    uint2 stack[GW_SCAP];     // (first child slot << 3 | children - 1, lane mask)
+    float4 il[2 * PW_ICAP];   // list: (com hi, mass), (com lo, lane mask bits)
+};
+
+// Parity-walk record of node x at its child slot: (com hi, mass), (com lo, 0) and
+// (first child slot, children, level, x) for an internal node, (-1, particle, 1, x)
+// for a one-particle leaf, (-2, first, count, x) for a bucket leaf.
+__device__ __forceinline__ void write_prec(float4 *__restrict__ prec, uint32_t slot, uint32_t x,
+                                           const uint8_t *__restrict__ level, const uint32_t *__restrict__ first,
+                                           const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ nk,
+                                           const uint32_t *__restrict__ koff, const float4 *__restrict__ cm32,
+                                           const float4 *__restrict__ cm32lo) {
+    prec[3 * (size_t)slot] = cm32[x];
+    const float4 lo = cm32lo[x];
+    prec[3 * (size_t)slot + 1] = make_float4(lo.x, lo.y, lo.z, 0.f);
+    const uint32_t c = cnt[x];
+    int4 b;
+    if (c == 0) b = make_int4((int)(1u + koff[x]), (int)nk[x], (int)level[x], (int)x);
+    else if (c == 1) b = make_int4(-1, (int)first[x], 1, (int)x);
+    else b = make_int4(-2, (int)first[x], (int)c, (int)x);
+    reinterpret_cast<int4 *>(prec)[3 * (size_t)slot + 2] = b;
+}
+
+__global__ void k_prec(size_t nnodes, const uint8_t *__restrict__ level, const uint32_t *__restrict__ first,
+                       const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ skip,
+                       const uint32_t *__restrict__ nk, const uint32_t *__restrict__ koff,
+                       const float4 *__restrict__ cm32, const float4 *__restrict__ cm32lo, float4 *__restrict__ prec) {
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nnodes) return;
+    if (k == 0) write_prec(prec, 0, 0, level, first, cnt, nk, koff, cm32, cm32lo);
+    if (cnt[k] != 0) return;
+    const uint32_t end = skip[k];
+    uint32_t slot = 1u + koff[k];
+    for (uint32_t ch = (uint32_t)k + 1; ch < end; ch = skip[ch], ++slot)
+        if (CHK_IDX(slot, nnodes)) write_prec(prec, slot, ch, level, first, cnt, nk, koff, cm32, cm32lo);
+}
+
+__global__ void __launch_bounds__(PW_WARPS * 32) k_walk_pgroup(
+    const int2 *__restrict__ groups, uint32_t *__restrict__ gcount, const float4 *__restrict__ prec,
+    const double4 *__restrict__ cm64, const float4 *__restrict__ p32, const float4 *__restrict__ p32lo,
+    const double *__restrict__ sx, const double *__restrict__ sy, const double *__restrict__ sz, const S2Table tab,
+    double theta2, float eps2f, size_t n, size_t nnodes, const AccOut out, unsigned *__restrict__ err) {
+    constexpr unsigned FULL = 0xFFFFFFFFu;
+    __shared__ PGroupSmem smem[PW_WARPS];
+    const int lane = threadIdx.x & 31;
+    uint2 *stack = smem[threadIdx.x >> 5].stack;
+    float4 *il = smem[threadIdx.x >> 5].il;
+    const unsigned lt = (1u << lane) - 1u, me = 1u << lane;
+    const uint32_t ngroups = gcount[0];
+    for (;;) {
+        uint32_t g = 0;
+        if (lane == 0) g = atomicAdd(gcount + 1, 1u);
+        g = __shfl_sync(FULL, g, 0);
+        if (g >= ngroups) break;
+        const int2 gr = groups[g];
+        if (!CHK(gr.x >= 0 && gr.y > 0 && gr.y <= 32 && (size_t)gr.x + (size_t)gr.y <= n, DERR_BOUNDS)) continue;
+        const bool active = lane < gr.y;
+        const size_t t = (size_t)gr.x + (active ? lane : 0);
+        const float4 qh = p32[t], ql = p32lo[t];
+        const double px = sx[t], py = sy[t], pz = sz[t];
+        const float lox = warp_min(active ? qh.x : INFINITY), loy = warp_min(active ? qh.y : INFINITY),
+                    loz = warp_min(active ? qh.z : INFINITY);
+        const float hix = warp_max(active ? qh.x : -INFINITY), hiy = warp_max(active ? qh.y : -INFINITY),
+                    hiz = warp_max(active ? qh.z : -INFINITY);
+        const unsigned gmask = gr.y == 32 ? FULL : ((1u << gr.y) - 1u);
+        float fa[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        unsigned nterm = 0;
+        auto eval = [&](int count) {
+            for (int k = 0; k < count; ++k) {
+                const float4 a = il[2 * k], l = il[2 * k + 1];
+                if ((__float_as_uint(l.w) & me) && a.w != 0.f) {
+                    add_force_ff(qh, ql, a.x, a.y, a.z, l.x, l.y, l.z, a.w, eps2f, fa);
+                    ++nterm;
+                }
+            }
+        };
+        // the lane bit of sorted particle p if it belongs to this group, else 0
+        auto selfbit = [&](int p) -> unsigned {
+            const int r = p - gr.x;
+            return (r >= 0 && r < gr.y) ? (1u << r) : 0u;
+        };
+        int top = 1, nil = 0;
+        if (lane == 0) stack[0] = make_uint2(0u, gmask);  // the root: slot 0, one node
+        __syncwarp();
+        while (top > 0) {
+            // pop whole ranges from the top, at most 32 nodes
+            const uint2 e = lane < top ? stack[top - 1 - lane] : make_uint2(0u, 0u);
+            const int nkl = lane < top ? (int)(e.x & 7u) + 1 : 0;
+            int cum = nkl;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(FULL, cum, o);
+                if (lane >= o) cum += v;
+            }
+            const bool take = lane < top && cum <= 32;
+            const int kr = __popc(__ballot_sync(FULL, take));
+            const int total = __shfl_sync(FULL, cum, kr - 1);
+            const unsigned starts = __reduce_or_sync(FULL, take ? (1u << (cum - nkl)) : 0u);
+            top -= kr;
+            __syncwarp();
+            const bool has = lane < total;
+            const unsigned upto = lane == 31 ? FULL : ((2u << lane) - 1u);
+            const int r = max(__popc(starts & upto) - 1, 0);
+            const uint32_t er = __shfl_sync(FULL, e.x, r);
+            const unsigned emask = __shfl_sync(FULL, e.y, r);
+            const int sr = __shfl_sync(FULL, cum - nkl, r);
+            float4 A = make_float4(0.f, 0.f, 0.f, 0.f), Lo = A;
+            int4 B = make_int4(0, 0, 0, 0);
+            if (has) {
+                const size_t slot = (size_t)(er >> 3) + (size_t)(lane - sr);
+                if (CHK_IDX(slot, nnodes)) {  // a bad slot reads as an empty node (A.w == 0)
+                    A = prec[3 * slot];
+                    Lo = prec[3 * slot + 1];
+                    B = reinterpret_cast<const int4 *>(prec)[3 * slot + 2];
+                }
+            }
+            const bool live = has && A.w != 0.f && emask != 0u;
+            unsigned add_mask = 0u;  // particles that take this node (or leaf) as a term
+            bool open = false, mixed = false, bucket = false;
+            if (live) {
+                if (B.x == -1) {
+                    add_mask = emask & ~selfbit(B.y);
+                } else if (B.x == -2) {
+                    bucket = true;
+                } else {
+                    const int L = B.z;
+                    const float dxn = fmaxf(fmaxf(lox - A.x, A.x - hix), 0.f);
+                    const float dyn = fmaxf(fmaxf(loy - A.y, A.y - hiy), 0.f);
+                    const float dzn = fmaxf(fmaxf(loz - A.z, A.z - hiz), 0.f);
+                    const float d2min = fmaf(dzn, dzn, fmaf(dyn, dyn, dxn * dxn));
+                    const float dxf = fmaxf(fabsf(A.x - lox), fabsf(A.x - hix));
+                    const float dyf = fmaxf(fabsf(A.y - loy), fabsf(A.y - hiy));
+                    const float dzf = fmaxf(fabsf(A.z - loz), fabsf(A.z - hiz));
+                    const float d2max = fmaf(dzf, dzf, fmaf(dyf, dyf, dxf * dxf));
+                    if (d2min > tab.hi2[L]) add_mask = emask;
+                    else if (d2max < tab.lo2[L]) open = true;
+                    else mixed = true;
+                }
+            }
+            // accepted nodes and leaves: list entries with their masks
+            const unsigned am = __ballot_sync(FULL, add_mask != 0u);
+            if (add_mask) {
+                float4 *sl = il + 2 * (nil + __popc(am & lt));
+                sl[0] = A;
+                sl[1] = make_float4(Lo.x, Lo.y, Lo.z, __uint_as_float(add_mask));
+            }
+            nil += __popc(am);
+            // nodes every particle of the mask opens: push their children with the mask
+            const unsigned om = __ballot_sync(FULL, open);
+            if (top + __popc(om) > GW_SCAP) {  // unreachable by the depth bound; flagged, never written
+                if (lane == 0) atomicOr(err, DERR_STACK_OVERFLOW);
+            } else {
+                if (open) stack[top + __popc(om & lt)] = make_uint2(((uint32_t)B.x << 3) | (uint32_t)(B.y - 1), emask);
+                top += __popc(om);
+            }
+            // nodes near the group: each particle of the mask decides for itself
+            unsigned mm = __ballot_sync(FULL, mixed);
+            while (mm) {
+                const int j = __ffs(mm) - 1;
+                mm &= mm - 1;
+                const float cx = __shfl_sync(FULL, A.x, j), cy = __shfl_sync(FULL, A.y, j),
+                            cz = __shfl_sync(FULL, A.z, j);
+                const int L = __shfl_sync(FULL, B.z, j), node = __shfl_sync(FULL, B.w, j);
+                const unsigned jm = __shfl_sync(FULL, emask, j);
+                bool acc = false, opn = false;
+                if (jm & me) {  // k_walk<2>'s test of this particle
+                    const float dx = cx - qh.x, dy = cy - qh.y, dz = cz - qh.z;
+                    const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                    if (d2 > tab.hi2[L]) {
+                        acc = true;
+                    } else if (d2 < tab.lo2[L]) {
+                        opn = true;
+                    } else {
+                        const double4 c64 = cm64[node];
+                        const double ex = __dsub_rn(c64.x, px), ey = __dsub_rn(c64.y, py), ez = __dsub_rn(c64.z, pz);
+                        const double e2 =
+                            __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
+                        acc = tab.s2[L] < __dmul_rn(theta2, e2);
+                        opn = !acc;
+                    }
+                }
+                const unsigned accm = __ballot_sync(FULL, acc), opm = __ballot_sync(FULL, opn);
+                if (accm) {
+                    if (nil >= PW_ICAP) {
+                        eval(nil);
+                        nil = 0;
+                        __syncwarp();
+                    }
+                    if (lane == j) {
+                        il[2 * nil] = A;
+                        il[2 * nil + 1] = make_float4(Lo.x, Lo.y, Lo.z, __uint_as_float(accm));
+                    }
+                    ++nil;
+                    __syncwarp();
+                }
+                if (opm) {
+                    if (top + 1 > GW_SCAP) {
+                        if (lane == 0) atomicOr(err, DERR_STACK_OVERFLOW);
+                    } else {
+                        if (lane == j) stack[top] = make_uint2(((uint32_t)B.x << 3) | (uint32_t)(B.y - 1), opm);
+                        ++top;
+                    }
+                    __syncwarp();
+                }
+            }
+            // leaves of coincident-key particles (rare): members one by one
+            unsigned bm = __ballot_sync(FULL, bucket);
+            while (bm) {
+                const int b = __ffs(bm) - 1;
+                bm &= bm - 1;
+                const int bf = __shfl_sync(FULL, B.y, b);
+                const int bc = CHK(bf >= 0 && (size_t)bf + (size_t)__shfl_sync(FULL, B.z, b) <= n, DERR_BOUNDS)
+                                   ? __shfl_sync(FULL, B.z, b) : 0;
+                const unsigned bmask = __shfl_sync(FULL, emask, b);
+                for (int j0 = 0; j0 < bc; j0 += 32) {
+                    if (nil > PW_ICAP - 32) {
+                        __syncwarp();
+                        eval(nil);
+                        nil = 0;
+                        __syncwarp();
+                    }
+                    const int jj = j0 + lane;
+                    float4 q = make_float4(0.f, 0.f, 0.f, 0.f), qlo = q;
+                    if (jj < bc) {
+                        q = p32[bf + jj];
+                        qlo = p32lo[bf + jj];
+                    }
+                    const unsigned mk = jj < bc ? (bmask & ~selfbit(bf + jj)) : 0u;
+                    const bool ok = mk != 0u && q.w != 0.f;
+                    const unsigned qm = __ballot_sync(FULL, ok);
+                    if (ok) {
+                        float4 *sl = il + 2 * (nil + __popc(qm & lt));
+                        sl[0] = q;
+                        sl[1] = make_float4(qlo.x, qlo.y, qlo.z, __uint_as_float(mk));
+                    }
+                    nil += __popc(qm);
+                }
+            }
+            __syncwarp();
+            if (nil > PW_ICAP - 32) {
+                eval(nil);
+                nil = 0;
+                __syncwarp();
+            }
+        }
+        if (nil) eval(nil);
+        __syncwarp();
+        const unsigned wterms = __reduce_add_sync(FULL, active ? nterm : 0u);
+        if (lane == 0 && wterms)
+            atomicAdd(reinterpret_cast<unsigned long long *>(err + EW_WALK_TERMS), (unsigned long long)wterms);
+        if (active)
+            store_acc(out, t, (double)fa[0] + (double)fa[3], (double)fa[1] + (double)fa[4],
+                      (double)fa[2] + (double)fa[5]);
+        __syncwarp();
+    }
+}
+
 inline int nblk(size_t n, int t = 256) { return (int)std::max<size_t>(1, (n + t - 1) / t); }
 
 }  // namespace
@@ -1163,6 +1474,59 @@ void tree_free(Ctx *c) {
         if (b->ptr) cudaFree(b->ptr);
     delete t;
     c->tree = nullptr;
+}
+
+namespace {
+// Structural invariants of the node arrays (checked build): pre-order with skip
+// pointers that move forward, a root at depth 0 over every particle, contiguous
+// particle ranges, children one level below their parent (1 to 8 of them,
+// tiling its range in order), leaves of one particle or buckets at depth 42.
+__global__ void k_tree_check(size_t nnodes, size_t n, const uint8_t *__restrict__ level,
+                             const uint32_t *__restrict__ first, const uint32_t *__restrict__ cnt,
+                             const uint32_t *__restrict__ skip) {
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nnodes) return;
+    const uint32_t s = skip[k], f = first[k], c = cnt[k];
+    const int L = level[k];
+    bool ok = s > k && s <= nnodes && f < n && L <= MAXL;
+    if (k == 0) ok = ok && L == 0 && f == 0 && s == nnodes;
+    if (ok) {
+        const size_t pe = s < nnodes ? (size_t)first[s] : n;
+        ok = pe > f && pe <= n;
+        if (ok && c > 0) {
+            ok = s == k + 1 && c == pe - f && (c == 1 || L == MAXL);
+        } else if (ok) {
+            ok = pe - f >= 2 && k + 1 < s;
+            uint32_t ch = (uint32_t)k + 1;
+            int nch = 0;
+            size_t pf = f;
+            while (ok && ch < s) {
+                const uint32_t sk = skip[ch];
+                ok = level[ch] == L + 1 && first[ch] == pf && sk > ch && sk <= s && ++nch <= 8;
+                pf = sk < nnodes ? (size_t)first[sk] : n;
+                ch = sk;
+            }
+            ok = ok && ch == s && pf == pe;
+        }
+    }
+    if (!CHK(ok, DERR_TREE)) return;
+}
+}  // namespace
+
+// Checked build: verifies the node arrays before any kernel follows their links,
+// and fails the call if they are broken.
+static gvs_status tree_check(Ctx *c, Tree *t, size_t nnodes) {
+#ifdef GVS_CHECKED
+    k_tree_check<<<nblk(nnodes), 256, 0, c->stream>>>(nnodes, c->n, as<uint8_t>(t->level), as<uint32_t>(t->first),
+                                                      as<uint32_t>(t->cnt), as<uint32_t>(t->skip));
+    c->prof.launches += 1;
+    GVS_TRY(check_launch(c, "tree check"));
+    const unsigned f = checked_take_bh(c->stream);
+    if (f) return fail(c, GVS_ERR_DEVICE, "tree build: invariants violated (device flags 0x%x)", f);
+#else
+    (void)c; (void)t; (void)nnodes;
+#endif
+    return GVS_OK;
 }
 
 // Builds (or reuses) the tree of the resident positions.
@@ -1253,7 +1617,8 @@ gvs_status tree_build(Ctx *c) {
     GVS_CUDA(c, ensure(c, t->first, nnodes * 4)); GVS_CUDA(c, ensure(c, t->cnt, nnodes * 4));
     GVS_CUDA(c, ensure(c, t->skip, nnodes * 4));
     k_nodes<<<nblk(n), 256, 0, st>>>(KH, KL, as<int>(t->delta), as<uint32_t>(t->off), n, as<uint8_t>(t->level),
-                                     as<uint32_t>(t->first), as<uint32_t>(t->cnt), as<uint32_t>(t->skip));
+                                     as<uint32_t>(t->first), as<uint32_t>(t->cnt), as<uint32_t>(t->skip), nnodes);
+    if (kChecked) GVS_TRY(tree_check(c, t, nnodes));
     // sorted particle data
     GVS_CUDA(c, ensure(c, t->sx, b8)); GVS_CUDA(c, ensure(c, t->sy, b8));
     GVS_CUDA(c, ensure(c, t->sz, b8)); GVS_CUDA(c, ensure(c, t->sm, b8));
@@ -1268,7 +1633,7 @@ gvs_status tree_build(Ctx *c) {
     GVS_CUDA(c, ensure(c, t->arrive, nnodes * 4));
     GVS_CUDA(c, ensure(c, t->leaf_of, n * 4));
     k_links<<<nblk(nnodes), 256, 0, st>>>(nnodes, as<uint32_t>(t->first), as<uint32_t>(t->cnt), as<uint32_t>(t->skip),
-                                          as<uint32_t>(t->parent), as<uint32_t>(t->nk), as<uint32_t>(t->leaf_of));
+                                          as<uint32_t>(t->parent), as<uint32_t>(t->nk), as<uint32_t>(t->leaf_of), n);
     c->prof.launches += 1;
     GVS_TRY(check_launch(c, "tree links"));
     t->n = n;
@@ -1297,16 +1662,24 @@ static gvs_status tree_moments64(Ctx *c, Tree *t) {
     return GVS_OK;
 }
 
+// First child slot of every node (exclusive scan of the child counts).
+static gvs_status koff_prepare(Ctx *c, Tree *t) {
+    if (t->koff_version == t->version) return GVS_OK;
+    GVS_CUDA(c, ensure(c, t->koff, t->nnodes * 4));
+    GVS_TRY(exclusive_scan_u32(c, as<uint32_t>(t->nk), as<uint32_t>(t->koff), t->nnodes, nullptr));
+    t->koff_version = t->version;
+    return GVS_OK;
+}
+
 // Child-slot records and particle groups of the current tree for the group walk.
 static gvs_status group_prepare(Ctx *c, Tree *t, int gsize) {
     if (t->grp_version == t->version && t->grp_size == gsize) return GVS_OK;
     const size_t nn = t->nnodes, n = t->n;
     cudaStream_t st = c->stream;
-    GVS_CUDA(c, ensure(c, t->koff, nn * 4));
     GVS_CUDA(c, ensure(c, t->krec, nn * 2 * sizeof(float4)));
     GVS_CUDA(c, ensure(c, t->groups, n * sizeof(int2)));
     GVS_CUDA(c, ensure(c, t->gcount, 16));
-    GVS_TRY(exclusive_scan_u32(c, as<uint32_t>(t->nk), as<uint32_t>(t->koff), nn, nullptr));
+    GVS_TRY(koff_prepare(c, t));
     S2f tab;
     for (int L = 0; L <= MAXL; ++L) {
         const double s = 2.0 * std::ldexp(t->root[3], -L);
@@ -1323,6 +1696,29 @@ static gvs_status group_prepare(Ctx *c, Tree *t, int gsize) {
     GVS_TRY(check_launch(c, "group walk setup"));
     t->grp_version = t->version;
     t->grp_size = gsize;
+    return GVS_OK;
+}
+
+// Parity-walk records (needs the mixed packing: cm32, cm32lo) and groups of <= 32
+// particles of the current tree.
+static gvs_status pgroup_prepare(Ctx *c, Tree *t) {
+    if (t->pgrp_version == t->version) return GVS_OK;
+    const size_t nn = t->nnodes, n = t->n;
+    cudaStream_t st = c->stream;
+    GVS_CUDA(c, ensure(c, t->prec, nn * 3 * sizeof(float4)));
+    GVS_CUDA(c, ensure(c, t->pgroups, n * sizeof(int2)));
+    GVS_CUDA(c, ensure(c, t->pgcount, 16));
+    GVS_TRY(koff_prepare(c, t));
+    k_prec<<<nblk(nn), 256, 0, st>>>(nn, as<uint8_t>(t->level), as<uint32_t>(t->first), as<uint32_t>(t->cnt),
+                                     as<uint32_t>(t->skip), as<uint32_t>(t->nk), as<uint32_t>(t->koff),
+                                     as<float4>(t->cm32), as<float4>(t->cm32lo), as<float4>(t->prec));
+    GVS_CUDA(c, cudaMemsetAsync(t->pgcount.ptr, 0, 8, st));
+    k_groups<<<nblk(nn), 256, 0, st>>>(nn, n, 32u, as<uint8_t>(t->level), as<uint32_t>(t->first),
+                                       as<uint32_t>(t->cnt), as<uint32_t>(t->skip), as<uint64_t>(t->khi),
+                                       as<uint64_t>(t->klo), as<int2>(t->pgroups), as<uint32_t>(t->pgcount));
+    c->prof.launches += 2;
+    GVS_TRY(check_launch(c, "parity walk setup"));
+    t->pgrp_version = t->version;
     return GVS_OK;
 }
 
@@ -1389,13 +1785,19 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
         tab.hi2[L] = (float)(hi * hi * (1.0 + 0x1p-19));
     }
     const AccOut out{as<uint32_t>(t->perm), as<double>(c->ax), as<double>(c->ay), as<double>(c->az),
-                     accumulate ? 1 : 0};
+                     accumulate ? 1 : 0, n};
     // FP32 with a group size set: the group walk (slot records fit 29 bits)
     // (128-particle groups amortise the walk over more particles; below 2^21 particles
     // they would leave too few groups to fill the GPU)
     const int gsize = c->bh_group >= 0 ? c->bh_group : (n >= (size_t(1) << 21) ? 128 : 64);
     const bool group = mode == 1 && gsize > 0 && nnodes < (size_t(1) << 29);
     if (group) GVS_TRY(group_prepare(c, t, gsize));
+    // MIXED: the parity group walk unless per-particle walks were asked for (group size 0)
+    const bool pgroup = mode == 2 && c->bh_group != 0 && nnodes < (size_t(1) << 29);
+    if (pgroup) {
+        GVS_TRY(pgroup_prepare(c, t));
+        GVS_CUDA(c, cudaMemsetAsync(as<uint32_t>(t->pgcount) + 1, 0, 4, st));
+    }
     if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], st));
     if (group) {
         GVS_CUDA(c, cudaMemsetAsync(as<uint32_t>(t->gcount) + 1, 0, 4, st));
@@ -1413,6 +1815,13 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
         else if (gsize == 64) GVS_TRY(guard ? launch(k_walk_group<2, true>) : launch(k_walk_group<2, false>));
         else GVS_TRY(guard ? launch(k_walk_group<1, true>) : launch(k_walk_group<1, false>));
         c->prof.launches += 2;
+    } else if (pgroup) {
+        int per_sm = 0;
+        GVS_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk_pgroup, PW_WARPS * 32, 0));
+        k_walk_pgroup<<<std::max(1, per_sm) * c->num_sms, PW_WARPS * 32, 0, st>>>(
+            as<int2>(t->pgroups), as<uint32_t>(t->pgcount), as<float4>(t->prec), as<double4>(t->cm64),
+            as<float4>(t->pos32), as<float4>(t->pos32lo), as<double>(t->sx), as<double>(t->sy), as<double>(t->sz), tab,
+            theta * theta, (float)(eps * eps), n, nnodes, out, err_ptr(c));
     } else if (mode == 0)
         k_walk<0><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, as<int4>(t->meta), nullptr, as<double4>(t->cm64),
                                                 nullptr, as<double>(t->sx), as<double>(t->sy), as<double>(t->sz),
@@ -1505,5 +1914,7 @@ gvs_status tree_export(Ctx *c, size_t cap, uint8_t *level, uint32_t *first, uint
     GVS_CUDA(c, cudaStreamSynchronize(st));
     return GVS_OK;
 }
+
+GVS_CHECKED_UNIT(bh)
 
 }  // namespace gvs

@@ -292,6 +292,10 @@ __global__ void __launch_bounds__(TJ) k_pack32(const double *__restrict__ X, con
         valid = s < n;
         o = perm[valid ? s : std::min((size_t)t * TJ, n - 1)];
     }
+    if (!CHK_IDX(o, n)) {  // n: the resident state's length (both paths)
+        o = 0;
+        valid = false;
+    }
     // tiles without any member (target-side padding) get a negative radius,
     // so they never trigger the near-field path of the real tile they are paired with
     const int nvalid = __syncthreads_count(valid);
@@ -385,6 +389,10 @@ __global__ void k_pack64(const double *__restrict__ X, const double *__restrict_
     if (s >= npad) return;
     bool valid = s < n;
     uint32_t o = perm[valid ? s : (s / TJ64) * TJ64 < n ? (s / TJ64) * TJ64 : 0];
+    if (!CHK_IDX(o, n)) {
+        o = 0;
+        valid = false;
+    }
     pack[s] = make_double4(X[o], Y[o], Z[o], valid ? M[o] : 0.0);
 }
 
@@ -693,7 +701,8 @@ __global__ void __launch_bounds__(NT, MINB) k_direct32_items(const float4 *__res
                                                        unsigned *__restrict__ counter, float eps2,
                                                        double *__restrict__ partial, size_t npad,
                                                        unsigned *__restrict__ err,
-                                                       unsigned long long *__restrict__ near_count) {
+                                                       unsigned long long *__restrict__ near_count, int ntiles,
+                                                       int nsplit) {
     constexpr int IPT = 2 * NP;
     extern __shared__ __align__(128) float4 smem[];
     __shared__ __align__(8) uint64_t bar[NSTAGE];
@@ -712,6 +721,9 @@ __global__ void __launch_bounds__(NT, MINB) k_direct32_items(const float4 *__res
         __syncthreads();
         if (k >= nitems) break;
         const int4 w = items[k];
+        if (!CHK(w.x >= 0 && w.x < ntiles && w.y >= 0 && w.z > 0 && w.y + w.z <= ntiles && w.w >= 0 &&
+                     w.w < nsplit, DERR_BOUNDS))
+            continue;  // block-uniform: every thread read the same item
         if (!direct_item<NT, NP, NSTAGE, MIXED, GUARD, UNR>(pack, w.x, w.y, w.z, eps2, partial + (size_t)w.w * 3 * npad,
                                                        npad, err, smem, bar, ci, wbox, phase, near_tiles))
             return;
@@ -806,6 +818,7 @@ __global__ void k_reduce(const double *__restrict__ partial, int nsplit, size_t 
 #pragma unroll
         for (int c = 0; c < 3; ++c) r[c] += partial[((size_t)js * 3 + c) * npad + s];
     uint32_t o = perm[s];
+    if (!CHK_IDX(o, n)) return;
     if (accumulate) {
         AX[o] += r[0]; AY[o] += r[1]; AZ[o] += r[2];
     } else {
@@ -1137,7 +1150,7 @@ __global__ void k_pack_w(const double *__restrict__ wx, const double *__restrict
     float a = 0.f, b = 0.f, c = 0.f;
     if (s < n) {
         const uint32_t o = perm[s];
-        a = (float)(scale * wx[o]); b = (float)(scale * wy[o]); c = (float)(scale * wz[o]);
+        if (CHK_IDX(o, n)) { a = (float)(scale * wx[o]); b = (float)(scale * wy[o]); c = (float)(scale * wz[o]); }
     }
     const size_t t = s / TJ, k = s % TJ;
     wpack[t * wtile_f4(TJ) + 2 * k] = make_float4(a, a, b, b);
@@ -1192,7 +1205,7 @@ __global__ void k_pack_w64(const double *__restrict__ wx, const double *__restri
     double a = 0, b = 0, c = 0;
     if (s < n) {
         const uint32_t o = perm[s];
-        a = scale * wx[o]; b = scale * wy[o]; c = scale * wz[o];
+        if (CHK_IDX(o, n)) { a = scale * wx[o]; b = scale * wy[o]; c = scale * wz[o]; }
     }
     wpack[s] = make_double4(a, b, c, 0.0);
 }
@@ -1209,6 +1222,7 @@ __global__ void k_reduce_vjp(const double *__restrict__ partial, int nsplit, siz
 #pragma unroll
         for (int k = 0; k < 7; ++k) r[k] += partial[((size_t)js * 7 + k) * npad + s];
     const uint32_t o = perm[s];
+    if (!CHK_IDX(o, n)) return;
     AX[o] = r[0]; AY[o] = r[1]; AZ[o] = r[2];
     GX[o] += r[3]; GY[o] += r[4]; GZ[o] += r[5];
     GM[o] += r[6];
@@ -1710,7 +1724,7 @@ constexpr int ENS_TJ = 128, ENS_NP = 2, ENS_NSTAGE = 3, ENS_UNR = 2;
 
 gvs_status ens_pack(Ctx *c, int ntiles, const uint32_t *map, float4 *pack) {
     k_pack32<ENS_TJ, true><<<ntiles, ENS_TJ, 0, c->stream>>>(as<double>(c->x), as<double>(c->y), as<double>(c->z),
-                                                            as<double>(c->m), nullptr, 0, pack, map);
+                                                            as<double>(c->m), nullptr, c->n, pack, map);
     c->prof.launches += 1;
     return check_launch(c, "ensemble pack");
 }
@@ -1720,7 +1734,7 @@ int ens_tile() { return ENS_TJ; }
 int ens_targets_per_block() { return ENS_TJ * 2 * ENS_NP; }
 
 gvs_status ens_pairs(Ctx *c, const float4 *pack, const int4 *items, int nitems, unsigned *counter, float eps2,
-                     double *partial, size_t npad) {
+                     double *partial, size_t npad, int ntiles, int nsplit) {
     const int smem = ENS_NSTAGE * tile_f4(ENS_TJ) * (int)sizeof(float4);
     const bool guard = !(eps2 > 0.f);
     auto kern = guard ? k_direct32_items<ENS_TJ, ENS_NP, ENS_NSTAGE, true, true, 4, ENS_UNR>
@@ -1731,7 +1745,8 @@ gvs_status ens_pairs(Ctx *c, const float4 *pack, const int4 *items, int nitems, 
     const int grid = std::max(1, std::min(nitems, c->num_sms * std::max(1, per_sm)));
     GVS_CUDA(c, cudaMemsetAsync(counter, 0, sizeof(unsigned), c->stream));
     unsigned long long *nearc = reinterpret_cast<unsigned long long *>(err_ptr(c) + EW_NEAR_TILES);
-    kern<<<grid, ENS_TJ, smem, c->stream>>>(pack, items, nitems, counter, eps2, partial, npad, err_ptr(c), nearc);
+    kern<<<grid, ENS_TJ, smem, c->stream>>>(pack, items, nitems, counter, eps2, partial, npad, err_ptr(c), nearc,
+                                            ntiles, nsplit);
     c->prof.launches += 1;
     return check_launch(c, "ensemble pair kernel");
 }
@@ -1813,5 +1828,7 @@ gvs_status direct_forces_subset(Ctx *c, int precision, double eps, const int64_t
     c->prof.launches += 1;
     return check_launch(c, "direct subset kernel");
 }
+
+GVS_CHECKED_UNIT(direct)
 
 }  // namespace gvs

@@ -22,7 +22,7 @@ namespace gvs {
 // direct.cu
 gvs_status ens_pack(Ctx *c, int ntiles, const uint32_t *map, float4 *pack);
 gvs_status ens_pairs(Ctx *c, const float4 *pack, const int4 *items, int nitems, unsigned *counter, float eps2,
-                     double *partial, size_t npad);
+                     double *partial, size_t npad, int ntiles, int nsplit);
 int ens_tile_float4s();
 int ens_tile();
 int ens_targets_per_block();
@@ -103,19 +103,28 @@ __global__ void k_iota_u32(uint32_t *a, size_t n) {
 __global__ void k_sys_gather(const uint32_t *__restrict__ perm, const uint32_t *__restrict__ sys_of, size_t n,
                              uint64_t *__restrict__ sk) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) sk[i] = sys_of[perm[i]];
+    if (i < n) {
+        const uint32_t j = perm[i];
+        sk[i] = CHK_IDX(j, n) ? sys_of[j] : 0;
+    }
 }
 
 __global__ void k_compose(const uint32_t *__restrict__ p1, const uint32_t *__restrict__ p2, size_t n,
                           uint32_t *__restrict__ out) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = p1[p2[i]];
+    if (i < n) {
+        const uint32_t j = p2[i];
+        out[i] = CHK_IDX(j, n) ? p1[j] : 0;
+    }
 }
 
 __global__ void k_slot_map(const uint32_t *__restrict__ perm, const uint32_t *__restrict__ pslot, size_t n,
-                           uint32_t *__restrict__ slot_orig) {
+                           uint32_t *__restrict__ slot_orig, size_t npad) {
     const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < n) slot_orig[pslot[s]] = perm[s];
+    if (s < n) {
+        const uint32_t d = pslot[s];
+        if (CHK_IDX(d, npad)) slot_orig[d] = perm[s];
+    }
 }
 
 // a = sum over the system's chunks (fixed order), sorted slot -> caller index.
@@ -127,11 +136,12 @@ __global__ void k_ens_reduce(const double *__restrict__ partial, size_t npad, si
     if (s >= n) return;
     const size_t ps = pslot[s];
     const int ns = (int)sys_sorted_nsplit[s];
+    const uint32_t o = perm[s];
+    if (!CHK_IDX(ps, npad) || !CHK_IDX(o, n)) return;
     double r[3] = {0, 0, 0};
     for (int k = 0; k < ns; ++k)
 #pragma unroll
         for (int c = 0; c < 3; ++c) r[c] += partial[((size_t)k * 3 + c) * npad + ps];
-    const uint32_t o = perm[s];
     AX[o] = r[0]; AY[o] = r[1]; AZ[o] = r[2];
 }
 
@@ -259,13 +269,13 @@ gvs_status ens_forces(Ctx *c) {
     (void)other;
     uint32_t *final_perm = as<uint32_t>(E->keys2);  // reuse as u32 storage (n * 8 bytes available)
     k_compose<<<nb(n), 256, 0, st>>>(p1, slot_sorted, n, final_perm);
-    k_slot_map<<<nb(n), 256, 0, st>>>(final_perm, as<uint32_t>(E->pslot), n, as<uint32_t>(E->slot_orig));
+    k_slot_map<<<nb(n), 256, 0, st>>>(final_perm, as<uint32_t>(E->pslot), n, as<uint32_t>(E->slot_orig), E->npad);
     c->prof.launches += 2;
     GVS_TRY(ens_pack(c, E->ntiles, as<uint32_t>(E->slot_orig), as<float4>(E->pack)));
     const float e2 = (float)(E->eps * E->eps);
     if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], st));
     GVS_TRY(ens_pairs(c, as<float4>(E->pack), as<int4>(E->items), E->nitems, as<unsigned>(E->counter), e2,
-                      as<double>(E->partial), E->npad));
+                      as<double>(E->partial), E->npad, E->ntiles, E->max_split));
     if (c->prof.on) {  // kernel time of the batched pair kernel
         GVS_CUDA(c, cudaEventRecord(c->prof.ev[1], st));
         GVS_CUDA(c, cudaEventSynchronize(c->prof.ev[1]));
@@ -322,6 +332,8 @@ gvs_status ens_steps(Ctx *c, double dt, long long nsteps, bool use_graph) {
     }
     return GVS_OK;
 }
+
+GVS_CHECKED_UNIT(ensemble)
 
 }  // namespace gvs
 

@@ -60,15 +60,36 @@ gvs_status check_launch(Ctx *c, const char *what) {
     return GVS_OK;
 }
 
+// Moves the checked build's per-unit flags into the context's error word.
+static gvs_status gather_checked_flags(Ctx *c) {
+#ifdef GVS_CHECKED
+    cudaStream_t st = c->stream;
+    const unsigned f = checked_take_bh(st) | checked_take_direct(st) | checked_take_sph(st) |
+                       checked_take_ensemble(st) | checked_take_sort(st);
+    if (f) {
+        unsigned w = 0;
+        GVS_CUDA(c, cudaMemcpy(&w, c->err_word.ptr, sizeof w, cudaMemcpyDeviceToHost));
+        w |= f;
+        GVS_CUDA(c, cudaMemcpy(c->err_word.ptr, &w, sizeof w, cudaMemcpyHostToDevice));
+    }
+#else
+    (void)c;
+#endif
+    return GVS_OK;
+}
+
 gvs_status read_device_errors(Ctx *c) {
     unsigned flags = 0;
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    GVS_TRY(gather_checked_flags(c));
     GVS_CUDA(c, cudaMemcpyAsync(&flags, c->err_word.ptr, sizeof flags, cudaMemcpyDeviceToHost, c->stream));
     GVS_CUDA(c, cudaStreamSynchronize(c->stream));
     if (flags) {
         GVS_CUDA(c, cudaMemsetAsync(c->err_word.ptr, 0, sizeof(unsigned), c->stream));
         gvs_status s = (flags & (DERR_MBAR_TIMEOUT | DERR_SPIN_TIMEOUT)) ? GVS_ERR_TIMEOUT : GVS_ERR_DEVICE;
         return fail(c, s, "device error word 0x%x (1 mbarrier timeout, 2 stack overflow, 4 neighbour overflow, "
-                          "8 non-finite, 16 tree, 32 bounds, 64 queue timeout)", flags);
+                          "8 non-finite, 16 tree invariant, 32 index out of range, 64 sort look-back timeout)",
+                    flags);
     }
     return GVS_OK;
 }
@@ -203,7 +224,9 @@ static gvs_status check_ctx(const gvs_ctx *ctx) {
 
 extern "C" {
 
-const char *gvs_version(void) { return "gravis-gb300 0.1.0 (sm_103a)"; }
+const char *gvs_version(void) {
+    return kChecked ? "gravis-gb300 0.1.0 (sm_103a, checked)" : "gravis-gb300 0.1.0 (sm_103a)";
+}
 
 gvs_status gvs_create(gvs_ctx **out, int device) {
     if (!out) return fail(nullptr, GVS_ERR_INVALID_ARG, "gvs_create: out is NULL");
@@ -251,7 +274,7 @@ gvs_status gvs_destroy(gvs_ctx *c) {
                      &c->ptype, &c->u, &c->h, &c->alpha, &c->rho, &c->pres, &c->cs, &c->du_dt, &c->omega,
                      &c->div_v, &c->max_mu, &c->dalpha_dt, &c->keys, &c->keys_alt, &c->perm, &c->perm_alt,
                      &c->exact_terms, &c->exact_sums,
-                     &c->sort_hist, &c->bbox_part, &c->jpack32, &c->jpack64, &c->partial, &c->scratch_a,
+                     &c->sort_hist, &c->sort_state, &c->bbox_part, &c->jpack32, &c->jpack64, &c->partial, &c->scratch_a,
                      &c->scratch_b, &c->err_word, &c->red_part, &c->l2_flush};
     for (DevBuf *b : all)
         if (b->ptr) cudaFree(b->ptr);
@@ -301,6 +324,8 @@ gvs_status gvs_sync(gvs_ctx *c) {
 gvs_status gvs_device_errors(gvs_ctx *c, unsigned *flags) {
     GVS_TRY(check_ctx(c));
     if (!flags) return fail(c, GVS_ERR_INVALID_ARG, "flags is NULL");
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    GVS_TRY(gather_checked_flags(c));
     GVS_CUDA(c, cudaMemcpyAsync(flags, c->err_word.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
     GVS_CUDA(c, cudaStreamSynchronize(c->stream));
     GVS_CUDA(c, cudaMemsetAsync(c->err_word.ptr, 0, sizeof(unsigned), c->stream));

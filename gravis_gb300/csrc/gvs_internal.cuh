@@ -30,7 +30,7 @@ enum DeviceError : unsigned {
     DERR_NAN = 1u << 3,            // non-finite value detected
     DERR_TREE = 1u << 4,           // tree build invariant violated
     DERR_BOUNDS = 1u << 5,         // checked build: index out of range
-    DERR_SPIN_TIMEOUT = 1u << 6,   // persistent-kernel queue wait hit its cap
+    DERR_SPIN_TIMEOUT = 1u << 6,   // a radix-sort look-back wait hit its cap
 };
 
 // Layout of the context's device word area (err_word, 64 u32): word 0 holds the
@@ -97,6 +97,7 @@ struct Ctx {
 
     // direct-sum scratch
     DevBuf keys, keys_alt, perm, perm_alt, sort_hist, bbox_part;
+    DevBuf sort_state;  // radix sort: digit histograms, tile counters, look-back status
     DevBuf jpack32, jpack64, partial;
     DevBuf exact_terms, exact_sums;  // FP64_EXACT for small systems: a source chunk's terms, running sums
     // generic scratch
@@ -161,6 +162,49 @@ gvs_status read_device_errors(Ctx *c);  // syncs the stream; DEVICE_ERROR if any
     } while (0)
 
 inline unsigned *err_ptr(Ctx *c) { return as<unsigned>(c->err_word); }
+
+// ---------------------------------------------------------------------------
+// checked build (-DGVS_CHECKED, built as libgvs_checked.so)
+// ---------------------------------------------------------------------------
+// Kernels test each index they compute -- through a permutation, a tree link, a
+// leaf or neighbour slot, a work item -- against the array it indexes.  A bad
+// index sets DERR_BOUNDS in this translation unit's flag word and the access is
+// skipped (no kernel traps); the tree build also verifies its invariants
+// (DERR_TREE).  read_device_errors gathers every unit's flags into the
+// context's error word.  In the normal build CHK_IDX and CHK are `true` and the
+// tests compile away.
+#ifdef GVS_CHECKED
+static __device__ unsigned g_checked_flags;
+__device__ __forceinline__ bool chk_fail(unsigned bit) {
+    atomicOr(&g_checked_flags, bit);
+    return false;
+}
+#define CHK_IDX(i, bound) (((size_t)(i) < (size_t)(bound)) ? true : ::gvs::chk_fail((unsigned)::gvs::DERR_BOUNDS))
+#define CHK(cond, bit) ((cond) ? true : ::gvs::chk_fail((unsigned)(bit)))
+// Reads and clears this translation unit's flag word (host side).
+static inline unsigned checked_take(cudaStream_t st) {
+    unsigned v = 0;
+    static const unsigned zero = 0;
+    if (cudaMemcpyFromSymbolAsync(&v, g_checked_flags, sizeof v, 0, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyToSymbolAsync(g_checked_flags, &zero, sizeof zero, 0, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return DERR_BOUNDS;
+    return v;
+}
+#define GVS_CHECKED_UNIT(name) \
+    unsigned checked_take_##name(cudaStream_t st) { return checked_take(st); }
+unsigned checked_take_bh(cudaStream_t st);
+unsigned checked_take_direct(cudaStream_t st);
+unsigned checked_take_sph(cudaStream_t st);
+unsigned checked_take_ensemble(cudaStream_t st);
+unsigned checked_take_sort(cudaStream_t st);
+constexpr bool kChecked = true;
+#else
+#define CHK_IDX(i, bound) true
+#define CHK(cond, bit) true
+#define GVS_CHECKED_UNIT(name)
+constexpr bool kChecked = false;
+#endif
 
 // ---------------------------------------------------------------------------
 // PTX helpers: mbarrier + untiled bulk copy (cp.async.bulk), sm_90+ / sm_103a

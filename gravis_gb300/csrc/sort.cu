@@ -7,34 +7,202 @@
 // low word then high word) so that the sorted order is the depth-first order
 // of the reference octree (crates/sim-core/src/octree.rs:156-239).
 //
-// One pass per 8-bit digit: (1) per-block digit histograms, (2) one exclusive
-// scan over the [digit][block] table, (3) a stable scatter in which each block
-// ranks its keys in index order with warp match/ballot and per-warp counters.
+// Onesweep form (one kernel per 8-bit digit pass, after Adinets and Merrill,
+// "Onesweep: a faster least significant digit radix sort for GPUs", 2022):
+//  1. one read of the keys counts the digits of every pass (global histograms);
+//  2. one tiny launch turns each pass's 256 counts into exclusive offsets;
+//  3. per pass, each block takes the next tile index from a counter, counts its
+//     tile's digits, publishes the counts, and adds up its predecessors' counts
+//     by decoupled look-back (a predecessor publishes its local count first and
+//     its inclusive prefix as soon as it knows it); then it scatters its keys
+//     stably: in index order within the tile (warp match and per-warp counts).
+// A block only waits on tiles that took their index before it did, and so are
+// already running; every wait is still bounded: after the cap the block sets
+// DERR_SPIN_TIMEOUT, counts the missing tile as empty and carries on.
+// 3 + passes launches per sort instead of five per pass.
 #include "gvs_internal.cuh"
 
 namespace gvs {
 
 namespace {
 constexpr int NT = 256;              // threads per block
-constexpr int IPT = 16;              // keys per thread per pass
-constexpr int TILE = NT * IPT;       // keys per block
+constexpr int IPT = 8;               // keys per thread per pass
+constexpr int TILE = NT * IPT;       // keys per tile
 constexpr int RADIX = 256;
 constexpr int NWARP = NT / 32;
+constexpr int MAXPASS = 8;
+constexpr uint32_t ST_INCL = 1u << 31;   // the tile's inclusive prefix (this digit, tiles 0..t)
+constexpr uint32_t ST_LOCAL = 1u << 30;  // only the tile's own count so far
+constexpr uint32_t ST_VALUE = ST_LOCAL - 1u;
+constexpr unsigned SPIN_CAP = 1u << 22;  // polls of one predecessor's status before giving up
 
+__device__ __forceinline__ uint32_t ld_status(const uint32_t *p) {
+    return *reinterpret_cast<const volatile uint32_t *>(p);
+}
+__device__ __forceinline__ void st_status(uint32_t *p, uint32_t v) { *reinterpret_cast<volatile uint32_t *>(p) = v; }
+
+// Digit counts of every pass in one read of the keys.
 template <class K>
-__global__ void __launch_bounds__(NT) k_hist(const K *__restrict__ keys, size_t n, int shift,
-                                             uint32_t *__restrict__ hist, int nblocks) {
-    __shared__ uint32_t h[RADIX];
-    for (int i = threadIdx.x; i < RADIX; i += NT) h[i] = 0;
+__global__ void __launch_bounds__(NT) k_os_hist(const K *__restrict__ keys, size_t n, int begin_bit, int npass,
+                                                uint32_t *__restrict__ ghist) {
+    __shared__ uint32_t h[MAXPASS][RADIX];
+    for (int i = threadIdx.x; i < MAXPASS * RADIX; i += NT) (&h[0][0])[i] = 0u;
     __syncthreads();
-    size_t base = (size_t)blockIdx.x * TILE;
-#pragma unroll 4
-    for (int k = 0; k < IPT; ++k) {
-        size_t idx = base + (size_t)k * NT + threadIdx.x;
-        if (idx < n) atomicAdd(&h[(unsigned)(keys[idx] >> shift) & 0xFFu], 1u);
+    for (size_t i = (size_t)blockIdx.x * NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) {
+        const K k = keys[i];
+        for (int p = 0; p < npass; ++p) atomicAdd(&h[p][(unsigned)(k >> (begin_bit + 8 * p)) & 0xFFu], 1u);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < RADIX; i += NT) hist[(size_t)i * nblocks + blockIdx.x] = h[i];
+    for (int i = threadIdx.x; i < npass * RADIX; i += NT) {
+        const uint32_t v = (&h[0][0])[i];
+        if (v) atomicAdd(ghist + i, v);
+    }
+}
+
+// ghist[p][*] -> exclusive offsets, one block of RADIX threads per pass.
+__global__ void __launch_bounds__(RADIX) k_os_scan(uint32_t *__restrict__ ghist) {
+    __shared__ uint32_t ws[RADIX / 32];
+    uint32_t *h = ghist + (size_t)blockIdx.x * RADIX;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const uint32_t v = h[t];
+    uint32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    uint32_t before = 0;
+    for (int k = 0; k < w; ++k) before += ws[k];
+    h[t] = before + x - v;
+}
+
+template <class K>
+__global__ void __launch_bounds__(NT) k_os_pass(const K *__restrict__ keys, const uint32_t *__restrict__ vals,
+                                                K *__restrict__ kout, uint32_t *__restrict__ vout, size_t n,
+                                                int shift, const uint32_t *__restrict__ gbase,
+                                                uint32_t *__restrict__ status, uint32_t *__restrict__ counter,
+                                                unsigned *__restrict__ err) {
+    __shared__ uint32_t tile_s;
+    __shared__ uint32_t hist[RADIX];
+    __shared__ uint32_t base[RADIX];
+    __shared__ uint32_t wcnt[NWARP][RADIX];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) tile_s = atomicAdd(counter, 1u);
+    for (int i = tid; i < RADIX; i += NT) hist[i] = 0u;
+    __syncthreads();
+    const uint32_t tile = tile_s;
+    const size_t tbase = (size_t)tile * TILE;
+    K key[IPT];
+    unsigned dig[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const size_t idx = tbase + (size_t)k * NT + tid;
+        dig[k] = 256u;  // out-of-range slots form their own group
+        key[k] = 0;
+        if (idx < n) {
+            key[k] = keys[idx];
+            dig[k] = (unsigned)(key[k] >> shift) & 0xFFu;
+            atomicAdd(&hist[dig[k]], 1u);
+        }
+    }
+    __syncthreads();
+    // publish this tile's counts, then look back for the prefix of the tiles before it
+    for (int d = tid; d < RADIX; d += NT) {
+        const uint32_t own = hist[d];
+        uint32_t *mine = status + (size_t)tile * RADIX + d;
+        if (tile == 0) {
+            st_status(mine, ST_INCL | own);
+            base[d] = gbase[d];
+            continue;
+        }
+        st_status(mine, ST_LOCAL | own);
+        uint32_t sum = 0;
+        for (long t = (long)tile - 1; t >= 0; --t) {
+            const uint32_t *p = status + (size_t)t * RADIX + d;
+            uint32_t v = 0;
+            for (unsigned it = 0; it < SPIN_CAP; ++it) {
+                v = ld_status(p);
+                if (v & (ST_INCL | ST_LOCAL)) break;
+            }
+            if (!(v & (ST_INCL | ST_LOCAL))) {
+                atomicOr(err, (unsigned)DERR_SPIN_TIMEOUT);
+                continue;
+            }
+            sum += v & ST_VALUE;
+            if (v & ST_INCL) break;
+        }
+        st_status(mine, ST_INCL | (sum + own));
+        base[d] = gbase[d] + sum;
+    }
+    __syncthreads();
+    // stable scatter: slices of NT keys in index order, warps in order, lanes in order
+    // (unrolled: the tile's keys stay in registers)
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        for (int i = tid; i < NWARP * RADIX; i += NT) (&wcnt[0][0])[i] = 0u;
+        __syncthreads();
+        const size_t idx = tbase + (size_t)k * NT + tid;
+        const bool valid = idx < n;
+        const unsigned d = dig[k];
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+        const unsigned rank = __popc(peers & ((1u << lane) - 1u));
+        if (valid && lane == __ffs(peers) - 1) wcnt[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            uint32_t off = base[d];
+            for (int w = 0; w < warp; ++w) off += wcnt[w][d];
+            const size_t dst = (size_t)off + rank;
+            if (CHK_IDX(dst, n)) {
+                kout[dst] = key[k];
+                vout[dst] = vals[idx];
+            }
+        }
+        __syncthreads();
+        for (int dd = tid; dd < RADIX; dd += NT) {
+            uint32_t s = 0;
+#pragma unroll
+            for (int w = 0; w < NWARP; ++w) s += wcnt[w][dd];
+            base[dd] += s;
+        }
+        __syncthreads();
+    }
+}
+
+template <class K>
+gvs_status radix_sort_impl(Ctx *c, K *keys, uint32_t *vals, K *keys_alt, uint32_t *vals_alt, size_t n,
+                           int begin_bit, int end_bit, K **keys_out, uint32_t **vals_out) {
+    K *kin = keys, *kout = keys_alt;
+    uint32_t *vin = vals, *vout = vals_alt;
+    if (n > 1) {
+        if (n >= (size_t)ST_LOCAL) return fail(c, GVS_ERR_INVALID_ARG, "radix sort: n = %zu exceeds 2^30", n);
+        const int npass = (end_bit - begin_bit + 7) / 8;
+        if (npass > MAXPASS) return fail(c, GVS_ERR_INVALID_ARG, "radix sort: %d passes", npass);
+        const size_t ntiles = (n + TILE - 1) / TILE;
+        // scratch: histograms [npass][256], tile counters [npass] (padded), status [npass][ntiles][256]
+        const size_t words = (size_t)npass * RADIX + 64 + (size_t)npass * ntiles * RADIX;
+        GVS_CUDA(c, ensure(c, c->sort_state, words * sizeof(uint32_t)));
+        uint32_t *ghist = as<uint32_t>(c->sort_state);
+        uint32_t *counters = ghist + (size_t)npass * RADIX;
+        uint32_t *status = counters + 64;
+        GVS_CUDA(c, cudaMemsetAsync(ghist, 0, words * sizeof(uint32_t), c->stream));
+        const int hblocks = (int)std::min<size_t>((n + NT - 1) / NT, (size_t)c->num_sms * 4);
+        k_os_hist<K><<<hblocks, NT, 0, c->stream>>>(kin, n, begin_bit, npass, ghist);
+        k_os_scan<<<npass, RADIX, 0, c->stream>>>(ghist);
+        c->prof.launches += 2;
+        for (int p = 0; p < npass; ++p) {
+            k_os_pass<K><<<(int)ntiles, NT, 0, c->stream>>>(kin, vin, kout, vout, n, begin_bit + 8 * p,
+                                                          ghist + (size_t)p * RADIX, status + (size_t)p * ntiles * RADIX,
+                                                          counters + p, err_ptr(c));
+            c->prof.launches += 1;
+            GVS_TRY(check_launch(c, "radix sort pass"));
+            K *tk = kin; kin = kout; kout = tk;
+            uint32_t *tv = vin; vin = vout; vout = tv;
+        }
+    }
+    *keys_out = kin;
+    *vals_out = vin;
+    return GVS_OK;
 }
 
 // Exclusive scan of m entries by one block of 1024 threads.
@@ -62,86 +230,14 @@ __global__ void __launch_bounds__(1024) k_scan1(uint32_t *a, int m) {
 }
 
 __global__ void k_add_u32(uint32_t *a, const uint32_t *b) { a[0] += b[0]; }
-
-template <class K>
-__global__ void __launch_bounds__(NT) k_scatter(const K *__restrict__ keys, const uint32_t *__restrict__ vals,
-                                                K *__restrict__ kout, uint32_t *__restrict__ vout, size_t n,
-                                                int shift, const uint32_t *__restrict__ hist, int nblocks) {
-    __shared__ uint32_t base[RADIX];
-    __shared__ uint32_t wcnt[NWARP][RADIX];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int i = tid; i < RADIX; i += NT) base[i] = hist[(size_t)i * nblocks + blockIdx.x];
-    const size_t tbase = (size_t)blockIdx.x * TILE;
-    for (int k = 0; k < IPT; ++k) {
-        for (int i = tid; i < NWARP * RADIX; i += NT) (&wcnt[0][0])[i] = 0u;
-        __syncthreads();
-        const size_t idx = tbase + (size_t)k * NT + tid;
-        const bool valid = idx < n;
-        K key = 0;
-        unsigned d = 256u;  // out-of-range lanes form their own group
-        if (valid) {
-            key = keys[idx];
-            d = (unsigned)(key >> shift) & 0xFFu;
-        }
-        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
-        const unsigned rank = __popc(peers & ((1u << lane) - 1u));
-        if (valid && lane == __ffs(peers) - 1) wcnt[warp][d] = __popc(peers);
-        __syncthreads();
-        if (valid) {
-            uint32_t off = base[d];
-            for (int w = 0; w < warp; ++w) off += wcnt[w][d];
-            const size_t dst = (size_t)off + rank;
-            kout[dst] = key;
-            vout[dst] = vals[idx];
-        }
-        __syncthreads();
-        for (int dd = tid; dd < RADIX; dd += NT) {
-            uint32_t s = 0;
-#pragma unroll
-            for (int w = 0; w < NWARP; ++w) s += wcnt[w][dd];
-            base[dd] += s;
-        }
-        __syncthreads();
-    }
-}
-
-}  // namespace
-
-// In-place exclusive scan of m counts; bsum holds ceil(m / 4096) + 1 words of scratch.
-void scan_counts_inplace(Ctx *c, uint32_t *a, size_t m, uint32_t *bsum);
-
-namespace {
-template <class K>
-gvs_status radix_sort_impl(Ctx *c, K *keys, uint32_t *vals, K *keys_alt, uint32_t *vals_alt, size_t n,
-                           int begin_bit, int end_bit, K **keys_out, uint32_t **vals_out) {
-    K *kin = keys, *kout = keys_alt;
-    uint32_t *vin = vals, *vout = vals_alt;
-    if (n > 1) {
-        const int nblocks = ceil_div((long long)n, TILE);
-        const size_t m = (size_t)RADIX * nblocks;
-        GVS_CUDA(c, ensure(c, c->sort_hist, (m + m / 1024 + 64) * sizeof(uint32_t)));
-        uint32_t *hist = as<uint32_t>(c->sort_hist);
-        uint32_t *bsum = hist + m;
-        for (int bit = begin_bit; bit < end_bit; bit += 8) {
-            k_hist<K><<<nblocks, NT, 0, c->stream>>>(kin, n, bit, hist, nblocks);
-            scan_counts_inplace(c, hist, m, bsum);
-            k_scatter<K><<<nblocks, NT, 0, c->stream>>>(kin, vin, kout, vout, n, bit, hist, nblocks);
-            c->prof.launches += 2;
-            GVS_TRY(check_launch(c, "radix sort pass"));
-            K *tk = kin; kin = kout; kout = tk;
-            uint32_t *tv = vin; vin = vout; vout = tv;
-        }
-    }
-    *keys_out = kin;
-    *vals_out = vin;
-    return GVS_OK;
-}
 }  // namespace
 
 gvs_status radix_sort_u64(Ctx *c, uint64_t *keys, uint32_t *vals, uint64_t *keys_alt, uint32_t *vals_alt, size_t n,
                           int begin_bit, int end_bit, uint64_t **keys_out, uint32_t **vals_out) {
     return radix_sort_impl<uint64_t>(c, keys, vals, keys_alt, vals_alt, n, begin_bit, end_bit, keys_out, vals_out);
 }
+
+GVS_CHECKED_UNIT(sort)
 
 }  // namespace gvs
 
@@ -211,22 +307,6 @@ __global__ void __launch_bounds__(SCAN_NT) k_scan_apply(const uint32_t *in, size
         }
 }
 }  // namespace
-
-// Three launches, each wide: block sums, one-block scan of the (few) block sums,
-// then the block-local scans plus their offsets.  In place is safe: every thread
-// reads its own elements before writing them.
-void scan_counts_inplace(Ctx *c, uint32_t *a, size_t m, uint32_t *bsum) {
-    if (m <= 4 * 1024) {  // small tables: one launch of one block beats three launches
-        k_scan1<<<1, 1024, 0, c->stream>>>(a, (int)m);
-        c->prof.launches += 1;
-        return;
-    }
-    const int nb = ceil_div((long long)m, SCAN_TILE);
-    k_scan_blocksum<<<nb, SCAN_NT, 0, c->stream>>>(a, m, bsum);
-    k_scan1<<<1, 1024, 0, c->stream>>>(bsum, nb);
-    k_scan_apply<<<nb, SCAN_NT, 0, c->stream>>>(a, m, bsum, a);
-    c->prof.launches += 3;
-}
 
 // out[i] = sum_{k<i} in[i], for i in [0, n); also returns the total in *total_dev[0] (device).
 gvs_status exclusive_scan_u32(Ctx *c, const uint32_t *in, uint32_t *out, size_t n, uint32_t *total_dev) {

@@ -283,6 +283,7 @@ __global__ void k_gather_sph(size_t n, const uint32_t *__restrict__ perm, const 
     const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const uint32_t o = perm[s];
+    if (!CHK_IDX(o, n)) return;
     gas[s] = ptype[o] == 4 ? 1 : 0;
     svx[s] = vx[o]; svy[s] = vy[o]; svz[s] = vz[o];
     sm[s] = m[o]; sh[s] = h[o]; su[s] = u[o]; salpha[s] = alpha[o];
@@ -351,6 +352,7 @@ __device__ __forceinline__ void density_sums_f64(const TreeView &tv, const doubl
     dws = 0.0;
     for (int k = 0; k < count; ++k) {
         const uint32_t j = row[k];
+        if (!CHK_IDX(j, tv.n)) continue;
         const double dx = xi - tv.sx[j], dy = yi - tv.sy[j], dz = zi - tv.sz[j];
         const double r = sqrt(dx * dx + dy * dy + dz * dz);
         if (r < 2.0 * h) {
@@ -449,10 +451,10 @@ __global__ void k_forces(const TreeView tv, const uint8_t *__restrict__ gas, con
     const double por2_i = rho_i > 0.0 ? p_i / (omega_i * rho_i * rho_i) : 0.0;
     double axa = 0.0, aya = 0.0, aza = 0.0, dua = 0.0, dva = 0.0, mmu = 0.0;
     const uint32_t *row = list + i * (size_t)kmax;
-    const int count = (int)cnt[i];
+    const int count = CHK(cnt[i] <= (uint32_t)kmax, DERR_BOUNDS) ? (int)cnt[i] : 0;
     for (int k = 0; k < count; ++k) {
         const uint32_t j = row[k];
-        if ((size_t)j == i) continue;
+        if ((size_t)j == i || !CHK_IDX(j, tv.n)) continue;
         const double dx = xi - tv.sx[j], dy = yi - tv.sy[j], dz = zi - tv.sz[j];
         const double r = sqrt(dx * dx + dy * dy + dz * dz);
         const double hj = sh[j];
@@ -577,10 +579,11 @@ __global__ void k_sph_src_hydro(size_t n, const double *__restrict__ svx, const 
 // with f(q) = s^4 (1 + 2q), s = 1 - q/2; rho = norm/h^3 S1, dW/dh sum = norm/h^4 S2.
 __device__ __forceinline__ void density_sums_mixed(const float4 *__restrict__ a4, const float4 *__restrict__ b4,
                                                    const uint32_t *row, int count, float4 pa, float4 pb, float ih,
-                                                   double &s1, double &s2) {
+                                                   double &s1, double &s2, size_t n) {
     float h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;
     for (int k = 0; k < count; ++k) {
         const uint32_t j = row[k];
+        if (!CHK_IDX(j, n)) continue;
         const float4 a = a4[j], b = b4[j];
         const float dx = __fadd_rn(__fsub_rn(pa.x, a.x), __fsub_rn(pb.x, b.x));
         const float dy = __fadd_rn(__fsub_rn(pa.y, a.y), __fsub_rn(pb.y, b.y));
@@ -631,7 +634,7 @@ __global__ void k_density_mixed(const TreeView tv, const float4 *__restrict__ po
     bool close = false, requeried = false;
     for (int it = 0; it < 5; ++it) {
         double s1, s2;
-        density_sums_mixed(a4, b4, row, count, pa, pb, (float)(1.0 / h), s1, s2);
+        density_sums_mixed(a4, b4, row, count, pa, pb, (float)(1.0 / h), s1, s2, tv.n);
         const double nh3 = norm3d() / (h * h * h);
         const double rho = nh3 * s1, dws = nh3 / h * s2;
         const double h_new = rho > 0.0 ? fmin(eta * cbrt(m_i / rho), h_max) : fmin(h, h_max);
@@ -692,6 +695,7 @@ __global__ void __launch_bounds__(128) k_density_redo(
     for (unsigned k = blockIdx.x * wpb + (threadIdx.x >> 5); k < m; k += gridDim.x * wpb) {
         const uint32_t code = redo_idx[k];
         const size_t i = code & 0x7FFFFFFFu;
+        if (!CHK_IDX(i, tv.n)) continue;  // warp-uniform: the warp reads one entry
         const double xi = tv.sx[i], yi = tv.sy[i], zi = tv.sz[i], m_i = sm[i];
         uint32_t *row = list + i * (size_t)kmax;
         double h = h0[i];
@@ -714,6 +718,7 @@ __global__ void __launch_bounds__(128) k_density_redo(
             double rho = 0.0, dws = 0.0;
             for (int q = lane; q < count; q += 32) {
                 const uint32_t j = row[q];
+                if (!CHK_IDX(j, tv.n)) continue;
                 const double dx = xi - tv.sx[j], dy = yi - tv.sy[j], dz = zi - tv.sz[j];
                 const double r = sqrt(dx * dx + dy * dy + dz * dz);
                 if (r < 2.0 * h) {
@@ -793,10 +798,10 @@ __global__ void __launch_bounds__(128) k_forces_mixed(
     for (int k = 0; k < 12; ++k) sum[k][0] = sum[k][1] = 0.f;
     float mmu = 0.f;
     const uint32_t *row = list + i * (size_t)kmax;
-    const int count = (int)cnt[i];
+    const int count = CHK(cnt[i] <= (uint32_t)kmax, DERR_BOUNDS) ? (int)cnt[i] : 0;
     for (int k = 0; k < count; ++k) {
         const uint32_t j = row[k];
-        if ((size_t)j == i) continue;
+        if ((size_t)j == i || !CHK_IDX(j, n)) continue;
         const float4 a = a4[j], b = b4[j];
         const float dx = __fadd_rn(__fsub_rn(pa.x, a.x), __fsub_rn(pb.x, b.x));
         const float dy = __fadd_rn(__fsub_rn(pa.y, a.y), __fsub_rn(pb.y, b.y));
@@ -906,6 +911,7 @@ __global__ void k_scatter_sph(size_t n, const uint32_t *__restrict__ perm, const
     const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const uint32_t o = perm[s];
+    if (!CHK_IDX(o, n)) return;
     omega[o] = somega[s];
     divv[o] = sdivv[s];
     maxmu[o] = smaxmu[s];
@@ -1217,5 +1223,7 @@ gvs_status sph_neighbors_export(Ctx *c, size_t cap, uint32_t *start, uint32_t *c
     }
     return GVS_OK;
 }
+
+GVS_CHECKED_UNIT(sph)
 
 }  // namespace gvs

@@ -113,7 +113,10 @@ gvs_status gvs_set_fault(gvs_ctx *ctx, const char *spec);
 gvs_status gvs_sync(gvs_ctx *ctx);
 /* Reads and clears the device error word.  Bits: 1 an mbarrier wait hit its cap,
  * 2 tree-walk stack overflow, 4 SPH neighbour row overflow, 8 non-finite value,
- * 16 tree invariant violated, 32 index out of range, 64 work-queue wait hit its cap. */
+ * 16 tree invariant violated and 32 index out of range (both raised only by the checked
+ * build, libgvs_checked.so, whose kernels test the indices they compute and skip bad
+ * accesses instead of trapping; gvs_version() then ends in "checked)"), 64 a radix-sort
+ * look-back wait hit its cap. */
 gvs_status gvs_device_errors(gvs_ctx *ctx, unsigned *flags);
 
 /* ---- state transfer (Particles <-> device) ------------------------------------ */
@@ -270,17 +273,22 @@ gvs_status gvs_autotune_direct(gvs_ctx *ctx, int precision, double softening, in
  * holds more than n/64 particles runs with 128-particle tiles (mixed-precision accuracy
  * needs tiles that are small against the system); the autotuner skips such shapes. */
 gvs_status gvs_set_direct_shape(gvs_ctx *ctx, int nthreads, int ipt, int min_blocks, int unroll);
-/* Walk of the FP32 Barnes-Hut (gvs_gravity_bh / ALGO_BH with GVS_PREC_FP32).
- * group_size 32, 64 or 128: one warp walks the tree for a group of up to that many
- * particles sharing a tree cell, opening a node unless s^2 < theta^2 d^2 with d the
- * distance from its COM to the group's bounding box.  Every particle then sums a
+/* Barnes-Hut walk forms (gvs_gravity_bh / ALGO_BH).
+ * FP32: group_size 32, 64 or 128: one warp walks the tree for a group of up to that
+ * many particles sharing a tree cell, opening a node unless s^2 < theta^2 d^2 with d
+ * the distance from its COM to the group's bounding box.  Every particle then sums a
  * refinement of its own Barnes-Hut node set (the reference's test accepts every node
- * the group accepts, up to the f32 rounding of the test at the opening boundary).  -1 (default): 128 from 2^21 particles, else 64.  0: the
- * per-particle walk with the reference's test on f32 positions.  FP64 and MIXED walks
- * are always per-particle.  A group whose walk takes more than `budget` iterations
- * (32 nodes each; 0 = the default 1024) is walked per particle instead: its box lies
- * close to much denser matter, which the group test would open down to single
- * particles. */
+ * the group accepts, up to the f32 rounding of the test at the opening boundary).
+ * -1 (default): 128 from 2^21 particles, else 64.  0: the per-particle walk with the
+ * reference's test on f32 positions.  A group whose walk takes more than `budget`
+ * iterations (32 nodes each; 0 = the default 1024) is walked per particle instead: its
+ * box lies close to much denser matter, which the group test would open down to
+ * single particles.
+ * MIXED: unless group_size is 0, warps of up to 32 particles of one tree cell walk
+ * together while every particle makes its own decision (the reference's test: an f32
+ * test outside a certified band, the f64 test inside it), so each particle sums
+ * exactly the terms of its own walk; 0: one walk per particle.
+ * FP64 walks are always per-particle. */
 gvs_status gvs_set_bh_walk(gvs_ctx *ctx, int group_size, int budget);
 /* Every candidate of the last gvs_autotune_direct with its kernel time (ms per force
  * evaluation).  Always sets *count; fills the arrays (any may be NULL) if cap >= *count.
