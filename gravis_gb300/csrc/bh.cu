@@ -62,13 +62,11 @@ struct Tree {
     DevBuf boxx, boxy, boxz;         // per node cell centre (f64)
     DevBuf sx, sy, sz, sm;           // sorted particle positions / masses (f64)
     DevBuf pos32, cm32, cm64, meta;
-    DevBuf pos32lo, cm32lo;  // mixed walk: f32 lo words of positions and COMs
+    DevBuf pos32lo;          // mixed walk: f32 lo words of the sorted positions
+    DevBuf mrec;             // mixed walk: per node (meta, f32 COM + mass, f32 COM lo word), 48 B
     // group walk (f32): child-slot records, groups of <= 32*NPL particles, work counter
     DevBuf nk, koff, krec, groups, gcount;
-    // parity group walk (mixed): child-slot records with f32 lo words and node ids,
-    // groups of <= 32 particles, work counter
-    DevBuf prec, pgroups, pgcount;
-    unsigned long long koff_version = ~0ull, pgrp_version = ~0ull;
+    unsigned long long koff_version = ~0ull;
     DevBuf parent, arrive;  // per node: parent index, children that finished their moments
     DevBuf leaf_of;         // per sorted particle: the leaf that holds it
     unsigned long long grp_version = ~0ull;
@@ -508,19 +506,27 @@ __global__ void k_moments32_up(size_t nnodes, const uint32_t *__restrict__ first
     }
 }
 
+// Per-node records of the walks: meta (skip, first, count, level) for every walk,
+// the f64 moments for the f64 walk and the mixed walk's band tests, and for the
+// mixed walk one 48-byte record (meta, f32 COM + mass, f32 lo word of the COM),
+// so that each step of that walk reads one block of memory.
 __global__ void k_pack_nodes(size_t nnodes, const uint8_t *__restrict__ level, const uint32_t *__restrict__ first,
                              const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ skip,
                              const double *__restrict__ mass, const double *__restrict__ cx,
-                             const double *__restrict__ cy, const double *__restrict__ cz, float4 *__restrict__ cm32,
-                             double4 *__restrict__ cm64, int4 *__restrict__ meta, float4 *__restrict__ cm32lo) {
+                             const double *__restrict__ cy, const double *__restrict__ cz,
+                             double4 *__restrict__ cm64, int4 *__restrict__ meta, float4 *__restrict__ mrec) {
     const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nnodes) return;
-    meta[k] = make_int4((int)skip[k], (int)first[k], (int)cnt[k], (int)level[k]);
-    if (cm32) cm32[k] = make_float4((float)cx[k], (float)cy[k], (float)cz[k], (float)mass[k]);
+    const int4 mt = make_int4((int)skip[k], (int)first[k], (int)cnt[k], (int)level[k]);
+    meta[k] = mt;
     if (cm64) cm64[k] = make_double4(cx[k], cy[k], cz[k], mass[k]);
-    if (cm32lo) {
+    if (mrec) {
         const float hx = (float)cx[k], hy = (float)cy[k], hz = (float)cz[k];
-        cm32lo[k] = make_float4((float)(cx[k] - (double)hx), (float)(cy[k] - (double)hy), (float)(cz[k] - (double)hz), 0.f);
+        mrec[3 * k] = make_float4(__int_as_float(mt.x), __int_as_float(mt.y), __int_as_float(mt.z),
+                                  __int_as_float(mt.w));
+        mrec[3 * k + 1] = make_float4(hx, hy, hz, (float)mass[k]);
+        mrec[3 * k + 2] = make_float4((float)(cx[k] - (double)hx), (float)(cy[k] - (double)hy),
+                                      (float)(cz[k] - (double)hz), 0.f);
     }
 }
 
@@ -616,8 +622,8 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
                                               const float4 *__restrict__ p32, const double *__restrict__ sx,
                                               const double *__restrict__ sy, const double *__restrict__ sz,
                                               const double *__restrict__ sm, const S2Table tab, double theta2,
-                                              double eps2, const AccOut out, const float4 *__restrict__ cm32lo,
-                                              const float4 *__restrict__ p32lo, unsigned *__restrict__ err) {
+                                              double eps2, const AccOut out, const float4 *__restrict__ p32lo,
+                                              const float4 *__restrict__ mrec, unsigned *__restrict__ err) {
     constexpr bool F64 = MODE == 0;
     unsigned nterm = 0;  // node and particle terms this particle summed (profile counter)
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -639,7 +645,21 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
         const uint32_t m = __reduce_min_sync(0xFFFFFFFFu, next);
         if ((size_t)m >= nnodes) break;
         if (next != m) continue;
-        const int4 mt = meta[m];
+        // the node's records, loaded together: one memory latency per step of the walk
+        // instead of a chain of dependent loads
+        int4 mt;
+        double4 c64v = make_double4(0.0, 0.0, 0.0, 0.0);
+        float4 c32v = make_float4(0.f, 0.f, 0.f, 0.f), c32l = c32v;
+        if (MODE == 2) {  // one 48-byte record: meta, COM hi + mass, COM lo
+            const float4 r0 = mrec[3 * (size_t)m];
+            c32v = mrec[3 * (size_t)m + 1];
+            c32l = mrec[3 * (size_t)m + 2];
+            mt = make_int4(__float_as_int(r0.x), __float_as_int(r0.y), __float_as_int(r0.z), __float_as_int(r0.w));
+        } else {
+            mt = meta[m];
+            if (F64) c64v = cm64[m];
+            else c32v = cm32[m];
+        }
         if (!CHK((size_t)mt.x > m && (size_t)mt.x <= nnodes, DERR_TREE)) {  // a skip pointer must move forward
             next = (uint32_t)nnodes;
             continue;
@@ -651,15 +671,15 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
                 if ((size_t)mt.y != t) {
                     ++nterm;
                     if (F64) {
-                        const double4 c = cm64[m];
+                        const double4 c = c64v;
                         if (c.w != 0.0) add_force64(px, py, pz, c.x, c.y, c.z, c.w, eps2, ax, ay, az);
                     } else if (MODE == 1) {
-                        const float4 c = cm32[m];
+                        const float4 c = c32v;
                         if (c.w != 0.f) add_force32(qx, qy, qz, c.x, c.y, c.z, c.w, eps2f, fx, fy, fz);
                     } else {
-                        const float4 c = cm32[m];
+                        const float4 c = c32v;
                         if (c.w != 0.f) {
-                            const float4 cl = cm32lo[m];
+                            const float4 cl = c32l;
                             add_force_ff(qh, ql, c.x, c.y, c.z, cl.x, cl.y, cl.z, c.w, eps2f, fa);
                         }
                     }
@@ -684,7 +704,7 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
             }
             next = (uint32_t)mt.x;
         } else if (F64) {
-            const double4 c = cm64[m];
+            const double4 c = c64v;
             if (c.w == 0.0) {
                 next = (uint32_t)mt.x;
             } else {
@@ -699,7 +719,7 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
                 }
             }
         } else {
-            const float4 c = cm32[m];
+            const float4 c = c32v;
             if (c.w == 0.f) {
                 next = (uint32_t)mt.x;
             } else {
@@ -723,7 +743,7 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
                     if (MODE == 1) {
                         add_force32(qx, qy, qz, c.x, c.y, c.z, c.w, eps2f, fx, fy, fz);
                     } else {
-                        const float4 cl = cm32lo[m];
+                        const float4 cl = c32l;
                         add_force_ff(qh, ql, c.x, c.y, c.z, cl.x, cl.y, cl.z, c.w, eps2f, fa);
                     }
                     next = (uint32_t)mt.x;
@@ -1176,283 +1196,6 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_walk_group(const int2 *__rest
     }
 }
 
-// ---- parity group walk (MIXED) --------------------------------------------------
-// The mixed walk's decisions -- the reference's opening test for every particle --
-// made for a warp of up to 32 particles at once (one per lane, a tree cell of at
-// most 32 particles).  The warp pops up to 32 nodes per iteration; each stack entry
-// carries the lane mask of the particles whose walk reaches it.  Per node:
-//  - the box of the group's particles (f32 hi words) bounds every particle's f32
-//    distance to the COM from below (d2min) and above (d2max): rounding to nearest
-//    is monotone, so each particle's own f32 d^2, computed as k_walk<2> computes it,
-//    lies in [d2min, d2max].  d2min > hi2[L]: every particle in the mask accepts;
-//    d2max < lo2[L]: every one opens (the certified bands of the mixed walk);
-//  - otherwise each particle in the mask makes its own k_walk<2> decision (the f32
-//    test, the reference's f64 test inside the band), and the node is accepted for
-//    the particles that accept it and opened for the others.
-// So every particle sums exactly the terms of its own walk.  Accepted nodes and
-// leaves go to a shared list with their lane masks; each lane adds the entries of
-// its bit as f32 terms on float-float separations with compensated sums.
-constexpr int PW_ICAP = 128;
-constexpr int PW_WARPS = 3;  // 3 x 15 KB of stack and list: within the 48 KB of static shared memory
-
-struct PGroupSmem {
-    uint2 stack[GW_SCAP];     // (first child slot << 3 | children - 1, lane mask)
-    float4 il[2 * PW_ICAP];   // list: (com hi, mass), (com lo, lane mask bits)
-};
-
-// Parity-walk record of node x at its child slot: (com hi, mass), (com lo, 0) and
-// (first child slot, children, level, x) for an internal node, (-1, particle, 1, x)
-// for a one-particle leaf, (-2, first, count, x) for a bucket leaf.
-__device__ __forceinline__ void write_prec(float4 *__restrict__ prec, uint32_t slot, uint32_t x,
-                                           const uint8_t *__restrict__ level, const uint32_t *__restrict__ first,
-                                           const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ nk,
-                                           const uint32_t *__restrict__ koff, const float4 *__restrict__ cm32,
-                                           const float4 *__restrict__ cm32lo) {
-    prec[3 * (size_t)slot] = cm32[x];
-    const float4 lo = cm32lo[x];
-    prec[3 * (size_t)slot + 1] = make_float4(lo.x, lo.y, lo.z, 0.f);
-    const uint32_t c = cnt[x];
-    int4 b;
-    if (c == 0) b = make_int4((int)(1u + koff[x]), (int)nk[x], (int)level[x], (int)x);
-    else if (c == 1) b = make_int4(-1, (int)first[x], 1, (int)x);
-    else b = make_int4(-2, (int)first[x], (int)c, (int)x);
-    reinterpret_cast<int4 *>(prec)[3 * (size_t)slot + 2] = b;
-}
-
-__global__ void k_prec(size_t nnodes, const uint8_t *__restrict__ level, const uint32_t *__restrict__ first,
-                       const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ skip,
-                       const uint32_t *__restrict__ nk, const uint32_t *__restrict__ koff,
-                       const float4 *__restrict__ cm32, const float4 *__restrict__ cm32lo, float4 *__restrict__ prec) {
-    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nnodes) return;
-    if (k == 0) write_prec(prec, 0, 0, level, first, cnt, nk, koff, cm32, cm32lo);
-    if (cnt[k] != 0) return;
-    const uint32_t end = skip[k];
-    uint32_t slot = 1u + koff[k];
-    for (uint32_t ch = (uint32_t)k + 1; ch < end; ch = skip[ch], ++slot)
-        if (CHK_IDX(slot, nnodes)) write_prec(prec, slot, ch, level, first, cnt, nk, koff, cm32, cm32lo);
-}
-
-__global__ void __launch_bounds__(PW_WARPS * 32) k_walk_pgroup(
-    const int2 *__restrict__ groups, uint32_t *__restrict__ gcount, const float4 *__restrict__ prec,
-    const double4 *__restrict__ cm64, const float4 *__restrict__ p32, const float4 *__restrict__ p32lo,
-    const double *__restrict__ sx, const double *__restrict__ sy, const double *__restrict__ sz, const S2Table tab,
-    double theta2, float eps2f, size_t n, size_t nnodes, const AccOut out, unsigned *__restrict__ err) {
-    constexpr unsigned FULL = 0xFFFFFFFFu;
-    __shared__ PGroupSmem smem[PW_WARPS];
-    const int lane = threadIdx.x & 31;
-    uint2 *stack = smem[threadIdx.x >> 5].stack;
-    float4 *il = smem[threadIdx.x >> 5].il;
-    const unsigned lt = (1u << lane) - 1u, me = 1u << lane;
-    const uint32_t ngroups = gcount[0];
-    for (;;) {
-        uint32_t g = 0;
-        if (lane == 0) g = atomicAdd(gcount + 1, 1u);
-        g = __shfl_sync(FULL, g, 0);
-        if (g >= ngroups) break;
-        const int2 gr = groups[g];
-        if (!CHK(gr.x >= 0 && gr.y > 0 && gr.y <= 32 && (size_t)gr.x + (size_t)gr.y <= n, DERR_BOUNDS)) continue;
-        const bool active = lane < gr.y;
-        const size_t t = (size_t)gr.x + (active ? lane : 0);
-        const float4 qh = p32[t], ql = p32lo[t];
-        const double px = sx[t], py = sy[t], pz = sz[t];
-        const float lox = warp_min(active ? qh.x : INFINITY), loy = warp_min(active ? qh.y : INFINITY),
-                    loz = warp_min(active ? qh.z : INFINITY);
-        const float hix = warp_max(active ? qh.x : -INFINITY), hiy = warp_max(active ? qh.y : -INFINITY),
-                    hiz = warp_max(active ? qh.z : -INFINITY);
-        const unsigned gmask = gr.y == 32 ? FULL : ((1u << gr.y) - 1u);
-        float fa[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        unsigned nterm = 0;
-        auto eval = [&](int count) {
-            for (int k = 0; k < count; ++k) {
-                const float4 a = il[2 * k], l = il[2 * k + 1];
-                if ((__float_as_uint(l.w) & me) && a.w != 0.f) {
-                    add_force_ff(qh, ql, a.x, a.y, a.z, l.x, l.y, l.z, a.w, eps2f, fa);
-                    ++nterm;
-                }
-            }
-        };
-        // the lane bit of sorted particle p if it belongs to this group, else 0
-        auto selfbit = [&](int p) -> unsigned {
-            const int r = p - gr.x;
-            return (r >= 0 && r < gr.y) ? (1u << r) : 0u;
-        };
-        int top = 1, nil = 0;
-        if (lane == 0) stack[0] = make_uint2(0u, gmask);  // the root: slot 0, one node
-        __syncwarp();
-        while (top > 0) {
-            // pop whole ranges from the top, at most 32 nodes
-            const uint2 e = lane < top ? stack[top - 1 - lane] : make_uint2(0u, 0u);
-            const int nkl = lane < top ? (int)(e.x & 7u) + 1 : 0;
-            int cum = nkl;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int v = __shfl_up_sync(FULL, cum, o);
-                if (lane >= o) cum += v;
-            }
-            const bool take = lane < top && cum <= 32;
-            const int kr = __popc(__ballot_sync(FULL, take));
-            const int total = __shfl_sync(FULL, cum, kr - 1);
-            const unsigned starts = __reduce_or_sync(FULL, take ? (1u << (cum - nkl)) : 0u);
-            top -= kr;
-            __syncwarp();
-            const bool has = lane < total;
-            const unsigned upto = lane == 31 ? FULL : ((2u << lane) - 1u);
-            const int r = max(__popc(starts & upto) - 1, 0);
-            const uint32_t er = __shfl_sync(FULL, e.x, r);
-            const unsigned emask = __shfl_sync(FULL, e.y, r);
-            const int sr = __shfl_sync(FULL, cum - nkl, r);
-            float4 A = make_float4(0.f, 0.f, 0.f, 0.f), Lo = A;
-            int4 B = make_int4(0, 0, 0, 0);
-            if (has) {
-                const size_t slot = (size_t)(er >> 3) + (size_t)(lane - sr);
-                if (CHK_IDX(slot, nnodes)) {  // a bad slot reads as an empty node (A.w == 0)
-                    A = prec[3 * slot];
-                    Lo = prec[3 * slot + 1];
-                    B = reinterpret_cast<const int4 *>(prec)[3 * slot + 2];
-                }
-            }
-            const bool live = has && A.w != 0.f && emask != 0u;
-            unsigned add_mask = 0u;  // particles that take this node (or leaf) as a term
-            bool open = false, mixed = false, bucket = false;
-            if (live) {
-                if (B.x == -1) {
-                    add_mask = emask & ~selfbit(B.y);
-                } else if (B.x == -2) {
-                    bucket = true;
-                } else {
-                    const int L = B.z;
-                    const float dxn = fmaxf(fmaxf(lox - A.x, A.x - hix), 0.f);
-                    const float dyn = fmaxf(fmaxf(loy - A.y, A.y - hiy), 0.f);
-                    const float dzn = fmaxf(fmaxf(loz - A.z, A.z - hiz), 0.f);
-                    const float d2min = fmaf(dzn, dzn, fmaf(dyn, dyn, dxn * dxn));
-                    const float dxf = fmaxf(fabsf(A.x - lox), fabsf(A.x - hix));
-                    const float dyf = fmaxf(fabsf(A.y - loy), fabsf(A.y - hiy));
-                    const float dzf = fmaxf(fabsf(A.z - loz), fabsf(A.z - hiz));
-                    const float d2max = fmaf(dzf, dzf, fmaf(dyf, dyf, dxf * dxf));
-                    if (d2min > tab.hi2[L]) add_mask = emask;
-                    else if (d2max < tab.lo2[L]) open = true;
-                    else mixed = true;
-                }
-            }
-            // accepted nodes and leaves: list entries with their masks
-            const unsigned am = __ballot_sync(FULL, add_mask != 0u);
-            if (add_mask) {
-                float4 *sl = il + 2 * (nil + __popc(am & lt));
-                sl[0] = A;
-                sl[1] = make_float4(Lo.x, Lo.y, Lo.z, __uint_as_float(add_mask));
-            }
-            nil += __popc(am);
-            // nodes every particle of the mask opens: push their children with the mask
-            const unsigned om = __ballot_sync(FULL, open);
-            if (top + __popc(om) > GW_SCAP) {  // unreachable by the depth bound; flagged, never written
-                if (lane == 0) atomicOr(err, DERR_STACK_OVERFLOW);
-            } else {
-                if (open) stack[top + __popc(om & lt)] = make_uint2(((uint32_t)B.x << 3) | (uint32_t)(B.y - 1), emask);
-                top += __popc(om);
-            }
-            // nodes near the group: each particle of the mask decides for itself
-            unsigned mm = __ballot_sync(FULL, mixed);
-            while (mm) {
-                const int j = __ffs(mm) - 1;
-                mm &= mm - 1;
-                const float cx = __shfl_sync(FULL, A.x, j), cy = __shfl_sync(FULL, A.y, j),
-                            cz = __shfl_sync(FULL, A.z, j);
-                const int L = __shfl_sync(FULL, B.z, j), node = __shfl_sync(FULL, B.w, j);
-                const unsigned jm = __shfl_sync(FULL, emask, j);
-                bool acc = false, opn = false;
-                if (jm & me) {  // k_walk<2>'s test of this particle
-                    const float dx = cx - qh.x, dy = cy - qh.y, dz = cz - qh.z;
-                    const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                    if (d2 > tab.hi2[L]) {
-                        acc = true;
-                    } else if (d2 < tab.lo2[L]) {
-                        opn = true;
-                    } else {
-                        const double4 c64 = cm64[node];
-                        const double ex = __dsub_rn(c64.x, px), ey = __dsub_rn(c64.y, py), ez = __dsub_rn(c64.z, pz);
-                        const double e2 =
-                            __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
-                        acc = tab.s2[L] < __dmul_rn(theta2, e2);
-                        opn = !acc;
-                    }
-                }
-                const unsigned accm = __ballot_sync(FULL, acc), opm = __ballot_sync(FULL, opn);
-                if (accm) {
-                    if (nil >= PW_ICAP) {
-                        eval(nil);
-                        nil = 0;
-                        __syncwarp();
-                    }
-                    if (lane == j) {
-                        il[2 * nil] = A;
-                        il[2 * nil + 1] = make_float4(Lo.x, Lo.y, Lo.z, __uint_as_float(accm));
-                    }
-                    ++nil;
-                    __syncwarp();
-                }
-                if (opm) {
-                    if (top + 1 > GW_SCAP) {
-                        if (lane == 0) atomicOr(err, DERR_STACK_OVERFLOW);
-                    } else {
-                        if (lane == j) stack[top] = make_uint2(((uint32_t)B.x << 3) | (uint32_t)(B.y - 1), opm);
-                        ++top;
-                    }
-                    __syncwarp();
-                }
-            }
-            // leaves of coincident-key particles (rare): members one by one
-            unsigned bm = __ballot_sync(FULL, bucket);
-            while (bm) {
-                const int b = __ffs(bm) - 1;
-                bm &= bm - 1;
-                const int bf = __shfl_sync(FULL, B.y, b);
-                const int bc = CHK(bf >= 0 && (size_t)bf + (size_t)__shfl_sync(FULL, B.z, b) <= n, DERR_BOUNDS)
-                                   ? __shfl_sync(FULL, B.z, b) : 0;
-                const unsigned bmask = __shfl_sync(FULL, emask, b);
-                for (int j0 = 0; j0 < bc; j0 += 32) {
-                    if (nil > PW_ICAP - 32) {
-                        __syncwarp();
-                        eval(nil);
-                        nil = 0;
-                        __syncwarp();
-                    }
-                    const int jj = j0 + lane;
-                    float4 q = make_float4(0.f, 0.f, 0.f, 0.f), qlo = q;
-                    if (jj < bc) {
-                        q = p32[bf + jj];
-                        qlo = p32lo[bf + jj];
-                    }
-                    const unsigned mk = jj < bc ? (bmask & ~selfbit(bf + jj)) : 0u;
-                    const bool ok = mk != 0u && q.w != 0.f;
-                    const unsigned qm = __ballot_sync(FULL, ok);
-                    if (ok) {
-                        float4 *sl = il + 2 * (nil + __popc(qm & lt));
-                        sl[0] = q;
-                        sl[1] = make_float4(qlo.x, qlo.y, qlo.z, __uint_as_float(mk));
-                    }
-                    nil += __popc(qm);
-                }
-            }
-            __syncwarp();
-            if (nil > PW_ICAP - 32) {
-                eval(nil);
-                nil = 0;
-                __syncwarp();
-            }
-        }
-        if (nil) eval(nil);
-        __syncwarp();
-        const unsigned wterms = __reduce_add_sync(FULL, active ? nterm : 0u);
-        if (lane == 0 && wterms)
-            atomicAdd(reinterpret_cast<unsigned long long *>(err + EW_WALK_TERMS), (unsigned long long)wterms);
-        if (active)
-            store_acc(out, t, (double)fa[0] + (double)fa[3], (double)fa[1] + (double)fa[4],
-                      (double)fa[2] + (double)fa[5]);
-        __syncwarp();
-    }
-}
-
 inline int nblk(size_t n, int t = 256) { return (int)std::max<size_t>(1, (n + t - 1) / t); }
 
 }  // namespace
@@ -1468,7 +1211,7 @@ void tree_free(Ctx *c) {
     DevBuf *all[] = {&t->bb, &t->bbpart, &t->khi, &t->klo, &t->khi2, &t->klo2, &t->perm, &t->perm2, &t->iota,
                      &t->iota2, &t->delta, &t->nown, &t->off, &t->total, &t->level, &t->first, &t->cnt, &t->skip,
                      &t->mass, &t->comx, &t->comy, &t->comz, &t->boxx, &t->boxy, &t->boxz, &t->sx, &t->sy,
-                     &t->sz, &t->sm, &t->pos32, &t->cm32, &t->cm64, &t->meta, &t->pos32lo, &t->cm32lo, &t->nk, &t->koff, &t->krec,
+                     &t->sz, &t->sm, &t->pos32, &t->cm32, &t->cm64, &t->meta, &t->pos32lo, &t->mrec, &t->nk, &t->koff, &t->krec,
                      &t->groups, &t->gcount, &t->parent, &t->arrive, &t->mo32, &t->leaf_of};
     for (DevBuf *b : all)
         if (b->ptr) cudaFree(b->ptr);
@@ -1699,29 +1442,6 @@ static gvs_status group_prepare(Ctx *c, Tree *t, int gsize) {
     return GVS_OK;
 }
 
-// Parity-walk records (needs the mixed packing: cm32, cm32lo) and groups of <= 32
-// particles of the current tree.
-static gvs_status pgroup_prepare(Ctx *c, Tree *t) {
-    if (t->pgrp_version == t->version) return GVS_OK;
-    const size_t nn = t->nnodes, n = t->n;
-    cudaStream_t st = c->stream;
-    GVS_CUDA(c, ensure(c, t->prec, nn * 3 * sizeof(float4)));
-    GVS_CUDA(c, ensure(c, t->pgroups, n * sizeof(int2)));
-    GVS_CUDA(c, ensure(c, t->pgcount, 16));
-    GVS_TRY(koff_prepare(c, t));
-    k_prec<<<nblk(nn), 256, 0, st>>>(nn, as<uint8_t>(t->level), as<uint32_t>(t->first), as<uint32_t>(t->cnt),
-                                     as<uint32_t>(t->skip), as<uint32_t>(t->nk), as<uint32_t>(t->koff),
-                                     as<float4>(t->cm32), as<float4>(t->cm32lo), as<float4>(t->prec));
-    GVS_CUDA(c, cudaMemsetAsync(t->pgcount.ptr, 0, 8, st));
-    k_groups<<<nblk(nn), 256, 0, st>>>(nn, n, 32u, as<uint8_t>(t->level), as<uint32_t>(t->first),
-                                       as<uint32_t>(t->cnt), as<uint32_t>(t->skip), as<uint64_t>(t->khi),
-                                       as<uint64_t>(t->klo), as<int2>(t->pgroups), as<uint32_t>(t->pgcount));
-    c->prof.launches += 2;
-    GVS_TRY(check_launch(c, "parity walk setup"));
-    t->pgrp_version = t->version;
-    return GVS_OK;
-}
-
 gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accumulate) {
     const size_t n = c->n;
     if (n == 0) return GVS_OK;
@@ -1734,12 +1454,10 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
                      : precision == GVS_PREC_FP32 ? 1 : 2;
     GVS_CUDA(c, ensure(c, t->meta, nnodes * sizeof(int4)));
     if (mode != 1) GVS_CUDA(c, ensure(c, t->cm64, nnodes * sizeof(double4)));
-    if (mode != 0) {
-        GVS_CUDA(c, ensure(c, t->cm32, nnodes * sizeof(float4)));
-        GVS_CUDA(c, ensure(c, t->pos32, n * sizeof(float4)));
-    }
+    if (mode != 0) GVS_CUDA(c, ensure(c, t->pos32, n * sizeof(float4)));
+    if (mode == 1) GVS_CUDA(c, ensure(c, t->cm32, nnodes * sizeof(float4)));
     if (mode == 2) {
-        GVS_CUDA(c, ensure(c, t->cm32lo, nnodes * sizeof(float4)));
+        GVS_CUDA(c, ensure(c, t->mrec, nnodes * 3 * sizeof(float4)));
         GVS_CUDA(c, ensure(c, t->pos32lo, n * sizeof(float4)));
     }
     if (t->precision != mode + 1) {
@@ -1747,9 +1465,8 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
         k_pack_nodes<<<nblk(nnodes), 256, 0, st>>>(nnodes, as<uint8_t>(t->level), as<uint32_t>(t->first),
                                                     as<uint32_t>(t->cnt), as<uint32_t>(t->skip), as<double>(t->mass),
                                                     as<double>(t->comx), as<double>(t->comy), as<double>(t->comz),
-                                                    mode == 2 ? as<float4>(t->cm32) : nullptr,
-                                                    mode != 1 ? as<double4>(t->cm64) : nullptr, as<int4>(t->meta),
-                                                    mode == 2 ? as<float4>(t->cm32lo) : nullptr);
+                                                    mode != 1 ? as<double4>(t->cm64) : nullptr,
+                                                    as<int4>(t->meta), mode == 2 ? as<float4>(t->mrec) : nullptr);
         if (mode != 0)
             k_pack_particles<<<nblk(n), 256, 0, st>>>(n, as<double>(t->sx), as<double>(t->sy), as<double>(t->sz),
                                                       as<double>(t->sm), as<float4>(t->pos32),
@@ -1792,12 +1509,6 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
     const int gsize = c->bh_group >= 0 ? c->bh_group : (n >= (size_t(1) << 21) ? 128 : 64);
     const bool group = mode == 1 && gsize > 0 && nnodes < (size_t(1) << 29);
     if (group) GVS_TRY(group_prepare(c, t, gsize));
-    // MIXED: the parity group walk unless per-particle walks were asked for (group size 0)
-    const bool pgroup = mode == 2 && c->bh_group != 0 && nnodes < (size_t(1) << 29);
-    if (pgroup) {
-        GVS_TRY(pgroup_prepare(c, t));
-        GVS_CUDA(c, cudaMemsetAsync(as<uint32_t>(t->pgcount) + 1, 0, 4, st));
-    }
     if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], st));
     if (group) {
         GVS_CUDA(c, cudaMemsetAsync(as<uint32_t>(t->gcount) + 1, 0, 4, st));
@@ -1815,13 +1526,6 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
         else if (gsize == 64) GVS_TRY(guard ? launch(k_walk_group<2, true>) : launch(k_walk_group<2, false>));
         else GVS_TRY(guard ? launch(k_walk_group<1, true>) : launch(k_walk_group<1, false>));
         c->prof.launches += 2;
-    } else if (pgroup) {
-        int per_sm = 0;
-        GVS_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk_pgroup, PW_WARPS * 32, 0));
-        k_walk_pgroup<<<std::max(1, per_sm) * c->num_sms, PW_WARPS * 32, 0, st>>>(
-            as<int2>(t->pgroups), as<uint32_t>(t->pgcount), as<float4>(t->prec), as<double4>(t->cm64),
-            as<float4>(t->pos32), as<float4>(t->pos32lo), as<double>(t->sx), as<double>(t->sy), as<double>(t->sz), tab,
-            theta * theta, (float)(eps * eps), n, nnodes, out, err_ptr(c));
     } else if (mode == 0)
         k_walk<0><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, as<int4>(t->meta), nullptr, as<double4>(t->cm64),
                                                 nullptr, as<double>(t->sx), as<double>(t->sy), as<double>(t->sz),
@@ -1833,11 +1537,10 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
                                                 as<double>(t->sz), as<double>(t->sm), tab, theta * theta, eps * eps,
                                                 out, nullptr, nullptr, err_ptr(c));
     else
-        k_walk<2><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, as<int4>(t->meta), as<float4>(t->cm32),
-                                                as<double4>(t->cm64), as<float4>(t->pos32), as<double>(t->sx),
-                                                as<double>(t->sy), as<double>(t->sz), as<double>(t->sm), tab,
-                                                theta * theta, eps * eps, out,
-                                                as<float4>(t->cm32lo), as<float4>(t->pos32lo), err_ptr(c));
+        k_walk<2><<<nblk(n, 128), 128, 0, st>>>(n, nnodes, nullptr, nullptr, as<double4>(t->cm64),
+                                                as<float4>(t->pos32), as<double>(t->sx), as<double>(t->sy),
+                                                as<double>(t->sz), as<double>(t->sm), tab, theta * theta, eps * eps,
+                                                out, as<float4>(t->pos32lo), as<float4>(t->mrec), err_ptr(c));
     c->prof.launches += 1;
     GVS_TRY(check_launch(c, "tree walk"));
     if (c->prof.on) {

@@ -284,11 +284,7 @@ gvs_status gvs_set_direct_shape(gvs_ctx *ctx, int nthreads, int ipt, int min_blo
  * iterations (32 nodes each; 0 = the default 1024) is walked per particle instead: its
  * box lies close to much denser matter, which the group test would open down to
  * single particles.
- * MIXED: unless group_size is 0, warps of up to 32 particles of one tree cell walk
- * together while every particle makes its own decision (the reference's test: an f32
- * test outside a certified band, the f64 test inside it), so each particle sums
- * exactly the terms of its own walk; 0: one walk per particle.
- * FP64 walks are always per-particle. */
+ * FP64 and MIXED walks are always per-particle. */
 gvs_status gvs_set_bh_walk(gvs_ctx *ctx, int group_size, int budget);
 /* Every candidate of the last gvs_autotune_direct with its kernel time (ms per force
  * evaluation).  Always sets *count; fills the arrays (any may be NULL) if cap >= *count.

@@ -384,38 +384,3 @@ def test_bh_kdk_energy(ctx):
     ctx.kdk_steps(G.ALGO_BH, G.PREC_FP64, eps, 0.5, 1e-3, 500)
     e1 = ctx.diagnostics(eps).total_energy
     assert abs(e1 - e0) / abs(e0) < 1e-3
-
-
-@pytest.mark.parametrize("theta", [0.0, 0.3, 0.5, 0.7, 1.0])
-@pytest.mark.parametrize("name", ["plummer1000", "collision4096", "lattice8", "close_pairs", "two", "one"])
-def test_parity_group_walk_equals_per_particle_walk(ctx, name, theta):
-    """The mixed walk's group form (default) makes every particle's own decisions: it
-    sums the same terms as the per-particle mixed walk (set_bh_walk(0)), in another
-    order, so the two agree to f32 rounding of compensated sums; both are within 1e-6
-    of the oracle's BarnesHut."""
-    p = cases()[name]
-    eps = 0.05
-    grp = p.copy()
-    grp.clear_accelerations()
-    ctx.set_bh_walk(-1)
-    ctx.profile(True)
-    G.BarnesHut(eps, theta, G.PREC_MIXED, ctx).compute_accelerations(grp)
-    terms_group = ctx.profile_read()["bh_walk_terms"]
-    ctx.profile(False)
-    per = p.copy()
-    per.clear_accelerations()
-    ctx.set_bh_walk(0)
-    try:
-        ctx.profile(True)
-        G.BarnesHut(eps, theta, G.PREC_MIXED, ctx).compute_accelerations(per)
-        terms_per = ctx.profile_read()["bh_walk_terms"]
-        ctx.profile(False)
-    finally:
-        ctx.set_bh_walk(-1)
-    assert terms_group == terms_per, (terms_group, terms_per)  # the same node sets
-    if p.count > 1:
-        assert rel_rms(grp.acc(), per.acc()) <= 1e-7, rel_rms(grp.acc(), per.acc())
-        r = to_oracle(p)
-        O.bh(r, eps, theta)
-        assert rel_rms(grp.acc(), r.acc()) <= 1e-6
-    assert ctx.device_errors() == 0
