@@ -977,6 +977,7 @@ def adjoint_ratio(ctx, G, n=16384, steps=1000, every=100, seed=42, eps=0.01, dt=
     out = {"workload": f"Plummer N={n} seed {seed}, eps={eps}, dt={dt}, {steps} steps, f64 checkpoints every {every}",
            "forward_ms": f_plain, "forward_with_checkpoints_ms": f_ck, "backward_ms": bwd,
            "adjoint_over_forward": bwd / f_plain, "vjp_kernel_ms": vjp_ms, "clocks": clk.summary()}
+    g64 = None
     if check_fp64:
         _, _, bwd64, g64, _ = run(G.PREC_FP64)
         out["grad_rel_err_mixed_vs_fp64_adjoint"] = {
@@ -985,7 +986,7 @@ def adjoint_ratio(ctx, G, n=16384, steps=1000, every=100, seed=42, eps=0.01, dt=
     if fd_dirs > 0:
         rng = np.random.default_rng(7)
         delta = 1e-6
-        errs = []
+        errs, errs64 = [], []
         for _ in range(fd_dirs):
             ux, uv, um = rng.standard_normal((n, 3)), rng.standard_normal((n, 3)), rng.standard_normal(n) * p.mass
             qs = []
@@ -998,10 +999,17 @@ def adjoint_ratio(ctx, G, n=16384, steps=1000, every=100, seed=42, eps=0.01, dt=
             fd = (qs[0] - qs[1]) / (2 * delta)
             ad = float((g["x"] * ux).sum() + (g["v"] * uv).sum() + (g["m"] * um).sum())
             errs.append(abs(ad - fd) / abs(fd))
+            if g64 is not None:
+                ad64 = float((g64["x"] * ux).sum() + (g64["v"] * uv).sum() + (g64["m"] * um).sum())
+                errs64.append(abs(ad64 - fd) / abs(fd))
         out["fd_check"] = {"directions": fd_dirs, "step": delta, "max_rel_err": float(max(errs)),
                            "median_rel_err": float(np.median(errs)), "bar": 1e-5,
                            "what": "mixed-precision adjoint directional derivative along random (x0, v0, m) "
                                    "directions against f64 central differences of the f64 forward run"}
+        if errs64:
+            out["fd_check_fp64_adjoint"] = {"max_rel_err": float(max(errs64)),
+                                            "median_rel_err": float(np.median(errs64)),
+                                            "what": "the f64 adjoint along the same directions"}
     return out
 
 

@@ -42,7 +42,7 @@ struct SphState {
     DevBuf sx, sy, sz, svx, svy, svz, sm, sh, su, salpha;  // sorted inputs
     DevBuf srho, spres, scs, somega, sdivv, smaxmu, sdalpha, sax, say, saz, sdu;  // sorted outputs
     DevBuf dtpart;
-    DevBuf pos4, node4, meta4;  // neighbour search: f32 positions, node records (see k_sph_f32copies)
+    DevBuf pos4, nrec;  // neighbour search: f32 positions, interleaved node records (see k_sph_f32copies)
     DevBuf a4, b4, c4, d4, e4, f4;  // mixed precision: packed sources (see k_sph_src_*)
     DevBuf redo_idx, redo_count;    // mixed precision: particles whose h iteration runs again in f64
     bool have_intermediates = false;
@@ -186,6 +186,8 @@ __device__ __forceinline__ int pref_box(const Prefilter &f, float4 b) {
 //
 // meta4 = (skip, first particle, count, depth): count > 0 for a leaf, minus the
 // subtree's particle count for an internal node.
+// Node k's records sit side by side (meta4[2k], node4[2k + 1] of one buffer): the
+// walk reads both at every step, so they share a cache line.
 __global__ void k_sph_f32copies(const TreeView tv, float4 *__restrict__ pos4, float4 *__restrict__ node4,
                                 int4 *__restrict__ meta4) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -193,8 +195,8 @@ __global__ void k_sph_f32copies(const TreeView tv, float4 *__restrict__ pos4, fl
     if (i < tv.nnodes) {
         const uint32_t c = tv.cnt[i], f = tv.first[i], sk = tv.skip[i];
         const uint32_t sub = (uint32_t)((sk < tv.nnodes ? (size_t)tv.first[sk] : tv.n) - f);
-        meta4[i] = make_int4((int)sk, (int)f, c > 0 ? (int)c : -(int)sub, (int)tv.level[i]);
-        node4[i] = c == 1 ? make_float4((float)tv.sx[f], (float)tv.sy[f], (float)tv.sz[f], 0.f)
+        meta4[2 * i] = make_int4((int)sk, (int)f, c > 0 ? (int)c : -(int)sub, (int)tv.level[i]);
+        node4[2 * i + 1] = c == 1 ? make_float4((float)tv.sx[f], (float)tv.sy[f], (float)tv.sz[f], 0.f)
                           : make_float4((float)tv.bx[i], (float)tv.by[i], (float)tv.bz[i],
                                         (float)ldexp(tv.root_hw, -(int)tv.level[i]));
     }
@@ -299,7 +301,9 @@ __device__ int ball_query_thread(const TreeView &tv, const float4 *__restrict__ 
     const Prefilter pf = prefilter(px, py, pz, radius, E);
     int count = 0;
     uint32_t k = 0;
-    while ((size_t)k < tv.nnodes) k = ball_visit(tv, pos4, meta4[k], node4[k], k, pf, px, py, pz, radius, row, kmax, count);
+    while ((size_t)k < tv.nnodes)
+        k = ball_visit(tv, pos4, meta4[2 * (size_t)k], node4[2 * (size_t)k + 1], k, pf, px, py, pz, radius, row, kmax,
+                       count);
     return count;
 }
 
@@ -335,7 +339,8 @@ __global__ void __launch_bounds__(128) k_neighbors(const TreeView tv, const floa
             const uint32_t k = __reduce_min_sync(0xFFFFFFFFu, next);
             if ((size_t)k >= tv.nnodes) break;
             if (next != k) continue;
-            next = ball_visit(tv, pos4, meta4[k], node4[k], k, pf, px, py, pz, radius, row, kmax, count);
+            next = ball_visit(tv, pos4, meta4[2 * (size_t)k], node4[2 * (size_t)k + 1], k, pf, px, py, pz, radius, row,
+                              kmax, count);
         }
         if (t < tv.n) {
             cnt[t] = active ? (uint32_t)count : 0u;
@@ -1007,7 +1012,7 @@ void sph_free(Ctx *c) {
     if (!s) return;
     DevBuf *all[] = {&s->list, &s->cnt, &s->gas, &s->sx, &s->sy, &s->sz, &s->svx, &s->svy, &s->svz, &s->sm,
                      &s->sh, &s->su, &s->salpha, &s->srho, &s->spres, &s->scs, &s->somega, &s->sdivv, &s->smaxmu,
-                     &s->sdalpha, &s->sax, &s->say, &s->saz, &s->sdu, &s->dtpart, &s->pos4, &s->node4, &s->meta4,
+                     &s->sdalpha, &s->sax, &s->say, &s->saz, &s->sdu, &s->dtpart, &s->pos4, &s->nrec,
                      &s->a4, &s->b4, &s->c4, &s->d4, &s->e4, &s->f4, &s->redo_idx, &s->redo_count};
     for (DevBuf *b : all)
         if (b->ptr) cudaFree(b->ptr);
@@ -1031,10 +1036,9 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
     GVS_CUDA(c, ensure(c, S->gas, n));
     GVS_CUDA(c, ensure(c, S->cnt, n * 4));
     GVS_CUDA(c, ensure(c, S->pos4, n * 16));
-    GVS_CUDA(c, ensure(c, S->node4, tv.nnodes * 16));
-    GVS_CUDA(c, ensure(c, S->meta4, tv.nnodes * 16));
-    k_sph_f32copies<<<nb(std::max(n, tv.nnodes)), 256, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4),
-                                                                as<int4>(S->meta4));
+    GVS_CUDA(c, ensure(c, S->nrec, tv.nnodes * 32));
+    k_sph_f32copies<<<nb(std::max(n, tv.nnodes)), 256, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->nrec),
+                                                                as<int4>(S->nrec));
     const bool mixed = prm->precision == GVS_PREC_MIXED;
     if (mixed) {
         DevBuf *f4s[] = {&S->a4, &S->b4, &S->c4, &S->d4, &S->e4, &S->f4};
@@ -1067,7 +1071,7 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
             GVS_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_neighbors, 128, 0));
             const int blocks = (int)std::min<size_t>(nb(n, 128), (size_t)std::max(1, per_sm) * c->num_sms);
             GVS_CUDA(c, cudaMemsetAsync(err_ptr(c) + EW_NEIGH_WORK, 0, 4, st));
-            k_neighbors<<<blocks, 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4), as<int4>(S->meta4),
+            k_neighbors<<<blocks, 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->nrec), as<int4>(S->nrec),
                                                 as<uint8_t>(S->gas), as<double>(S->sh), 1.1, S->kmax,
                                                 as<uint32_t>(S->list), as<uint32_t>(S->cnt), err_ptr(c),
                                                 err_ptr(c) + EW_NEIGH_WORK);
@@ -1075,20 +1079,20 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
         if (mixed) {
             GVS_CUDA(c, cudaMemsetAsync(S->redo_count.ptr, 0, 4, st));
             k_density_mixed<<<nb(n, 128), 128, 0, st>>>(
-                tv, as<float4>(S->pos4), as<float4>(S->node4), as<int4>(S->meta4), as<float4>(S->a4), as<float4>(S->b4),
+                tv, as<float4>(S->pos4), as<float4>(S->nrec), as<int4>(S->nrec), as<float4>(S->a4), as<float4>(S->b4),
                 as<uint8_t>(S->gas), as<double>(S->sm), as<double>(S->su), as<double>(S->sh), as<uint32_t>(S->list),
                 as<uint32_t>(S->cnt), S->kmax, prm->gamma, prm->eta, prm->h_max, as<double>(S->srho),
                 as<double>(S->somega), as<double>(S->spres), as<double>(S->scs), err_ptr(c),
                 as<uint32_t>(S->redo_idx), as<unsigned>(S->redo_count));
             k_density_redo<<<std::max(1, c->num_sms * 2), 128, 0, st>>>(
-                tv, as<float4>(S->pos4), as<float4>(S->node4), as<int4>(S->meta4), as<double>(S->sm), as<double>(S->su),
+                tv, as<float4>(S->pos4), as<float4>(S->nrec), as<int4>(S->nrec), as<double>(S->sm), as<double>(S->su),
                 as<double>(c->scratch_b), as<double>(S->sh), as<uint32_t>(S->list), as<uint32_t>(S->cnt), S->kmax,
                 prm->gamma, prm->eta, prm->h_max, as<double>(S->srho), as<double>(S->somega), as<double>(S->spres),
                 as<double>(S->scs), err_ptr(c), as<uint32_t>(S->redo_idx), as<unsigned>(S->redo_count),
                 err_ptr(c) + EW_SPH_REDO);
             c->prof.launches += 1;
         } else
-            k_density<<<nb(n, 128), 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->node4), as<int4>(S->meta4), as<uint8_t>(S->gas),
+            k_density<<<nb(n, 128), 128, 0, st>>>(tv, as<float4>(S->pos4), as<float4>(S->nrec), as<int4>(S->nrec), as<uint8_t>(S->gas),
                                                   as<double>(S->sm), as<double>(S->su),
                                                   as<double>(S->sh), as<uint32_t>(S->list), as<uint32_t>(S->cnt),
                                                   S->kmax, prm->gamma, prm->eta, prm->h_max, as<double>(S->srho),
