@@ -581,24 +581,31 @@ __device__ __forceinline__ void add_force64(double px, double py, double pz, dou
     az = __dadd_rn(az, __dmul_rn(f, dz));
 }
 
-// f32 monopole term on a float-float separation (hi - hi) + (lo - lo), summed into
-// (hi, lo) two-sum accumulators.
-__device__ __forceinline__ void tsum32(float &hi, float &lo, float v) {
-    const float s = hi + v;
-    const float bp = s - hi;
-    lo += (hi - (s - bp)) + (v - bp);
-    hi = s;
-}
+// Compensated accumulators of the mixed walk: x and y as one f32x2 pair, z alone.
+struct FFAcc {
+    f2 hxy = 0ull, lxy = 0ull;
+    float hz = 0.f, lz = 0.f;
+};
 
+// f32 monopole term on a float-float separation (hi - hi) + (lo - lo), added to
+// (hi, lo) accumulators by Knuth's two-sum (error-free: the product is rounded
+// once, then added).  x and y run as packed f32x2 operations, z as scalars: the
+// same operations per component, one instruction for two.
 __device__ __forceinline__ void add_force_ff(float4 q, float4 ql, float sx, float sy, float sz, float sxl, float syl,
-                                             float szl, float m, float eps2, float *acc) {
-    const float dx = (sx - q.x) + (sxl - ql.x), dy = (sy - q.y) + (syl - ql.y), dz = (sz - q.z) + (szl - ql.z);
+                                             float szl, float m, float eps2, FFAcc &acc) {
+    const f2 dxy = add2(sub2(pk(sx, sy), pk(q.x, q.y)), sub2(pk(sxl, syl), pk(ql.x, ql.y)));
+    const float dz = __fadd_rn(__fsub_rn(sz, q.z), __fsub_rn(szl, ql.z));
+    float dx, dy;
+    upk(dxy, dx, dy);
     const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
     const float ri = rsqrt_approx(r2);
-    const float f = m * ri * ri * ri;
-    tsum32(acc[0], acc[3], f * dx);
-    tsum32(acc[1], acc[4], f * dy);
-    tsum32(acc[2], acc[5], f * dz);
+    const float f = __fmul_rn(__fmul_rn(__fmul_rn(m, ri), ri), ri);
+    two_sum2(acc.hxy, acc.lxy, mul2(pk(f, f), dxy));
+    const float v = __fmul_rn(f, dz);
+    const float sum = __fadd_rn(acc.hz, v);
+    const float bp = __fsub_rn(sum, acc.hz);
+    acc.lz = __fadd_rn(acc.lz, __fadd_rn(__fsub_rn(acc.hz, __fsub_rn(sum, bp)), __fsub_rn(v, bp)));
+    acc.hz = sum;
 }
 
 __device__ __forceinline__ void add_force32(float px, float py, float pz, float sx, float sy, float sz, float m,
@@ -639,7 +646,7 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
     const float theta2f = (float)theta2, eps2f = (float)eps2;
     double ax = 0, ay = 0, az = 0;
     float fx = 0, fy = 0, fz = 0;
-    float fa[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // mixed: (hi x, y, z, lo x, y, z)
+    FFAcc fa;  // mixed: compensated sums
     uint32_t next = active ? 0u : 0xFFFFFFFFu;
     for (;;) {
         const uint32_t m = __reduce_min_sync(0xFFFFFFFFu, next);
@@ -759,9 +766,12 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
     if (!active) return;
     if (MODE == 1) { ax = fx; ay = fy; az = fz; }
     if (MODE == 2) {
-        ax = (double)fa[0] + (double)fa[3];
-        ay = (double)fa[1] + (double)fa[4];
-        az = (double)fa[2] + (double)fa[5];
+        float hx, hy, lx, ly;
+        upk(fa.hxy, hx, hy);
+        upk(fa.lxy, lx, ly);
+        ax = (double)hx + (double)lx;
+        ay = (double)hy + (double)ly;
+        az = (double)fa.hz + (double)fa.lz;
     }
     store_acc(out, t, ax, ay, az);
 }
