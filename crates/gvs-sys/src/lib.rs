@@ -137,6 +137,14 @@ unsafe extern "C" {
     pub fn gvs_adjoint_backward(ctx: *mut gvs_ctx, dl_dx: *const f64, dl_dy: *const f64, dl_dz: *const f64,
         dl_dvx: *const f64, dl_dvy: *const f64, dl_dvz: *const f64, g_x: *mut f64, g_y: *mut f64,
         g_z: *mut f64, g_vx: *mut f64, g_vy: *mut f64, g_vz: *mut f64, g_m: *mut f64) -> gvs_status;
+    pub fn gvs_adjoint_checkpoints(ctx: *mut gvs_ctx, cap: c_longlong, count: *mut c_longlong,
+        steps: *mut c_longlong) -> gvs_status;
+    pub fn gvs_adjoint_checkpoint_read(ctx: *mut gvs_ctx, k: c_longlong, x: *mut f64, y: *mut f64, z: *mut f64,
+        vx: *mut f64, vy: *mut f64, vz: *mut f64) -> gvs_status;
+    pub fn gvs_adjoint_prepare(ctx: *mut gvs_ctx, precision: c_int, softening: f64, dt: f64,
+        nsteps: c_longlong, checkpoint_every: c_longlong) -> gvs_status;
+    pub fn gvs_adjoint_checkpoint_write(ctx: *mut gvs_ctx, k: c_longlong, x: *const f64, y: *const f64,
+        z: *const f64, vx: *const f64, vy: *const f64, vz: *const f64) -> gvs_status;
     pub fn gvs_ensemble_setup(ctx: *mut gvs_ctx, nsys: c_int, sizes: *const i64,
         softening: f64) -> gvs_status;
     pub fn gvs_ensemble_forces(ctx: *mut gvs_ctx) -> gvs_status;

@@ -79,6 +79,10 @@ SIGNATURES = {
     "gvs_ensemble_kdk_steps": (_ST, [_P, _d, _ll, _i]),
     "gvs_adjoint_forward": (_ST, [_P, _i, _d, _d, _ll, _ll]),
     "gvs_adjoint_backward": (_ST, [_P] + [_P] * 13),
+    "gvs_adjoint_checkpoints": (_ST, [_P, _ll, _P, _P]),
+    "gvs_adjoint_checkpoint_read": (_ST, [_P, _ll] + [_P] * 6),
+    "gvs_adjoint_prepare": (_ST, [_P, _i, _d, _d, _ll, _ll]),
+    "gvs_adjoint_checkpoint_write": (_ST, [_P, _ll] + [_P] * 6),
     "gvs_sph_params_default": (_ST, [C.POINTER(SphParams)]),
     "gvs_sph_compute": (_ST, [_P, C.POINTER(SphParams), _P, _P, _P, _P]),
     "gvs_sph_timestep": (_ST, [_P, C.POINTER(SphParams), C.POINTER(_d)]),

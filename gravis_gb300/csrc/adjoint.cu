@@ -18,6 +18,8 @@
 // so round-off never accumulates over more than `every` steps.
 #include "gvs_internal.cuh"
 
+#include <algorithm>
+
 namespace gvs {
 
 namespace {
@@ -28,6 +30,7 @@ struct AdjState {
     int precision = GVS_PREC_MIXED;
     double eps = 0.0, dt = 0.0;
     bool have_forward = false;
+    std::vector<char> written;                  // checkpoints present (all after a forward run)
     DevBuf ck;                                  // [nck][6][n] f64 checkpoints (x, y, z, vx, vy, vz)
     DevBuf lx, ly, lz, lvx, lvy, lvz, gm;       // adjoints
     DevBuf vhx, vhy, vhz;                       // v' of the current step
@@ -114,9 +117,12 @@ static long long ck_slot(const AdjState *A, long long s) {
     return (s % A->every == 0) ? s / A->every : -1;
 }
 
-gvs_status adjoint_forward(Ctx *c, int precision, double eps, double dt, long long nsteps, long long every) {
+// The plan of a forward run (sizes, step, forces) and its checkpoint storage, with no
+// checkpoint present yet.
+static gvs_status adjoint_plan(Ctx *c, AdjState *A, int precision, double eps, double dt, long long nsteps,
+                               long long every) {
     const size_t n = c->n;
-    AdjState *A = adj_of(c);
+    A->have_forward = false;
     A->n = n;
     A->nsteps = nsteps;
     A->every = every;
@@ -124,7 +130,17 @@ gvs_status adjoint_forward(Ctx *c, int precision, double eps, double dt, long lo
     A->precision = precision;
     A->eps = eps;
     A->dt = dt;
+    A->written.assign((size_t)A->nck, 0);
     GVS_CUDA(c, ensure(c, A->ck, (size_t)A->nck * 6 * n * sizeof(double)));
+    return GVS_OK;
+}
+
+// Step index of checkpoint k (the inverse of ck_slot).
+static long long ck_step(const AdjState *A, long long k) { return k == A->nck - 1 ? A->nsteps : k * A->every; }
+
+gvs_status adjoint_forward(Ctx *c, int precision, double eps, double dt, long long nsteps, long long every) {
+    AdjState *A = adj_of(c);
+    GVS_TRY(adjoint_plan(c, A, precision, eps, dt, nsteps, every));
     GVS_TRY(gravity(c, GVS_ALGO_DIRECT, precision, eps, 0.0, false));  // a(x_0)
     GVS_TRY(store_ck(c, A, 0));
     const double half = 0.5 * dt;
@@ -135,6 +151,7 @@ gvs_status adjoint_forward(Ctx *c, int precision, double eps, double dt, long lo
         const long long slot = ck_slot(A, s);
         if (slot >= 0) GVS_TRY(store_ck(c, A, slot));
     }
+    std::fill(A->written.begin(), A->written.end(), 1);
     A->have_forward = true;
     return GVS_OK;
 }
@@ -230,7 +247,9 @@ extern "C" gvs_status gvs_adjoint_backward(gvs_ctx *ctx, const double *dl_dx, co
     if (n == 0) return fail(c, GVS_ERR_STATE, "no particles");
     cudaSetDevice(c->device);
     AdjState *A = adj_of(c);
-    if (!A->have_forward || A->n != n) return fail(c, GVS_ERR_STATE, "gvs_adjoint_backward needs gvs_adjoint_forward");
+    if (!A->have_forward || A->n != n)
+        return fail(c, GVS_ERR_STATE,
+                    "gvs_adjoint_backward needs gvs_adjoint_forward, or gvs_adjoint_prepare and every checkpoint");
     GVS_CUDA(c, ensure(c, c->scratch_b, 13 * b));
     double *io = as<double>(c->scratch_b);
     const double *in[6] = {dl_dx, dl_dy, dl_dz, dl_dvx, dl_dvy, dl_dvz};
@@ -249,4 +268,81 @@ extern "C" gvs_status gvs_adjoint_backward(gvs_ctx *ctx, const double *dl_dx, co
         if (out[k]) GVS_CUDA(c, cudaMemcpyAsync(out[k], grad[k], b, cudaMemcpyDeviceToHost, c->stream));
     GVS_CUDA(c, cudaStreamSynchronize(c->stream));
     return read_device_errors(c);
+}
+
+// ---- checkpoints in and out --------------------------------------------------------
+// The f64 checkpoints of a forward run leave the device (to be written as NBODY003
+// snapshots, crates/sim-core/src/snapshot.rs:40-65, by the host) and come back into a
+// fresh context, so that the backward sweep can run in another process or after a
+// restart and give the same gradients bit for bit.
+
+static gvs_status adj_args(Ctx *c, const char *what) {
+    if (!c) return fail(nullptr, GVS_ERR_INVALID_ARG, "null context");
+    AdjState *A = static_cast<AdjState *>(c->adj);
+    if (!A || A->nck == 0) return fail(c, GVS_ERR_STATE, "%s needs gvs_adjoint_forward or gvs_adjoint_prepare", what);
+    if (A->n != c->n)
+        return fail(c, GVS_ERR_STATE, "%s: the resident state has %zu particles, the checkpoints %zu", what, c->n, A->n);
+    return GVS_OK;
+}
+
+extern "C" gvs_status gvs_adjoint_checkpoints(gvs_ctx *ctx, long long cap, long long *count, long long *steps) {
+    Ctx *c = reinterpret_cast<Ctx *>(ctx);
+    GVS_TRY(adj_args(c, "gvs_adjoint_checkpoints"));
+    if (!count) return fail(c, GVS_ERR_INVALID_ARG, "count is NULL");
+    const AdjState *A = static_cast<AdjState *>(c->adj);
+    *count = A->nck;
+    if (steps && cap >= A->nck)
+        for (long long k = 0; k < A->nck; ++k) steps[k] = ck_step(A, k);
+    return GVS_OK;
+}
+
+extern "C" gvs_status gvs_adjoint_prepare(gvs_ctx *ctx, int precision, double softening, double dt, long long nsteps,
+                                          long long checkpoint_every) {
+    Ctx *c = reinterpret_cast<Ctx *>(ctx);
+    if (!c) return fail(nullptr, GVS_ERR_INVALID_ARG, "null context");
+    if (precision < GVS_PREC_FP64_EXACT || precision > GVS_PREC_MIXED)
+        return fail(c, GVS_ERR_INVALID_ARG, "bad precision %d", precision);
+    if (!(softening >= 0.0) || !(dt > 0.0) || nsteps < 1 || checkpoint_every < 1)
+        return fail(c, GVS_ERR_INVALID_ARG, "need softening >= 0, dt > 0, nsteps >= 1, checkpoint_every >= 1");
+    if (c->n == 0) return fail(c, GVS_ERR_STATE, "no particles");
+    cudaSetDevice(c->device);
+    return adjoint_plan(c, adj_of(c), precision, softening, dt, nsteps, checkpoint_every);
+}
+
+extern "C" gvs_status gvs_adjoint_checkpoint_read(gvs_ctx *ctx, long long k, double *x, double *y, double *z,
+                                                  double *vx, double *vy, double *vz) {
+    Ctx *c = reinterpret_cast<Ctx *>(ctx);
+    GVS_TRY(adj_args(c, "gvs_adjoint_checkpoint_read"));
+    AdjState *A = static_cast<AdjState *>(c->adj);
+    if (k < 0 || k >= A->nck) return fail(c, GVS_ERR_INVALID_ARG, "checkpoint %lld of %lld", k, A->nck);
+    if (!A->written[(size_t)k]) return fail(c, GVS_ERR_STATE, "checkpoint %lld has not been written", k);
+    if (!x || !y || !z || !vx || !vy || !vz) return fail(c, GVS_ERR_INVALID_ARG, "null output array");
+    cudaSetDevice(c->device);
+    const size_t n = A->n, b = n * sizeof(double);
+    const double *src = as<double>(A->ck) + (size_t)k * 6 * n;
+    double *out[6] = {x, y, z, vx, vy, vz};
+    for (int f = 0; f < 6; ++f)
+        GVS_CUDA(c, cudaMemcpyAsync(out[f], src + (size_t)f * n, b, cudaMemcpyDeviceToHost, c->stream));
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return GVS_OK;
+}
+
+extern "C" gvs_status gvs_adjoint_checkpoint_write(gvs_ctx *ctx, long long k, const double *x, const double *y,
+                                                   const double *z, const double *vx, const double *vy,
+                                                   const double *vz) {
+    Ctx *c = reinterpret_cast<Ctx *>(ctx);
+    GVS_TRY(adj_args(c, "gvs_adjoint_checkpoint_write"));
+    AdjState *A = static_cast<AdjState *>(c->adj);
+    if (k < 0 || k >= A->nck) return fail(c, GVS_ERR_INVALID_ARG, "checkpoint %lld of %lld", k, A->nck);
+    if (!x || !y || !z || !vx || !vy || !vz) return fail(c, GVS_ERR_INVALID_ARG, "null input array");
+    cudaSetDevice(c->device);
+    const size_t n = A->n, b = n * sizeof(double);
+    double *dst = as<double>(A->ck) + (size_t)k * 6 * n;
+    const double *in[6] = {x, y, z, vx, vy, vz};
+    for (int f = 0; f < 6; ++f)
+        GVS_CUDA(c, cudaMemcpyAsync(dst + (size_t)f * n, in[f], b, cudaMemcpyHostToDevice, c->stream));
+    GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    A->written[(size_t)k] = 1;
+    A->have_forward = std::all_of(A->written.begin(), A->written.end(), [](char w) { return w != 0; });
+    return GVS_OK;
 }

@@ -127,6 +127,7 @@ class Context:
         if st != L.OK:
             raise L.GvsError(st, L.last_error(None))
         self.h = h.value
+        self._adj_run = None  # (softening, dt) of the last adjoint forward run
 
     def close(self):
         if getattr(self, "h", None):
@@ -208,6 +209,73 @@ class Context:
 
     def adjoint_forward(self, precision: int, softening: float, dt: float, nsteps: int, checkpoint_every: int = 100):
         self._ck(self._lib.gvs_adjoint_forward(self.h, precision, softening, dt, nsteps, checkpoint_every))
+        self._adj_run = (softening, dt)
+
+    def adjoint_checkpoint_steps(self) -> list:
+        """Step index of every checkpoint of the last forward run: 0, every, ..., nsteps."""
+        count = C.c_longlong()
+        self._ck(self._lib.gvs_adjoint_checkpoints(self.h, 0, C.byref(count), None))
+        steps = np.zeros(count.value, dtype=np.int64)
+        self._ck(self._lib.gvs_adjoint_checkpoints(self.h, count.value, C.byref(count), _ptr(steps)))
+        return [int(s) for s in steps]
+
+    def adjoint_checkpoint(self, k: int) -> tuple:
+        """Checkpoint k's f64 positions and velocities, (n, 3) arrays in caller order."""
+        n = self._lib.gvs_count(self.h)
+        a = np.zeros((6, n))
+        self._ck(self._lib.gvs_adjoint_checkpoint_read(self.h, k, *(_ptr(a[f]) for f in range(6))))
+        return a[:3].T.copy(), a[3:].T.copy()
+
+    def adjoint_save_checkpoints(self, directory: str, particles: Particles) -> list:
+        """Writes every checkpoint of the last forward run as an NBODY003 snapshot
+        (snapshot.rs:40-65), directory/checkpoint_<step>.nbody: time = step * dt, the
+        run's softening and dt, the checkpoint's positions and velocities, and the masses,
+        particle types and gas fields of `particles` (the state the run started from).
+        Returns the paths in step order."""
+        import os
+        if self._adj_run is None:
+            raise L.GvsError(L.ERR_STATE, "adjoint_save_checkpoints needs adjoint_forward")
+        softening, dt = self._adj_run
+        paths = []
+        for k, step in enumerate(self.adjoint_checkpoint_steps()):
+            x, v = self.adjoint_checkpoint(k)
+            p = particles.copy()
+            p.x, p.y, p.z = (np.ascontiguousarray(x[:, d]) for d in range(3))
+            p.vx, p.vy, p.vz = (np.ascontiguousarray(v[:, d]) for d in range(3))
+            path = os.path.join(directory, f"checkpoint_{step:09d}.nbody")
+            with open(path, "wb") as fh:
+                Snapshot.capture(p, step * dt, step, softening, dt).write_to(fh)
+            paths.append(path)
+        return paths
+
+    def adjoint_load_checkpoints(self, paths, precision: int):
+        """Reads the NBODY003 checkpoints of one forward run (any order), makes the first
+        (step 0) the resident state and fills the backward sweep's checkpoints with them,
+        so that adjoint_backward gives the gradients of that run bit for bit."""
+        snaps = []
+        for path in paths:
+            with open(path, "rb") as fh:
+                snaps.append(Snapshot.read_from(fh))
+        snaps.sort(key=lambda s: s.step)
+        steps = [s.step for s in snaps]
+        if not snaps or steps[0] != 0 or len(steps) < 2:
+            raise ValueError("adjoint checkpoints: need step 0 and at least one later step")
+        nsteps, every = steps[-1], steps[1]
+        want = list(range(0, nsteps, every)) + [nsteps]
+        if steps != want:
+            raise ValueError(f"adjoint checkpoints: steps {steps} are not 0, {every}, ..., {nsteps}")
+        s0 = snaps[0]
+        for s in snaps[1:]:
+            if (s.softening, s.dt, s.particles.count) != (s0.softening, s0.dt, s0.particles.count) or \
+                    not np.array_equal(s.particles.mass, s0.particles.mass):
+                raise ValueError(f"adjoint checkpoints: step {s.step} is not from the run of step 0")
+        self.set_state(s0.particles)
+        self._ck(self._lib.gvs_adjoint_prepare(self.h, precision, s0.softening, s0.dt, nsteps, every))
+        self._adj_run = (s0.softening, s0.dt)
+        for k, s in enumerate(snaps):
+            q = s.particles
+            arrs = [np.ascontiguousarray(getattr(q, f), dtype=np.float64) for f in ("x", "y", "z", "vx", "vy", "vz")]
+            self._ck(self._lib.gvs_adjoint_checkpoint_write(self.h, k, *(_ptr(a) for a in arrs)))
 
     def adjoint_backward(self, dl_dx: np.ndarray, dl_dv: np.ndarray | None = None) -> dict:
         """dl_dx, dl_dv: (n, 3) arrays.  Returns dL/dx0, dL/dv0 (n, 3) and dL/dm (n,) through the dynamics."""

@@ -197,6 +197,23 @@ gvs_status gvs_adjoint_forward(gvs_ctx *ctx, int precision, double softening, do
 gvs_status gvs_adjoint_backward(gvs_ctx *ctx, const double *dl_dx, const double *dl_dy, const double *dl_dz,
                                 const double *dl_dvx, const double *dl_dvy, const double *dl_dvz, double *g_x,
                                 double *g_y, double *g_z, double *g_vx, double *g_vy, double *g_vz, double *g_m);
+/* Checkpoints of the last forward run, for writing as NBODY003 snapshots
+ * (crates/sim-core/src/snapshot.rs:40-65) and reading back in another process.
+ * gvs_adjoint_checkpoints: their number, and (if cap >= *count) the step of each:
+ * 0, every, 2 every, ..., nsteps.  gvs_adjoint_checkpoint_read: checkpoint k's f64
+ * positions and velocities (host arrays of n, caller order).
+ * gvs_adjoint_prepare: the plan of a forward run (the arguments of gvs_adjoint_forward)
+ * on the resident state, without running it; gvs_adjoint_checkpoint_write then fills
+ * checkpoint k, and once every checkpoint is written gvs_adjoint_backward runs as after
+ * the forward run itself, with the same gradients bit for bit (the resident masses are
+ * the ones the forward run used). */
+gvs_status gvs_adjoint_checkpoints(gvs_ctx *ctx, long long cap, long long *count, long long *steps);
+gvs_status gvs_adjoint_checkpoint_read(gvs_ctx *ctx, long long k, double *x, double *y, double *z, double *vx,
+                                       double *vy, double *vz);
+gvs_status gvs_adjoint_prepare(gvs_ctx *ctx, int precision, double softening, double dt, long long nsteps,
+                               long long checkpoint_every);
+gvs_status gvs_adjoint_checkpoint_write(gvs_ctx *ctx, long long k, const double *x, const double *y,
+                                        const double *z, const double *vx, const double *vy, const double *vz);
 
 /* ---- batched ensembles (no reference counterpart; each system is the reference's
  * BruteForce + LeapfrogKDK problem, gravity.rs:47-80, integrator.rs:42-76) ----------- */

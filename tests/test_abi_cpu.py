@@ -39,6 +39,11 @@ def test_null_context_is_invalid_arg(lib):
     assert lib.gvs_create(None, 0) == L.ERR_INVALID_ARG
     assert lib.gvs_set_bh_walk(None, 64, 0) == L.ERR_INVALID_ARG
     assert lib.gvs_set_direct_shape(None, 256, 4, 2, 2) == L.ERR_INVALID_ARG
+    n = C.c_longlong()
+    assert lib.gvs_adjoint_checkpoints(None, 0, C.byref(n), None) == L.ERR_INVALID_ARG
+    assert lib.gvs_adjoint_prepare(None, 3, 0.01, 1e-3, 10, 5) == L.ERR_INVALID_ARG
+    assert lib.gvs_adjoint_checkpoint_read(None, 0, *([None] * 6)) == L.ERR_INVALID_ARG
+    assert lib.gvs_adjoint_checkpoint_write(None, 0, *([None] * 6)) == L.ERR_INVALID_ARG
 
 
 def test_ic_args_validated(lib):

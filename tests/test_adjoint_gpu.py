@@ -129,3 +129,47 @@ def test_fp64_adjoint_vs_finite_differences_4096(ctx):
         errs.append(abs(ad - fd) / abs(fd))
     print(f"8 directions: relative error max {max(errs):.2e}, median {np.median(errs):.2e}")
     assert max(errs) <= 1e-5, errs
+
+
+@pytest.mark.parametrize("prec", [G.PREC_FP64, G.PREC_MIXED])
+def test_checkpoints_as_snapshots_restart_backward(ctx, prec, tmp_path):
+    """The forward run's checkpoints, written as NBODY003 snapshots (snapshot.rs:40-65)
+    and read into a fresh context, give the same gradients bit for bit; each checkpoint
+    is the state of a plain KDK run of that many steps."""
+    n, eps, dt, nsteps, every = 384, 0.05, 1e-3, 250, 100
+    p, xstar = setup(n, 5, eps, dt, nsteps, ctx)
+    ctx.set_state(p)
+    ctx.adjoint_forward(prec, eps, dt, nsteps, every)
+    assert ctx.adjoint_checkpoint_steps() == [0, 100, 200, 250]
+    paths = ctx.adjoint_save_checkpoints(str(tmp_path), p)
+    q = G.Particles(n)
+    ctx.get_state(q)
+    x = np.stack([q.x, q.y, q.z], 1)
+    dl_dx = 2.0 * p.mass[:, None] * (x - xstar)
+    dl_dv = 0.1 * np.random.default_rng(2).standard_normal((n, 3))
+    g1 = ctx.adjoint_backward(dl_dx, dl_dv)
+    # a snapshot read back holds the checkpoint (time = step * dt, the run's eps and dt)
+    with open(paths[1], "rb") as fh:
+        s = G.Snapshot.read_from(fh)
+    assert (s.step, s.time, s.softening, s.dt) == (100, 100 * dt, eps, dt)
+    xs, vs = ctx.adjoint_checkpoint(1)
+    assert np.array_equal(np.stack([s.particles.x, s.particles.y, s.particles.z], 1), xs)
+    assert np.array_equal(np.stack([s.particles.vx, s.particles.vy, s.particles.vz], 1), vs)
+    assert np.array_equal(s.particles.mass, p.mass)
+    # checkpoint 1 is the state after 100 plain KDK steps
+    _, x100 = forward_loss(ctx, p, xstar, eps, dt, 100, prec)
+    assert np.array_equal(x100, xs)
+    c2 = G.Context(0)
+    try:
+        c2.adjoint_load_checkpoints(reversed(paths), prec)
+        g2 = c2.adjoint_backward(dl_dx, dl_dv)
+        r = G.Particles(n)
+        c2.get_state(r)  # the initial state again, as after the original run's sweep
+        assert np.array_equal(r.x, p.x) and np.array_equal(r.vz, p.vz)
+        # a set with a gap (0, 100, 250: step 200 missing) is refused
+        with pytest.raises(ValueError):
+            c2.adjoint_load_checkpoints([paths[0], paths[1], paths[3]], prec)
+    finally:
+        c2.close()
+    for k in ("x", "v", "m"):
+        assert np.array_equal(g1[k], g2[k]), k
