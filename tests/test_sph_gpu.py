@@ -245,3 +245,83 @@ def test_sph_mixed_steps_track_f64(ctx):
     a, b = runs
     for f in ("x", "vx", "internal_energy", "density"):
         assert rel(getattr(b, f), getattr(a, f)) <= 1e-6, (f, rel(getattr(b, f), getattr(a, f)))
+
+
+# ---- the reference's own SPH unit tests, on the GPU path ----------------------------
+def ref_lattice(n_side, spacing, u, h):
+    """The lattices of forces.rs:241-262 and solver.rs:219-241, built with add_gas."""
+    p = G.Particles()
+    for ix in range(n_side):
+        for iy in range(n_side):
+            for iz in range(n_side):
+                p.add_gas(ix * spacing, iy * spacing, iz * spacing, 0.0, 0.0, 0.0, 1.0, u, h)
+    return p
+
+
+@pytest.mark.parametrize("prec", [G.PREC_FP64_EXACT, G.PREC_MIXED])
+def test_uniform_pressure_zero_acceleration(ctx, prec):
+    """forces.rs:239-290: a uniform lattice (8^3, spacing 0.5, u 1, h 1): interior
+    particles (2.5 h from every face) feel |a| < 1; the f64 form equals the oracle."""
+    p = ref_lattice(8, 0.5, 1.0, 1.0)
+    q = to_oracle(p)
+    sph = G.SphSolver(ctx)
+    sph.params.precision = prec
+    sph.compute(p)
+    edge = 7 * 0.5
+    margin = 2.5 * p.smoothing_length
+    interior = ((p.x >= margin) & (p.y >= margin) & (p.z >= margin) & (p.x <= edge - margin)
+                & (p.y <= edge - margin) & (p.z <= edge - margin))
+    assert interior.any()
+    amag = np.sqrt(p.ax ** 2 + p.ay ** 2 + p.az ** 2)
+    print(f"interior particles {int(interior.sum())}, max |a| {amag[interior].max():.3e}")
+    assert amag[interior].max() < 1.0
+    O.Sph().compute(q)
+    assert rel(p.ax, q.ax) <= (1e-10 if prec == G.PREC_FP64_EXACT else 1e-6)
+
+
+@pytest.mark.parametrize("prec", [G.PREC_FP64_EXACT, G.PREC_MIXED])
+def test_viscosity_only_for_approaching(ctx, prec):
+    """forces.rs:292-332: two gas particles 1 apart (h 1): mu_max > 0 when they
+    approach (vx +-0.5), exactly 0 when they recede."""
+    sph = G.SphSolver(ctx)
+    sph.params.precision = prec
+    for v, approaching in ((0.5, True), (-0.5, False)):
+        p = G.Particles()
+        p.add_gas(0.0, 0.0, 0.0, v, 0.0, 0.0, 1.0, 1.0, 1.0)
+        p.add_gas(1.0, 0.0, 0.0, -v, 0.0, 0.0, 1.0, 1.0, 1.0)
+        inter = sph.compute(p)
+        if approaching:
+            assert inter.max_mu[0] > 0.0
+        else:
+            assert inter.max_mu[0] == 0.0
+
+
+@pytest.mark.parametrize("prec", [G.PREC_FP64_EXACT, G.PREC_MIXED])
+def test_static_gas_ball_stable(ctx, prec):
+    """solver.rs:219-266: a 6^3 gas lattice (spacing 0.5, u 1, h 0.8) with direct-sum
+    gravity (eps 0.1): five step_with_sph steps from dt 1e-3 keep 0 < dt < 1 and every
+    particle within r < 100; the f64 run stays on the oracle's trajectory."""
+    p = ref_lattice(6, 0.5, 1.0, 0.8)
+    q = to_oracle(p)
+    grav = G.BruteForce(0.1, G.PREC_FP64_EXACT if prec == G.PREC_FP64_EXACT else G.PREC_MIXED, ctx)
+    sph = G.SphSolver(ctx)
+    sph.params.precision = prec
+    p.clear_accelerations()
+    grav.compute_accelerations(p)
+    sph.compute(p)
+    dt = 0.001
+    for _ in range(5):
+        dt = G.step_with_sph(p, grav, sph, dt)
+        assert 0.0 < dt < 1.0, dt
+    r = np.sqrt(p.x ** 2 + p.y ** 2 + p.z ** 2)
+    assert r.max() < 100.0
+    if prec == G.PREC_FP64_EXACT:
+        og = O.gravity(O.GRAV_BF, 0.1)
+        s = O.Sph()
+        q.clear_accelerations()
+        O.bf_serial(q, 0.1)
+        s.compute(q)
+        odt = 0.001
+        for _ in range(5):
+            odt = s.step(q, og, odt)
+        assert rel(p.x, q.x) <= 1e-9 and abs(dt - odt) <= 1e-9 * odt
