@@ -1519,7 +1519,8 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
     const int gsize = c->bh_group >= 0 ? c->bh_group : (n >= (size_t(1) << 21) ? 128 : 64);
     const bool group = mode == 1 && gsize > 0 && nnodes < (size_t(1) << 29);
     if (group) GVS_TRY(group_prepare(c, t, gsize));
-    if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], st));
+    int span = -1;  // profile timing span
+    GVS_TRY(prof_begin(c, st, &span));
     if (group) {
         GVS_CUDA(c, cudaMemsetAsync(as<uint32_t>(t->gcount) + 1, 0, 4, st));
         const bool guard = eps == 0.0;
@@ -1554,11 +1555,7 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
     c->prof.launches += 1;
     GVS_TRY(check_launch(c, "tree walk"));
     if (c->prof.on) {
-        GVS_CUDA(c, cudaEventRecord(c->prof.ev[1], st));
-        GVS_CUDA(c, cudaEventSynchronize(c->prof.ev[1]));
-        float ms = 0.f;
-        GVS_CUDA(c, cudaEventElapsedTime(&ms, c->prof.ev[0], c->prof.ev[1]));
-        c->prof.force_ms += ms;
+        GVS_TRY(prof_end(c, span, st, &c->prof.force_ms));
         c->prof.force_launches += 1;
     }
     return GVS_OK;

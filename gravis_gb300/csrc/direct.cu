@@ -1473,18 +1473,15 @@ gvs_status launch32_t(Ctx *c, float eps2, int nsplit_req, double **partial_out, 
     const int nsplit_eff = ceil_div(ntiles, tps);
     GVS_CUDA(c, ensure(c, c->partial, (size_t)nsplit_eff * 3 * npad * sizeof(double)));
     dim3 grid(iblocks, nsplit_eff);
-    if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], c->stream));
+    int span = -1;  // profile timing span
+    GVS_TRY(prof_begin(c, c->stream, &span));
     unsigned long long *nearc = reinterpret_cast<unsigned long long *>(err_ptr(c) + EW_NEAR_TILES);
     kern<<<grid, NT, smem, c->stream>>>(as<float4>(c->jpack32), ntiles, tps, eps2, as<double>(c->partial), npad,
                                         err_ptr(c), nearc);
     c->prof.launches += 1;
     GVS_TRY(check_launch(c, "direct f32 kernel"));
     if (c->prof.on) {
-        GVS_CUDA(c, cudaEventRecord(c->prof.ev[1], c->stream));
-        GVS_CUDA(c, cudaEventSynchronize(c->prof.ev[1]));
-        float ms = 0.f;
-        GVS_CUDA(c, cudaEventElapsedTime(&ms, c->prof.ev[0], c->prof.ev[1]));
-        c->prof.force_ms += ms;
+        GVS_TRY(prof_end(c, span, c->stream, &c->prof.force_ms));
         c->prof.force_launches += 1;
         c->prof.force_flops += 20.0 * (double)n * (double)n;
         c->prof.force_bytes += (double)nsplit_eff * (double)npad * 24.0 + (double)iblocks * nsplit_eff * tps *
@@ -1546,17 +1543,14 @@ gvs_status launch64(Ctx *c, double eps2, double **partial_out, int *nsplit_out, 
     const int smem = NSTAGE * TJ64 * (int)sizeof(double4);
     auto kern = eps2 > 0.0 ? k_direct64<NT, IPT, NSTAGE, false> : k_direct64<NT, IPT, NSTAGE, true>;
     set_smem(kern, smem);
-    if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], c->stream));
+    int span = -1;  // profile timing span
+    GVS_TRY(prof_begin(c, c->stream, &span));
     kern<<<dim3(iblocks, nsplit_eff), NT, smem, c->stream>>>(as<double4>(c->jpack64), ntiles, tps, eps2,
                                                               as<double>(c->partial), npad, err_ptr(c));
     c->prof.launches += 1;
     GVS_TRY(check_launch(c, "direct f64 kernel"));
     if (c->prof.on) {
-        GVS_CUDA(c, cudaEventRecord(c->prof.ev[1], c->stream));
-        GVS_CUDA(c, cudaEventSynchronize(c->prof.ev[1]));
-        float ms = 0.f;
-        GVS_CUDA(c, cudaEventElapsedTime(&ms, c->prof.ev[0], c->prof.ev[1]));
-        c->prof.force_ms += ms;
+        GVS_TRY(prof_end(c, span, c->stream, &c->prof.force_ms));
         c->prof.force_launches += 1;
         c->prof.force_flops += 20.0 * (double)n * (double)n;
     }
@@ -1573,7 +1567,8 @@ gvs_status direct_forces(Ctx *c, int precision, double eps, bool accumulate) {
     if (n == 0) return GVS_OK;
     const double eps2 = eps * eps;
     if (precision == GVS_PREC_FP64_EXACT) {
-        if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], c->stream));
+        int span = -1;  // profile timing span
+        GVS_TRY(prof_begin(c, c->stream, &span));
         if (n <= EXACT_SPLIT_MAX) {
             const int C = (int)std::max<size_t>(1, std::min<size_t>(n, EXACT_TERMS_BYTES / (24 * n)));
             GVS_CUDA(c, ensure(c, c->exact_terms, (size_t)C * n * 24));
@@ -1601,11 +1596,7 @@ gvs_status direct_forces(Ctx *c, int precision, double eps, bool accumulate) {
         }
         GVS_TRY(check_launch(c, "direct exact kernel"));
         if (c->prof.on) {
-            GVS_CUDA(c, cudaEventRecord(c->prof.ev[1], c->stream));
-            GVS_CUDA(c, cudaEventSynchronize(c->prof.ev[1]));
-            float ms = 0.f;
-            GVS_CUDA(c, cudaEventElapsedTime(&ms, c->prof.ev[0], c->prof.ev[1]));
-            c->prof.force_ms += ms;
+            GVS_TRY(prof_end(c, span, c->stream, &c->prof.force_ms));
             c->prof.force_launches += 1;
             c->prof.force_flops += 20.0 * (double)n * (double)(n - 1);
         }
@@ -1647,6 +1638,7 @@ gvs_status direct_force_vjp(Ctx *c, int precision, double eps, const double *wx,
     double *partial = nullptr;
     int nsplit_eff = 1;
     size_t npad = 0;
+    int span = -1;  // profile timing span
     if (precision == GVS_PREC_MIXED || precision == GVS_PREC_FP32) {
         constexpr int NT = 128, NP = 1, NSTAGE = 3, TJ = NT, IPT = 2 * NP;
         constexpr int TF4 = tile_f4(TJ), WF4 = wtile_f4(TJ);
@@ -1674,7 +1666,7 @@ gvs_status direct_force_vjp(Ctx *c, int precision, double eps, const double *wx,
         nsplit_eff = ceil_div(ntiles, tps);
         GVS_CUDA(c, ensure(c, c->partial, (size_t)nsplit_eff * 7 * npad * sizeof(double)));
         partial = as<double>(c->partial);
-        if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], st));
+        GVS_TRY(prof_begin(c, st, &span));
         kern<<<dim3(iblocks, nsplit_eff), NT, smem, st>>>(as<float4>(c->jpack32), as<float4>(c->scratch_a), ntiles,
                                                           tps, e2, partial, npad, err_ptr(c));
     } else {
@@ -1697,18 +1689,14 @@ gvs_status direct_force_vjp(Ctx *c, int precision, double eps, const double *wx,
         nsplit_eff = ceil_div(ntiles, tps);
         GVS_CUDA(c, ensure(c, c->partial, (size_t)nsplit_eff * 7 * npad * sizeof(double)));
         partial = as<double>(c->partial);
-        if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], st));
+        GVS_TRY(prof_begin(c, st, &span));
         k_force_vjp64<NT, NSTAGE><<<dim3(iblocks, nsplit_eff), NT, 0, st>>>(
             as<double4>(c->jpack64), as<double4>(c->scratch_a), ntiles, tps, eps2, partial, npad);
     }
     c->prof.launches += 1;
     GVS_TRY(check_launch(c, "force+VJP kernel"));
     if (c->prof.on) {
-        GVS_CUDA(c, cudaEventRecord(c->prof.ev[1], st));
-        GVS_CUDA(c, cudaEventSynchronize(c->prof.ev[1]));
-        float ms = 0.f;
-        GVS_CUDA(c, cudaEventElapsedTime(&ms, c->prof.ev[0], c->prof.ev[1]));
-        c->prof.vjp_ms += ms;
+        GVS_TRY(prof_end(c, span, st, &c->prof.vjp_ms));
         c->prof.vjp_launches += 1;
     }
     k_reduce_vjp<<<ceil_div((long long)n, 256), 256, 0, st>>>(partial, nsplit_eff, npad, n, as<uint32_t>(c->perm),
@@ -1795,8 +1783,10 @@ gvs_status autotune_direct(Ctx *c, int precision, double eps, int *best_nt, int 
         c->tune.nsplit = 0;
         GVS_TRY(direct_forces(c, precision, eps, false));  // warm (also builds the order)
         c->prof.on = true;
+        GVS_TRY(prof_settle(c));
         const double ms0 = c->prof.force_ms;
         for (int r = 0; r < 2; ++r) GVS_TRY(direct_forces(c, precision, eps, false));
+        GVS_TRY(prof_settle(c));
         const double t = (c->prof.force_ms - ms0) / 2.0;
         c->prof.on = was_on;
         c->tune_report.push_back({c->tune, t});

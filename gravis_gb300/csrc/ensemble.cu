@@ -273,15 +273,12 @@ gvs_status ens_forces(Ctx *c) {
     c->prof.launches += 2;
     GVS_TRY(ens_pack(c, E->ntiles, as<uint32_t>(E->slot_orig), as<float4>(E->pack)));
     const float e2 = (float)(E->eps * E->eps);
-    if (c->prof.on) GVS_CUDA(c, cudaEventRecord(c->prof.ev[0], st));
+    int span = -1;  // profile timing span
+    GVS_TRY(prof_begin(c, st, &span));
     GVS_TRY(ens_pairs(c, as<float4>(E->pack), as<int4>(E->items), E->nitems, as<unsigned>(E->counter), e2,
                       as<double>(E->partial), E->npad, E->ntiles, E->max_split));
     if (c->prof.on) {  // kernel time of the batched pair kernel
-        GVS_CUDA(c, cudaEventRecord(c->prof.ev[1], st));
-        GVS_CUDA(c, cudaEventSynchronize(c->prof.ev[1]));
-        float ms = 0.f;
-        GVS_CUDA(c, cudaEventElapsedTime(&ms, c->prof.ev[0], c->prof.ev[1]));
-        c->prof.force_ms += ms;
+        GVS_TRY(prof_end(c, span, st, &c->prof.force_ms));
         c->prof.force_launches += 1;
         c->prof.force_flops += 20.0 * E->pairs;
     }

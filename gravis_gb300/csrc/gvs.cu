@@ -146,6 +146,47 @@ static gvs_status kdk_one(Ctx *c, int algo, int precision, double eps, double th
     return GVS_OK;
 }
 
+gvs_status prof_begin(Ctx *c, cudaStream_t st, int *slot) {
+    *slot = -1;
+    if (!c->prof.on) return GVS_OK;
+    Prof &p = c->prof;
+    if (p.used + 2 > (int)p.pool.size()) {
+        if (p.pool.size() >= 1024) {
+            GVS_TRY(prof_settle(c));  // a long run without a read: settle, then reuse the pool
+        } else {
+            for (int k = 0; k < 2; ++k) {
+                cudaEvent_t e = nullptr;
+                GVS_CUDA(c, cudaEventCreate(&e));
+                p.pool.push_back(e);
+            }
+        }
+    }
+    *slot = p.used;
+    p.used += 2;
+    GVS_CUDA(c, cudaEventRecord(p.pool[(size_t)*slot], st));
+    return GVS_OK;
+}
+
+gvs_status prof_end(Ctx *c, int slot, cudaStream_t st, double *acc) {
+    if (slot < 0) return GVS_OK;
+    GVS_CUDA(c, cudaEventRecord(c->prof.pool[(size_t)slot + 1], st));
+    c->prof.spans.emplace_back(slot, acc);
+    return GVS_OK;
+}
+
+gvs_status prof_settle(Ctx *c) {
+    Prof &p = c->prof;
+    for (const auto &sp : p.spans) {
+        GVS_CUDA(c, cudaEventSynchronize(p.pool[(size_t)sp.first + 1]));
+        float ms = 0.f;
+        GVS_CUDA(c, cudaEventElapsedTime(&ms, p.pool[(size_t)sp.first], p.pool[(size_t)sp.first + 1]));
+        *sp.second += ms;
+    }
+    p.spans.clear();
+    p.used = 0;
+    return GVS_OK;
+}
+
 }  // namespace gvs
 
 using namespace gvs;
@@ -247,6 +288,9 @@ gvs_status gvs_create(gvs_ctx **out, int device) {
     c->device = device;
     c->num_sms = prop.multiProcessorCount;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreate(&c->prof.ev[0]) != cudaSuccess || cudaEventCreate(&c->prof.ev[1]) != cudaSuccess) {
         delete c;
         return fail(nullptr, GVS_ERR_LAUNCH, "stream/event creation failed");
@@ -265,6 +309,7 @@ gvs_status gvs_destroy(gvs_ctx *c) {
     if (!c) return GVS_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->side) cudaStreamSynchronize(c->side);
     if (c->sgraph.exec) cudaGraphExecDestroy(c->sgraph.exec);
     tree_free(c);
     sph_free(c);
@@ -281,6 +326,10 @@ gvs_status gvs_destroy(gvs_ctx *c) {
     if (c->pinned) cudaFreeHost(c->pinned);
     for (int k = 0; k < 2; ++k)
         if (c->prof.ev[k]) cudaEventDestroy(c->prof.ev[k]);
+    for (cudaEvent_t e : c->prof.pool) cudaEventDestroy(e);
+    if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+    if (c->join_ev) cudaEventDestroy(c->join_ev);
+    if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return GVS_OK;
@@ -690,6 +739,7 @@ struct EventSlots {
 
 gvs_status gvs_profile_enable(gvs_ctx *c, int on) {
     GVS_TRY(check_ctx(c));
+    GVS_TRY(prof_settle(c));  // spans of the previous profile go to the counters reset below
     c->prof.on = on != 0;
     c->prof.force_ms = 0.0;
     c->prof.force_launches = 0;
@@ -708,6 +758,7 @@ gvs_status gvs_profile_read(gvs_ctx *c, gvs_profile *out) {
     GVS_TRY(check_ctx(c));
     if (!out) return fail(c, GVS_ERR_INVALID_ARG, "out is NULL");
     GVS_CUDA(c, cudaStreamSynchronize(c->stream));
+    GVS_TRY(prof_settle(c));
     out->force_ms = c->prof.force_ms;
     out->force_launches = c->prof.force_launches;
     out->launches = c->prof.launches;

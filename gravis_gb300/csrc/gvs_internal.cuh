@@ -65,6 +65,11 @@ template <class T> T *as(DevBuf &b) { return reinterpret_cast<T *>(b.ptr); }
 struct Prof {
     bool on = false;
     cudaEvent_t ev[2] = {nullptr, nullptr};
+    // timed spans: event pairs recorded on the kernels' streams and read at the next
+    // settle (profile read), so that timing never blocks the host between launches
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::pair<int, double *>> spans;  // (first event of the pair, where its ms go)
+    int used = 0;
     double force_ms = 0.0;   // summed device time of force kernels
     long long force_launches = 0;
     long long launches = 0;  // every kernel this context launched
@@ -87,6 +92,11 @@ struct Ctx {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    // a second stream for work that runs beside the main stream's (gravity beside the
+    // SPH pass of a step), forked and joined with the two events
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    cudaEvent_t sph_join = nullptr;  // set while an SPH pass must wait for it before adding its accelerations
     std::string last_error;
 
     // resident state, caller order, capacity >= n
@@ -148,6 +158,12 @@ gvs_status fail(Ctx *c, gvs_status s, const char *fmt, ...);
 gvs_status cuda_fail(Ctx *c, cudaError_t e, const char *what);
 gvs_status check_launch(Ctx *c, const char *what);
 gvs_status read_device_errors(Ctx *c);  // syncs the stream; DEVICE_ERROR if any flag
+// Profile timing: prof_begin records the start of a span on `st` (slot -1 when the
+// profile is off), prof_end its end, whose device time is added to *acc at the next
+// prof_settle (which waits for every recorded span; gvs_profile_read calls it).
+gvs_status prof_begin(Ctx *c, cudaStream_t st, int *slot);
+gvs_status prof_end(Ctx *c, int slot, cudaStream_t st, double *acc);
+gvs_status prof_settle(Ctx *c);
 
 #define GVS_CUDA(c, expr)                                                  \
     do {                                                                   \

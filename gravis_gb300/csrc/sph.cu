@@ -1021,6 +1021,8 @@ void sph_free(Ctx *c) {
 }
 
 // SphSolver::compute (solver.rs:61-80) on the resident state: a and du/dt accumulate.
+__global__ void k_clear_flag(unsigned *err, unsigned bit) { atomicAnd(err, ~bit); }
+
 gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
     const size_t n = c->n;
     if (n == 0) return GVS_OK;
@@ -1104,10 +1106,10 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
         GVS_CUDA(c, cudaMemcpyAsync(&flags, c->err_word.ptr, 4, cudaMemcpyDeviceToHost, st));
         GVS_CUDA(c, cudaStreamSynchronize(st));
         if (!(flags & DERR_NEIGH_OVERFLOW)) break;
-        // rows too narrow: clear the flag and rerun with twice the width
-        unsigned rest = flags & ~(unsigned)DERR_NEIGH_OVERFLOW;
-        GVS_CUDA(c, cudaMemcpyAsync(c->err_word.ptr, &rest, 4, cudaMemcpyHostToDevice, st));
-        GVS_CUDA(c, cudaStreamSynchronize(st));
+        // rows too narrow: clear the flag (atomically: gravity may be setting others on
+        // the side stream) and rerun with twice the width
+        k_clear_flag<<<1, 1, 0, st>>>(err_ptr(c), (unsigned)DERR_NEIGH_OVERFLOW);
+        GVS_TRY(check_launch(c, "sph flag clear"));
         if (attempt == 3) return fail(c, GVS_ERR_DEVICE, "SPH neighbour rows overflow at kmax=%d", S->kmax);
         S->kmax *= 2;
     }
@@ -1134,6 +1136,8 @@ gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
                                          as<double>(S->say), as<double>(S->saz), as<double>(S->sdu),
                                          as<double>(S->sdivv), as<double>(S->smaxmu), as<double>(S->sdalpha));
     }
+    // the SPH accelerations add to gravity's, after them (as the reference's step does)
+    if (c->sph_join) GVS_CUDA(c, cudaStreamWaitEvent(st, c->sph_join, 0));
     k_scatter_sph<<<nb(n), 256, 0, st>>>(n, tv.perm, as<uint8_t>(S->gas), as<double>(S->srho), as<double>(S->sh),
                                          as<double>(S->spres), as<double>(S->scs), as<double>(S->somega),
                                          as<double>(S->sax), as<double>(S->say), as<double>(S->saz),
@@ -1184,8 +1188,33 @@ gvs_status sph_step(Ctx *c, const gvs_sph_params *prm, int algo, int precision, 
     c->prof.launches += 1;
     c->pos_version++;
     GVS_TRY(check_launch(c, "sph kick/drift"));
-    GVS_TRY(gravity(c, algo, precision, eps, theta, true));
-    GVS_TRY(sph_compute(c, prm));
+    if (c->has_gas && algo != GVS_ALGO_NONE) {
+        // Gravity and the SPH pass read the same new positions and tree and write
+        // disjoint buffers: gravity runs on the side stream while the neighbour search,
+        // density and forces run on the main one, and the SPH scatter waits for gravity
+        // before adding its accelerations to gravity's.
+        TreeView tv;
+        GVS_TRY(tree_view(c, &tv));  // the tree both passes read, built once, on the main stream
+        GVS_CUDA(c, cudaEventRecord(c->fork_ev, c->stream));
+        GVS_CUDA(c, cudaStreamWaitEvent(c->side, c->fork_ev, 0));
+        cudaStream_t main_stream = c->stream;
+        c->stream = c->side;
+        const gvs_status g = gravity(c, algo, precision, eps, theta, true);
+        c->stream = main_stream;
+        GVS_CUDA(c, cudaEventRecord(c->join_ev, c->side));
+        if (g != GVS_OK) {
+            GVS_CUDA(c, cudaStreamWaitEvent(c->stream, c->join_ev, 0));
+            return g;
+        }
+        c->sph_join = c->join_ev;
+        const gvs_status s = sph_compute(c, prm);
+        c->sph_join = nullptr;
+        GVS_CUDA(c, cudaStreamWaitEvent(c->stream, c->join_ev, 0));
+        GVS_TRY(s);
+    } else {
+        GVS_TRY(gravity(c, algo, precision, eps, theta, true));
+        GVS_TRY(sph_compute(c, prm));
+    }
     k_sph_kick2<<<nb(n), 256, 0, c->stream>>>(n, half, dt, as<uint8_t>(c->ptype), as<double>(c->vx),
                                               as<double>(c->vy), as<double>(c->vz), as<double>(c->ax),
                                               as<double>(c->ay), as<double>(c->az), as<double>(c->u),

@@ -325,3 +325,35 @@ def test_static_gas_ball_stable(ctx, prec):
         for _ in range(5):
             odt = s.step(q, og, odt)
         assert rel(p.x, q.x) <= 1e-9 and abs(dt - odt) <= 1e-9 * odt
+
+
+@pytest.mark.parametrize("algo,gprec", [(G.ALGO_BH, G.PREC_FP32), (G.ALGO_BH, G.PREC_MIXED),
+                                        (G.ALGO_DIRECT, G.PREC_FP64_EXACT)])
+def test_sph_step_with_gravity_beside_is_deterministic(ctx, algo, gprec):
+    """step_with_sph runs gravity on a second stream beside the SPH pass; the SPH
+    scatter waits for it.  Three steps in two contexts give the same state bit for
+    bit (the oracle comparisons of the step are test_sph_steps_match_oracle and the
+    static gas ball)."""
+    p0 = G.gas_sphere_1r(20000)
+    eps = 0.3 * (4.0 / 3.0 * np.pi / p0.count) ** (1.0 / 3.0)
+    fields = ("x", "vx", "internal_energy", "density", "alpha_visc", "ax", "du_dt")
+    runs = []
+    for _ in range(2):
+        c = G.Context(0)
+        try:
+            grav = G.BarnesHut(eps, 0.5, gprec, c) if algo == G.ALGO_BH else G.BruteForce(eps, gprec, c)
+            sph = G.SphSolver(c)
+            sph.params.precision = G.PREC_MIXED
+            p = p0.copy()
+            grav.compute_accelerations(p)
+            sph.compute(p)
+            dt = 1e-4
+            for _ in range(3):
+                dt = min(G.step_with_sph(p, grav, sph, dt), 1.5 * dt)
+            runs.append((p, dt))
+        finally:
+            c.close()
+    (a, dta), (b, dtb) = runs
+    assert dta == dtb
+    for f in fields:
+        assert np.array_equal(getattr(a, f), getattr(b, f)), f
