@@ -84,32 +84,50 @@ __global__ void __launch_bounds__(NT) k_os_pass(const K *__restrict__ keys, cons
                                                 uint32_t *__restrict__ status, uint32_t *__restrict__ counter,
                                                 unsigned *__restrict__ err) {
     __shared__ uint32_t tile_s;
-    __shared__ uint32_t hist[RADIX];
     __shared__ uint32_t base[RADIX];
-    __shared__ uint32_t wcnt[NWARP][RADIX];
+    __shared__ uint32_t wcnt[NWARP][RADIX];  // per warp: digit counts so far, then the warps' exclusive prefix
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) tile_s = atomicAdd(counter, 1u);
-    for (int i = tid; i < RADIX; i += NT) hist[i] = 0u;
+    for (int i = tid; i < NWARP * RADIX; i += NT) (&wcnt[0][0])[i] = 0u;
     __syncthreads();
     const uint32_t tile = tile_s;
-    const size_t tbase = (size_t)tile * TILE;
+    // warp w holds keys [w * 32 IPT, (w + 1) * 32 IPT) of the tile, slice k at lane offsets
+    // k * 32: index order is (warp, slice, lane) order, so ranking slice by slice within
+    // each warp and then warp by warp keeps the sort stable with no block barrier per slice
+    const size_t wbase = (size_t)tile * TILE + (size_t)warp * (32 * IPT);
     K key[IPT];
-    unsigned dig[IPT];
+    unsigned dig[IPT], rank[IPT];
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
-        const size_t idx = tbase + (size_t)k * NT + tid;
-        dig[k] = 256u;  // out-of-range slots form their own group
+        const size_t idx = wbase + (size_t)k * 32 + lane;
+        dig[k] = RADIX;  // out-of-range slots: no digit, never stored
         key[k] = 0;
         if (idx < n) {
             key[k] = keys[idx];
             dig[k] = (unsigned)(key[k] >> shift) & 0xFFu;
-            atomicAdd(&hist[dig[k]], 1u);
         }
     }
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const unsigned d = dig[k];
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+        const unsigned before = d < RADIX ? wcnt[warp][d] : 0u;
+        rank[k] = before + __popc(peers & ((1u << lane) - 1u));
+        __syncwarp();
+        if (d < RADIX && lane == __ffs(peers) - 1) wcnt[warp][d] = before + __popc(peers);
+        __syncwarp();
+    }
     __syncthreads();
-    // publish this tile's counts, then look back for the prefix of the tiles before it
+    // per digit: the tile's count, published, then the prefix of the tiles before it by
+    // decoupled look-back; and the warps' exclusive prefix within the tile
     for (int d = tid; d < RADIX; d += NT) {
-        const uint32_t own = hist[d];
+        uint32_t own = 0;
+#pragma unroll
+        for (int w = 0; w < NWARP; ++w) {
+            const uint32_t c = wcnt[w][d];
+            wcnt[w][d] = own;
+            own += c;
+        }
         uint32_t *mine = status + (size_t)tile * RADIX + d;
         if (tile == 0) {
             st_status(mine, ST_INCL | own);
@@ -136,36 +154,18 @@ __global__ void __launch_bounds__(NT) k_os_pass(const K *__restrict__ keys, cons
         base[d] = gbase[d] + sum;
     }
     __syncthreads();
-    // stable scatter: slices of NT keys in index order, warps in order, lanes in order
-    // (unrolled: the tile's keys stay in registers)
+    // stable scatter: tile base + earlier warps' count + rank within the warp
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
-        for (int i = tid; i < NWARP * RADIX; i += NT) (&wcnt[0][0])[i] = 0u;
-        __syncthreads();
-        const size_t idx = tbase + (size_t)k * NT + tid;
-        const bool valid = idx < n;
         const unsigned d = dig[k];
-        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
-        const unsigned rank = __popc(peers & ((1u << lane) - 1u));
-        if (valid && lane == __ffs(peers) - 1) wcnt[warp][d] = __popc(peers);
-        __syncthreads();
-        if (valid) {
-            uint32_t off = base[d];
-            for (int w = 0; w < warp; ++w) off += wcnt[w][d];
-            const size_t dst = (size_t)off + rank;
+        if (d < RADIX) {
+            const size_t idx = wbase + (size_t)k * 32 + lane;
+            const size_t dst = (size_t)base[d] + wcnt[warp][d] + rank[k];
             if (CHK_IDX(dst, n)) {
                 kout[dst] = key[k];
                 vout[dst] = vals[idx];
             }
         }
-        __syncthreads();
-        for (int dd = tid; dd < RADIX; dd += NT) {
-            uint32_t s = 0;
-#pragma unroll
-            for (int w = 0; w < NWARP; ++w) s += wcnt[w][dd];
-            base[dd] += s;
-        }
-        __syncthreads();
     }
 }
 
