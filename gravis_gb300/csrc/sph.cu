@@ -804,19 +804,21 @@ __global__ void __launch_bounds__(128) k_forces_mixed(
     float mmu = 0.f;
     const uint32_t *row = list + i * (size_t)kmax;
     const int count = CHK(cnt[i] <= (uint32_t)kmax, DERR_BOUNDS) ? (int)cnt[i] : 0;
+    uint32_t jn = count > 0 ? row[0] : 0u;  // the next row entry, read one neighbour ahead
     for (int k = 0; k < count; ++k) {
-        const uint32_t j = row[k];
+        const uint32_t j = jn;
+        if (k + 1 < count) jn = row[k + 1];
         if ((size_t)j == i || !CHK_IDX(j, n)) continue;
-        const float4 a = a4[j], b = b4[j];
+        // all six records at once: one memory round trip per neighbour (the quarter of
+        // the rows beyond both radii read theirs for nothing, from cache)
+        const float4 a = a4[j], b = b4[j], e = e4[j], c = c4[j], d = d4[j], f = f4[j];
         const float dx = __fadd_rn(__fsub_rn(pa.x, a.x), __fsub_rn(pb.x, b.x));
         const float dy = __fadd_rn(__fsub_rn(pa.y, a.y), __fsub_rn(pb.y, b.y));
         const float dz = __fadd_rn(__fsub_rn(pa.z, a.z), __fsub_rn(pb.z, b.z));
         const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
         const float r = __fsqrt_rn(d2);  // correctly rounded: the net SPH force is a small remainder of the pair terms
-        const float4 e = e4[j];
         const float hj = e.x;
         if (r >= 2.0f * hi_f && r >= 2.0f * hj) continue;
-        const float4 c = c4[j], d = d4[j], f = f4[j];
         const float mj = a.w;
         const float dvx = __fadd_rn(__fsub_rn(pc.x, c.x), __fsub_rn(pd.x, d.x));
         const float dvy = __fadd_rn(__fsub_rn(pc.y, c.y), __fsub_rn(pd.y, d.y));
