@@ -274,7 +274,7 @@ extern "C" gvs_status gvs_diagnostics_noalloc(int device, void *stream, size_t n
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
     double *part = g_diag_scratch_ptr[device].load(std::memory_order_acquire);
-    if (!part) {  // one-time set-up on this device (make this first call before any stream capture)
+    if (!part) {  // one-time set-up on this device
         std::lock_guard<std::mutex> lock(g_diag_setup_mu);
         part = g_diag_scratch_ptr[device].load(std::memory_order_relaxed);
         if (!part) {

@@ -263,7 +263,7 @@ gvs_status gvs_sph_neighbors(gvs_ctx *ctx, size_t cap, size_t *total, uint32_t *
  * Scratch is a fixed ~270 KB array inside the library image that every GPU loading the
  * library keeps until the process exits; n above 4,194,304 is rejected with
  * GVS_ERR_INVALID_ARG.  The first call on a device looks the array's address up
- * (cudaGetSymbolAddress), so make that first call before any stream capture.  All calls
+ * (cudaGetSymbolAddress) and keeps it for the later calls.  All calls
  * share the array and each overwrites what it reads: calls on one device that overlap on
  * the GPU (other streams or other host threads) race and must be serialised by the
  * caller. */
