@@ -1159,7 +1159,7 @@ gvs_status sph_timestep(Ctx *c, const gvs_sph_params *prm, double *dt_out) {
     const size_t n = c->n;
     SphState *S = sph_of(c);
     if (!S->have_intermediates) return fail(c, GVS_ERR_STATE, "compute_timestep needs a prior SPH compute");
-    const int nbk = std::max(1, std::min(c->num_sms * 2, nb(n)));
+    const int nbk = std::max(1, std::min(c->num_sms * 8, nb(n)));  // enough warps to cover the f64 and load latency
     GVS_CUDA(c, ensure(c, S->dtpart, (size_t)nbk * 8));
     k_dt_part<<<nbk, 256, 0, c->stream>>>(n, as<uint8_t>(c->ptype), as<double>(c->h), as<double>(c->ax),
                                           as<double>(c->ay), as<double>(c->az), as<double>(c->cs),

@@ -257,13 +257,7 @@ class Context:
             with open(path, "rb") as fh:
                 snaps.append(Snapshot.read_from(fh))
         snaps.sort(key=lambda s: s.step)
-        steps = [s.step for s in snaps]
-        if not snaps or steps[0] != 0 or len(steps) < 2:
-            raise ValueError("adjoint checkpoints: need step 0 and at least one later step")
-        nsteps, every = steps[-1], steps[1]
-        want = list(range(0, nsteps, every)) + [nsteps]
-        if steps != want:
-            raise ValueError(f"adjoint checkpoints: steps {steps} are not 0, {every}, ..., {nsteps}")
+        nsteps, every = checkpoint_plan([s.step for s in snaps])
         s0 = snaps[0]
         for s in snaps[1:]:
             if (s.softening, s.dt, s.particles.count) != (s0.softening, s0.dt, s0.particles.count) or \
@@ -579,6 +573,18 @@ def compute_diagnostics(p: Particles, softening: float, time: float = 0.0, step:
     d = c.diagnostics(softening, with_potential)
     d.time, d.step = time, step
     return d
+
+
+def checkpoint_plan(steps) -> tuple:
+    """(nsteps, every) of the forward run whose checkpoints sit at `steps` (sorted):
+    0, every, 2 every, ..., and nsteps, the last one.  Raises ValueError for any other set."""
+    steps = [int(s) for s in steps]
+    if len(steps) < 2 or steps[0] != 0:
+        raise ValueError("adjoint checkpoints: need step 0 and at least one later step")
+    nsteps, every = steps[-1], steps[1]
+    if every < 1 or steps != list(range(0, nsteps, every)) + [nsteps]:
+        raise ValueError(f"adjoint checkpoints: steps {steps} are not 0, {every}, ..., {nsteps}")
+    return nsteps, every
 
 
 # ---- snapshots ----------------------------------------------------------------------

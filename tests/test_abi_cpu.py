@@ -131,3 +131,15 @@ def test_no_device_reported(lib):
     assert lib.gvs_create(C.byref(h), 0) == L.ERR_NO_DEVICE
     with pytest.raises(G.GvsError):
         G.Context(0)
+
+
+def test_adjoint_checkpoint_plan():
+    """The checkpoint steps a forward run leaves (0, every, ..., nsteps) and the sets a
+    restart refuses."""
+    from gravis_gb300.engine import checkpoint_plan
+    assert checkpoint_plan([0, 100, 200, 250]) == (250, 100)
+    assert checkpoint_plan([0, 100, 200]) == (200, 100)
+    assert checkpoint_plan([0, 7]) == (7, 7)
+    for bad in ([0], [100, 200], [0, 100, 250], [0, 100, 200, 200], [0, 0, 100]):
+        with pytest.raises(ValueError):
+            checkpoint_plan(bad)
