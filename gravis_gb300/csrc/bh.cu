@@ -525,8 +525,9 @@ __global__ void k_pack_nodes(size_t nnodes, const uint8_t *__restrict__ level, c
         mrec[3 * k] = make_float4(__int_as_float(mt.x), __int_as_float(mt.y), __int_as_float(mt.z),
                                   __int_as_float(mt.w));
         mrec[3 * k + 1] = make_float4(hx, hy, hz, (float)mass[k]);
+        // .w: the largest |hi word| of the COM, for the walk's decision band
         mrec[3 * k + 2] = make_float4((float)(cx[k] - (double)hx), (float)(cy[k] - (double)hy),
-                                      (float)(cz[k] - (double)hz), 0.f);
+                                      (float)(cz[k] - (double)hz), fmaxf(fabsf(hx), fmaxf(fabsf(hy), fabsf(hz))));
     }
 }
 
@@ -537,18 +538,38 @@ __global__ void k_pack_particles(size_t n, const double *__restrict__ sx, const 
     if (i >= n) return;
     const float hx = (float)sx[i], hy = (float)sy[i], hz = (float)sz[i];
     p32[i] = make_float4(hx, hy, hz, (float)sm[i]);
-    if (p32lo)
-        p32lo[i] = make_float4((float)(sx[i] - (double)hx), (float)(sy[i] - (double)hy), (float)(sz[i] - (double)hz), 0.f);
+    if (p32lo)  // .w: the largest |hi word| of the position, for the mixed walk's decision band
+        p32lo[i] = make_float4((float)(sx[i] - (double)hx), (float)(sy[i] - (double)hy), (float)(sz[i] - (double)hz),
+                               fmaxf(fabsf(hx), fmaxf(fabsf(hy), fabsf(hz))));
 }
 
 // ---- walk -------------------------------------------------------------------
 struct S2Table {
     double s2[MAXL + 1];   // (2 * half_width_L)^2, half_width_L = hw0 * 2^-L
     float s2f[MAXL + 1];
-    // mixed walk: accept for sure if d^2 > hi2, open for sure if d^2 < lo2 (f32 d^2 of the
-    // hi words), else decide with the reference's f64 test (see bh_forces)
-    float lo2[MAXL + 1], hi2[MAXL + 1];
+    // mixed walk: the opening radius s / theta in f32 (clamped to 3e38); the walk decides
+    // with the f32 distance of the hi words outside a certified band around it and with the
+    // reference's f64 test inside (see mixed_band)
+    float rcf[MAXL + 1];
 };
+
+// The mixed walk's band around the opening radius rc = s / theta, in which the f32
+// distance of the hi words cannot decide.  Hi words round f64 coordinates to nearest,
+// so each component of the f32 difference of a node COM c and a particle p is within
+// 2^-24 (|c| + |p| + |c - p|) <= 2^-23 (Mc + Mp)(1 + 2^-25) of the true one (M: the
+// largest |coordinate| of the hi words), and the distance within sqrt(3) of that,
+// < 0.87 * 2^-22 (Mc + Mp).  The band half-width is three times that bound plus
+// 2^-20 rc, which covers the f32 rounding of rc and keeps the decision far (relative
+// 2^-20) from the rounding of the reference's f64 test.  The squared limits carry a
+// factor 1 +- 2^-19 for the f32 rounding of d^2 and of the limits themselves (at most
+// ~6 * 2^-24 relative).  Outside the band: d^2 > hi2 means d > rc for sure (accept),
+// d^2 < lo2 means d < rc for sure (open).
+__device__ __forceinline__ void mixed_band(float rc, float mc, float mp, float &lo2, float &hi2) {
+    const float dl = fmaf(0x1.8p-22f, mc + mp, 0x1p-20f * rc);
+    const float hi = rc + dl, lo = rc - dl;
+    hi2 = hi * hi * (1.0f + 0x1p-19f);
+    lo2 = lo > 0.f ? lo * lo * (1.0f - 0x1p-19f) : -1.0f;
+}
 
 // Where a walk leaves its sums: caller-order acceleration arrays, written (or
 // added to) at perm[i] for sorted particle i.
@@ -733,11 +754,13 @@ __global__ void __launch_bounds__(128) k_walk(size_t n, size_t nnodes, const int
                 const float dx = c.x - qx, dy = c.y - qy, dz = c.z - qz;
                 const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
                 bool accept;
+                float lo2 = 0.f, hi2 = 0.f;
+                if (MODE == 2) mixed_band(tab.rcf[mt.w], c32l.w, ql.w, lo2, hi2);
                 if (MODE == 1) {
                     accept = tab.s2f[mt.w] < theta2f * d2;
-                } else if (d2 > tab.hi2[mt.w]) {
+                } else if (d2 > hi2) {
                     accept = true;
-                } else if (d2 < tab.lo2[mt.w]) {
+                } else if (d2 < lo2) {
                     accept = false;
                 } else {  // near the boundary: the reference's f64 test
                     const double4 c64 = cm64[m];
@@ -1495,11 +1518,6 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
         GVS_TRY(check_launch(c, "walk packing"));
         t->precision = mode + 1;
     }
-    // the mixed walk's certified margin: X bounds every coordinate (the root cell);
-    // f32 rounding moves the hi-word distance by at most ~1.3 E, E = 2^-21 X
-    const double X = std::max(std::fabs(t->root[0]), std::max(std::fabs(t->root[1]), std::fabs(t->root[2]))) +
-                     t->root[3];
-    const double E = std::ldexp(X, -21);
     S2Table tab;
     for (int L = 0; L <= MAXL; ++L) {
         const double hw = ldexp(t->root[3], -L);  // exact: child half width = parent * 0.5
@@ -1507,9 +1525,7 @@ gvs_status bh_forces(Ctx *c, double eps, double theta, int precision, bool accum
         tab.s2[L] = s * s;
         tab.s2f[L] = (float)(s * s);
         const double rc = theta > 0.0 ? s / theta : INFINITY;  // accept iff d > s / theta
-        const double lo = rc - 3.0 * E, hi = rc + 3.0 * E;
-        tab.lo2[L] = lo > 0.0 ? (float)(lo * lo * (1.0 - 0x1p-19)) : -1.0f;
-        tab.hi2[L] = (float)(hi * hi * (1.0 + 0x1p-19));
+        tab.rcf[L] = (float)std::min(rc, 3.0e38);  // finite: the band's limits stay ordered (no inf - inf)
     }
     const AccOut out{as<uint32_t>(t->perm), as<double>(c->ax), as<double>(c->ay), as<double>(c->az),
                      accumulate ? 1 : 0, n};

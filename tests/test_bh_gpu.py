@@ -198,6 +198,46 @@ def test_bh_mixed_walk_large(ctx, theta):
     assert err <= 1e-6
 
 
+def walk_terms(ctx, p, eps, theta, prec):
+    """Accelerations and the terms summed by a per-particle walk."""
+    q = p.copy()
+    q.clear_accelerations()
+    try:
+        ctx.profile(True)
+        G.BarnesHut(eps, theta, prec, ctx).compute_accelerations(q)
+        terms = ctx.profile_read()["bh_walk_terms"]
+    finally:
+        ctx.profile(False)
+    return q.acc(), terms
+
+
+def massless(n=5000):
+    p = G.PlummerSphere(n, seed=8).generate()
+    p.mass[::7] = 0.0  # one particle in seven: leaves and buckets of zero mass
+    return with_duplicates(p, 12, at=7)  # a bucket of massless particles
+
+
+@pytest.mark.parametrize("theta", [0.3, 0.5, 0.7])
+@pytest.mark.parametrize("case", ["collision", "buckets", "close_pairs", "massless", "lattice"])
+def test_bh_mixed_walk_makes_the_f64_walks_decisions(ctx, case, theta):
+    """The mixed walk decides with the f32 distance of the hi words outside a certified
+    band around s/theta (from the pair's own coordinate magnitudes) and with the
+    reference's f64 test inside it, so it sums exactly the terms of the f64 walk (the
+    reference's decisions): the two walks' term counts agree, and the forces within 1e-6."""
+    p = {"collision": lambda: G.collision(1 << 17, seed=7),
+         "buckets": lambda: with_duplicates(G.PlummerSphere(3000, seed=5).generate(), 99, at=17),
+         "close_pairs": lambda: close_pairs(3000, 40),
+         "massless": massless,
+         "lattice": lambda: lattice(16, 0.25)}[case]()
+    eps = 1e-3 if case == "collision" else 0.01
+    a64, n64 = walk_terms(ctx, p, eps, theta, G.PREC_FP64)
+    am, nm = walk_terms(ctx, p, eps, theta, G.PREC_MIXED)
+    err = rel_rms(am, a64)
+    print(f"{case} theta={theta}: {nm} terms (f64 walk {n64}), mixed vs f64 rel RMS {err:.1e}")
+    assert nm == n64 > 0
+    assert err <= 1e-6, err
+
+
 def test_bh_vs_direct_subset(ctx):
     """Accuracy of the walk against the exact f64 direct sum on a random subset."""
     n = 1 << 17
