@@ -21,7 +21,7 @@ const NVCC_FLAGS: &[&str] = &[
     "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills", "-diag-suppress", "1444,177",
 ];
 /// Per-file flags, as in gravis_gb300/build.py's FILE_FLAGS.
-const FILE_FLAGS: &[(&str, &[&str])] = &[("sph.cu", &["--fmad=false"])];
+const FILE_FLAGS: &[(&str, &[&str])] = &[("sph.cu", &["--fmad=false"]), ("ics_dev.cu", &["--fmad=false"])];
 
 fn nvcc(cuda_home: &Path) -> PathBuf {
     if let Ok(p) = env::var("NVCC") {

@@ -48,7 +48,7 @@ def _stale(obj: str, src: str) -> bool:
 
 # Per-file flags: the SPH kernels restate the reference's f64 arithmetic
 # statement by statement, so a*b+c must round twice there.
-FILE_FLAGS = {"sph.cu": ["--fmad=false"]}
+FILE_FLAGS = {"sph.cu": ["--fmad=false"], "ics_dev.cu": ["--fmad=false"]}
 
 
 def _compile(nvcc: str, src: str, extra: list[str], build_dir: str) -> str:

@@ -412,6 +412,27 @@ gvs_status gvs_set_state(gvs_ctx *c, size_t n, const double *x, const double *y,
     return GVS_OK;
 }
 
+gvs_status gvs_ic_plummer_device(gvs_ctx *c, size_t n, uint64_t seed, double scale_radius, double total_mass) {
+    GVS_TRY(check_ctx(c));
+    if (n == 0 || !(scale_radius > 0.0) || !(total_mass > 0.0))
+        return fail(c, GVS_ERR_INVALID_ARG, "need n >= 1, scale_radius > 0, total_mass > 0");
+    if (n > (size_t(1) << 27)) return fail(c, GVS_ERR_INVALID_ARG, "device Plummer ICs: n = %zu above 2^27", n);
+    if (c->fault_kind == 1) return fail(c, GVS_ERR_INJECTED, "injected allocation fault");
+    cudaSetDevice(c->device);
+    GVS_TRY(alloc_state(c, n));
+    const size_t b = n * sizeof(double);
+    c->pos_version++;
+    GVS_TRY(clear_acc(c));
+    c->has_gas = false;
+    GVS_CUDA(c, cudaMemsetAsync(c->ptype.ptr, 0, n, c->stream));
+    DevBuf *zero[] = {&c->rho, &c->pres, &c->cs, &c->du_dt, &c->div_v, &c->max_mu, &c->dalpha_dt, &c->u, &c->h,
+                      &c->alpha};
+    for (DevBuf *d : zero) GVS_CUDA(c, cudaMemsetAsync(d->ptr, 0, b, c->stream));
+    c->step_counter = 0;
+    GVS_TRY(ic_plummer_device(c, n, seed, scale_radius, total_mass));
+    return read_device_errors(c);
+}
+
 gvs_status gvs_get_state(gvs_ctx *c, double *x, double *y, double *z, double *vx, double *vy, double *vz, double *ax,
                          double *ay, double *az) {
     GVS_TRY(check_ctx(c));

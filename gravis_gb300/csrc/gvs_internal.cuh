@@ -418,6 +418,8 @@ gvs_status sph_step(Ctx *c, const gvs_sph_params *prm, int algo, int precision, 
 gvs_status sph_neighbors_export(Ctx *c, size_t cap, uint32_t *start, uint32_t *count, uint32_t *idx, size_t *total);
 void sph_free(Ctx *c);
 
+// ics_dev.cu: PlummerSphere::generate on the device into the resident x..m (n allocated)
+gvs_status ic_plummer_device(Ctx *c, size_t n, uint64_t seed, double a, double total_mass);
 // adjoint.cu
 void adj_free(Ctx *c);
 // ensemble.cu

@@ -29,16 +29,27 @@
 
 #include "../../include/gvs.h"
 
+namespace gvs {
+// The ChaCha20 key of ChaCha20Rng::seed_from_u64(seed): eight PCG32 (XSH-RR) outputs of
+// the seed (used by the host generators below and by the device Plummer generator).
+void chacha_key_from_seed(uint64_t seed, uint32_t key[8]) {
+    uint64_t st = seed;
+    for (int i = 0; i < 8; ++i) {
+        st = st * 6364136223846793005ull + 11634580027462260723ull;
+        const uint32_t xs = (uint32_t)(((st >> 18) ^ st) >> 27);
+        const unsigned rot = (unsigned)(st >> 59) & 31u;
+        key[i] = rot ? (xs >> rot) | (xs << (32 - rot)) : xs;
+    }
+}
+}  // namespace gvs
+
 namespace {
 
 const double PI = 3.14159265358979323846;
 
 class ChaCha20Rng {
   public:
-    explicit ChaCha20Rng(uint64_t seed) {
-        uint64_t st = seed;
-        for (int i = 0; i < 8; ++i) key_[i] = pcg32(st);
-    }
+    explicit ChaCha20Rng(uint64_t seed) { gvs::chacha_key_from_seed(seed, key_); }
     uint32_t next_u32() {
         if (idx_ >= 16) {
             block(ctr_++, buf_);
@@ -60,12 +71,6 @@ class ChaCha20Rng {
     }
 
   private:
-    static uint32_t pcg32(uint64_t &s) {
-        s = s * 6364136223846793005ull + 11634580027462260723ull;
-        uint32_t xs = (uint32_t)(((s >> 18) ^ s) >> 27);
-        unsigned rot = (unsigned)(s >> 59) & 31u;
-        return rot ? (xs >> rot) | (xs << (32 - rot)) : xs;
-    }
     static uint32_t rl(uint32_t v, int c) { return (v << c) | (v >> (32 - c)); }
     void block(uint64_t counter, uint32_t out[16]) const {
         uint32_t s[16] = {0x61707865u, 0x3320646eu, 0x79622d32u, 0x6b206574u};

@@ -207,6 +207,11 @@ class Context:
     def ensemble_kdk_steps(self, dt: float, nsteps: int, use_graph: bool = True):
         self._ck(self._lib.gvs_ensemble_kdk_steps(self.h, dt, nsteps, 1 if use_graph else 0))
 
+    def ic_plummer_device(self, n: int, seed: int = 42, scale_radius: float = 1.0, total_mass: float = 1.0):
+        """PlummerSphere(n, scale_radius, total_mass, seed).generate() on the GPU, into the
+        resident state: the host generator's stream and draws, values within a few ulps."""
+        self._ck(self._lib.gvs_ic_plummer_device(self.h, n, seed, scale_radius, total_mass))
+
     def adjoint_forward(self, precision: int, softening: float, dt: float, nsteps: int, checkpoint_every: int = 100):
         self._ck(self._lib.gvs_adjoint_forward(self.h, precision, softening, dt, nsteps, checkpoint_every))
         self._adj_run = (softening, dt)

@@ -316,6 +316,15 @@ gvs_status gvs_autotune_report(gvs_ctx *ctx, int cap, int *count, int *nthreads,
 gvs_status gvs_ic_plummer(size_t n, uint64_t seed, double scale_radius, double total_mass, double *x, double *y,
                           double *z, double *vx, double *vy, double *vz, double *mass);
 
+/* PlummerSphere::generate on the GPU, straight into ctx's resident state (n particles,
+ * masses total_mass / n, gas-free, accelerations zero): the same ChaCha20 stream and draw
+ * sequence as gvs_ic_plummer (every particle starts at the same stream word), values
+ * within a few ulps of it (CUDA's pow/sin/cos against the C library's, parallel COM
+ * sums).  n <= 2^27; scratch ~(4 log2 n + 5) * 24 n bytes during the call.
+ * GVS_ERR_STATE if a rejection decision lies within 2^-40 of its threshold, where the
+ * two libraries could decide differently (use gvs_ic_plummer then). */
+gvs_status gvs_ic_plummer_device(gvs_ctx *ctx, size_t n, uint64_t seed, double scale_radius, double total_mass);
+
 /* TwoBody::generate (scenarios/two_body.rs:49-94): 2 particles at periapsis, COM frame. */
 gvs_status gvs_ic_two_body(double mass_ratio, double e, double a, double *x, double *y, double *z, double *vx,
                            double *vy, double *vz, double *mass);

@@ -44,6 +44,7 @@ def test_null_context_is_invalid_arg(lib):
     assert lib.gvs_adjoint_prepare(None, 3, 0.01, 1e-3, 10, 5) == L.ERR_INVALID_ARG
     assert lib.gvs_adjoint_checkpoint_read(None, 0, *([None] * 6)) == L.ERR_INVALID_ARG
     assert lib.gvs_adjoint_checkpoint_write(None, 0, *([None] * 6)) == L.ERR_INVALID_ARG
+    assert lib.gvs_ic_plummer_device(None, 10, 1, 1.0, 1.0) == L.ERR_INVALID_ARG
 
 
 def test_ic_args_validated(lib):
