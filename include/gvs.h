@@ -320,7 +320,8 @@ gvs_status gvs_ic_plummer(size_t n, uint64_t seed, double scale_radius, double t
  * masses total_mass / n, gas-free, accelerations zero): the same ChaCha20 stream and draw
  * sequence as gvs_ic_plummer (every particle starts at the same stream word), values
  * within a few ulps of it (CUDA's pow/sin/cos against the C library's, parallel COM
- * sums).  n <= 2^27; scratch ~(4 log2 n + 5) * 24 n bytes during the call.
+ * sums).  n <= 2^27; scratch of about 48 n log2(n) + 100 n bytes during the call
+ * (19 GB at n = 2^24).
  * GVS_ERR_STATE if a rejection decision lies within 2^-40 of its threshold, where the
  * two libraries could decide differently (use gvs_ic_plummer then). */
 gvs_status gvs_ic_plummer_device(gvs_ctx *ctx, size_t n, uint64_t seed, double scale_radius, double total_mass);
