@@ -174,6 +174,7 @@ unsafe extern "C" {
         z: *mut f64, vx: *mut f64, vy: *mut f64, vz: *mut f64, mass: *mut f64) -> gvs_status;
     pub fn gvs_ic_plummer_device(ctx: *mut gvs_ctx, n: usize, seed: u64, scale_radius: f64,
         total_mass: f64) -> gvs_status;
+    pub fn gvs_ic_collision_device(ctx: *mut gvs_ctx, n: usize, seed: u64, separation: f64) -> gvs_status;
     pub fn gvs_ic_two_body(mass_ratio: f64, e: f64, a: f64, x: *mut f64, y: *mut f64, z: *mut f64,
         vx: *mut f64, vy: *mut f64, vz: *mut f64, mass: *mut f64) -> gvs_status;
     pub fn gvs_ic_evrard(n: usize, seed: u64, total_mass: f64, radius: f64, u0: f64, x: *mut f64, y: *mut f64,

@@ -81,6 +81,7 @@ SIGNATURES = {
     "gvs_adjoint_backward": (_ST, [_P] + [_P] * 13),
     "gvs_adjoint_checkpoints": (_ST, [_P, _ll, _P, _P]),
     "gvs_ic_plummer_device": (_ST, [_P, _sz, _u64, _d, _d]),
+    "gvs_ic_collision_device": (_ST, [_P, _sz, _u64, _d]),
     "gvs_adjoint_checkpoint_read": (_ST, [_P, _ll] + [_P] * 6),
     "gvs_adjoint_prepare": (_ST, [_P, _i, _d, _d, _ll, _ll]),
     "gvs_adjoint_checkpoint_write": (_ST, [_P, _ll] + [_P] * 6),

@@ -412,11 +412,9 @@ gvs_status gvs_set_state(gvs_ctx *c, size_t n, const double *x, const double *y,
     return GVS_OK;
 }
 
-gvs_status gvs_ic_plummer_device(gvs_ctx *c, size_t n, uint64_t seed, double scale_radius, double total_mass) {
-    GVS_TRY(check_ctx(c));
-    if (n == 0 || !(scale_radius > 0.0) || !(total_mass > 0.0))
-        return fail(c, GVS_ERR_INVALID_ARG, "need n >= 1, scale_radius > 0, total_mass > 0");
-    if (n > (size_t(1) << 27)) return fail(c, GVS_ERR_INVALID_ARG, "device Plummer ICs: n = %zu above 2^27", n);
+// The resident state of an n-particle gas-free system with zero accelerations, whose
+// x..m a device generator then fills.
+static gvs_status device_ics_prepare(gvs_ctx *c, size_t n) {
     if (c->fault_kind == 1) return fail(c, GVS_ERR_INJECTED, "injected allocation fault");
     cudaSetDevice(c->device);
     GVS_TRY(alloc_state(c, n));
@@ -429,7 +427,25 @@ gvs_status gvs_ic_plummer_device(gvs_ctx *c, size_t n, uint64_t seed, double sca
                       &c->alpha};
     for (DevBuf *d : zero) GVS_CUDA(c, cudaMemsetAsync(d->ptr, 0, b, c->stream));
     c->step_counter = 0;
+    return GVS_OK;
+}
+
+gvs_status gvs_ic_plummer_device(gvs_ctx *c, size_t n, uint64_t seed, double scale_radius, double total_mass) {
+    GVS_TRY(check_ctx(c));
+    if (n == 0 || !(scale_radius > 0.0) || !(total_mass > 0.0))
+        return fail(c, GVS_ERR_INVALID_ARG, "need n >= 1, scale_radius > 0, total_mass > 0");
+    if (n > (size_t(1) << 27)) return fail(c, GVS_ERR_INVALID_ARG, "device Plummer ICs: n = %zu above 2^27", n);
+    GVS_TRY(device_ics_prepare(c, n));
     GVS_TRY(ic_plummer_device(c, n, seed, scale_radius, total_mass));
+    return read_device_errors(c);
+}
+
+gvs_status gvs_ic_collision_device(gvs_ctx *c, size_t n, uint64_t seed, double separation) {
+    GVS_TRY(check_ctx(c));
+    if (n < 2 || !(separation > 0.0)) return fail(c, GVS_ERR_INVALID_ARG, "need n >= 2, separation > 0");
+    if (n > (size_t(1) << 27)) return fail(c, GVS_ERR_INVALID_ARG, "device collision ICs: n = %zu above 2^27", n);
+    GVS_TRY(device_ics_prepare(c, n));
+    GVS_TRY(ic_collision_device(c, n, seed, separation));
     return read_device_errors(c);
 }
 

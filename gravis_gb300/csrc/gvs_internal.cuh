@@ -420,6 +420,7 @@ void sph_free(Ctx *c);
 
 // ics_dev.cu: PlummerSphere::generate on the device into the resident x..m (n allocated)
 gvs_status ic_plummer_device(Ctx *c, size_t n, uint64_t seed, double a, double total_mass);
+gvs_status ic_collision_device(Ctx *c, size_t n, uint64_t seed, double separation);
 // adjoint.cu
 void adj_free(Ctx *c);
 // ensemble.cu

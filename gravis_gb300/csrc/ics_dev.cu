@@ -143,14 +143,28 @@ __global__ void k_starts(const uint32_t *__restrict__ J, int levels, uint32_t H,
     start[i] = 2u * h;
 }
 
+// What is drawn: one Plummer sphere (PlummerSphere::generate), or two spheres of n/2 and
+// n - n/2 particles from one stream, offset by -+separation/2 on x and approaching at
+// +-vrel/2 (ics.cpp's gvs_ic_collision).
+struct Spheres {
+    double a;               // scale radius
+    double mass_a, mass_b;  // sampler's total mass for particles i < na and i >= na
+    double particle_mass;
+    size_t na;              // n for one sphere
+    double separation, vrel;
+    int two;
+};
+
 // sample_plummer_particle (plummer_sphere.rs:13-58) from word start[i], as ics.cpp's
-// plummer_particle; mass total_mass / n.
+// plummer_particle, then the sphere's offset.
 __global__ void k_plummer(const uint32_t *__restrict__ w, const uint32_t *__restrict__ start, size_t n, uint32_t W,
-                          double a, double total_mass, double *__restrict__ x, double *__restrict__ y,
+                          const Spheres sp, double *__restrict__ x, double *__restrict__ y,
                           double *__restrict__ z, double *__restrict__ vx, double *__restrict__ vy,
                           double *__restrict__ vz, double *__restrict__ m, unsigned *__restrict__ flags) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const bool first = i < sp.na;
+    const double a = sp.a, total_mass = first ? sp.mass_a : sp.mass_b;
     uint32_t p = start[i];
     if ((size_t)p + 14 > W) {  // not even the shortest particle fits: the budget ran out
         atomicOr(flags, F_BUDGET);
@@ -161,7 +175,7 @@ __global__ void k_plummer(const uint32_t *__restrict__ w, const uint32_t *__rest
     const double ct = draw_range(w, p + 2, -1.0, 1.0);
     const double st = sqrt(1.0 - ct * ct);
     const double phi = draw_range(w, p + 4, 0.0, 2.0 * PI_D);
-    x[i] = r * st * cos(phi);
+    double px = r * st * cos(phi);
     y[i] = r * st * sin(phi);
     z[i] = r * ct;
     const double v_esc = sqrt(2.0 * 1.0 * total_mass / sqrt(r * r + a * a));
@@ -187,10 +201,16 @@ __global__ void k_plummer(const uint32_t *__restrict__ w, const uint32_t *__rest
     const double cv = draw_range(w, p, -1.0, 1.0);
     const double sv = sqrt(1.0 - cv * cv);
     const double pv = draw_range(w, p + 2, 0.0, 2.0 * PI_D);
-    vx[i] = v * sv * cos(pv);
+    double pvx = v * sv * cos(pv);
     vy[i] = v * sv * sin(pv);
     vz[i] = v * cv;
-    m[i] = total_mass / (double)n;
+    if (sp.two) {
+        px = px + (first ? -0.5 : 0.5) * sp.separation;
+        pvx = pvx + (first ? 0.5 : -0.5) * sp.vrel;
+    }
+    x[i] = px;
+    vx[i] = pvx;
+    m[i] = sp.particle_mass;
 }
 
 // Sums of m, m x, m y, m z, m vx, m vy, m vz: per block in a fixed tree, then the blocks
@@ -251,8 +271,8 @@ struct Scratch {
 
 }  // namespace
 
-// PlummerSphere::generate into the resident state arrays x..m (length n).
-gvs_status ic_plummer_device(Ctx *c, size_t n, uint64_t seed, double a, double total_mass) {
+// The spheres into the resident state arrays x..m (length n).
+static gvs_status ic_spheres_device(Ctx *c, size_t n, uint64_t seed, const Spheres &sph) {
     cudaStream_t st = c->stream;
     Key key;
     chacha_key_from_seed(seed, key.k);
@@ -281,7 +301,7 @@ gvs_status ic_plummer_device(Ctx *c, size_t n, uint64_t seed, double a, double t
     k_starts<<<grid_of(n), 256, 0, st>>>(J, levels, H, n, start, flags);
     double *x = as<double>(c->x), *y = as<double>(c->y), *z = as<double>(c->z);
     double *vx = as<double>(c->vx), *vy = as<double>(c->vy), *vz = as<double>(c->vz), *m = as<double>(c->m);
-    k_plummer<<<grid_of(n, 128), 128, 0, st>>>(w, start, n, W, a, total_mass, x, y, z, vx, vy, vz, m, flags);
+    k_plummer<<<grid_of(n, 128), 128, 0, st>>>(w, start, n, W, sph, x, y, z, vx, vy, vz, m, flags);
     double *part = static_cast<double *>(sp.p);
     k_com_part<<<nparts, COM_NT, 0, st>>>(n, x, y, z, vx, vy, vz, m, part);
     k_com_shift<<<(unsigned)std::min<size_t>(grid_of(n), (size_t)c->num_sms * 8), 256, 0, st>>>(n, nparts, part, x, y,
@@ -295,8 +315,33 @@ gvs_status ic_plummer_device(Ctx *c, size_t n, uint64_t seed, double a, double t
     if (hf & F_TIE)
         return fail(c, GVS_ERR_STATE,
                     "device Plummer ICs: a rejection decision lies within 2^-40 of its threshold; "
-                    "generate these ICs on the host (gvs_ic_plummer)");
+                    "generate these ICs on the host (gvs_ic_plummer / gvs_ic_collision)");
     return GVS_OK;
+}
+
+gvs_status ic_plummer_device(Ctx *c, size_t n, uint64_t seed, double a, double total_mass) {
+    Spheres sp{};
+    sp.a = a;
+    sp.mass_a = sp.mass_b = total_mass;
+    sp.particle_mass = total_mass / (double)n;
+    sp.na = n;
+    return ic_spheres_device(c, n, seed, sp);
+}
+
+// gvs_ic_collision (ics.cpp): the host's constants, computed here the same way.
+gvs_status ic_collision_device(Ctx *c, size_t n, uint64_t seed, double separation) {
+    Spheres sp{};
+    const size_t na = n / 2;
+    const double m = 1.0 / (double)n;
+    sp.a = 1.0;
+    sp.mass_a = (double)na * m;
+    sp.mass_b = (double)(n - na) * m;
+    sp.particle_mass = m;
+    sp.na = na;
+    sp.separation = separation;
+    sp.vrel = sqrt(2.0 * 1.0 * 1.0 / separation);
+    sp.two = 1;
+    return ic_spheres_device(c, n, seed, sp);
 }
 
 }  // namespace gvs

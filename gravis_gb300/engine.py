@@ -212,6 +212,10 @@ class Context:
         resident state: the host generator's stream and draws, values within a few ulps."""
         self._ck(self._lib.gvs_ic_plummer_device(self.h, n, seed, scale_radius, total_mass))
 
+    def ic_collision_device(self, n: int, seed: int = 7, separation: float = 20.0):
+        """collision(n, seed, separation) on the GPU, into the resident state."""
+        self._ck(self._lib.gvs_ic_collision_device(self.h, n, seed, separation))
+
     def adjoint_forward(self, precision: int, softening: float, dt: float, nsteps: int, checkpoint_every: int = 100):
         self._ck(self._lib.gvs_adjoint_forward(self.h, precision, softening, dt, nsteps, checkpoint_every))
         self._adj_run = (softening, dt)

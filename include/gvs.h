@@ -325,6 +325,9 @@ gvs_status gvs_ic_plummer(size_t n, uint64_t seed, double scale_radius, double t
  * GVS_ERR_STATE if a rejection decision lies within 2^-40 of its threshold, where the
  * two libraries could decide differently (use gvs_ic_plummer then). */
 gvs_status gvs_ic_plummer_device(gvs_ctx *ctx, size_t n, uint64_t seed, double scale_radius, double total_mass);
+/* gvs_ic_collision (two Plummer spheres from one stream, the Barnes-Hut workload's ICs) on
+ * the GPU into ctx's resident state, on the same terms as gvs_ic_plummer_device. */
+gvs_status gvs_ic_collision_device(gvs_ctx *ctx, size_t n, uint64_t seed, double separation);
 
 /* TwoBody::generate (scenarios/two_body.rs:49-94): 2 particles at periapsis, COM frame. */
 gvs_status gvs_ic_two_body(double mass_ratio, double e, double a, double *x, double *y, double *z, double *vx,

@@ -46,6 +46,19 @@ def test_device_plummer_matches_host(ctx, n, seed, a, mass):
           f"host {1e3 * (t1 - t0):.1f} ms, device {1e3 * (t2 - t1):.1f} ms")
 
 
+@pytest.mark.parametrize("n,seed", [(2, 7), (1001, 7), (1 << 20, 7)])
+def test_device_collision_matches_host(ctx, n, seed):
+    """The Barnes-Hut workload's ICs (two Plummer spheres from one stream, gvs_ic_collision)."""
+    host = G.collision(n, seed=seed)
+    ctx.ic_collision_device(n, seed)
+    q = G.Particles(n)
+    ctx.get_state(q)
+    for f in FIELDS:
+        h, d = getattr(host, f), getattr(q, f)
+        err = float(np.abs(d - h).max()) / max(np.abs(h).max(), 1e-300)
+        assert err <= 1e-13, (f, err)
+
+
 def test_device_plummer_resident_state_steps(ctx):
     """The generated state (masses total_mass / n included) is a normal resident state:
     the direct-sum KDK runs on it and gives the trajectory of the host ICs uploaded."""
@@ -74,3 +87,5 @@ def test_device_plummer_rejects_bad_arguments(ctx):
         ctx.ic_plummer_device(0, 1)
     with pytest.raises(G.GvsError):
         ctx.ic_plummer_device(10, 1, scale_radius=-1.0)
+    with pytest.raises(G.GvsError):
+        ctx.ic_collision_device(1, 7)
