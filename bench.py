@@ -461,7 +461,7 @@ def headline_extras(ctx, G, L, a, p, eps, peaks) -> dict:
                                   forms["fp64"]["interactions_per_s"])
     extras["headline_extras_s"] = time.perf_counter() - t0
     for name, fn in (("plummer1k", wl_plummer1k), ("bh", wl_bh), ("sph", wl_sph), ("ensemble", wl_ensemble),
-                     ("adjoint", wl_adjoint)):
+                     ("adjoint", wl_adjoint), ("device_ics", wl_device_ics)):
         t0 = time.perf_counter()
         try:
             extras[name] = fn(ctx, G, L, a, peaks, extra=True)
@@ -472,6 +472,28 @@ def headline_extras(ctx, G, L, a, p, eps, peaks) -> dict:
 
 
 # ---- workloads ---------------------------------------------------------------------------
+def wl_device_ics(ctx, G, L, a, peaks, extra=False) -> dict:
+    """PlummerSphere::generate on the GPU (gvs_ic_plummer_device) against the host generator
+    (gvs_ic_plummer, one core) at the headline's N and seed: wall time of each call, and the
+    largest difference relative to the largest coordinate."""
+    n, seed = a.n, a.seed
+    ctx.ic_plummer_device(min(n, 4096), seed)  # warm: module load, first allocations
+    t0 = time.perf_counter()
+    ctx.ic_plummer_device(n, seed)
+    t1 = time.perf_counter()
+    q = G.Particles(n)
+    ctx.get_state(q)
+    t2 = time.perf_counter()
+    host = G.PlummerSphere(n, seed=seed).generate()
+    t3 = time.perf_counter()
+    worst = max(float(np.abs(getattr(q, f) - getattr(host, f)).max()) / float(np.abs(getattr(host, f)).max())
+                for f in ("x", "y", "z", "vx", "vy", "vz"))
+    return {"n": n, "seed": seed, "device_ms": 1e3 * (t1 - t0), "host_ms": 1e3 * (t3 - t2),
+            "speedup": (t3 - t2) / max(t1 - t0, 1e-9), "max_rel_diff_vs_host": worst,
+            "how": "wall clock around each call; the device call ends with the state resident (no copy)"}
+
+
+
 def wl_plummer1k(ctx, G, L, a, peaks, extra=False) -> dict:
     """The headless plummer run: N=1000, seed 42, eps=0.01, dt=1e-3, 10^4 KDK steps."""
     n, eps, dt = 1000, 0.01, 1e-3
