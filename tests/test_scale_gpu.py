@@ -9,7 +9,8 @@ restatement of sim-core on the workloads' own initial conditions.
   the particles skip the f64 replay).
 - Mixed BH walk (barnes_hut.rs:44-135) at N = 2^22, theta 0.5 and 0.7,
   eps 1e-3: 4096 random targets against the oracle's BarnesHut on the same
-  tree, within 1e-6 relative RMS.
+  tree, within 1e-6 relative RMS; and exactly as many terms as the f64 walk
+  (the same opening decisions for all 2^22 particles).
 - SPH (neighbors.rs:56-119, density.rs:42-157, forces.rs:80-225) on the
   rho ~ 1/r gas sphere at N = 2^18 and 2^20: neighbour lists identical in set
   and order; f64 density, h, Omega, P, c within 1e-12 and a, du/dt, div v,
@@ -88,6 +89,27 @@ def test_bh_parity_walk_at_benchmark_size(ctx, theta):
     per = np.sqrt(((got - ref) ** 2).sum(1) / (ref ** 2).sum(1))
     print(f"theta={theta}: mixed walk vs oracle BarnesHut rel RMS {rel:.2e}, per-particle max {per.max():.2e}")
     assert rel <= 1e-6, rel
+
+
+@pytest.mark.parametrize("theta", [0.5, 0.7])
+def test_bh_mixed_walk_terms_equal_f64_walk_at_benchmark_size(ctx, theta):
+    """At N = 2^22 the mixed walk sums exactly the f64 walk's terms (the reference's
+    decisions, barnes_hut.rs:85-91): the f32 test with its certified band never decides
+    a node the other way."""
+    n, eps = 1 << 22, 1e-3
+    p = G.collision(n, seed=7)
+    terms = {}
+    for prec in (G.PREC_FP64, G.PREC_MIXED):
+        q = p.copy()
+        q.clear_accelerations()
+        try:
+            ctx.profile(True)
+            G.BarnesHut(eps, theta, prec, ctx).compute_accelerations(q)
+            terms[prec] = ctx.profile_read()["bh_walk_terms"]
+        finally:
+            ctx.profile(False)
+    print(f"theta={theta}: {terms[G.PREC_MIXED]} terms (f64 walk {terms[G.PREC_FP64]})")
+    assert terms[G.PREC_MIXED] == terms[G.PREC_FP64] > 0
 
 
 def csr_positions(start, count):
