@@ -210,6 +210,18 @@ impl Context {
         self.with(|c| unsafe { check(c, sys::gvs_diagnostics(c, softening, with_potential as c_int, &mut d)) })?;
         Ok(d)
     }
+
+    /// `PlummerSphere::generate` (plummer_sphere.rs:106-133) on the GPU, into the resident
+    /// state: the reference's stream and draws, within a few ulps of the host sampler.
+    pub fn plummer_on_device(&self, n: usize, seed: u64, scale_radius: f64, total_mass: f64) -> Result<()> {
+        self.with(|c| unsafe { check(c, sys::gvs_ic_plummer_device(c, n, seed, scale_radius, total_mass)) })
+    }
+
+    /// Two Plummer spheres from one stream on a head-on orbit (the Barnes-Hut workload's
+    /// initial conditions) on the GPU, into the resident state.
+    pub fn collision_on_device(&self, n: usize, seed: u64, separation: f64) -> Result<()> {
+        self.with(|c| unsafe { check(c, sys::gvs_ic_collision_device(c, n, seed, separation)) })
+    }
 }
 
 /// `GravitySolver` on the GPU: BruteForce or BarnesHut.
