@@ -627,7 +627,29 @@ def wl_bh(ctx, G, L, a, peaks, extra=False) -> dict:
            "e2e": e2e, "headline": "the parity walk; the group walk is faster but parity-unpinned"}
     if not a.no_extras or extra:
         res["cpu_baseline"] = cpu_bh_sample(G, theta, eps)
+    if extra:
+        res["parity_other_configs"] = bh_parity_configs(ctx, G, eps, dt)
     return res
+
+
+def bh_parity_configs(ctx, G, eps, dt, steps=2) -> dict:
+    """The parity walk's KDK step at the workload's other sizes and opening angles
+    (N = 2^22, 2^24; theta = 0.5, 0.7), on collision ICs generated on the device."""
+    out = {}
+    for n, theta in ((1 << 22, 0.7), (1 << 24, 0.5), (1 << 24, 0.7)):
+        ctx.ic_collision_device(n, 7)
+        ctx.compute_forces(G.ALGO_BH, G.PREC_MIXED, eps, theta)
+        ctx.kdk_steps(G.ALGO_BH, G.PREC_MIXED, eps, theta, dt, 1)  # warm
+        ctx.profile(True)
+        ms = step_events(ctx, lambda: ctx.kdk_steps(G.ALGO_BH, G.PREC_MIXED, eps, theta, dt, 1), steps)
+        prof = ctx.profile_read()
+        ctx.profile(False)
+        launches = max(1, prof["force_launches"])
+        out[f"n{n}_theta{theta}"] = {"value": n * steps / (sum(ms) * 1e-3), "unit": UNIT,
+                                     "ms_per_step": sum(ms) / steps, "walk_ms": prof["force_ms"] / launches,
+                                     "terms_per_particle": prof["bh_walk_terms"] / launches / n}
+    out["how"] = f"{steps} CUDA-event-timed KDK steps after one warm step, L2 flushed before each"
+    return out
 
 
 def cpu_bh_sample(G, theta, eps, n=1 << 20):
