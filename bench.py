@@ -794,6 +794,13 @@ def wl_sph(ctx, G, L, a, peaks, extra=False) -> dict:
                          "host arrays, wall clock"}
     if not a.no_extras or extra:
         res["cpu_baseline"] = cpu_sph_sample(G, n=n)
+    if extra:  # the workload's larger size, mixed, a bounded run
+        import copy
+        b = copy.copy(a)
+        b.n, b.steps, b.warmup, b.sph_precision, b.no_extras = 1 << 20, 3, 2, "mixed", True
+        r20 = wl_sph(ctx, G, L, b, peaks, extra=False)
+        res[f"n{b.n}"] = {k: r20[k] for k in ("value", "ms_per_step", "clocks", "roofline", "e2e", "config")
+                          if k in r20}
     return res
 
 
