@@ -144,3 +144,16 @@ def test_adjoint_checkpoint_plan():
     for bad in ([0], [100, 200], [0, 100, 250], [0, 100, 200, 200], [0, 0, 100]):
         with pytest.raises(ValueError):
             checkpoint_plan(bad)
+
+
+def test_cold_collapse_ic_properties(lib):
+    """galaxy.rs:11-56: the requested count, particles at rest, and every particle within
+    the sphere plus a 10 % margin for the COM shift."""
+    p = G.ColdCollapse(500).generate()
+    assert p.count == 500
+    q = G.ColdCollapse(100).generate()
+    assert not q.vx.any() and not q.vy.any() and not q.vz.any()
+    radius = 2.0
+    r = G.ColdCollapse(1000, radius=radius).generate()
+    margin = radius * 0.1
+    assert (r.x ** 2 + r.y ** 2 + r.z ** 2 <= (radius + margin) ** 2).all()

@@ -6,6 +6,8 @@ f32 terms on float-float separations).
   force_accuracy_theta_05 / _03   (:52-72)  RMS relative force error against BruteForce
   force_accuracy_monotonic        (:74-101) the error grows with theta
   virial_equilibrium_plummer_bh   (:142-193) N = 500, 10 t_dyn, virial ratio and energy
+and determinism.rs (both solvers, twice, bit for bit) and the cold collapse of galaxy.rs
+(energy with BarnesHut; its IC properties are checked on the CPU in test_abi_cpu.py).
 
 energy_conservation_kepler_bh (:103-140) is left out: on two bodies the walk opens the root
 and sums the single pair exactly (the Kepler tests of the direct sum cover that orbit), and
@@ -89,3 +91,47 @@ def test_virial_equilibrium_plummer_bh(ctx, prec):
     print(f"Plummer BH virial max deviation {worst:.4f}, dE/E {de:.3e}")
     assert worst < 0.5
     assert de < 0.01
+
+
+# ---- determinism.rs and galaxy.rs (the cold collapse) --------------------------------
+def run_sim(p, algo, prec, eps, theta, dt, steps):
+    """determinism.rs:12-27 in a fresh context: forces, then `steps` KDK steps."""
+    c = G.Context(0)
+    try:
+        c.set_state(p)
+        c.compute_forces(algo, prec, eps, theta)
+        c.kdk_steps(algo, prec, eps, theta, dt, steps)
+        q = G.Particles(p.count)
+        c.get_state(q)
+    finally:
+        c.close()
+    return np.stack([q.x, q.y, q.z], 1)
+
+
+@pytest.mark.parametrize("algo,prec", [(G.ALGO_DIRECT, G.PREC_FP64_EXACT), (G.ALGO_DIRECT, G.PREC_MIXED),
+                                       (G.ALGO_BH, G.PREC_FP64), (G.ALGO_BH, G.PREC_MIXED),
+                                       (G.ALGO_BH, G.PREC_FP32)],
+                         ids=["bf-exact", "bf-mixed", "bh-f64", "bh-mixed", "bh-f32"])
+def test_deterministic(algo, prec):
+    """determinism.rs:29-69: N = 200 seed 42, eps 0.05, dt 1e-3, 50 steps, twice: the same
+    positions bit for bit."""
+    p = G.PlummerSphere(200, seed=42).generate()
+    a = run_sim(p, algo, prec, 0.05, 0.5, 1e-3, 50)
+    b = run_sim(p, algo, prec, 0.05, 0.5, 1e-3, 50)
+    assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("prec", WALKS, ids=["f64", "mixed"])
+def test_cold_collapse_energy_conservation(ctx, prec):
+    """galaxy.rs:58-89: ColdCollapse N = 500, suggested eps and dt, BarnesHut theta 0.5,
+    100 steps: |dE/E| < 5 %."""
+    sc = G.ColdCollapse(500)
+    p = sc.generate()
+    eps, dt = sc.suggested_softening(), sc.suggested_dt()
+    ctx.set_state(p)
+    ctx.compute_forces(G.ALGO_BH, prec, eps, 0.5)
+    e0 = ctx.diagnostics(eps).total_energy
+    ctx.kdk_steps(G.ALGO_BH, prec, eps, 0.5, dt, 100)
+    drift = abs((ctx.diagnostics(eps).total_energy - e0) / e0)
+    print(f"cold collapse dE/E over 100 steps {drift:.3e}")
+    assert drift < 0.05
