@@ -135,3 +135,26 @@ def test_cold_collapse_energy_conservation(ctx, prec):
     drift = abs((ctx.diagnostics(eps).total_energy - e0) / e0)
     print(f"cold collapse dE/E over 100 steps {drift:.3e}")
     assert drift < 0.05
+
+
+@pytest.mark.parametrize("prec", WALKS, ids=["f64", "mixed"])
+def test_barnes_hut_scaling_is_nlogn(ctx, prec):
+    """scaling.rs:14-80 with the walk's summed terms in place of wall time (a GPU at
+    N <= 20000 is bound by launch latency, not by the walk's work): Plummer seed 42,
+    theta 0.5, eps 0.05, N = 2^14 ... 2^18; the log-log slope of the work over the last
+    four sizes lies in [0.8, 1.8] (N log N, not N^2)."""
+    ns = [1 << 14, 1 << 15, 1 << 16, 1 << 17, 1 << 18]
+    work = []
+    for n in ns:
+        p = G.PlummerSphere(n, seed=42).generate()
+        p.clear_accelerations()
+        try:
+            ctx.profile(True)
+            G.BarnesHut(0.05, 0.5, prec, ctx).compute_accelerations(p)
+            work.append(ctx.profile_read()["bh_walk_terms"])
+        finally:
+            ctx.profile(False)
+    x, y = np.log(ns[1:]), np.log(work[1:])
+    slope = float(((x - x.mean()) * (y - y.mean())).sum() / ((x - x.mean()) ** 2).sum())
+    print("terms: " + ", ".join(f"N={n}: {w}" for n, w in zip(ns, work)) + f"; log-log slope {slope:.3f}")
+    assert 0.8 <= slope <= 1.8

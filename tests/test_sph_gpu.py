@@ -357,3 +357,25 @@ def test_sph_step_with_gravity_beside_is_deterministic(ctx, algo, gprec):
     assert dta == dtb
     for f in fields:
         assert np.array_equal(getattr(a, f), getattr(b, f)), f
+
+
+@pytest.mark.parametrize("prec", [G.PREC_FP64_EXACT, G.PREC_MIXED])
+def test_cold_collapse_gas_smoke(ctx, prec):
+    """tests/cold_collapse_gas.rs: ColdCollapse N = 500 as gas, BruteForce gravity at the
+    suggested softening, 50 step_with_sph steps from min(dt, suggested dt), dt growth capped
+    at 1.5x: positions, densities and internal energies stay finite."""
+    sc = G.ColdCollapse(500, sph=True)
+    p = sc.generate()
+    assert p.has_gas()
+    grav = G.BruteForce(sc.suggested_softening(), G.PREC_FP64_EXACT, ctx)
+    sph = G.SphSolver(ctx)
+    sph.params.precision = prec
+    p.clear_accelerations()
+    grav.compute_accelerations(p)
+    inter = sph.compute(p)
+    dt = min(sph.compute_timestep(p, inter), sc.suggested_dt())
+    for step in range(50):
+        dtn = G.step_with_sph(p, grav, sph, dt)
+        dt = min(dtn, 1.5 * dt)
+        if step % 10 == 0:
+            assert np.isfinite(p.x).all() and np.isfinite(p.density).all() and np.isfinite(p.internal_energy).all()
