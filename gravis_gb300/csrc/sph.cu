@@ -1022,9 +1022,10 @@ void sph_free(Ctx *c) {
     c->sph = nullptr;
 }
 
-// SphSolver::compute (solver.rs:61-80) on the resident state: a and du/dt accumulate.
+// Clears one bit of the error word, atomically (other streams may be setting others).
 __global__ void k_clear_flag(unsigned *err, unsigned bit) { atomicAnd(err, ~bit); }
 
+// SphSolver::compute (solver.rs:61-80) on the resident state: a and du/dt accumulate.
 gvs_status sph_compute(Ctx *c, const gvs_sph_params *prm) {
     const size_t n = c->n;
     if (n == 0) return GVS_OK;
