@@ -292,7 +292,7 @@ gvs_status gvs_create(gvs_ctx **out, int device) {
         cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreate(&c->prof.ev[0]) != cudaSuccess || cudaEventCreate(&c->prof.ev[1]) != cudaSuccess) {
-        delete c;
+        gvs_destroy(c);  // releases whichever streams and events were created
         return fail(nullptr, GVS_ERR_LAUNCH, "stream/event creation failed");
     }
     if (ensure(c, c->err_word, 256) != cudaSuccess ||

@@ -323,7 +323,8 @@ gvs_status gvs_ic_plummer(size_t n, uint64_t seed, double scale_radius, double t
  * sums).  n <= 2^27; scratch of about 48 n log2(n) + 100 n bytes during the call
  * (19 GB at n = 2^24).
  * GVS_ERR_STATE if a rejection decision lies within 2^-40 of its threshold, where the
- * two libraries could decide differently (use gvs_ic_plummer then). */
+ * two libraries could decide differently (use gvs_ic_plummer then); after any error the
+ * resident state is allocated for n particles but its contents are unspecified. */
 gvs_status gvs_ic_plummer_device(gvs_ctx *ctx, size_t n, uint64_t seed, double scale_radius, double total_mass);
 /* gvs_ic_collision (two Plummer spheres from one stream, the Barnes-Hut workload's ICs) on
  * the GPU into ctx's resident state, on the same terms as gvs_ic_plummer_device. */
