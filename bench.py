@@ -53,7 +53,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s on 1 GB300: mixed vs FP64 at force rel err <=1e-6; adjoint/fwd"
 UNIT = "particle-steps/s"
-WORKLOADS = ("direct", "plummer1k", "bh", "sph", "ensemble", "adjoint", "precision")
+WORKLOADS = ("direct", "plummer1k", "bh", "sph", "ensemble", "adjoint", "precision", "device_ics")
 
 
 def parse():
@@ -1113,7 +1113,7 @@ def run_workload(a, d):
     ctx = G.Context(d.local)
     peaks = Peaks(ctx, d.local)
     fn = {"plummer1k": wl_plummer1k, "bh": wl_bh, "sph": wl_sph, "ensemble": wl_ensemble, "adjoint": wl_adjoint,
-          "precision": wl_precision}[a.workload]
+          "precision": wl_precision, "device_ics": wl_device_ics}[a.workload]
     res = {"metric": METRIC, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic",
            "workload": a.workload}
