@@ -241,17 +241,34 @@ __global__ void __launch_bounds__(COM_NT) k_com_part(size_t n, const double *__r
     if (threadIdx.x < 7) part[(size_t)blockIdx.x * 7 + threadIdx.x] = sh[threadIdx.x][0];
 }
 
-__global__ void k_com_shift(size_t n, int nparts, const double *__restrict__ part, double *__restrict__ x,
+// The blocks' partial sums in a fixed tree (one block of COM_FINAL threads, nparts <=
+// COM_FINAL), then the total mass and the COM position and velocity.
+constexpr int COM_FINAL = 1024;
+__global__ void __launch_bounds__(COM_FINAL) k_com_final(const double *__restrict__ part, int nparts,
+                                                          double *__restrict__ com) {
+    __shared__ double sh[COM_FINAL];
+    double tot[7];
+    for (int k = 0; k < 7; ++k) {
+        sh[threadIdx.x] = (int)threadIdx.x < nparts ? part[(size_t)threadIdx.x * 7 + k] : 0.0;
+        __syncthreads();
+        for (int s = COM_FINAL / 2; s > 0; s >>= 1) {
+            if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+            __syncthreads();
+        }
+        tot[k] = sh[0];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        com[0] = tot[0];
+        for (int k = 1; k < 7; ++k) com[k] = tot[0] != 0.0 ? tot[k] / tot[0] : 0.0;
+    }
+}
+
+__global__ void k_com_shift(size_t n, const double *__restrict__ com, double *__restrict__ x,
                             double *__restrict__ y, double *__restrict__ z, double *__restrict__ vx,
                             double *__restrict__ vy, double *__restrict__ vz) {
     __shared__ double c[7];
-    if (threadIdx.x == 0) {
-        double s[7] = {0, 0, 0, 0, 0, 0, 0};
-        for (int b = 0; b < nparts; ++b)
-            for (int k = 0; k < 7; ++k) s[k] += part[(size_t)b * 7 + k];
-        c[0] = s[0];
-        for (int k = 1; k < 7; ++k) c[k] = s[0] != 0.0 ? s[k] / s[0] : 0.0;
-    }
+    if (threadIdx.x < 7) c[threadIdx.x] = com[threadIdx.x];
     __syncthreads();
     if (c[0] == 0.0) return;  // shift_to_com_frame leaves a massless system alone
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
@@ -284,11 +301,11 @@ static gvs_status ic_spheres_device(Ctx *c, size_t n, uint64_t seed, const Spher
     while (levels < 63 && (size_t(1) << levels) < n) ++levels;
     const size_t jn = (size_t)levels * (H + 1);
     Scratch sw, sj, ss, sp, sf;
-    const int nparts = (int)std::min<size_t>(1024, grid_of(n, COM_NT));
+    const int nparts = (int)std::min<size_t>(COM_FINAL, grid_of(n, COM_NT));
     GVS_CUDA(c, cudaMalloc(&sw.p, (size_t)W * 4));
     GVS_CUDA(c, cudaMalloc(&sj.p, jn * 4));
     GVS_CUDA(c, cudaMalloc(&ss.p, n * 4));
-    GVS_CUDA(c, cudaMalloc(&sp.p, (size_t)nparts * 7 * sizeof(double)));
+    GVS_CUDA(c, cudaMalloc(&sp.p, ((size_t)nparts + 1) * 7 * sizeof(double)));  // partials, then the COM
     GVS_CUDA(c, cudaMalloc(&sf.p, 16));
     GVS_CUDA(c, cudaMemsetAsync(sf.p, 0, 16, st));
     uint32_t *w = static_cast<uint32_t *>(sw.p), *J = static_cast<uint32_t *>(sj.p);
@@ -303,10 +320,12 @@ static gvs_status ic_spheres_device(Ctx *c, size_t n, uint64_t seed, const Spher
     double *vx = as<double>(c->vx), *vy = as<double>(c->vy), *vz = as<double>(c->vz), *m = as<double>(c->m);
     k_plummer<<<grid_of(n, 128), 128, 0, st>>>(w, start, n, W, sph, x, y, z, vx, vy, vz, m, flags);
     double *part = static_cast<double *>(sp.p);
+    double *com = part + (size_t)nparts * 7;
     k_com_part<<<nparts, COM_NT, 0, st>>>(n, x, y, z, vx, vy, vz, m, part);
-    k_com_shift<<<(unsigned)std::min<size_t>(grid_of(n), (size_t)c->num_sms * 8), 256, 0, st>>>(n, nparts, part, x, y,
-                                                                                              z, vx, vy, vz);
-    c->prof.launches += 5 + (levels - 1);
+    k_com_final<<<1, COM_FINAL, 0, st>>>(part, nparts, com);
+    k_com_shift<<<(unsigned)std::min<size_t>(grid_of(n), (size_t)c->num_sms * 8), 256, 0, st>>>(n, com, x, y, z, vx,
+                                                                                              vy, vz);
+    c->prof.launches += 6 + (levels - 1);
     GVS_TRY(check_launch(c, "device Plummer ICs"));
     unsigned hf = 0;
     GVS_CUDA(c, cudaMemcpyAsync(&hf, flags, 4, cudaMemcpyDeviceToHost, st));
